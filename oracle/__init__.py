@@ -1,0 +1,31 @@
+"""Parity oracle for the descent time step -- TEST INFRASTRUCTURE ONLY.
+
+Two checkers live here, and nothing in the product path imports them:
+
+* ``oracle.restated`` -- ctypes binding of ``phybs_oracle.cpp``, a C++
+  restatement of the reference's CPU solver templated on float/double
+  (FP32 parity and the all-FP64 reference).  Built by :func:`build`.
+* ``oracle.ref`` -- ctypes binding of ``_ref/libphybs_ref.so``, the reference's
+  own CPU solver compiled headless from the reference sources
+  (``ref_build/Makefile``).  Only buildable where the reference tree exists;
+  its outputs are frozen into ``tests/golden`` for everywhere else.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libphybs_ref.so")
+REFERENCE_TREE = os.environ.get("PHYBS_REFERENCE", "/root/reference")
+
+
+def build(reference: bool = True, verbose: bool = False) -> None:
+    """Compile the restated oracle; also the reference harness when the
+    reference tree is present."""
+    src = os.path.join(HERE, "phybs_oracle.cpp")
+    if (not os.path.exists(ORACLE_SO)) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", ORACLE_SO, src]
+        subprocess.run(cmd, check=True, capture_output=not verbose)
+    if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "FVM")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={REFERENCE_TREE}", "-j8"],
+                       check=True, capture_output=not verbose)
