@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Benchmark: frames/s of the descent time step at relative residual <= 1e-4.
+
+Workload (the 1M-tet roofline configuration): a 50 x 50 x 80 cube box of edge
+0.005 m, 5-tet split (1,000,000 tets, 210,681 nodes), interior nodes jittered
++-0.1 cell from the seed, neo-Hookean with E = 10^U(4, 6) Pa drawn from the
+seed and Poisson 0.4; the top face (z = max) pinned, the bottom face driven to
+1.5x the rest length linearly over 30 steps; gravity; h = 1/30 s; every frame
+iterates until |g| <= 1e-4 |g_0| (FP64 norms).  Synthetic data: the mesh is
+generated, nothing is downloaded.
+
+A "step" of this benchmark is one frame: the prescribed-boundary upload and
+one pbs_step() solve through the C ABI.  ``value`` is frames/s with the state
+resident in HBM, timed with CUDA events on the library's stream; ``e2e`` adds
+the per-frame read-back of all positions to host memory through
+pbs_read_positions (host wall clock around synchronised calls).
+
+``--impl reference`` times the CPU restatement of the reference's descent
+step (serial, like DescentOptimize) on the same workload: each step is a
+bounded sample of 32 iterations of a frame, converted to frames/s with the
+iterations a frame takes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at residual<=1e-4, 1M tets: warm-started vs plain descent, 1 GB300"
+UNIT = "frames/s"
+# Algorithmic bytes of one tet-iteration (per-tet indices 16 B + Dm^-1 36 B +
+# volume 4 B, plus per node x, x~, x_last, H_d (4 x 12 B), mass 4 B read and
+# x_next 12 B written, amortised over tets): 56 + 64 N / T.
+STATIC_BYTES_PER_TET = 56.0
+BYTES_PER_NODE = 64.0
+# Iterations one frame of the box workload takes (mean over frames 1-8 of
+# the GPU solve, seed 0); used only by the CPU reference arm, which times a
+# bounded sample of iterations and cannot afford whole frames at 1M tets.
+REFERENCE_ITERS_PER_FRAME = 2000.0
+CPU_SAMPLE_ITERS = 32
+
+
+def box_workload(seed: int, scale: float = 1.0):
+    from phybs_gb300 import meshes as M
+    nx, ny, nz = (max(2, int(round(50 * scale))), max(2, int(round(50 * scale))), max(2, int(round(80 * scale))))
+    rng = np.random.default_rng(seed)
+    young = float(10.0 ** rng.uniform(4.0, 6.0))
+    m = M.box_mesh(nx, ny, nz, edge=0.005 / scale if scale != 1.0 else 0.005, jitter=0.1, seed=seed,
+                   young=young, poisson=0.4, pin="both")
+    z = m.rest[:, 2]
+    bottom = np.nonzero(z <= z.min() + 1e-9)[0].astype(np.int32)
+    length = float(z.max() - z.min())
+    return m, bottom, length, young
+
+
+def bottom_positions(m, bottom, length, frame):
+    x = m.rest[bottom].astype(np.float32).copy()
+    x[:, 2] -= np.float32(0.5 * length * min((frame + 1) / 30.0, 1.0))
+    return x
+
+
+def solver_params(h=1 / 30, tol=1e-4, max_iters=20000):
+    from phybs_gb300 import _lib as L
+    from phybs_gb300.solver import make_params
+    return make_params("gpu_reference", h=h, tol=tol, max_iters=max_iters, control=L.PBS_CONTROL_RESTART,
+                       energy_slack=16.0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int = 0):
+        self.idx = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def cpu_baseline_sample(m, bottom, length, frame, iters=CPU_SAMPLE_ITERS):
+    """Serial CPU restatement of the reference step: seconds per iteration on
+    the full mesh (one Jacobi-diagonal refresh and four energy checks per 32
+    iterations, as the reference's schedule has)."""
+    from oracle import restated as O
+    from phybs_gb300.solver import lame_arrays
+    mu, lam = lame_arrays(m.young, m.poisson)
+    pm = m.pin_mask()
+    r = O.rest(m.rest, m.tets, pm, prec=32)
+    st = O.StepState(m.rest)
+    st.x0[bottom] = bottom_positions(m, bottom, length, frame)
+    p = O.make_params(h=1 / 30, max_iters=iters, tol=0.0, control=1, body_force_scale=1.0, energy_clamp=1)
+    t0 = time.perf_counter()
+    stats = O.step(st, p, m.tets, r, mu, lam, pm, prec=32)
+    dt = time.perf_counter() - t0
+    return dt / max(stats.passes, 1), stats.passes
+
+
+def run_reference(args):
+    m, bottom, length, young = box_workload(args.seed, args.scale)
+    ipf = REFERENCE_ITERS_PER_FRAME
+    times = []
+    for s in range(args.warmup + args.steps):
+        spi, _ = cpu_baseline_sample(m, bottom, length, s)
+        if s >= args.warmup:
+            times.append(spi * ipf)
+    sec_per_frame = float(np.mean(times))
+    value = 1.0 / sec_per_frame
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"box {m.n_tets} tets / {m.n_nodes} nodes, plain descent to |g|<=1e-4|g0|",
+                   "seed": args.seed, "young": young},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{CPU_SAMPLE_ITERS} iterations of each frame on the full mesh (serial FP32 "
+                                   f"restatement of DescentOptimize), x {ipf:.0f} iterations/frame"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world):
+    import ctypes
+
+    import torch
+
+    from phybs_gb300 import _lib as L
+    from phybs_gb300.solver import DescentSolver
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    m, bottom, length, young = box_workload(args.seed, args.scale)
+    s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
+    stream = torch.cuda.ExternalStream(s.stream())
+    pin_xyz = torch.empty((args.warmup + 2 * args.steps + 1, bottom.size, 3), dtype=torch.float32,
+                          pin_memory=True).numpy()
+    for f in range(pin_xyz.shape[0]):
+        pin_xyz[f] = bottom_positions(m, bottom, length, f)
+    out = torch.empty((m.n_nodes, 3), dtype=torch.float32, pin_memory=True).numpy()
+    frame = 0
+    iters = []
+    for _ in range(args.warmup):
+        s.set_node_positions(bottom, pin_xyz[frame])
+        s.step()
+        frame += 1
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- value: state resident in HBM
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    passes = 0
+    launches = 0
+    statuses = []
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            s.set_node_positions(bottom, pin_xyz[frame])
+            it = s.step(raise_on_error=False)
+            st = s.stats()
+            iters.append(it)
+            passes += st["passes"]
+            launches += 4 + 2 * 16 * st["graph_launches"]
+            statuses.append(st["status"])
+            frame += 1
+        e1.record(stream)
+        barrier()
+    dev_ms = e0.elapsed_time(e1)
+    t_dev = dev_ms / 1e3
+    if world > 1:
+        t = torch.tensor([t_dev], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * args.steps / t_dev
+    # ---- e2e: same frames plus position read-back to pinned host memory
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_node_positions(bottom, pin_xyz[frame])
+        s.step(raise_on_error=False)
+        s.positions(out)
+        frame += 1
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([t_e2e], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = world * args.steps / t_e2e
+    # ---- per-kernel times on the launching stream, and the roofline
+    tet_ms, node_ms = s.profile_kernels(20)
+    peak, peak_kind = measured_peak()
+    T, N = m.n_tets, m.n_nodes
+    alg_bytes = STATIC_BYTES_PER_TET * T + BYTES_PER_NODE * N
+    pass_ms = tet_ms + node_ms
+    achieved = alg_bytes / (pass_ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    mean_iters = float(np.mean(iters))
+    if rank != 0:
+        s.close()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3 * world / world,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"box 50x50x80 cubes, 5-tet split: {T} tets / {N} nodes; bottom face pulled to "
+                               f"1.5x over 30 frames; plain descent (no warm start) to |g|<=1e-4|g0|",
+                   "seed": args.seed, "young": young, "h": 1 / 30, "tol": 1e-4,
+                   "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "iterations_per_frame": mean_iters, "iterations_per_s": passes / t_dev,
+        "status": statuses,
+        "roofline": {"bound": "hbm", "kernel": "descent pass = k_tet + k_node", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": (traffic or {}).get("bytes_per_pass"),
+                     "algorithmic_bytes_per_pass": alg_bytes, "tet_ms": tet_ms, "node_ms": node_ms},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(bottom.size * 16),
+                "d2h_bytes_per_step": int(N * 12)},
+    }
+    line["clocks"] = clk.summary()
+    if not args.no_cpu_baseline:
+        spi, n = cpu_baseline_sample(m, bottom, length, frame)
+        cpu_value = 1.0 / (spi * mean_iters)
+        line["cpu_baseline"] = {"value": cpu_value, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{n} iterations of one frame on the full mesh (serial FP32 "
+                                          f"restatement of DescentOptimize), x {mean_iters:.0f} iterations/frame "
+                                          f"measured on the GPU"}
+    print(json.dumps(line))
+    s.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--scale", type=float, default=1.0, help="mesh resolution scale (1.0 = the 1M-tet box)")
+    ap.add_argument("--max-iters", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("gloo")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * phybs.h - C ABI of the GB300-native descent time step.
+ *
+ * One handle holds one packed set of tet meshes ("instances") resident on
+ * the GPU, and advances all of them by one implicit-Euler step per
+ * pbs_step() call: the step's energy is minimised by Jacobi-preconditioned
+ * descent with Chebyshev acceleration and an energy line search every few
+ * iterations.  This is the entry-point set of PhyBS's
+ *   CUDAInterface (FVM/CUDAInterface.h:20-102)   and
+ *   DescentOptimize (FVM/DescentOptimize.h:11-54)
+ * as its step loop (FVM/fvm.cpp:35-47, 172-189, 216-217) drives them:
+ * construct from a TetMesh, set the material, step, read positions back.
+ *
+ * Conventions
+ *   - positions / forces: 3*N floats, interleaved xyz (Eigen 3xN column-major,
+ *     the layout of TetMesh::getNodes().data()).
+ *   - tets: 4*T int32, 0-based node ids, 4 consecutive ids per tet
+ *     (TetMesh::getTets().data()).  Tets must be positively oriented.
+ *   - every function returns PBS_OK (0) or a negative PBS_E_* code; the
+ *     library never exits the process and never prints.
+ *   - one handle = one CUDA stream on the current device; a handle is not
+ *     thread-safe.  Calls are synchronous unless stated otherwise.
+ *   - there is no CPU path: without a usable GB300 (sm_103) every call that
+ *     needs the device fails with PBS_E_CUDA / PBS_E_NO_DEVICE.
+ */
+#ifndef PHYBS_H
+#define PHYBS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBS_OK 0
+#define PBS_E_INVALID_ARG (-1)
+#define PBS_E_CUDA (-2)
+#define PBS_E_NONFINITE (-3)   /* a step produced NaN/Inf energy or residual   */
+#define PBS_E_ITER_CAP (-4)    /* the device-side pass cap ended a step         */
+#define PBS_E_BAD_MESH (-5)    /* bad index, zero-volume or inverted rest tet   */
+#define PBS_E_NO_DEVICE (-6)   /* no CUDA device, or not compute capability 10.3 */
+#define PBS_E_OUT_OF_MEMORY (-7)
+#define PBS_E_CAPACITY (-8)    /* a size beyond a documented fixed maximum      */
+
+/* Materials.  Both are the neo-Hookean energy
+ *   Psi = mu/2 (I1 - 3) - mu ln J + lambda/2 (ln J)^2,
+ * evaluated through the invariants (IsotropicNeohookeanMaterial.cpp:146)
+ * or through the principal stretches of the modified SVD
+ * (IsotropicMaterial.cpp:360-409, Xu et al. 2015). */
+#define PBS_MATERIAL_NEOHOOKEAN 0
+#define PBS_MATERIAL_STRETCH 1
+
+/* Line-search rejection behaviour. */
+#define PBS_CONTROL_REFERENCE 0 /* alpha *= shrink; iterations -= k - 8; redo k (DescentOptimize.cpp:166-177) */
+#define PBS_CONTROL_RESTART 1   /* alpha *= shrink; restore x and the Chebyshev history; budget unchanged   */
+
+/* Energy clamp per tet. */
+#define PBS_CLAMP_CPU 0 /* e > 1e-6 ? e : 0   (IsotropicNeohookeanMaterial.cpp:171) */
+#define PBS_CLAMP_GPU 1 /* max(e, 0)          (CUDAInterface.cu:549)               */
+
+typedef struct pbs_handle pbs_handle;
+
+/* Mesh description (deep-copied by pbs_create; the caller keeps ownership). */
+typedef struct pbs_mesh_desc {
+    int n_nodes;
+    const float *rest;       /* 3*n_nodes rest positions                          */
+    const float *positions;  /* 3*n_nodes initial positions, or NULL for rest     */
+    int n_tets;
+    const int *tets;         /* 4*n_tets                                          */
+    const int *pin_mask;     /* n_nodes, > 0 = pinned (fixed within a step), or NULL */
+    int n_instances;         /* >= 1; instances are disjoint node/tet ranges      */
+    const int *instance_node_ptr; /* n_instances+1, or NULL when n_instances == 1 */
+    const int *instance_tet_ptr;  /* n_instances+1, or NULL when n_instances == 1 */
+    float density;           /* kg/m^3, lumped mass = density * vol / 4 per corner */
+    float gravity;           /* m/s^2 along -y (the reference uses 9.8)           */
+} pbs_mesh_desc;
+
+/* Step parameters.  pbs_default_params() returns the reference preset: the
+ * constants of DescentOptimize.cpp:59-77,146-240 and CUDAInterface.cu:911-1006
+ * (h = 0.03, 96 iterations, alpha 0.1 / 0.7 / 0.01, line search every 8,
+ * Hessian diagonal every 32, rho profile {1:0.96, 7:0.991, 10:0.999},
+ * damping 0.99, warm start 0.2, CPU energy clamp, gravity and external
+ * forces counted twice in the gradient as DescentOptimize does). */
+typedef struct pbs_step_params {
+    float h;                  /* time step, s                                   */
+    int max_iters;            /* the reference's `iterations`                   */
+    float tol;                /* stop when |g| <= tol * |g_0| (FP64 norms); 0 = off */
+    int control;              /* PBS_CONTROL_*                                  */
+    float alpha0, alpha_min, alpha_shrink;
+    int line_search_every;    /* energy check period (8)                        */
+    int hessian_every;        /* Jacobi diagonal refresh period (32)            */
+    int n_profile;            /* Chebyshev rho profile entries (<= 4)           */
+    int profile_k[4];
+    float profile_rho[4];
+    float damping;            /* v = damping * (x - x0) / h                      */
+    float warm_start;         /* x_init = x~ + warm_start * h * (v - v_old)      */
+    float body_force_scale;  /* times gravity + external forces enter the gradient:
+                                 2 = DescentOptimize.cpp:107 with IsotropicNeohookeanMaterial.cpp:140,
+                                 1 = CUDAInterface.cu:600-602 (physical)          */
+    int energy_clamp;         /* PBS_CLAMP_*                                     */
+    int pass_cap;             /* hard cap on device passes per step; 0 = max_iters + 16 */
+    float energy_slack;       /* line-search rounding allowance: reject only if
+                                 E > E_old + energy_slack * 2^-24 * sqrt(sum of squared
+                                 energy terms); 0 = the reference's strict E > E_old */
+} pbs_step_params;
+
+typedef struct pbs_stats {
+    int passes;               /* iterations executed, including redone ones (max over instances) */
+    int iterations;           /* accepted iterations k at exit (max over instances) */
+    int rejections;           /* line-search rejections (sum over instances)      */
+    int converged;            /* instances that met tol                          */
+    int status;               /* worst per-instance status (PBS_OK or PBS_E_*)    */
+    float alpha;              /* instance 0 */
+    float rho, omega;         /* instance 0 Chebyshev state */
+    double energy;            /* instance 0 energy at its last check             */
+    double residual_ratio;    /* instance 0 |g_k| / |g_0|                         */
+    double device_ms;         /* device time of the last pbs_step (CUDA events)   */
+    int graph_launches;       /* captured 16-pass graphs launched by the last step */
+} pbs_stats;
+
+void pbs_default_params(pbs_step_params *p);
+const char *pbs_error_string(int code);
+
+/* CUDAInterface::CUDAInterface (CUDAInterface.cu:641-740): copies the mesh to
+ * the device, precomputes Dm^-1, volumes, lumped masses (FP64) and the
+ * deterministic node -> (tet, corner) gather, and resets the state.  The
+ * material starts as neo-Hookean with E = 5e5, nu = 0.45 (TetMesh.cpp:185)
+ * until pbs_set_material is called. */
+int pbs_create(const pbs_mesh_desc *desc, pbs_handle **out);
+void pbs_destroy(pbs_handle *h);
+
+/* Lame parameters as the reference forms them from (E, nu)
+ * (IsotropicNeohookeanMaterial.cpp:57-58, CUDAInterface.cu:704-705):
+ * mu = E / (2 (1 + nu)), lambda = 2 mu / (1 - 2 nu) when reference_formula
+ * is nonzero, else the textbook lambda = 2 mu nu / (1 - 2 nu). */
+void pbs_lame(float young, float poisson, int reference_formula, float *mu, float *lambda);
+
+/* Material model and per-tet (count == n_tets) or uniform (count == 1) Lame
+ * parameters (IsotropicMaterial::m_mus / m_lambdas). */
+int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lambda, int count);
+
+int pbs_set_params(pbs_handle *h, const pbs_step_params *p);
+int pbs_get_params(pbs_handle *h, pbs_step_params *p);
+
+/* One time step of every instance (CUDAInterface::doDescentOpt,
+ * CUDAInterface.cu:911-1007 / DescentOptimize::doDescentOpt).  ext: 3*N
+ * external forces for this step (copied in), or NULL for none.  The external
+ * forces are cleared after the step, as fvm.cpp:188 does.  iters_out may be
+ * NULL.  Returns PBS_E_NONFINITE / PBS_E_ITER_CAP when an instance ended that
+ * way (the state is still advanced). */
+int pbs_step(pbs_handle *h, const float *ext, int *iters_out);
+
+/* Positions after the last step (the hostNode output of doDescentOpt). */
+int pbs_read_positions(pbs_handle *h, float *out);
+/* CUDAInterface::updateNodePositions (CUDAInterface.cu:771). */
+int pbs_update_positions(pbs_handle *h, const float *positions);
+/* Velocities (3*N) and the previous step's velocities, for snapshots. */
+int pbs_read_velocities(pbs_handle *h, float *v, float *v_old);
+int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old);
+/* Overwrite the positions of `count` nodes (caller numbering; ids: count ints,
+ * xyz: 3*count floats) before the next step.  This is how a caller prescribes
+ * the motion of pinned nodes: the reference has no such call, its harness
+ * writes TetMesh::getNodes() directly (pinned nodes stay where they are put
+ * within a step, DescentOptimize.cpp:109-113 / CUDAInterface.cu:578-585). */
+int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float *xyz);
+/* CUDAInterface::reset (CUDAInterface.cu:776): rest positions, zero velocities. */
+int pbs_reset(pbs_handle *h);
+int pbs_get_stats(pbs_handle *h, pbs_stats *s);
+
+/* Mesh sizes and the device-side gather structure, for parity checks.
+ * row_ptr: n_nodes+1; entries: 4*n_tets, entry = 4*tet + corner, ordered per
+ * node by ascending tet then corner. */
+int pbs_get_sizes(pbs_handle *h, int *n_nodes, int *n_tets, int *n_instances);
+int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries);
+/* Rest data as the device holds it: Dm^-1 row-major (9T), signed volume det/6
+ * (T), lumped mass with pins = 1e8 (N), gravity_y = -g * lumped mass (N). */
+int pbs_get_rest_data(pbs_handle *h, float *dm_inv9, float *signed_vol, float *mass, float *grav_y);
+
+/* Evaluate the per-tet kernel at the given positions (NULL = current):
+ * corner forces (12*T, corner-major xyz; the reference's P * AN columns and
+ * their negated sum), clamped energy (T) and the 12 Jacobi-diagonal entries
+ * (12*T).  Any output may be NULL. */
+int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, float *energy, float *hess_diag);
+/* Elastic forces (3*N) and Hessian diagonal (3*N) assembled by the
+ * deterministic gather at the given positions (NULL = current). */
+int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag);
+
+/* The CUDA stream (cudaStream_t) every call of this handle launches on, so a
+ * caller can order its own work or record timing events on it. */
+int pbs_get_stream(pbs_handle *h, void **stream);
+/* Time the two kernels of one descent pass separately with CUDA events on the
+ * handle's stream: runs `passes` passes from the current state (the state is
+ * left as it was) and returns the mean milliseconds per launch of the per-tet
+ * kernel and of the per-node kernel. */
+int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms);
+
+/* Node-node 3N x 3N stiffness pattern of the mesh, bit-identical to
+ * IsotropicMaterial::allocateGlobalStiffnessMatrix (IsotropicMaterial.cpp:554-644):
+ * CSR row pointers (3N+1), column indices (nnz), the CSR slot of each diagonal
+ * entry (3N) and the 48 slots per tet (kIDinCSRval).  Call with col == NULL to
+ * get nnz only.  Host-side; needs no device. */
+int pbs_stiffness_pattern(int n_nodes, int n_tets, const int *tets, int *nnz, int *row_ptr, int *col,
+                          int *diag_idx, int *kid48);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHYBS_H */

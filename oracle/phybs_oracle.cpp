@@ -426,7 +426,7 @@ typedef struct orc_params {
     int n_profile;
     int profile_k[4];
     float profile_rho[4];
-    float damping, warm_start, gravity;
+    float damping, warm_start;
     float body_force_scale;  // times gravity + external forces enter the gradient (2: DescentOptimize.cpp:52 with
                              // IsotropicNeohookeanMaterial.cpp:140; 1: CUDAInterface.cu:600-602)
     int energy_clamp;
@@ -570,8 +570,9 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             if (alpha < (R)p->alpha_min) break;
             ++passes;
             if (k % p->line_search_every == 0) {
-                // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:118-144), with
-                // the external-work term -f_ext . x over free nodes.
+                // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:118-144): the
+                // gravity term 0.5 m 2 g y is -gravity_y . y; plus the external work
+                // -f_ext . x over free nodes.
                 R Ee = 0;
                 for (int i = 0; i < m.t; ++i) {
                     M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
@@ -582,7 +583,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     if (m.pinned[i]) continue;
                     R d2 = 0, w = 0;
                     for (int d = 0; d < 3; ++d) { R dd = x[3 * i + d] - xt[3 * i + d]; d2 += dd * dd; w += ex[3 * i + d] * x[3 * i + d]; }
-                    En += R(0.5) * m.mass[i] * (d2 * h2inv + 2 * (R)p->gravity * x[3 * i + 1]) - w;
+                    En += R(0.5) * m.mass[i] * d2 * h2inv - m.grav_y[i] * x[3 * i + 1] - w;
                 }
                 E = Ee + En;
                 if (k != 0 && E > Eold) {

@@ -29,7 +29,7 @@ class OrcParams(C.Structure):
                 ("alpha0", C.c_float), ("alpha_min", C.c_float), ("alpha_shrink", C.c_float),
                 ("line_search_every", C.c_int), ("hessian_every", C.c_int), ("n_profile", C.c_int),
                 ("profile_k", C.c_int * 4), ("profile_rho", C.c_float * 4), ("damping", C.c_float),
-                ("warm_start", C.c_float), ("gravity", C.c_float), ("body_force_scale", C.c_float),
+                ("warm_start", C.c_float), ("body_force_scale", C.c_float),
                 ("energy_clamp", C.c_int), ("material", C.c_int), ("hessian_closed", C.c_int)]
 
 
@@ -41,7 +41,7 @@ class OrcStats(C.Structure):
 
 def make_params(h=0.03, max_iters=96, tol=0.0, control=0, alpha0=0.1, alpha_min=0.01, alpha_shrink=0.7,
                 line_search_every=8, hessian_every=32, profile=((1, 0.96), (7, 0.991), (10, 0.999)),
-                damping=0.99, warm_start=0.2, gravity=9.8, body_force_scale=2.0, energy_clamp=0, material=0,
+                damping=0.99, warm_start=0.2, body_force_scale=2.0, energy_clamp=0, material=0,
                 hessian_closed=0) -> OrcParams:
     p = OrcParams()
     p.h, p.max_iters, p.tol, p.control = h, max_iters, tol, control
@@ -51,7 +51,7 @@ def make_params(h=0.03, max_iters=96, tol=0.0, control=0, alpha0=0.1, alpha_min=
     for i, (k, r) in enumerate(profile):
         p.profile_k[i] = k
         p.profile_rho[i] = r
-    p.damping, p.warm_start, p.gravity, p.body_force_scale = damping, warm_start, gravity, body_force_scale
+    p.damping, p.warm_start, p.body_force_scale = damping, warm_start, body_force_scale
     p.energy_clamp, p.material, p.hessian_closed = energy_clamp, material, hessian_closed
     return p
 
@@ -148,3 +148,51 @@ def step(state: StepState, params: OrcParams, tets, r: Rest, mu, lam, pin_mask, 
                    _p(_d(r.grav_y)), _p(_i(pin_mask)), _p(state.x0), _p(state.v), _p(state.v_old), _p(ext_a),
                    _p(state.cheb), C.byref(st))
     return st
+
+
+def incidence(tets, n_nodes):
+    """Node -> (tet, corner) gather lists in canonical order (per node: ascending
+    tet id, then corner), entry = 4*tet + corner.  Plain loops; small meshes."""
+    lists = [[] for _ in range(n_nodes)]
+    for t, q in enumerate(np.asarray(tets).reshape(-1, 4).tolist()):
+        for c, node in enumerate(q):
+            lists[node].append(4 * t + c)
+    row = [0]
+    ent = []
+    for li in lists:
+        ent.extend(li)
+        row.append(len(ent))
+    return np.array(row, np.int32), np.array(ent, np.int32)
+
+
+def stiffness_pattern(tets, n_nodes):
+    """IsotropicMaterial::allocateGlobalStiffnessMatrix (IsotropicMaterial.cpp:554-644)
+    restated with Python sets: rows 3n+d, sorted unique columns, the CSR slot of
+    each diagonal and the 48 slots per tet."""
+    tets = np.asarray(tets).reshape(-1, 4).tolist()
+    nb = [set() for _ in range(n_nodes)]
+    for q in tets:
+        for a in q:
+            nb[a].update(q)
+    row = [0]
+    col = []
+    for n in range(n_nodes):
+        cols = [3 * m + e for m in sorted(nb[n]) for e in range(3)]
+        for _ in range(3):
+            col.extend(cols)
+            row.append(len(col))
+    row = np.array(row, np.int32)
+    col = np.array(col, np.int32)
+
+    def slot(r, c):
+        lo, hi = row[r], row[r + 1]
+        return lo + int(np.searchsorted(col[lo:hi], c))
+
+    diag = np.array([slot(r, r) for r in range(3 * n_nodes)], np.int32)
+    kid = np.zeros(48 * len(tets), np.int32)
+    for t, q in enumerate(tets):
+        for fi in range(4):
+            for fj in range(3):
+                for ni in range(4):
+                    kid[48 * t + (fi * 3 + fj) * 4 + ni] = slot(3 * q[fi] + fj, 3 * q[ni])
+    return row, col, diag, kid

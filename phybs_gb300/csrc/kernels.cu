@@ -1,0 +1,621 @@
+// Device kernels of the descent time step (sm_103a).
+//
+// One descent iteration ("pass") is two launches:
+//   k_tet   one thread per tet: gathers the 4 corner displacements (float4),
+//           forms G, the first Piola-Kirchhoff stress and the 12 corner
+//           forces; on Hessian-refresh passes the 12 Jacobi-diagonal terms; on
+//           line-search passes the clamped tet energies plus the node energy
+//           terms, reduced in FP64.  The instance's last block to finish
+//           decides accept / reject (DescentOptimize.cpp:162-183) before any
+//           node moves.  Replaces computeForceKd (CUDAInterface.cu:495-568)
+//           and its 13-25 atomics per tet.
+//   k_node  one thread per node: sums its incident corner forces in the
+//           canonical (tet, corner) order -- no atomics, so forces are
+//           bit-reproducible -- forms the gradient, takes the Jacobi step with
+//           Chebyshev extrapolation (updateNodesNextIter + updateChebyshev,
+//           CUDAInterface.cu:572-623) in step form, d' = (omega-1) d +
+//           omega alpha delta, u' = u + d' in compensated FP32, or restores the
+//           saved state after a rejection.  |g|^2 is reduced in FP64; the last
+//           block runs the stopping / Chebyshev / iteration-count logic, so a
+//           step needs no host round trip (the reference syncs every 8
+//           iterations, CUDAInterface.cu:886-890).
+#include "../../include/phybs.h"
+#include "phybs_internal.cuh"
+#include "tet_math.cuh"
+
+namespace pbs {
+
+// ------------------------------------------------------------ reductions
+// Deterministic block sum: fixed shuffle tree per warp, then warp 0 sums the
+// warp totals in warp order.  Result valid in thread 0.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// ------------------------------------------------------------ rest state
+// Dm^-1 and det Dm / 6 in FP64 from the rest positions (TetMesh.cpp:190-204,
+// CUDAInterface.cu:273-325); per-tet lumped-mass share density*|vol|/4.
+__global__ void k_rest(DevMesh m, const double *rest, float density, float4 *row0, float4 *row1, float4 *row2,
+                       double *tmass, int *bad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.Tp) return;
+    const int4 q = m.tets[t];
+    if (q.x < 0) {
+        row0[t] = row1[t] = row2[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        tmass[t] = 0.0;
+        return;
+    }
+    const int id[4] = {q.x, q.y, q.z, q.w};
+    double p[4][3];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) p[c][d] = rest[3 * (size_t)id[c] + d];
+    double Dm[9];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Dm[3 * d + c] = p[c + 1][d] - p[0][d];
+    double C[9];
+    cofactor3<double>(Dm, C);
+    const double det = Dm[0] * C[0] + Dm[1] * C[1] + Dm[2] * C[2];
+    if (!(det > 0.0) || !isfinite(det)) atomicOr(bad, 1);
+    const double inv = 1.0 / det;  // Dm^-1 = C^T / det
+    row0[t] = make_float4((float)(C[0] * inv), (float)(C[3] * inv), (float)(C[6] * inv), (float)(det / 6.0));
+    row1[t] = make_float4((float)(C[1] * inv), (float)(C[4] * inv), (float)(C[7] * inv), 0.f);
+    row2[t] = make_float4((float)(C[2] * inv), (float)(C[5] * inv), (float)(C[8] * inv), 0.f);
+    tmass[t] = (double)density * fabs(det) / 6.0 * 0.25;
+}
+
+// Lumped mass by the deterministic gather (FP64), gravity = -g * mass before
+// pinning (TetMesh.cpp:205), pinned mass 1e8 (TetMesh.cpp:212-216).
+__global__ void k_mass(DevMesh m, const double *tmass, const int *state, float gravity, float4 *info) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    double s = 0.0;
+    for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) s += tmass[m.inc[j] >> 2];
+    const int st = state[i];
+    const float mass = (float)s;
+    info[i] = make_float4(st == 1 ? 1e8f : mass, (float)(-(double)gravity * s), (float)st, mass);
+}
+
+__global__ void k_set_lame(int Tp, const float *mu, const float *lambda, int count, float4 *row1, float4 *row2,
+                           const int *tet_user) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Tp) return;
+    const int u = tet_user[t];
+    if (u < 0) return;
+    const int src = count == 1 ? 0 : u;
+    row1[t].w = mu[src];
+    row2[t].w = lambda[src];
+}
+
+// ------------------------------------------------------------ step control
+__global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_inst) return;
+    InstCtl c = ctl[b];
+    c.k = 0;
+    c.iters = p.max_iters;
+    c.done = (c.tet_end == c.tet_begin || p.max_iters <= 0) ? 1 : 0;
+    c.passes = 0;
+    c.rejections = 0;
+    c.converged = 0;
+    c.status = PBS_OK;
+    c.par = 0;
+    c.action = ACT_STEP;
+    c.counter_t = 0;
+    c.counter_n = 0;
+    c.alpha = p.alpha0;
+    c.energy = 0.0;
+    c.energy_old = 0.0;
+    c.g0 = -1.0;
+    c.ratio = -1.0;
+    ctl[b] = c;
+    if (!c.done) atomicAdd(active, 1);
+}
+
+__device__ __forceinline__ const InstCtl &node_ctl(const DevMesh &m, const DevState &st, int i) {
+    return st.ctl[m.nblk_inst[i / BLOCK]];
+}
+
+// DescentOptimize::initialization (DescentOptimize.cpp:90-96) /
+// initDescentOpt (CUDAInterface.cu:482-493) in displacement form:
+// u~ = u0 + h v, u_init = u~ + warm_start h (v - v_old); plus the external-
+// force upload.  Writes parity 0 (k_init_ctl resets it).
+__global__ void k_prologue(DevMesh m, DevParams p, DevState st, const float *ext_user, const int *pad2user) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const int u = pad2user[i];
+    if (u < 0) return;
+    const float4 hi = st.u0h[i], lo = st.u0l[i], v = st.v[i], vo = st.vold[i];
+    float th[3] = {hi.x, hi.y, hi.z}, tl[3] = {lo.x, lo.y, lo.z};
+    const float vv[3] = {v.x, v.y, v.z}, dv[3] = {v.x - vo.x, v.y - vo.y, v.z - vo.z};
+    const float w = p.warm_start * p.h;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) add_comp(th[d], tl[d], p.h * vv[d]);
+    float xh[3] = {th[0], th[1], th[2]}, xl[3] = {tl[0], tl[1], tl[2]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) add_comp(xh[d], xl[d], w * dv[d]);
+    st.th[i] = make_float4(th[0], th[1], th[2], 0.f);
+    st.tl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
+    st.uh[i] = make_float4(xh[0], xh[1], xh[2], 0.f);
+    st.ul[i] = make_float4(xl[0], xl[1], xl[2], 0.f);
+    st.dd[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ext_user) e = make_float4(ext_user[3 * (size_t)u], ext_user[3 * (size_t)u + 1], ext_user[3 * (size_t)u + 2], 0.f);
+    st.ext[i] = e;
+}
+
+// v_old <- v; v = damping (u - u0) / h; u0 <- u  (DescentOptimize.cpp:238-240)
+__global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2user) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    if (pad2user[i] < 0) return;
+    const size_t off = (size_t)node_ctl(m, st, i).par * m.Np + i;
+    const float4 hi = st.uh[off], lo = st.ul[off];
+    const float4 h0 = st.u0h[i], l0 = st.u0l[i];
+    const float dx = (hi.x - h0.x) + (lo.x - l0.x);
+    const float dy = (hi.y - h0.y) + (lo.y - l0.y);
+    const float dz = (hi.z - h0.z) + (lo.z - l0.z);
+    st.vold[i] = st.v[i];
+    st.v[i] = make_float4(__fdiv_rn(p.damping * dx, p.h), __fdiv_rn(p.damping * dy, p.h), __fdiv_rn(p.damping * dz, p.h),
+                          0.f);
+    st.u0h[i] = hi;
+    st.u0l[i] = lo;
+}
+
+// ------------------------------------------------------------ one pass
+// Energy terms of one free node: 1/2 m |u - u~|^2 / h^2 - g_y u_y - f_ext . u
+// (DescentOptimize.cpp:128-142 / CUDAInterface.cu:589-597), measured from the
+// rest shape so that no large constant rides along in the sum.
+__device__ __forceinline__ double node_energy(const DevState &st, const float4 &info, const float4 &uh,
+                                              const float4 &ul, int i, float h2inv) {
+    const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
+    const float dx = (uh.x - th.x) + (ul.x - tl.x);
+    const float dy = (uh.y - th.y) + (ul.y - tl.y);
+    const float dz = (uh.z - th.z) + (ul.z - tl.z);
+    const double uy = (double)uh.y + ul.y;
+    return 0.5 * (double)info.x * ((double)dx * dx + (double)dy * dy + (double)dz * dz) * (double)h2inv -
+           (double)info.y * uy - ((double)ex.x * ((double)uh.x + ul.x) + (double)ex.y * uy + (double)ex.z * ((double)uh.z + ul.z));
+}
+
+template <int MATERIAL>
+__global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState st) {
+    __shared__ double sh[BLOCK / 32];
+    __shared__ int is_last;
+    const int b = blockIdx.x;
+    InstCtl *cp = st.ctl + m.tblk_inst[b];
+    if (cp->done) return;
+    const int k = cp->k;
+    const bool check = (k % p.ls_every) == 0;
+    const bool do_h = (k % p.hd_every) == 0;
+    const size_t cur = (size_t)cp->par * m.Np;
+    const float4 *U = st.uh + cur;
+    const int t = b * BLOCK + threadIdx.x;
+    double e = 0.0;
+    const int4 q = m.tets[t];
+    if (q.x >= 0) {
+        const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+        const float svol = r0.w, mu = r1.w, lambda = r2.w;
+        Kin<float> kin;
+        disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
+        kinematics(kin);
+        float P[9];
+        if (MATERIAL == PBS_MATERIAL_STRETCH) pk1_stretch(kin, mu, lambda, P);
+        else pk1_neohookean<float>(kin, mu, lambda, P);
+        float f[12];
+        corner_forces(P, dinv, svol, f);
+        float4 *out = reinterpret_cast<float4 *>(st.tf + 12 * (size_t)t);
+        out[0] = make_float4(f[0], f[1], f[2], f[3]);
+        out[1] = make_float4(f[4], f[5], f[6], f[7]);
+        out[2] = make_float4(f[8], f[9], f[10], f[11]);
+        if (check) e = (double)clamp_energy(energy_density<float>(kin, mu, lambda) * fabsf(svol), p.clamp_cpu);
+        if (do_h) {
+            float kd[12];
+            hessian_diag(kin, mu, lambda, dinv, svol, kd);
+            float4 *ho = reinterpret_cast<float4 *>(st.hd + 12 * (size_t)t);
+            ho[0] = make_float4(kd[0], kd[1], kd[2], kd[3]);
+            ho[1] = make_float4(kd[4], kd[5], kd[6], kd[7]);
+            ho[2] = make_float4(kd[8], kd[9], kd[10], kd[11]);
+        }
+    }
+    if (!check) return;
+    // line-search pass: add this block's share of the instance's node terms
+    double e2 = e * e;
+    {
+        const int nb = cp->tblk_end - cp->tblk_begin;
+        for (int i = cp->node_begin + (b - cp->tblk_begin) * BLOCK + threadIdx.x; i < cp->node_end; i += nb * BLOCK) {
+            const float4 info = m.info[i];
+            if (info.z != 0.f) continue;
+            const double en = node_energy(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+            e += en;
+            e2 += en * en;
+        }
+    }
+    const double se = block_sum(e, sh);
+    const double se2 = block_sum(e2, sh);
+    if (threadIdx.x == 0) {
+        st.tpart[b] = make_double2(se, se2);
+        __threadfence();
+        const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
+        is_last = (prev == (unsigned int)(cp->tblk_end - cp->tblk_begin - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // the instance's last block: fixed-order sums, then accept / reject
+    double E = 0.0, E2 = 0.0;
+    for (int j = cp->tblk_begin + threadIdx.x; j < cp->tblk_end; j += BLOCK) {
+        const double2 v = __ldcg(st.tpart + j);
+        E += v.x;
+        E2 += v.y;
+    }
+    E = block_sum(E, sh);
+    E2 = block_sum(E2, sh);
+    if (threadIdx.x != 0) return;
+    InstCtl c = *cp;
+    c.counter_t = 0;
+    c.energy = E;
+    // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
+    // error of order 2^-24 sqrt(sum e_i^2); slack 0 is the reference's strict test
+    const double tau = (double)p.energy_slack * 5.9604644775390625e-8 * sqrt(E2);
+    if (k != 0 && E > c.energy_old + tau) {
+        c.action = ACT_RESTORE;
+        c.alpha = (float)((double)c.alpha * (double)p.alpha_shrink);
+        c.rejections += 1;
+        if (p.control == PBS_CONTROL_REFERENCE) c.iters -= k - p.ls_every;
+    } else {
+        c.action = ACT_SAVE_STEP;
+        c.energy_old = E;
+    }
+    if (!isfinite(E)) {
+        c.status = PBS_E_NONFINITE;
+        c.done = 1;
+    }
+    *cp = c;
+    if (c.done) atomicSub(st.active, 1);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState st) {
+    __shared__ double sh[BLOCK / 32];
+    __shared__ int is_last;
+    const int b = blockIdx.x;
+    InstCtl *cp = st.ctl + m.nblk_inst[b];
+    if (cp->done) return;
+    const int k = cp->k;
+    const bool check = (k % p.ls_every) == 0;
+    const int action = check ? cp->action : ACT_STEP;
+    const bool do_h = (k % p.hd_every) == 0;
+    const float alpha = cp->alpha;
+    float rho = cp->rho, omega = cp->omega;
+    chebyshev_schedule(p, k, rho, omega);
+    const size_t cur = (size_t)cp->par * m.Np, nxt = (size_t)(1 - cp->par) * m.Np;
+    const int i = b * BLOCK + threadIdx.x;
+    const float4 info = m.info[i];
+    double r2 = 0.0;
+    if (info.z != 2.f) {
+        const float4 uh = st.uh[cur + i], ul = st.ul[cur + i], dd = st.dd[cur + i];
+        float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (action == ACT_RESTORE) {
+            // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
+            // x_last = x_{k-1} = u - d (the reference does not restore it), or
+            // restarts it under PBS_CONTROL_RESTART
+            nh = st.oh[i];
+            nl = st.ol[i];
+            if (info.z == 0.f && p.control == PBS_CONTROL_REFERENCE)
+                nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
+                                 ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
+        } else {
+            if (action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:181)
+                st.oh[i] = uh;
+                st.ol[i] = ul;
+            }
+            if (info.z == 0.f) {
+                float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
+                const int a = m.inc_ptr[i], e_ = m.inc_ptr[i + 1];
+                for (int j = a; j < e_; ++j) {
+                    const int ent = m.inc[j];
+                    const size_t o = 12 * (size_t)(ent >> 2) + 3 * (ent & 3);
+                    fx += st.tf[o];
+                    fy += st.tf[o + 1];
+                    fz += st.tf[o + 2];
+                    if (do_h) {
+                        hx += st.hd[o];
+                        hy += st.hd[o + 1];
+                        hz += st.hd[o + 2];
+                    }
+                }
+                const float mh = info.x * p.h2inv;
+                float4 D;
+                if (do_h) {
+                    D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
+                    st.diag[i] = D;
+                } else {
+                    D = st.diag[i];
+                }
+                const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
+                const float gx = ((uh.x - th.x) + (ul.x - tl.x)) * mh - fx - p.body_scale * ex.x;
+                const float gy = ((uh.y - th.y) + (ul.y - tl.y)) * mh - fy - p.body_scale * (ex.y + info.y);
+                const float gz = ((uh.z - th.z) + (ul.z - tl.z)) * mh - fz - p.body_scale * ex.z;
+                r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
+                // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
+                // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
+                // d' = (omega - 1) d + omega delta
+                const float dx = alpha * (gx / -D.x), dy = alpha * (gy / -D.y), dz = alpha * (gz / -D.z);
+                if (omega != 1.0f)
+                    nd = make_float4((omega - 1.f) * dd.x + omega * dx, (omega - 1.f) * dd.y + omega * dy,
+                                     (omega - 1.f) * dd.z + omega * dz, 0.f);
+                else
+                    nd = make_float4(dx, dy, dz, 0.f);
+                add_comp(nh.x, nl.x, nd.x);
+                add_comp(nh.y, nl.y, nd.y);
+                add_comp(nh.z, nl.z, nd.z);
+            }
+        }
+        st.uh[nxt + i] = nh;
+        st.ul[nxt + i] = nl;
+        st.dd[nxt + i] = nd;
+    }
+    const double sr = block_sum(r2, sh);
+    if (threadIdx.x == 0) {
+        st.npart[b] = sr;
+        __threadfence();
+        const unsigned int prev = atomicAdd(&cp->counter_n, 1u);
+        is_last = (prev == (unsigned int)(cp->nblk_end - cp->nblk_begin - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double R2 = 0.0;
+    for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += BLOCK) R2 += __ldcg(st.npart + j);
+    R2 = block_sum(R2, sh);
+    if (threadIdx.x != 0) return;
+    InstCtl c = *cp;
+    c.counter_n = 0;
+    c.passes += 1;
+    if (action == ACT_RESTORE) {
+        c.par = 1 - c.par;  // the restored state; k is redone
+    } else {
+        const double r = sqrt(R2);
+        if (k == 0) c.g0 = r;
+        c.ratio = c.g0 > 0.0 ? r / c.g0 : 0.0;
+        if (p.tol > 0.f && k > 0 && r <= (double)p.tol * c.g0) {
+            c.converged = 1;  // keep x_k (the current parity)
+            c.done = 1;
+        } else {
+            c.rho = rho;
+            c.omega = omega;
+            c.par = 1 - c.par;
+            c.k = k + 1;
+        }
+        if (!isfinite(R2)) {
+            c.status = PBS_E_NONFINITE;
+            c.done = 1;
+        }
+    }
+    if (!c.done) {
+        if (c.k >= c.iters || c.alpha < p.alpha_min) c.done = 1;
+        else if (c.passes >= p.pass_cap) { c.done = 1; c.status = PBS_E_ITER_CAP; }
+    }
+    *cp = c;
+    if (c.done) atomicSub(st.active, 1);
+}
+
+// ------------------------------------------------------------ helpers
+// x = X + u (u as hi + lo)
+__global__ void k_pack_positions(DevMesh m, const float4 *uh, const float4 *ul, const int *pad2user, float *dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const int u = pad2user[i];
+    if (u < 0) return;
+    const float4 X = m.rest[i], h = uh[i], l = ul[i];
+    dst[3 * (size_t)u] = X.x + (h.x + l.x);
+    dst[3 * (size_t)u + 1] = X.y + (h.y + l.y);
+    dst[3 * (size_t)u + 2] = X.z + (h.z + l.z);
+}
+
+// u = x - X exactly as (hi, lo)
+__device__ __forceinline__ void split_disp(float x, float X, float &hi, float &lo) { two_sum(x, -X, hi, lo); }
+
+__global__ void k_unpack_positions(DevMesh m, const float *src, const int *pad2user, float4 *uh, float4 *ul) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const int u = pad2user[i];
+    if (u < 0) {
+        uh[i] = ul[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 X = m.rest[i];
+    float h[3], l[3];
+    split_disp(src[3 * (size_t)u], X.x, h[0], l[0]);
+    split_disp(src[3 * (size_t)u + 1], X.y, h[1], l[1]);
+    split_disp(src[3 * (size_t)u + 2], X.z, h[2], l[2]);
+    uh[i] = make_float4(h[0], h[1], h[2], 0.f);
+    ul[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
+__global__ void k_scatter_positions(DevMesh m, int count, const int *ids, const float *xyz, float4 *uh, float4 *ul) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= count) return;
+    const int i = ids[j];
+    const float4 X = m.rest[i];
+    float h[3], l[3];
+    split_disp(xyz[3 * (size_t)j], X.x, h[0], l[0]);
+    split_disp(xyz[3 * (size_t)j + 1], X.y, h[1], l[1]);
+    split_disp(xyz[3 * (size_t)j + 2], X.z, h[2], l[2]);
+    uh[i] = make_float4(h[0], h[1], h[2], 0.f);
+    ul[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
+__global__ void k_pack(int Np, const float4 *src, const int *pad2user, float *dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Np) return;
+    const int u = pad2user[i];
+    if (u < 0) return;
+    const float4 x = src[i];
+    dst[3 * (size_t)u] = x.x;
+    dst[3 * (size_t)u + 1] = x.y;
+    dst[3 * (size_t)u + 2] = x.z;
+}
+
+__global__ void k_unpack(int Np, const float *src, const int *pad2user, float4 *dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Np) return;
+    const int u = pad2user[i];
+    if (u < 0) {
+        dst[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    dst[i] = make_float4(src[3 * (size_t)u], src[3 * (size_t)u + 1], src[3 * (size_t)u + 2], 0.f);
+}
+
+template <int MATERIAL>
+__global__ void k_eval_tets(DevMesh m, const float4 *U, int clamp_cpu, float *tf, float *energy, float *hd) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.Tp) return;
+    const int4 q = m.tets[t];
+    float f[12] = {0}, kd[12] = {0}, e = 0.f;
+    if (q.x >= 0) {
+        const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+        Kin<float> kin;
+        disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
+        kinematics(kin);
+        float P[9];
+        if (MATERIAL == PBS_MATERIAL_STRETCH) pk1_stretch(kin, r1.w, r2.w, P);
+        else pk1_neohookean<float>(kin, r1.w, r2.w, P);
+        corner_forces(P, dinv, r0.w, f);
+        e = clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), clamp_cpu);
+        hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
+    }
+    for (int j = 0; j < 12; ++j) {
+        if (tf) tf[12 * (size_t)t + j] = f[j];
+        if (hd) hd[12 * (size_t)t + j] = kd[j];
+    }
+    if (energy) energy[t] = e;
+}
+
+__global__ void k_gather(DevMesh m, const float *tf, const float *hd, const int *pad2user, float *fo, float *ho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const int u = pad2user[i];
+    if (u < 0) return;
+    float s[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+        const int ent = m.inc[j];
+        const size_t o = 12 * (size_t)(ent >> 2) + 3 * (ent & 3);
+        for (int d = 0; d < 3; ++d) {
+            s[d] += tf[o + d];
+            s[3 + d] += hd[o + d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (fo) fo[3 * (size_t)u + d] = s[d];
+        if (ho) ho[3 * (size_t)u + d] = s[3 + d];
+    }
+}
+
+// ------------------------------------------------------------ launchers
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+cudaError_t launch_rest(cudaStream_t s, const DevMesh &m, const double *rest_pad, float density, float4 *row0,
+                        float4 *row1, float4 *row2, double *tmass, int *bad) {
+    k_rest<<<nblk(m.Tp, 128), 128, 0, s>>>(m, rest_pad, density, row0, row1, row2, tmass, bad);
+    return cudaGetLastError();
+}
+cudaError_t launch_mass(cudaStream_t s, const DevMesh &m, const double *tmass, const int *state, float gravity,
+                        float4 *info) {
+    k_mass<<<nblk(m.Np, 128), 128, 0, s>>>(m, tmass, state, gravity, info);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_lame(cudaStream_t s, int Tp, const int4 *, const float *mu, const float *lambda, int count,
+                            float4 *row1, float4 *row2, const int *tet_user) {
+    k_set_lame<<<nblk(Tp, 256), 256, 0, s>>>(Tp, mu, lambda, count, row1, row2, tet_user);
+    return cudaGetLastError();
+}
+cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, InstCtl *ctl, int *active) {
+    k_init_ctl<<<nblk(n_inst, 128), 128, 0, s>>>(n_inst, p, ctl, active);
+    return cudaGetLastError();
+}
+cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
+                            const int *pad2user) {
+    k_prologue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, ext_user, pad2user);
+    return cudaGetLastError();
+}
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
+    if (material == PBS_MATERIAL_STRETCH)
+        k_tet<PBS_MATERIAL_STRETCH><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
+    else
+        k_tet<PBS_MATERIAL_NEOHOOKEAN><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    k_node<<<m.n_nblk, BLOCK, 0, s>>>(m, p, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
+    cudaError_t e = launch_tet_only(s, m, p, st, material);
+    if (e != cudaSuccess) return e;
+    return launch_node_only(s, m, p, st);
+}
+cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user) {
+    k_epilogue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, pad2user);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack_positions(cudaStream_t s, const DevMesh &m, const float4 *uh, const float4 *ul,
+                                  const int *pad2user, float *dst_user) {
+    k_pack_positions<<<nblk(m.Np, 256), 256, 0, s>>>(m, uh, ul, pad2user, dst_user);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack_positions(cudaStream_t s, const DevMesh &m, const float *src_user, const int *pad2user,
+                                    float4 *uh, float4 *ul) {
+    k_unpack_positions<<<nblk(m.Np, 256), 256, 0, s>>>(m, src_user, pad2user, uh, ul);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack(cudaStream_t s, int Np, const float4 *src, const int *pad2user, float *dst_user) {
+    k_pack<<<nblk(Np, 256), 256, 0, s>>>(Np, src, pad2user, dst_user);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack(cudaStream_t s, int Np, const float *src_user, const int *pad2user, float4 *dst) {
+    k_unpack<<<nblk(Np, 256), 256, 0, s>>>(Np, src_user, pad2user, dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_scatter_positions(cudaStream_t s, const DevMesh &m, int count, const int *ids_pad,
+                                     const float *xyz, float4 *uh, float4 *ul) {
+    if (count <= 0) return cudaSuccess;
+    k_scatter_positions<<<nblk(count, 256), 256, 0, s>>>(m, count, ids_pad, xyz, uh, ul);
+    return cudaGetLastError();
+}
+cudaError_t launch_eval_tets(cudaStream_t s, const DevMesh &m, const float4 *uh, int material, int clamp_cpu,
+                             float *tf, float *energy, float *hd) {
+    if (material == PBS_MATERIAL_STRETCH)
+        k_eval_tets<PBS_MATERIAL_STRETCH><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, clamp_cpu, tf, energy, hd);
+    else
+        k_eval_tets<PBS_MATERIAL_NEOHOOKEAN><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, clamp_cpu, tf, energy, hd);
+    return cudaGetLastError();
+}
+cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, const float *hd, const int *pad2user,
+                          float *force_user, float *hd_user) {
+    k_gather<<<nblk(m.Np, 128), 128, 0, s>>>(m, tf, hd, pad2user, force_user, hd_user);
+    return cudaGetLastError();
+}
+
+}  // namespace pbs

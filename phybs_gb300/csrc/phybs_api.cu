@@ -1,0 +1,789 @@
+// Host side of the C ABI (include/phybs.h): mesh packing, device memory,
+// the graph-captured pass loop and parity/debug entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/phybs.h"
+#include "phybs_internal.cuh"
+
+using namespace pbs;
+
+namespace {
+
+constexpr int CHUNK_PASSES = 16;  // passes per captured graph launch
+
+template <typename T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        return cudaMalloc((void **)&p, std::max<size_t>(count, 1) * sizeof(T));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct pbs_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int N = 0, T = 0, B = 0, Np = 0, Tp = 0, n_tblk = 0, n_nblk = 0;
+    int material = PBS_MATERIAL_NEOHOOKEAN;
+    float density = 1000.f, gravity = 9.8f;
+    pbs_step_params params{};
+    DevParams dparams{};
+    std::vector<int> user2pad, h_pad2user, h_tet_user, h_node_state;
+    std::vector<float> h_rest;  // user layout, for reset
+
+    // device mesh
+    DevBuf<int4> tets;
+    DevBuf<float4> row0, row1, row2, info, rest4;
+    DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
+    // device state
+    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag;
+    DevBuf<float> tf, hd, staging, staging2;
+    DevBuf<double2> tpart;
+    DevBuf<double> npart;
+    DevBuf<InstCtl> ctl;
+    DevBuf<int> active;
+    // host pinned
+    int *h_active = nullptr;   // 2 slots
+    InstCtl *h_ctl = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_chunk[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    double last_ms = 0.0;
+    pbs_stats stats{};
+
+    DevMesh mesh() const {
+        DevMesh m;
+        m.Np = Np; m.Tp = Tp; m.n_inst = B; m.n_tblk = n_tblk; m.n_nblk = n_nblk;
+        m.tets = tets.p; m.row0 = row0.p; m.row1 = row1.p; m.row2 = row2.p;
+        m.inc_ptr = inc_ptr.p; m.inc = inc.p; m.info = info.p; m.rest = rest4.p;
+        m.tblk_inst = tblk_inst.p; m.nblk_inst = nblk_inst.p;
+        return m;
+    }
+    DevState state() const {
+        DevState s;
+        s.uh = uh.p; s.ul = ul.p; s.dd = dd.p; s.oh = oh.p; s.ol = ol.p; s.u0h = u0h.p; s.u0l = u0l.p;
+        s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
+        s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
+        return s;
+    }
+    void release() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        DevBuf<int4> *i4[] = {&tets};
+        for (auto b : i4) b->release();
+        DevBuf<float4> *f4[] = {&row0, &row1, &row2, &info, &rest4, &uh, &ul, &dd, &oh, &ol, &u0h, &u0l, &th, &tl,
+                                &v, &vold, &ext, &diag};
+        for (auto b : f4) b->release();
+        DevBuf<int> *ii[] = {&inc_ptr, &inc, &tblk_inst, &nblk_inst, &pad2user, &tet_user, &node_state, &bad, &active,
+                             &staging_ids};
+        for (auto b : ii) b->release();
+        tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
+        if (h_active) cudaFreeHost(h_active);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        h_active = nullptr; h_ctl = nullptr;
+        cudaEvent_t evs[] = {ev_start, ev_end, ev_chunk[0], ev_chunk[1]};
+        for (auto e : evs) if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+#define CK(x)                                                   \
+    do {                                                        \
+        cudaError_t e__ = (x);                                  \
+        if (e__ != cudaSuccess) {                               \
+            return e__ == cudaErrorMemoryAllocation ? PBS_E_OUT_OF_MEMORY : PBS_E_CUDA; \
+        }                                                       \
+    } while (0)
+
+static void to_dev_params(const pbs_step_params &p, DevParams &d) {
+    d.h = p.h;
+    d.h2inv = 1.0f / (p.h * p.h);
+    d.max_iters = p.max_iters;
+    d.tol = p.tol;
+    d.control = p.control;
+    d.alpha0 = p.alpha0; d.alpha_min = p.alpha_min; d.alpha_shrink = p.alpha_shrink;
+    d.ls_every = p.line_search_every; d.hd_every = p.hessian_every;
+    d.n_profile = p.n_profile;
+    for (int i = 0; i < 4; ++i) { d.profile_k[i] = p.profile_k[i]; d.profile_rho[i] = p.profile_rho[i]; }
+    d.damping = p.damping; d.warm_start = p.warm_start; d.body_scale = p.body_force_scale;
+    d.clamp_cpu = p.energy_clamp == PBS_CLAMP_CPU ? 1 : 0;
+    d.pass_cap = p.pass_cap > 0 ? p.pass_cap : p.max_iters + 16;
+    d.energy_slack = p.energy_slack;
+}
+
+extern "C" {
+
+void pbs_default_params(pbs_step_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->h = 0.03f;
+    p->max_iters = 96;
+    p->tol = 0.0f;
+    p->control = PBS_CONTROL_REFERENCE;
+    p->alpha0 = 0.1f; p->alpha_min = 0.01f; p->alpha_shrink = 0.7f;
+    p->line_search_every = 8;
+    p->hessian_every = 32;
+    p->n_profile = 3;
+    p->profile_k[0] = 1; p->profile_k[1] = 7; p->profile_k[2] = 10;
+    p->profile_rho[0] = 0.96f; p->profile_rho[1] = 0.991f; p->profile_rho[2] = 0.999f;
+    p->damping = 0.99f;
+    p->warm_start = 0.2f;
+    p->body_force_scale = 2.0f;
+    p->energy_clamp = PBS_CLAMP_CPU;
+    p->pass_cap = 0;
+    p->energy_slack = 0.0f;
+}
+
+const char *pbs_error_string(int code) {
+    switch (code) {
+        case PBS_OK: return "ok";
+        case PBS_E_INVALID_ARG: return "invalid argument";
+        case PBS_E_CUDA: return "CUDA error";
+        case PBS_E_NONFINITE: return "non-finite energy or residual";
+        case PBS_E_ITER_CAP: return "pass cap reached";
+        case PBS_E_BAD_MESH: return "bad mesh (index out of range, or non-positive rest volume)";
+        case PBS_E_NO_DEVICE: return "no compute capability 10.3 CUDA device";
+        case PBS_E_OUT_OF_MEMORY: return "out of device memory";
+        case PBS_E_CAPACITY: return "size beyond the fixed maximum";
+        default: return "unknown error";
+    }
+}
+
+void pbs_lame(float young, float poisson, int reference_formula, float *mu, float *lambda) {
+    float m = 0.5f * young / (1.0f + poisson);
+    float l = m * 2.0f / (1.0f - 2.0f * poisson);
+    if (!reference_formula) l *= poisson;
+    if (mu) *mu = m;
+    if (lambda) *lambda = l;
+}
+
+static int validate_params(const pbs_step_params *p) {
+    if (!p) return PBS_E_INVALID_ARG;
+    if (!(p->h > 0.f) || p->max_iters < 0 || p->line_search_every <= 0 || p->hessian_every <= 0 ||
+        p->n_profile < 0 || p->n_profile > 4 || !(p->alpha0 > 0.f) || !(p->alpha_shrink > 0.f) ||
+        p->alpha_shrink >= 1.f || (p->control != PBS_CONTROL_REFERENCE && p->control != PBS_CONTROL_RESTART) ||
+        p->tol < 0.f || p->pass_cap < 0 || !(p->energy_slack >= 0.f))
+        return PBS_E_INVALID_ARG;
+    return PBS_OK;
+}
+
+int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
+    if (!d || !out || d->n_nodes <= 0 || d->n_tets <= 0 || !d->rest || !d->tets || d->n_instances < 1 ||
+        !(d->density > 0.f))
+        return PBS_E_INVALID_ARG;
+    if (d->n_instances > 1 && (!d->instance_node_ptr || !d->instance_tet_ptr)) return PBS_E_INVALID_ARG;
+    *out = nullptr;
+    int dev = 0, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PBS_E_NO_DEVICE;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PBS_E_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return PBS_E_NO_DEVICE;
+    if (prop.major != 10 || prop.minor != 3) return PBS_E_NO_DEVICE;
+
+    const int N = d->n_nodes, T = d->n_tets, B = d->n_instances;
+    std::vector<int> nptr(B + 1), tptr(B + 1);
+    if (B == 1) { nptr = {0, N}; tptr = {0, T}; }
+    else {
+        std::memcpy(nptr.data(), d->instance_node_ptr, sizeof(int) * (B + 1));
+        std::memcpy(tptr.data(), d->instance_tet_ptr, sizeof(int) * (B + 1));
+    }
+    if (nptr[0] != 0 || tptr[0] != 0 || nptr[B] != N || tptr[B] != T) return PBS_E_INVALID_ARG;
+    for (int b = 0; b < B; ++b)
+        if (nptr[b + 1] < nptr[b] || tptr[b + 1] < tptr[b]) return PBS_E_INVALID_ARG;
+
+    pbs_handle *h = new (std::nothrow) pbs_handle();
+    if (!h) return PBS_E_OUT_OF_MEMORY;
+    h->device = dev;
+    h->N = N; h->T = T; h->B = B;
+    h->density = d->density; h->gravity = d->gravity;
+    pbs_default_params(&h->params);
+    to_dev_params(h->params, h->dparams);
+
+    // ---- packing: each instance starts on a PAD boundary
+    std::vector<InstCtl> ctl(B);
+    int pn = 0, pt = 0;
+    h->user2pad.assign(N, -1);
+    std::vector<int> node_off(B), tet_off(B);
+    for (int b = 0; b < B; ++b) {
+        node_off[b] = pn; tet_off[b] = pt;
+        int nn = nptr[b + 1] - nptr[b], nt = tptr[b + 1] - tptr[b];
+        std::memset(&ctl[b], 0, sizeof(InstCtl));
+        ctl[b].node_begin = pn; ctl[b].node_end = pn + nn;
+        ctl[b].tet_begin = pt; ctl[b].tet_end = pt + nt;
+        ctl[b].nblk_begin = pn / BLOCK; ctl[b].tblk_begin = pt / BLOCK;
+        pn += round_up(std::max(nn, 1), PAD);
+        pt += round_up(std::max(nt, 1), PAD);
+        ctl[b].nblk_end = pn / BLOCK; ctl[b].tblk_end = pt / BLOCK;
+        ctl[b].rho = 0.f; ctl[b].omega = 1.f; ctl[b].alpha = h->params.alpha0;
+        for (int i = nptr[b]; i < nptr[b + 1]; ++i) h->user2pad[i] = node_off[b] + (i - nptr[b]);
+    }
+    const int Np = pn, Tp = pt;
+    h->Np = Np; h->Tp = Tp; h->n_tblk = Tp / BLOCK; h->n_nblk = Np / BLOCK;
+    h->h_pad2user.assign(Np, -1);
+    for (int i = 0; i < N; ++i) h->h_pad2user[h->user2pad[i]] = i;
+    h->h_tet_user.assign(Tp, -1);
+    std::vector<int4> tets_pad(Tp, make_int4(-1, -1, -1, -1));
+    std::vector<int> tblk(h->n_tblk), nblk(h->n_nblk);
+    for (int b = 0; b < B; ++b) {
+        for (int j = ctl[b].tblk_begin; j < ctl[b].tblk_end; ++j) tblk[j] = b;
+        for (int j = ctl[b].nblk_begin; j < ctl[b].nblk_end; ++j) nblk[j] = b;
+        for (int t = tptr[b]; t < tptr[b + 1]; ++t) {
+            int tp = tet_off[b] + (t - tptr[b]);
+            h->h_tet_user[tp] = t;
+            int id[4];
+            for (int c = 0; c < 4; ++c) {
+                int u = d->tets[4 * (size_t)t + c];
+                if (u < nptr[b] || u >= nptr[b + 1]) { delete h; return PBS_E_BAD_MESH; }
+                id[c] = h->user2pad[u];
+            }
+            tets_pad[tp] = make_int4(id[0], id[1], id[2], id[3]);
+        }
+    }
+    // ---- canonical node -> (tet, corner) gather (ascending tet, then corner)
+    std::vector<int> iptr(Np + 1, 0), ient(4 * (size_t)T);
+    for (int tp = 0; tp < Tp; ++tp) {
+        if (tets_pad[tp].x < 0) continue;
+        const int *q = &tets_pad[tp].x;
+        for (int c = 0; c < 4; ++c) iptr[q[c] + 1]++;
+    }
+    for (int i = 0; i < Np; ++i) iptr[i + 1] += iptr[i];
+    {
+        std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+        for (int tp = 0; tp < Tp; ++tp) {
+            if (tets_pad[tp].x < 0) continue;
+            const int *q = &tets_pad[tp].x;
+            for (int c = 0; c < 4; ++c) ient[fill[q[c]]++] = 4 * tp + c;
+        }
+    }
+    h->h_node_state.assign(Np, 2);
+    for (int i = 0; i < N; ++i) h->h_node_state[h->user2pad[i]] = (d->pin_mask && d->pin_mask[i] > 0) ? 1 : 0;
+    std::vector<double> rest_pad(3 * (size_t)Np, 0.0);
+    std::vector<float4> rest4(Np, make_float4(0.f, 0.f, 0.f, 0.f));
+    const float *p0 = d->positions ? d->positions : d->rest;
+    for (int i = 0; i < N; ++i) {
+        int ip = h->user2pad[i];
+        for (int k = 0; k < 3; ++k) {
+            float r = d->rest[3 * (size_t)i + k];
+            if (!std::isfinite(r) || !std::isfinite(p0[3 * (size_t)i + k])) { delete h; return PBS_E_INVALID_ARG; }
+            rest_pad[3 * (size_t)ip + k] = r;
+        }
+        rest4[ip] = make_float4(d->rest[3 * (size_t)i], d->rest[3 * (size_t)i + 1], d->rest[3 * (size_t)i + 2], 0.f);
+    }
+    h->h_rest.assign(d->rest, d->rest + 3 * (size_t)N);
+
+    auto fail = [&](int code) { h->release(); delete h; return code; };
+#define CKC(x) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) return fail(e__ == cudaErrorMemoryAllocation ? PBS_E_OUT_OF_MEMORY : PBS_E_CUDA); } while (0)
+    CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CKC(cudaEventCreate(&h->ev_start));
+    CKC(cudaEventCreate(&h->ev_end));
+    CKC(cudaEventCreateWithFlags(&h->ev_chunk[0], cudaEventDisableTiming));
+    CKC(cudaEventCreateWithFlags(&h->ev_chunk[1], cudaEventDisableTiming));
+    CKC(cudaMallocHost((void **)&h->h_active, 2 * sizeof(int)));
+    CKC(cudaMallocHost((void **)&h->h_ctl, B * sizeof(InstCtl)));
+    CKC(h->tets.alloc(Tp)); CKC(h->row0.alloc(Tp)); CKC(h->row1.alloc(Tp)); CKC(h->row2.alloc(Tp));
+    CKC(h->info.alloc(Np)); CKC(h->inc_ptr.alloc(Np + 1)); CKC(h->inc.alloc(4 * (size_t)T));
+    CKC(h->tblk_inst.alloc(h->n_tblk)); CKC(h->nblk_inst.alloc(h->n_nblk));
+    CKC(h->pad2user.alloc(Np)); CKC(h->tet_user.alloc(Tp)); CKC(h->node_state.alloc(Np)); CKC(h->bad.alloc(1));
+    CKC(h->uh.alloc(2 * (size_t)Np)); CKC(h->ul.alloc(2 * (size_t)Np)); CKC(h->dd.alloc(2 * (size_t)Np));
+    CKC(h->oh.alloc(Np)); CKC(h->ol.alloc(Np)); CKC(h->u0h.alloc(Np)); CKC(h->u0l.alloc(Np));
+    CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
+    CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
+    CKC(h->tf.alloc(12 * (size_t)Tp)); CKC(h->hd.alloc(12 * (size_t)Tp));
+    CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
+    CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
+    CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
+    cudaStream_t s = h->stream;
+    CKC(cudaMemcpyAsync(h->tets.p, tets_pad.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->inc_ptr.p, iptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->inc.p, ient.data(), sizeof(int) * 4 * (size_t)T, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->tblk_inst.p, tblk.data(), sizeof(int) * h->n_tblk, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->nblk_inst.p, nblk.data(), sizeof(int) * h->n_nblk, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->pad2user.p, h->h_pad2user.data(), sizeof(int) * Np, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->tet_user.p, h->h_tet_user.data(), sizeof(int) * Tp, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->node_state.p, h->h_node_state.data(), sizeof(int) * Np, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->ctl.p, ctl.data(), sizeof(InstCtl) * B, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->rest4.p, rest4.data(), sizeof(float4) * Np, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemsetAsync(h->v.p, 0, sizeof(float4) * Np, s));
+    CKC(cudaMemsetAsync(h->vold.p, 0, sizeof(float4) * Np, s));
+    CKC(cudaMemsetAsync(h->diag.p, 0, sizeof(float4) * Np, s));
+    CKC(cudaMemsetAsync(h->ext.p, 0, sizeof(float4) * Np, s));
+    CKC(cudaMemsetAsync(h->tf.p, 0, sizeof(float) * 12 * (size_t)Tp, s));
+    CKC(cudaMemsetAsync(h->hd.p, 0, sizeof(float) * 12 * (size_t)Tp, s));
+    {
+        DevBuf<float4> *zero[] = {&h->uh, &h->ul, &h->dd};
+        for (auto b : zero) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * 2 * (size_t)Np, s));
+        DevBuf<float4> *zero1[] = {&h->oh, &h->ol, &h->u0h, &h->u0l, &h->th, &h->tl};
+        for (auto b : zero1) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * (size_t)Np, s));
+    }
+    CKC(cudaMemsetAsync(h->bad.p, 0, sizeof(int), s));
+    {
+        // FP64 rest state on the device
+        DevBuf<double> rest_d, tmass;
+        CKC(rest_d.alloc(3 * (size_t)Np));
+        if (tmass.alloc(Tp) != cudaSuccess) { rest_d.release(); return fail(PBS_E_OUT_OF_MEMORY); }
+        cudaError_t e = cudaMemcpyAsync(rest_d.p, rest_pad.data(), sizeof(double) * 3 * (size_t)Np, cudaMemcpyHostToDevice, s);
+        DevMesh m = h->mesh();
+        if (e == cudaSuccess) e = launch_rest(s, m, rest_d.p, h->density, h->row0.p, h->row1.p, h->row2.p, tmass.p, h->bad.p);
+        if (e == cudaSuccess) e = launch_mass(s, m, tmass.p, h->node_state.p, h->gravity, h->info.p);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        rest_d.release();
+        tmass.release();
+        CKC(e);
+    }
+    int bad = 0;
+    CKC(cudaMemcpy(&bad, h->bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) return fail(PBS_E_BAD_MESH);
+    if (d->positions) {
+        CKC(cudaMemcpyAsync(h->staging.p, d->positions, sizeof(float) * 3 * (size_t)N, cudaMemcpyHostToDevice, s));
+        CKC(launch_unpack_positions(s, h->mesh(), h->staging.p, h->pad2user.p, h->u0h.p, h->u0l.p));
+        CKC(cudaStreamSynchronize(s));
+    }
+    // default material: TetMesh.cpp:185 (E = 5e5, nu = 0.45), the reference's Lame formula
+    float mu, lam;
+    pbs_lame(5e5f, 0.45f, 1, &mu, &lam);
+    int rc = pbs_set_material(h, PBS_MATERIAL_NEOHOOKEAN, &mu, &lam, 1);
+    if (rc != PBS_OK) return fail(rc);
+    CKC(cudaStreamSynchronize(s));
+    *out = h;
+    return PBS_OK;
+#undef CKC
+}
+
+void pbs_destroy(pbs_handle *h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->release();
+    delete h;
+}
+
+int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lambda, int count) {
+    if (!h || !mu || !lambda || (count != 1 && count != h->T)) return PBS_E_INVALID_ARG;
+    if (model != PBS_MATERIAL_NEOHOOKEAN && model != PBS_MATERIAL_STRETCH) return PBS_E_INVALID_ARG;
+    for (int i = 0; i < count; ++i)
+        if (!std::isfinite(mu[i]) || !std::isfinite(lambda[i])) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    // stage mu and lambda through the (3N-float) staging buffer's neighbour
+    DevBuf<float> buf;
+    CK(buf.alloc(2 * (size_t)count));
+    cudaError_t e = cudaMemcpyAsync(buf.p, mu, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf.p + count, lambda, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = launch_set_lame(h->stream, h->Tp, h->tets.p, buf.p, buf.p + count, count, h->row1.p, h->row2.p, h->tet_user.p);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    buf.release();
+    CK(e);
+    if (h->material != model) h->graph_valid = false;
+    h->material = model;
+    return PBS_OK;
+}
+
+int pbs_set_params(pbs_handle *h, const pbs_step_params *p) {
+    if (!h) return PBS_E_INVALID_ARG;
+    int rc = validate_params(p);
+    if (rc != PBS_OK) return rc;
+    h->params = *p;
+    to_dev_params(h->params, h->dparams);
+    h->graph_valid = false;
+    return PBS_OK;
+}
+
+int pbs_get_params(pbs_handle *h, pbs_step_params *p) {
+    if (!h || !p) return PBS_E_INVALID_ARG;
+    *p = h->params;
+    return PBS_OK;
+}
+
+static int ensure_graph(pbs_handle *h) {
+    if (h->graph_valid) return PBS_OK;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    DevMesh m = h->mesh();
+    DevState st = h->state();
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < CHUNK_PASSES && e == cudaSuccess; ++i) e = launch_pass(h->stream, m, h->dparams, st, h->material);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return PBS_E_CUDA; }
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    h->graph_valid = true;
+    return PBS_OK;
+}
+
+int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_graph(h);
+    if (rc != PBS_OK) return rc;
+    cudaStream_t s = h->stream;
+    DevMesh m = h->mesh();
+    DevState st = h->state();
+    CK(cudaEventRecord(h->ev_start, s));
+    if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
+    CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
+    CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
+    // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
+    // of chunk j-1 while chunk j runs, so the device never idles on the poll.
+    const int max_chunks = (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES;
+    int launched = 0;
+    for (int j = 0; j < max_chunks; ++j) {
+        ++launched;
+        CK(cudaGraphLaunch(h->graph, s));
+        CK(cudaMemcpyAsync(h->h_active + (j & 1), h->active.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(h->ev_chunk[j & 1], s));
+        if (j >= 1) {
+            CK(cudaEventSynchronize(h->ev_chunk[(j - 1) & 1]));
+            if (h->h_active[(j - 1) & 1] == 0) break;
+        }
+    }
+    CK(launch_epilogue(s, m, h->dparams, st, h->pad2user.p));
+    CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(InstCtl) * h->B, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(h->ev_end, s));
+    CK(cudaMemsetAsync(h->ext.p, 0, sizeof(float4) * h->Np, s));  // fvm.cpp:188 resetExternalForce
+    CK(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev_start, h->ev_end);
+    h->last_ms = ms;
+    pbs_stats S{};
+    S.status = PBS_OK;
+    for (int b = 0; b < h->B; ++b) {
+        const InstCtl &c = h->h_ctl[b];
+        S.passes = std::max(S.passes, c.passes);
+        S.iterations = std::max(S.iterations, c.k);
+        S.rejections += c.rejections;
+        S.converged += c.converged;
+        if (c.status != PBS_OK && S.status == PBS_OK) S.status = c.status;
+        if (c.status == PBS_E_NONFINITE) S.status = PBS_E_NONFINITE;
+    }
+    S.alpha = h->h_ctl[0].alpha;
+    S.rho = h->h_ctl[0].rho;
+    S.omega = h->h_ctl[0].omega;
+    S.energy = h->h_ctl[0].energy;
+    S.residual_ratio = h->h_ctl[0].ratio;
+    S.device_ms = ms;
+    S.graph_launches = launched;
+    h->stats = S;
+    if (iters_out) *iters_out = S.iterations;
+    return S.status;
+}
+
+int pbs_read_positions(pbs_handle *h, float *out) {
+    if (!h || !out) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(launch_pack_positions(h->stream, h->mesh(), h->u0h.p, h->u0l.p, h->pad2user.p, h->staging.p));
+    CK(cudaMemcpyAsync(out, h->staging.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+static int upload_user(pbs_handle *h, const float *src, float4 *dst) {
+    for (size_t i = 0; i < 3 * (size_t)h->N; ++i)
+        if (!std::isfinite(src[i])) return PBS_E_INVALID_ARG;
+    CK(cudaMemcpyAsync(h->staging.p, src, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_unpack(h->stream, h->Np, h->staging.p, h->pad2user.p, dst));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+static int download_user(pbs_handle *h, const float4 *src, float *dst) {
+    CK(launch_pack(h->stream, h->Np, src, h->pad2user.p, h->staging.p));
+    CK(cudaMemcpyAsync(dst, h->staging.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+static int upload_positions(pbs_handle *h, const float *positions, float4 *hi, float4 *lo) {
+    for (size_t i = 0; i < 3 * (size_t)h->N; ++i)
+        if (!std::isfinite(positions[i])) return PBS_E_INVALID_ARG;
+    CK(cudaMemcpyAsync(h->staging.p, positions, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_unpack_positions(h->stream, h->mesh(), h->staging.p, h->pad2user.p, hi, lo));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+int pbs_update_positions(pbs_handle *h, const float *positions) {
+    if (!h || !positions) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    return upload_positions(h, positions, h->u0h.p, h->u0l.p);
+}
+
+int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float *xyz) {
+    if (!h || count < 0 || count > h->N || (count > 0 && (!ids || !xyz))) return PBS_E_INVALID_ARG;
+    if (count == 0) return PBS_OK;
+    CK(cudaSetDevice(h->device));
+    std::vector<int> pad(count);
+    for (int i = 0; i < count; ++i) {
+        if (ids[i] < 0 || ids[i] >= h->N) return PBS_E_INVALID_ARG;
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(xyz[3 * (size_t)i + k])) return PBS_E_INVALID_ARG;
+        pad[i] = h->user2pad[ids[i]];
+    }
+    CK(cudaMemcpyAsync(h->staging_ids.p, pad.data(), sizeof(int) * count, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->staging.p, xyz, sizeof(float) * 3 * (size_t)count, cudaMemcpyHostToDevice, h->stream));
+    CK(launch_scatter_positions(h->stream, h->mesh(), count, h->staging_ids.p, h->staging.p, h->u0h.p, h->u0l.p));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+int pbs_get_stream(pbs_handle *h, void **stream) {
+    if (!h || !stream) return PBS_E_INVALID_ARG;
+    *stream = (void *)h->stream;
+    return PBS_OK;
+}
+
+int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
+    if (!h || passes <= 0 || !tet_ms || !node_ms) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    DevParams p = h->dparams;
+    p.max_iters = passes + 1;
+    p.tol = 0.f;
+    p.pass_cap = passes + 1;
+    DevMesh m = h->mesh();
+    DevState st = h->state();
+    std::vector<cudaEvent_t> ev(2 * passes + 1, nullptr);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
+    if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+    for (int i = 0; i < passes && e == cudaSuccess; ++i) {
+        e = launch_tet_only(s, m, p, st, h->material);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 1], s);
+        if (e == cudaSuccess) e = launch_node_only(s, m, p, st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 2], s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    double tt = 0.0, tn = 0.0;
+    for (int i = 0; i < passes && e == cudaSuccess; ++i) {
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, ev[2 * i], ev[2 * i + 1]);
+        cudaEventElapsedTime(&b, ev[2 * i + 1], ev[2 * i + 2]);
+        tt += a;
+        tn += b;
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    CK(e);
+    *tet_ms = tt / passes;
+    *node_ms = tn / passes;
+    return PBS_OK;
+}
+
+int pbs_read_velocities(pbs_handle *h, float *v, float *v_old) {
+    if (!h || (!v && !v_old)) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = PBS_OK;
+    if (v) rc = download_user(h, h->v.p, v);
+    if (rc == PBS_OK && v_old) rc = download_user(h, h->vold.p, v_old);
+    return rc;
+}
+
+int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old) {
+    if (!h || (!v && !v_old)) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = PBS_OK;
+    if (v) rc = upload_user(h, v, h->v.p);
+    if (rc == PBS_OK && v_old) rc = upload_user(h, v_old, h->vold.p);
+    return rc;
+}
+
+int pbs_reset(pbs_handle *h) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemsetAsync(h->u0h.p, 0, sizeof(float4) * h->Np, h->stream));
+    CK(cudaMemsetAsync(h->u0l.p, 0, sizeof(float4) * h->Np, h->stream));
+    CK(cudaMemsetAsync(h->v.p, 0, sizeof(float4) * h->Np, h->stream));
+    CK(cudaMemsetAsync(h->vold.p, 0, sizeof(float4) * h->Np, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return PBS_OK;
+}
+
+int pbs_get_stats(pbs_handle *h, pbs_stats *s) {
+    if (!h || !s) return PBS_E_INVALID_ARG;
+    *s = h->stats;
+    return PBS_OK;
+}
+
+int pbs_get_sizes(pbs_handle *h, int *n_nodes, int *n_tets, int *n_instances) {
+    if (!h) return PBS_E_INVALID_ARG;
+    if (n_nodes) *n_nodes = h->N;
+    if (n_tets) *n_tets = h->T;
+    if (n_instances) *n_instances = h->B;
+    return PBS_OK;
+}
+
+int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {
+    if (!h || !row_ptr || !entries) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    std::vector<int> iptr(h->Np + 1), ient(4 * (size_t)h->T);
+    CK(cudaMemcpy(iptr.data(), h->inc_ptr.p, sizeof(int) * (h->Np + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ient.data(), h->inc.p, sizeof(int) * 4 * (size_t)h->T, cudaMemcpyDeviceToHost));
+    // translate padded ids back to the caller's numbering
+    row_ptr[0] = 0;
+    size_t w = 0;
+    for (int u = 0; u < h->N; ++u) {
+        int ip = h->user2pad[u];
+        for (int j = iptr[ip]; j < iptr[ip + 1]; ++j) {
+            int tp = ient[j] >> 2, c = ient[j] & 3;
+            entries[w++] = 4 * h->h_tet_user[tp] + c;
+        }
+        row_ptr[u + 1] = (int)w;
+    }
+    return PBS_OK;
+}
+
+int pbs_get_rest_data(pbs_handle *h, float *dm_inv9, float *signed_vol, float *mass, float *grav_y) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    std::vector<float4> r0(h->Tp), r1(h->Tp), r2(h->Tp), inf(h->Np);
+    CK(cudaMemcpy(r0.data(), h->row0.p, sizeof(float4) * h->Tp, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(r1.data(), h->row1.p, sizeof(float4) * h->Tp, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(r2.data(), h->row2.p, sizeof(float4) * h->Tp, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(inf.data(), h->info.p, sizeof(float4) * h->Np, cudaMemcpyDeviceToHost));
+    for (int tp = 0; tp < h->Tp; ++tp) {
+        int t = h->h_tet_user[tp];
+        if (t < 0) continue;
+        if (dm_inv9) {
+            float *o = dm_inv9 + 9 * (size_t)t;
+            o[0] = r0[tp].x; o[1] = r0[tp].y; o[2] = r0[tp].z;
+            o[3] = r1[tp].x; o[4] = r1[tp].y; o[5] = r1[tp].z;
+            o[6] = r2[tp].x; o[7] = r2[tp].y; o[8] = r2[tp].z;
+        }
+        if (signed_vol) signed_vol[t] = r0[tp].w;
+    }
+    for (int u = 0; u < h->N; ++u) {
+        int ip = h->user2pad[u];
+        if (mass) mass[u] = inf[ip].x;
+        if (grav_y) grav_y[u] = inf[ip].y;
+    }
+    return PBS_OK;
+}
+
+// The saved-state buffers are rewritten at iteration 0 of every step, so
+// between steps they serve as scratch for evaluating given positions.
+static int eval_common(pbs_handle *h, const float *positions, const float4 **xsrc) {
+    if (positions) {
+        int rc = upload_positions(h, positions, h->oh.p, h->ol.p);
+        if (rc != PBS_OK) return rc;
+        *xsrc = h->oh.p;
+    } else {
+        *xsrc = h->u0h.p;
+    }
+    return PBS_OK;
+}
+
+int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, float *energy, float *hess_diag) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    const float4 *x;
+    int rc = eval_common(h, positions, &x);
+    if (rc != PBS_OK) return rc;
+    // per-tet outputs land in tf / hd / staging2 (padded order), then are
+    // compacted into the caller's tet order on the host
+    CK(launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, h->staging2.p, h->hd.p));
+    std::vector<float> tf(12 * (size_t)h->Tp), hd(12 * (size_t)h->Tp), en(h->Tp);
+    CK(cudaMemcpyAsync(tf.data(), h->tf.p, sizeof(float) * tf.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(hd.data(), h->hd.p, sizeof(float) * hd.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(en.data(), h->staging2.p, sizeof(float) * en.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int tp = 0; tp < h->Tp; ++tp) {
+        int t = h->h_tet_user[tp];
+        if (t < 0) continue;
+        if (corner_forces) std::memcpy(corner_forces + 12 * (size_t)t, &tf[12 * (size_t)tp], 12 * sizeof(float));
+        if (hess_diag) std::memcpy(hess_diag + 12 * (size_t)t, &hd[12 * (size_t)tp], 12 * sizeof(float));
+        if (energy) energy[t] = en[tp];
+    }
+    return PBS_OK;
+}
+
+int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    const float4 *x;
+    int rc = eval_common(h, positions, &x);
+    if (rc != PBS_OK) return rc;
+    DevBuf<float> out;
+    CK(out.alloc(6 * (size_t)h->N));
+    cudaError_t e = launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, nullptr, h->hd.p);
+    if (e == cudaSuccess) e = launch_gather(h->stream, h->mesh(), h->tf.p, h->hd.p, h->pad2user.p, out.p, out.p + 3 * (size_t)h->N);
+    if (e == cudaSuccess && forces) e = cudaMemcpyAsync(forces, out.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && hess_diag) e = cudaMemcpyAsync(hess_diag, out.p + 3 * (size_t)h->N, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    out.release();
+    CK(e);
+    return PBS_OK;
+}
+
+// IsotropicMaterial::allocateGlobalStiffnessMatrix (IsotropicMaterial.cpp:554-644):
+// rows 3n+d hold the sorted columns 3m+e of every node m sharing a tet with n.
+int pbs_stiffness_pattern(int n_nodes, int n_tets, const int *tets, int *nnz, int *row_ptr, int *col, int *diag_idx,
+                          int *kid48) {
+    if (n_nodes <= 0 || n_tets < 0 || !tets || !nnz) return PBS_E_INVALID_ARG;
+    std::vector<int64_t> pairs;
+    pairs.reserve(16 * (size_t)n_tets);
+    for (int t = 0; t < n_tets; ++t)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) {
+                int na = tets[4 * (size_t)t + a], nb = tets[4 * (size_t)t + b];
+                if (na < 0 || na >= n_nodes || nb < 0 || nb >= n_nodes) return PBS_E_BAD_MESH;
+                pairs.push_back(((int64_t)na << 32) | (uint32_t)nb);
+            }
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    std::vector<int> nptr(n_nodes + 1, 0);
+    for (int64_t pr : pairs) nptr[(pr >> 32) + 1]++;
+    for (int i = 0; i < n_nodes; ++i) nptr[i + 1] += nptr[i];
+    const int64_t total = 9 * (int64_t)pairs.size();
+    if (total > INT32_MAX) return PBS_E_CAPACITY;
+    *nnz = (int)total;
+    if (!col) return PBS_OK;
+    if (!row_ptr) return PBS_E_INVALID_ARG;
+    row_ptr[0] = 0;
+    for (int n = 0; n < n_nodes; ++n) {
+        int deg = nptr[n + 1] - nptr[n];
+        for (int d = 0; d < 3; ++d) {
+            int r = 3 * n + d;
+            int start = 9 * nptr[n] + d * 3 * deg;
+            row_ptr[r + 1] = start + 3 * deg;
+            for (int j = 0; j < deg; ++j) {
+                int m = (int)(pairs[nptr[n] + j] & 0xffffffff);
+                for (int e = 0; e < 3; ++e) col[start + 3 * j + e] = 3 * m + e;
+            }
+        }
+    }
+    auto slot = [&](int r, int c) {
+        const int *b = col + row_ptr[r], *e = col + row_ptr[r + 1];
+        return (int)(std::lower_bound(b, e, c) - col);
+    };
+    if (diag_idx)
+        for (int r = 0; r < 3 * n_nodes; ++r) diag_idx[r] = slot(r, r);
+    if (kid48)
+        for (int t = 0; t < n_tets; ++t)
+            for (int fi = 0; fi < 4; ++fi)
+                for (int fj = 0; fj < 3; ++fj) {
+                    int gki = 3 * tets[4 * (size_t)t + fi] + fj;
+                    for (int ni = 0; ni < 4; ++ni) kid48[48 * (size_t)t + (fi * 3 + fj) * 4 + ni] = slot(gki, 3 * tets[4 * (size_t)t + ni]);
+                }
+    return PBS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// Internal device layout of a descent-step handle.
+//
+// HBM layout (Np / Tp = node / tet counts padded so that every instance starts
+// on a PAD boundary and every 256-wide block belongs to one instance):
+//   tets        int4[Tp]           padded node ids of the 4 corners
+//   row0..2     float4[Tp] each    rows of Dm^-1; .w = {det Dm/6, mu, lambda}
+//   uh, ul      float4[2][Np]      displacement u = x - X as an FP32 (hi, lo)
+//                                  pair, ping-ponged between passes
+//   dd          float4[2][Np]      last step d = u_k - u_{k-1} (Chebyshev history)
+//   oh, ol      float4[Np]         displacement saved at the last accepted
+//                                  line-search check (the reference's x_old)
+//   u0h, u0l    float4[Np]         displacement at the start of the step
+//   th, tl      float4[Np]         inertial target x~ - X (hi, lo)
+//   v, vold     float4[Np]         velocities of this and the previous step
+//   ext, diag   float4[Np]         external force; Jacobi diagonal + M/h^2
+//   info        float4[Np]         {effective mass (pins 1e8), gravity_y,
+//                                   state 0 free / 1 pinned / 2 padding, lumped mass}
+//   rest        float4[Np]         rest positions X
+//   inc_ptr     int[Np+1], inc int[4T]   node -> 4*tet+corner gather, canonical order
+//   tf, hd      float[12*Tp]       per-tet corner forces / Jacobi-diagonal terms
+//   tpart       double2[n_tblk]    per tet-block {sum e, sum e^2} of the energy
+//   npart       double[n_nblk]     per node-block |g|^2
+//   ctl         InstCtl[n_inst]    per-instance descent state
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pbs {
+
+constexpr int PAD = 256;    // instance alignment (tets and nodes)
+constexpr int BLOCK = 256;  // threads per block of the step kernels
+
+// Step parameters as the kernels see them (a by-value kernel argument).
+struct DevParams {
+    float h, h2inv;
+    int max_iters;
+    float tol;
+    int control;
+    float alpha0, alpha_min, alpha_shrink;
+    int ls_every, hd_every;
+    int n_profile;
+    int profile_k[4];
+    float profile_rho[4];
+    float damping, warm_start, body_scale;
+    int clamp_cpu;
+    int pass_cap;
+    float energy_slack;  // reject only if E > E_old + slack * 2^-24 * sqrt(sum e^2)
+};
+
+// What the node kernel does in a pass (decided by the tet kernel's last block
+// on line-search passes).
+enum PassAction : int { ACT_STEP = 0, ACT_SAVE_STEP = 1, ACT_RESTORE = 2 };
+
+// Per-instance descent state.
+struct __align__(16) InstCtl {
+    int k, iters, done, passes;
+    int rejections, converged, status, par;
+    int action, pad0;
+    unsigned int counter_t, counter_n;
+    float alpha, rho, omega, pad1;
+    double energy, energy_old, g0, ratio;
+    // static ranges (padded indices)
+    int node_begin, node_end, tet_begin, tet_end;
+    int tblk_begin, tblk_end, nblk_begin, nblk_end;
+};
+
+struct DevMesh {
+    int Np, Tp, n_inst;
+    int n_tblk, n_nblk;
+    const int4 *tets;
+    const float4 *row0, *row1, *row2;
+    const int *inc_ptr, *inc;
+    const float4 *info, *rest;
+    const int *tblk_inst, *nblk_inst;
+};
+
+struct DevState {
+    float4 *uh, *ul, *dd;  // [2][Np] each
+    float4 *oh, *ol, *u0h, *u0l, *th, *tl;
+    float4 *v, *vold, *ext, *diag;
+    float *tf, *hd;
+    double2 *tpart;
+    double *npart;
+    InstCtl *ctl;
+    int *active;  // instances not yet done
+};
+
+// Chebyshev omega for iteration k from the persistent (rho, omega), as
+// DescentOptimize.cpp:211-230 / CUDAInterface.cu:967-986 compute it in FP32.
+__device__ __host__ __forceinline__ void chebyshev_schedule(const DevParams &p, int k, float &rho, float &omega) {
+    if (k == 0) { rho = 0.0f; omega = 1.0f; }
+#ifdef __CUDA_ARCH__
+    omega = __fdiv_rn(4.0f, __fsub_rn(4.0f, __fmul_rn(__fmul_rn(rho, rho), omega)));
+#else
+    omega = 4.0f / (4.0f - rho * rho * omega);
+#endif
+    for (int i = 0; i < p.n_profile; ++i) {
+        if (k == p.profile_k[i] - 1) { rho = 0.0f; omega = 1.0f; }
+        if (k == p.profile_k[i]) {
+            rho = p.profile_rho[i];
+#ifdef __CUDA_ARCH__
+            omega = __fdiv_rn(2.0f, __fsub_rn(2.0f, __fmul_rn(rho, rho)));
+#else
+            omega = 2.0f / (2.0f - rho * rho);
+#endif
+            break;
+        }
+    }
+}
+
+// Launchers (kernels.cu)
+cudaError_t launch_rest(cudaStream_t s, const DevMesh &m, const double *rest_pad, float density, float4 *row0,
+                        float4 *row1, float4 *row2, double *tmass, int *bad);
+cudaError_t launch_mass(cudaStream_t s, const DevMesh &m, const double *tmass, const int *state, float gravity,
+                        float4 *info);
+cudaError_t launch_set_lame(cudaStream_t s, int Tp, const int4 *tets, const float *mu, const float *lambda, int count,
+                            float4 *row1, float4 *row2, const int *tet_user);
+cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, InstCtl *ctl, int *active);
+cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
+                            const int *pad2user);
+cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
+cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user);
+// positions (user layout) <-> displacement pairs
+cudaError_t launch_pack_positions(cudaStream_t s, const DevMesh &m, const float4 *uh, const float4 *ul,
+                                  const int *pad2user, float *dst_user);
+cudaError_t launch_unpack_positions(cudaStream_t s, const DevMesh &m, const float *src_user, const int *pad2user,
+                                    float4 *uh, float4 *ul);
+cudaError_t launch_pack(cudaStream_t s, int Np, const float4 *src, const int *pad2user, float *dst_user);
+cudaError_t launch_unpack(cudaStream_t s, int Np, const float *src_user, const int *pad2user, float4 *dst);
+cudaError_t launch_scatter_positions(cudaStream_t s, const DevMesh &m, int count, const int *ids_pad,
+                                     const float *xyz, float4 *uh, float4 *ul);
+cudaError_t launch_eval_tets(cudaStream_t s, const DevMesh &m, const float4 *uh, int material, int clamp_cpu,
+                             float *tf, float *energy, float *hd);
+cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, const float *hd, const int *pad2user,
+                          float *force_user, float *hd_user);
+
+}  // namespace pbs

@@ -1,0 +1,346 @@
+// Per-tet constitutive math for the descent step (device side).
+//
+// The device keeps node state as displacements u = x - X from the rest shape,
+// so every tet works with the displacement gradient G = Du * Dm^-1
+// (F = I + G).  All quantities below are written in terms of G so that none
+// of them is a difference of O(1) numbers: in FP32 the reference's
+// F - F^-T, I1 - 3 and ln det F lose ~|G| relative digits to cancellation,
+// which puts the line-search energy's rounding noise above the energy changes
+// of late iterations and stalls the solve short of a 1e-4 relative residual.
+//
+// Identities used (exact for 3x3):
+//   det(I + G) = 1 + d,  d = tr G + c2 + c3,  c2 = sum of principal 2x2 minors
+//                        of G (= tr cof G), c3 = det G
+//   cof(I + G) = (1 + tr G) I - G^T + cof G,   F^-T = cof(F) / J
+//   F - F^-T   = [(c2 + c3) I + J G + G^T - cof G] / J
+//   I1 - 3 - 2 ln J = |G|^2 + 2 (tr G - ln(1 + d))
+//                   = |G|^2 - 2 (c2 + c3) + 2 phi(d),  phi(d) = d - log1p(d)
+//
+// Reference semantics reproduced:
+//   F = Ds * Dm^-1                                      TetMesh.cpp:307-316
+//   neo-Hookean P = mu (F - F^-T) + lambda ln J F^-T     IsotropicNeohookeanMaterial.cpp:146
+//   stretch-based P = U diag(P^) V^T,
+//       P^_i = mu s_i + (lambda sum_j ln s_j - mu) / s_i  IsotropicNeohookeanMaterial.cpp:92-102
+//       with the modified SVD of IsotropicMaterial.cpp:16-60 (U, V rotations,
+//       an inversion's sign on the smallest singular value)
+//   corner forces H = P * AN, AN = -(det Dm / 6) Dm^-T   TetMesh.cpp:279-294
+//       (computeANs' cross-product normals equal -(det Dm/6) Dm^-T exactly),
+//       corners 1..3 = H's columns, corner 0 = minus their sum
+//   energy vol * (mu/2 (I1-3) - mu ln J + lambda/2 ln^2 J), clamped
+//                                                        IsotropicNeohookeanMaterial.cpp:164-171
+//   Jacobi diagonal: diagonal of K = -df/dx (IsotropicMaterial.cpp:503-552,
+//       which builds the full 12x12 element matrix from Xu et al.'s
+//       SVD-derivative dP/dF).  For this energy, restricted to one row d of F,
+//       dP_dj/dF_dq = mu delta_jq + (mu + lambda - lambda ln J) G'_dj G'_dq with
+//       G' = F^-T, hence the closed form
+//         K_cc,dd = svol [mu |w_c|^2 + (mu + lambda - lambda ln J) (G'_d . w_c)^2]
+//       w_c = row c-1 of Dm^-1 (w_0 = -sum of rows), svol = det Dm / 6.
+//
+// SVD (stretch material): own implementation of the classic route of
+// McAdams et al. 2011 -- cyclic Jacobi eigen-analysis of a symmetric 3x3 with
+// exact rotations, sorting (det V kept +1), Givens QR for U -- applied to
+// S = F^T F - I = G + G^T + G^T G, whose eigenvalues s_i give sigma_i - 1
+// without cancellation (sigma_i^2 = 1 + s_i, ln sigma_i = log1p(s_i) / 2).
+// Near-inverted tets (det F < 1e-3) redo the SVD in FP64.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace pbs {
+
+template <typename T> __device__ __forceinline__ T log1p_t(T x);
+template <> __device__ __forceinline__ float log1p_t<float>(float x) { return log1pf(x); }
+template <> __device__ __forceinline__ double log1p_t<double>(double x) { return log1p(x); }
+template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
+template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt(x); }
+template <typename T> __device__ __forceinline__ T sqrt_t(T x);
+template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double sqrt_t<double>(double x) { return sqrt(x); }
+
+// Cofactor matrix of a 3x3 (row-major): cof(A) = det(A) A^-T.
+template <typename T> __device__ __forceinline__ void cofactor3(const T m[9], T c[9]) {
+    c[0] = m[4] * m[8] - m[5] * m[7];
+    c[1] = m[5] * m[6] - m[3] * m[8];
+    c[2] = m[3] * m[7] - m[4] * m[6];
+    c[3] = m[2] * m[7] - m[1] * m[8];
+    c[4] = m[0] * m[8] - m[2] * m[6];
+    c[5] = m[1] * m[6] - m[0] * m[7];
+    c[6] = m[1] * m[5] - m[2] * m[4];
+    c[7] = m[2] * m[3] - m[0] * m[5];
+    c[8] = m[0] * m[4] - m[1] * m[3];
+}
+
+// G = Du * Dinv with Du columns u1-u0, u2-u0, u3-u0.
+template <typename T>
+__device__ __forceinline__ void disp_gradient(const float4 &u0, const float4 &u1, const float4 &u2, const float4 &u3,
+                                              const float dinv[9], T G[9]) {
+    const T du[9] = {(T)u1.x - (T)u0.x, (T)u2.x - (T)u0.x, (T)u3.x - (T)u0.x,
+                     (T)u1.y - (T)u0.y, (T)u2.y - (T)u0.y, (T)u3.y - (T)u0.y,
+                     (T)u1.z - (T)u0.z, (T)u2.z - (T)u0.z, (T)u3.z - (T)u0.z};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            G[3 * r + c] = du[3 * r] * (T)dinv[c] + du[3 * r + 1] * (T)dinv[3 + c] + du[3 * r + 2] * (T)dinv[6 + c];
+}
+
+// Everything a tet needs about F = I + G.
+template <typename T> struct Kin {
+    T G[9], cofG[9];
+    T tr, c2, c3, d;  // det F = 1 + d
+    T lnJ;            // log1p(d)
+};
+
+template <typename T> __device__ __forceinline__ void kinematics(Kin<T> &k) {
+    cofactor3<T>(k.G, k.cofG);
+    k.tr = k.G[0] + k.G[4] + k.G[8];
+    k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
+    k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+    k.d = k.tr + k.c2 + k.c3;
+    k.lnJ = log1p_t<T>(k.d);
+}
+
+// F^-T = [(1 + tr G) I - G^T + cof G] / J
+template <typename T> __device__ __forceinline__ void inv_transpose(const Kin<T> &k, T FiT[9]) {
+    const T invJ = T(1) / (T(1) + k.d);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            FiT[3 * i + j] = ((i == j ? T(1) + k.tr : T(0)) - k.G[3 * j + i] + k.cofG[3 * i + j]) * invJ;
+}
+
+// Neo-Hookean P = mu (F - F^-T) + lambda ln J F^-T, cancellation-free.
+template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T> &k, T mu, T lambda, T P[9]) {
+    const T J = T(1) + k.d;
+    const T invJ = T(1) / J;
+    const T lg = lambda * k.lnJ;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const T diag = (i == j) ? T(1) : T(0);
+            const T fmf = (diag * (k.c2 + k.c3) + J * k.G[3 * i + j] + k.G[3 * j + i] - k.cofG[3 * i + j]) * invJ;
+            const T fit = (diag * (T(1) + k.tr) - k.G[3 * j + i] + k.cofG[3 * i + j]) * invJ;
+            P[3 * i + j] = mu * fmf + lg * fit;
+        }
+}
+
+// phi(d) = d - log1p(d) >= 0, by its Taylor series where that is exact to FP32.
+template <typename T> __device__ __forceinline__ T phi_log1p(T d) {
+    if (fabs(d) < T(0.1)) {
+        T s = T(0.125);
+        s = T(-1.0 / 7.0) + d * s;
+        s = T(1.0 / 6.0) + d * s;
+        s = T(-0.2) + d * s;
+        s = T(0.25) + d * s;
+        s = T(-1.0 / 3.0) + d * s;
+        s = T(0.5) + d * s;
+        return d * d * s;
+    }
+    return d - log1p_t<T>(d);
+}
+
+// Psi / vol = mu (|G|^2/2 - c2 - c3 + phi(d)) + lambda/2 ln^2 J
+template <typename T> __device__ __forceinline__ T energy_density(const Kin<T> &k, T mu, T lambda) {
+    T g2 = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g2 += k.G[i] * k.G[i];
+    return mu * (T(0.5) * g2 - k.c2 - k.c3 + phi_log1p<T>(k.d)) + T(0.5) * lambda * k.lnJ * k.lnJ;
+}
+
+__device__ __forceinline__ float clamp_energy(float e, int clamp_cpu) {
+    if (clamp_cpu) return e > 1e-6f ? e : 0.0f;  // IsotropicNeohookeanMaterial.cpp:171
+    return fmaxf(e, 0.0f);                       // CUDAInterface.cu:549
+}
+
+// ---------------------------------------------------------------- SVD
+// One Jacobi rotation annihilating a_pq of a symmetric 3x3 (r = third index),
+// accumulated into V's columns p and q.
+template <typename T>
+__device__ __forceinline__ void jacobi_rotate(T &app, T &aqq, T &apq, T &arp, T &arq, T V[9], int p, int q) {
+    const T off = apq;
+    const T scale = fabs(app) + fabs(aqq);
+    if (fabs(off) <= T(1e-37) + scale * (sizeof(T) == 4 ? T(1e-9) : T(1e-18))) { apq = T(0); return; }
+    const T theta = (aqq - app) / (T(2) * off);
+    T t = T(1) / (fabs(theta) + sqrt_t<T>(theta * theta + T(1)));
+    t = theta < T(0) ? -t : t;
+    const T c = rsqrt_t<T>(t * t + T(1));
+    const T s = t * c;
+    app -= t * off;
+    aqq += t * off;
+    apq = T(0);
+    const T rp = arp, rq = arq;
+    arp = c * rp - s * rq;
+    arq = s * rp + c * rq;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T vp = V[3 * k + p], vq = V[3 * k + q];
+        V[3 * k + p] = c * vp - s * vq;
+        V[3 * k + q] = s * vp + c * vq;
+    }
+}
+
+// Zero B[i][j] with a rotation of rows j and i; U <- U * G^T.
+template <typename T> __device__ __forceinline__ void givens_qr_step(T B[9], T U[9], int j, int i) {
+    const T a = B[3 * j + j], b = B[3 * i + j];
+    const T r2 = a * a + b * b;
+    T c = T(1), s = T(0);
+    if (r2 > T(1e-37)) {
+        const T inv = rsqrt_t<T>(r2);
+        c = a * inv;
+        s = b * inv;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T bj = B[3 * j + k], bi = B[3 * i + k];
+        B[3 * j + k] = c * bj + s * bi;
+        B[3 * i + k] = -s * bj + c * bi;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T uj = U[3 * k + j], ui = U[3 * k + i];
+        U[3 * k + j] = c * uj + s * ui;
+        U[3 * k + i] = -s * uj + c * ui;
+    }
+}
+
+// Modified SVD of F = I + G: rotations U, V; s_i = sigma_i^2 - 1 (descending);
+// sign = sign of the smallest singular value (-1 for an inverted tet).
+template <typename T, int SWEEPS>
+__device__ __forceinline__ void svd_disp(const T G[9], T U[9], T s[3], T V[9], T &sign3) {
+    // S = G + G^T + G^T G
+    T a00 = T(2) * G[0] + G[0] * G[0] + G[3] * G[3] + G[6] * G[6];
+    T a11 = T(2) * G[4] + G[1] * G[1] + G[4] * G[4] + G[7] * G[7];
+    T a22 = T(2) * G[8] + G[2] * G[2] + G[5] * G[5] + G[8] * G[8];
+    T a01 = G[1] + G[3] + G[0] * G[1] + G[3] * G[4] + G[6] * G[7];
+    T a02 = G[2] + G[6] + G[0] * G[2] + G[3] * G[5] + G[6] * G[8];
+    T a12 = G[5] + G[7] + G[1] * G[2] + G[4] * G[5] + G[7] * G[8];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? T(1) : T(0);
+    for (int sweep = 0; sweep < SWEEPS; ++sweep) {
+        jacobi_rotate<T>(a00, a11, a01, a02, a12, V, 0, 1);
+        jacobi_rotate<T>(a00, a22, a02, a01, a12, V, 0, 2);
+        jacobi_rotate<T>(a11, a22, a12, a01, a02, V, 1, 2);
+    }
+    T e0 = a00, e1 = a11, e2 = a22;
+    auto swap_cols = [&](int i, int j) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const T t = V[3 * r + i];
+            V[3 * r + i] = -V[3 * r + j];
+            V[3 * r + j] = t;
+        }
+    };
+    if (e0 < e1) { swap_cols(0, 1); T t = e0; e0 = e1; e1 = t; }
+    if (e0 < e2) { swap_cols(0, 2); T t = e0; e0 = e2; e2 = t; }
+    if (e1 < e2) { swap_cols(1, 2); T t = e1; e1 = e2; e2 = t; }
+    s[0] = e0; s[1] = e1; s[2] = e2;
+    // B = F V = V + G V, then QR for U
+    T B[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            B[3 * r + c] = V[3 * r + c] + G[3 * r] * V[c] + G[3 * r + 1] * V[3 + c] + G[3 * r + 2] * V[6 + c];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) U[k] = (k % 4 == 0) ? T(1) : T(0);
+    givens_qr_step<T>(B, U, 0, 1);
+    givens_qr_step<T>(B, U, 0, 2);
+    givens_qr_step<T>(B, U, 1, 2);
+    sign3 = B[8] < T(0) ? T(-1) : T(1);
+}
+
+template <typename T> __device__ __forceinline__ void stretch_pk1(const T G[9], T mu, T lambda, float P[9]) {
+    T U[9], s[3], V[9], sign3;
+    svd_disp<T, sizeof(T) == 4 ? 4 : 8>(G, U, s, V, sign3);
+    T sig[3], ph[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sig[i] = sqrt_t<T>(T(1) + s[i]);
+    sig[2] *= sign3;
+    // sum_j ln sigma_j; an inverted tet (sigma_3 < 0) gives NaN as in the reference
+    const T L = T(0.5) * (log1p_t<T>(s[0]) + log1p_t<T>(s[1]) + log1p_t<T>(s[2])) +
+                (sign3 < T(0) ? T(NAN) : T(0));
+    // P^_i = mu sigma_i + (lambda L - mu) / sigma_i = (mu s_i + lambda L) / sigma_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i) ph[i] = (mu * s[i] + lambda * L) / sig[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            P[3 * i + j] = (float)(U[3 * i] * ph[0] * V[3 * j] + U[3 * i + 1] * ph[1] * V[3 * j + 1] +
+                                   U[3 * i + 2] * ph[2] * V[3 * j + 2]);
+}
+
+// Stretch-based P (IsotropicMaterial.cpp:370-384); FP64 when det F < 1e-3.
+__device__ __forceinline__ void pk1_stretch(const Kin<float> &k, float mu, float lambda, float P[9]) {
+    if (1.0f + k.d < 1e-3f) {
+        double Gd[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Gd[i] = k.G[i];
+        stretch_pk1<double>(Gd, (double)mu, (double)lambda, P);
+    } else {
+        stretch_pk1<float>(k.G, mu, lambda, P);
+    }
+}
+
+// Corner forces f[3c + d]: H = -svol * P * Dinv^T; corner 0 = -(sum of 1..3).
+__device__ __forceinline__ void corner_forces(const float P[9], const float dinv[9], float svol, float f[12]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float s0 = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float h = -svol * (P[3 * d] * dinv[3 * c] + P[3 * d + 1] * dinv[3 * c + 1] + P[3 * d + 2] * dinv[3 * c + 2]);
+            f[3 * (c + 1) + d] = h;
+            s0 += h;
+        }
+        f[d] = -s0;
+    }
+}
+
+// 12 Jacobi-diagonal entries (corner-major) from the closed form above.
+__device__ __forceinline__ void hessian_diag(const Kin<float> &k, float mu, float lambda, const float dinv[9],
+                                             float svol, float kd[12]) {
+    float FiT[9];
+    inv_transpose<float>(k, FiT);
+    const float beta = mu + lambda - lambda * k.lnJ;
+    float w[4][3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        w[1][q] = dinv[q];
+        w[2][q] = dinv[3 + q];
+        w[3][q] = dinv[6 + q];
+        w[0][q] = -(dinv[q] + dinv[3 + q] + dinv[6 + q]);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float ww = w[c][0] * w[c][0] + w[c][1] * w[c][1] + w[c][2] * w[c][2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float gw = FiT[3 * d] * w[c][0] + FiT[3 * d + 1] * w[c][1] + FiT[3 * d + 2] * w[c][2];
+            kd[3 * c + d] = svol * (mu * ww + beta * gw * gw);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- compensated sums
+// Error-free transformation a + b = s + e (Knuth's TwoSum); the _rn
+// intrinsics keep the compiler from contracting or reassociating it.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) + b, renormalised so that |lo| <= ulp(hi) / 2.
+__device__ __forceinline__ void add_comp(float &hi, float &lo, float b) {
+    float s, e;
+    two_sum(hi, b, s, e);
+    lo = __fadd_rn(lo, e);
+    const float s2 = __fadd_rn(s, lo);
+    lo = __fsub_rn(lo, __fsub_rn(s2, s));
+    hi = s2;
+}
+
+}  // namespace pbs

@@ -1,0 +1,322 @@
+"""GPU parity: the sm_103a path through the C ABI against the restated oracle
+and the reference's own outputs (tests/golden).
+
+Bars (BASELINE the benchmark spec): per-tet forces within 1e-5 (max-norm relative),
+positions after a step at a fixed iteration count within 1e-4 of the
+bounding-box diagonal, the gather CSR and its order bit-exact.  Each test also
+states the error against the all-FP64 oracle where it applies.
+"""
+import numpy as np
+import pytest
+
+from oracle import restated as O
+from phybs_gb300 import _lib as L
+from phybs_gb300 import meshes as M
+from phybs_gb300.solver import CUDAInterface, DescentSolver, make_params
+from tests._util import bbox_diag, elastic_from_ref, golden_names, load_golden, rel_max
+
+pytestmark = pytest.mark.gpu
+
+NAMES = golden_names()
+FORCE_TOL = 1e-5       # per-tet corner forces, max-norm relative
+POS_TOL = 1e-4         # positions / bounding-box diagonal
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from phybs_gb300.build import build
+    build()
+
+
+@pytest.fixture(scope="module", params=NAMES)
+def g(request):
+    d = load_golden(request.param)
+    d["name"] = request.param
+    return d
+
+
+def mesh_of(g):
+    return M.TetMeshData(g["rest"], g["tets"], g["pins"], g["young"], g["poisson"], name=g["name"])
+
+
+def solver_of(g, material=L.PBS_MATERIAL_NEOHOOKEAN, preset="cpu_reference", **kw):
+    p = make_params(preset, h=float(g["h"]), max_iters=int(g["iters"]), **kw)
+    return DescentSolver(mesh_of(g), positions=g["traj_x0"], material=material, mu=g["mu"], lam=g["lam"], params=p)
+
+
+def pin_mask(g):
+    m = np.zeros(g["rest"].shape[0], np.int32)
+    m[g["pins"]] = 1
+    return m
+
+
+def test_rest_data(g):
+    s = solver_of(g)
+    dinv, svol, mass, gy = s.rest_data()
+    assert rel_max(dinv, g["dminv"]) < 5e-6
+    assert rel_max(np.abs(svol), g["vol"]) < 2e-6
+    assert rel_max(mass, g["mass"]) < 2e-6
+    assert rel_max(gy, g["gravity"][:, 1]) < 2e-6
+    s.close()
+
+
+def test_incidence_bit_exact(g):
+    s = solver_of(g)
+    row, ent = s.incidence()
+    row_o, ent_o = O.incidence(g["tets"], g["rest"].shape[0])
+    assert np.array_equal(row, row_o) and np.array_equal(ent, ent_o)
+    s.close()
+
+
+@pytest.mark.parametrize("material", [L.PBS_MATERIAL_NEOHOOKEAN, L.PBS_MATERIAL_STRETCH])
+def test_per_tet_corner_forces(g, material):
+    s = solver_of(g, material=material)
+    cf, en, hd = s.eval_tets(g["probe_x"])
+    ref = {}
+    for prec in (32, 64):
+        ref[prec], _, _ = O.tet_eval(g["probe_x"], g["tets"], g["dminv"], g["an"], g["vol"], g["mu"], g["lam"],
+                                     material=material, prec=prec, energy=False, hdiag=False)
+    err64 = rel_max(cf, ref[64])
+    assert err64 < FORCE_TOL, err64
+    # the oracle's own FP32 run sits at the same distance from FP64
+    assert rel_max(ref[32], ref[64]) < FORCE_TOL
+    s.close()
+
+
+def test_node_forces_vs_reference(g):
+    for material, key in ((L.PBS_MATERIAL_NEOHOOKEAN, "probe_force_nh"), (L.PBS_MATERIAL_STRETCH, "probe_force_stretch")):
+        s = solver_of(g, material=material)
+        f, _ = s.eval_nodes(g["probe_x"])
+        f = f.astype(np.float64)
+        f[g["pins"]] = 0.0
+        assert rel_max(f, elastic_from_ref(g, key)) < 2e-5
+        s.close()
+
+
+def test_energy_and_hessian_diagonal(g):
+    s = solver_of(g)
+    _, en, _ = s.eval_tets(g["probe_x"])
+    assert rel_max(en, g["probe_energy"]) < 2e-5
+    _, hd = s.eval_nodes(g["probe_x"])
+    _, hd64 = O.node_eval(g["probe_x"], g["tets"], g["dminv"], g["an"], g["vol"], g["mu"], g["lam"],
+                          hessian_closed=1, prec=64)
+    assert rel_max(hd, hd64) < 1e-5
+    assert rel_max(hd, g["probe_hdiag"]) < 5e-3  # the reference's FP32 SVD-route noise
+    s.close()
+
+
+def test_trajectory_vs_reference(g):
+    """DescentOptimize steps at the fixed iteration count: positions within 1e-4
+    of the bbox diagonal of the reference's, the same line-search alpha."""
+    s = solver_of(g)
+    diag = bbox_diag(g["rest"])
+    for k in range(g["traj_x"].shape[0]):
+        s.step()
+        x = s.positions()
+        err = np.abs(x - g["traj_x"][k]).max() / diag
+        assert err < POS_TOL, (g["name"], k, err)
+        st = s.stats()
+        assert abs(st["alpha"] - g["traj_scalars"][k, 0]) < 1e-6, (k, st)
+    s.close()
+
+
+def test_step_control_matches_oracle(g):
+    """Same passes, rejections and final alpha as the FP32 restatement, and the
+    error against the FP64 restatement stated."""
+    s = solver_of(g)
+    pm = pin_mask(g)
+    r32 = O.rest(g["rest"], g["tets"], pm, prec=32)
+    r64 = O.rest(g["rest"], g["tets"], pm, prec=64)
+    p = O.make_params(h=float(g["h"]), max_iters=int(g["iters"]))
+    s32, s64 = O.StepState(g["traj_x0"]), O.StepState(g["traj_x0"])
+    diag = bbox_diag(g["rest"])
+    for k in range(2):
+        s.step()
+        st = s.stats()
+        o32 = O.step(s32, p, g["tets"], r32, g["mu"], g["lam"], pm, prec=32)
+        O.step(s64, p, g["tets"], r64, g["mu"], g["lam"], pm, prec=64)
+        assert (st["passes"], st["rejections"]) == (o32.passes, o32.rejections)
+        x = s.positions()
+        assert np.abs(x - s32.x0).max() / diag < POS_TOL
+        assert np.abs(x - s64.x0).max() / diag < 5e-4
+    s.close()
+
+
+def test_bitwise_determinism():
+    g = load_golden("ellipsoid_small")
+    outs = []
+    for _ in range(2):
+        s = solver_of(g)
+        for _ in range(2):
+            s.step()
+        outs.append(s.positions())
+        s.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_batched_instances_equal_single_runs():
+    """Packing meshes of uneven size into one launch changes nothing: every
+    instance's trajectory is bit-identical to its own single-mesh run."""
+    gs = [load_golden(n) for n in ("bar_small", "model_bar", "ellipsoid_small")]
+    h, iters = 1 / 30, 48
+    rest, tets, pins, mu, lam, x0 = [], [], [], [], [], []
+    nptr, tptr = [0], [0]
+    for g in gs:
+        off = nptr[-1]
+        rest.append(g["rest"]); tets.append(g["tets"] + off); pins.append(g["pins"] + off)
+        mu.append(g["mu"]); lam.append(g["lam"]); x0.append(g["traj_x0"])
+        nptr.append(off + g["rest"].shape[0]); tptr.append(tptr[-1] + g["tets"].shape[0])
+    mesh = M.TetMeshData(np.concatenate(rest), np.concatenate(tets), np.concatenate(pins), 1e5, 0.4,
+                         instance_node_ptr=np.array(nptr), instance_tet_ptr=np.array(tptr))
+    p = make_params(h=h, max_iters=iters)
+    sb = DescentSolver(mesh, positions=np.concatenate(x0), mu=np.concatenate(mu), lam=np.concatenate(lam), params=p)
+    for _ in range(2):
+        sb.step()
+    xb = sb.positions()
+    for i, g in enumerate(gs):
+        s = DescentSolver(mesh_of(g), positions=g["traj_x0"], mu=g["mu"], lam=g["lam"], params=p)
+        for _ in range(2):
+            s.step()
+        assert np.array_equal(s.positions(), xb[nptr[i]:nptr[i + 1]]), i
+        s.close()
+    sb.close()
+
+
+def test_gpu_reference_preset_matches_oracle():
+    """CUDAInterface semantics (gravity once, max(e,0) clamp) against the
+    restatement run with the same switches."""
+    g = load_golden("bar_small")
+    s = solver_of(g, preset="gpu_reference")
+    pm = pin_mask(g)
+    r32 = O.rest(g["rest"], g["tets"], pm, prec=32)
+    p = O.make_params(h=float(g["h"]), max_iters=int(g["iters"]), body_force_scale=1.0, energy_clamp=1)
+    st = O.StepState(g["traj_x0"])
+    for _ in range(3):
+        s.step()
+        O.step(st, p, g["tets"], r32, g["mu"], g["lam"], pm, prec=32)
+    assert np.abs(s.positions() - st.x0).max() / bbox_diag(g["rest"]) < POS_TOL
+    s.close()
+
+
+@pytest.mark.parametrize("control", [L.PBS_CONTROL_REFERENCE, L.PBS_CONTROL_RESTART])
+def test_residual_stop_matches_oracle(control):
+    """Iterate to |g| <= 1e-4 |g_0| (FP64 norms) with a single-stage rho = 0.99."""
+    g = load_golden("bar_small")
+    prof = ((10, 0.99),)
+    s = solver_of(g, max_iters=4000, tol=1e-4, profile=prof, control=control, body_force_scale=1.0)
+    pm = pin_mask(g)
+    r64 = O.rest(g["rest"], g["tets"], pm, prec=64)
+    p = O.make_params(h=float(g["h"]), max_iters=4000, tol=1e-4, profile=prof, control=control,
+                      body_force_scale=1.0)
+    st = O.StepState(g["traj_x0"])
+    for _ in range(2):
+        it = s.step()
+        o = O.step(st, p, g["tets"], r64, g["mu"], g["lam"], pm, prec=64)
+        stats = s.stats()
+        assert stats["converged"] == 1 and o.converged == 1
+        assert stats["residual_ratio"] <= 1e-4
+        assert abs(it - o.k_final) <= max(8, 0.1 * o.k_final), (it, o.k_final)
+    assert np.abs(s.positions() - st.x0).max() / bbox_diag(g["rest"]) < POS_TOL
+    s.close()
+
+
+def test_stretch_material_step_matches_oracle():
+    g = load_golden("ellipsoid_small")
+    s = solver_of(g, material=L.PBS_MATERIAL_STRETCH)
+    pm = pin_mask(g)
+    r32 = O.rest(g["rest"], g["tets"], pm, prec=32)
+    p = O.make_params(h=float(g["h"]), max_iters=int(g["iters"]), material=1)
+    st = O.StepState(g["traj_x0"])
+    for _ in range(2):
+        s.step()
+        O.step(st, p, g["tets"], r32, g["mu"], g["lam"], pm, prec=32)
+    assert np.abs(s.positions() - st.x0).max() / bbox_diag(g["rest"]) < POS_TOL
+    s.close()
+
+
+def test_config1_bar_100_steps_vs_restatement():
+    """Configuration 1 (40x10x10 cubes, 6-tet split, x = 0 pinned, gravity,
+    h = 1/30, 96 iterations, 100 steps): every step within 1e-4 of the bbox
+    diagonal of the FP32 restatement; the first three steps also against the
+    reference's own trajectory."""
+    g = load_golden("bar_config1")
+    s = solver_of(g)
+    pm = pin_mask(g)
+    r32 = O.rest(g["rest"], g["tets"], pm, prec=32)
+    p = O.make_params(h=float(g["h"]), max_iters=96)
+    st = O.StepState(g["traj_x0"])
+    diag = bbox_diag(g["rest"])
+    worst = 0.0
+    for k in range(100):
+        s.step()
+        O.step(st, p, g["tets"], r32, g["mu"], g["lam"], pm, prec=32)
+        x = s.positions()
+        err = np.abs(x - st.x0).max() / diag
+        worst = max(worst, err)
+        assert err < POS_TOL, (k, err)
+        if k < g["traj_x"].shape[0]:
+            assert np.abs(x - g["traj_x"][k]).max() / diag < POS_TOL
+    s.close()
+
+
+def test_state_roundtrip_and_reset():
+    g = load_golden("bar_small")
+    s = solver_of(g)
+    s.step()
+    x = s.positions()
+    v, vo = s.velocities()
+    s2 = solver_of(g)
+    s2.update_positions(x)
+    s2.write_velocities(v, vo)
+    s.step()
+    s2.step()
+    assert np.array_equal(s.positions(), s2.positions())
+    s.reset()
+    assert np.array_equal(s.positions(), g["rest"])
+    assert not s.velocities()[0].any()
+    s.close()
+    s2.close()
+
+
+def test_nonfinite_input_reports_status():
+    g = load_golden("bar_small")
+    s = solver_of(g)
+    ext = np.zeros_like(g["rest"])
+    ext[5, 1] = np.nan
+    s.step(ext, raise_on_error=False)
+    assert s.last_status == L.PBS_E_NONFINITE
+    s.close()
+
+
+def test_pass_cap_reports_status():
+    g = load_golden("bar_small")
+    s = solver_of(g, pass_cap=5)
+    s.step(raise_on_error=False)
+    assert s.last_status == L.PBS_E_ITER_CAP and s.stats()["passes"] == 5
+    s.close()
+
+
+def test_bad_meshes_rejected():
+    m = M.bar_mesh(2, 2, 2)
+    bad = m.tets.copy()
+    bad[0, [2, 3]] = bad[0, [3, 2]]  # inverted rest tet
+    with pytest.raises(L.PhybsError) as e:
+        DescentSolver(M.TetMeshData(m.rest, bad, m.pins, 1e5, 0.4))
+    assert e.value.code == L.PBS_E_BAD_MESH
+    bad = m.tets.copy()
+    bad[1, 0] = m.n_nodes + 3  # index out of range
+    with pytest.raises(L.PhybsError) as e:
+        DescentSolver(M.TetMeshData(m.rest, bad, m.pins, 1e5, 0.4))
+    assert e.value.code == L.PBS_E_BAD_MESH
+
+
+def test_cuda_interface_wrapper():
+    """CUDAInterface's call shape (fvm.cpp:44-47, 187-188)."""
+    g = load_golden("model_bar")
+    n, t = g["rest"].shape[0], g["tets"].shape[0]
+    ci = CUDAInterface(n, g["traj_x0"].ravel(), g["rest"].ravel(), pin_mask(g), t, g["tets"].ravel(),
+                       float(g["young"]), float(g["poisson"]), 1000.0)
+    host = np.zeros(3 * n, np.float32)
+    ci.doDescentOpt(0.03, 96, np.zeros(3 * n, np.float32), host)
+    assert np.isfinite(host).all() and np.abs(host.reshape(-1, 3) - g["rest"]).max() > 0
+    ci.reset()
