@@ -50,7 +50,8 @@ extern "C" {
 
 /* Line-search rejection behaviour. */
 #define PBS_CONTROL_REFERENCE 0 /* alpha *= shrink; iterations -= k - 8; redo k (DescentOptimize.cpp:166-177) */
-#define PBS_CONTROL_RESTART 1   /* alpha *= shrink; restore x and the Chebyshev history; budget unchanged   */
+#define PBS_CONTROL_RESTART 1   /* alpha *= shrink; restore x, restart the Chebyshev history and rho schedule;
+                                   the iteration budget is unchanged                                          */
 
 /* Energy clamp per tet. */
 #define PBS_CLAMP_CPU 0 /* e > 1e-6 ? e : 0   (IsotropicNeohookeanMaterial.cpp:171) */

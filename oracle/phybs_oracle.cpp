@@ -565,7 +565,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
         int iters = p->max_iters;
         int passes = 0, rejections = 0, converged = 0;
         double g0 = -1, ratio = -1;
-        int k;
+        int k, k_restart = 0;  // RESTART control runs the rho schedule from the last restart
         for (k = 0; k < iters; ++k) {
             if (alpha < (R)p->alpha_min) break;
             ++passes;
@@ -592,7 +592,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     if (p->control == 0) iters -= k - p->line_search_every;
                     k -= 1;
                     x = xold;
-                    if (p->control == 1) xlast = xold;
+                    if (p->control == 1) { xlast = xold; k_restart = k + 1; }
                     continue;
                 }
                 Eold = E;
@@ -621,11 +621,12 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             if (p->tol > 0 && k > 0 && r <= (double)p->tol * g0) { converged = 1; break; }
             for (size_t id = 0; id < N3; ++id) xnext[id] = x[id] + alpha * (g[id] / -hq[id]);
             // Chebyshev schedule (DescentOptimize.cpp:211-233)
-            if (k == 0) { rho = 0; omega = 1; }
+            const int ks = k - k_restart;
+            if (ks == 0) { rho = 0; omega = 1; }
             omega = R(4) / (R(4) - rho * rho * omega);
             for (int i = 0; i < p->n_profile; i++) {
-                if (k == p->profile_k[i] - 1) { rho = 0; omega = 1; }
-                if (k == p->profile_k[i]) { rho = (R)p->profile_rho[i]; omega = R(2) / (R(2) - rho * rho); break; }
+                if (ks == p->profile_k[i] - 1) { rho = 0; omega = 1; }
+                if (ks == p->profile_k[i]) { rho = (R)p->profile_rho[i]; omega = R(2) / (R(2) - rho * rho); break; }
             }
             if (omega != R(1))
                 for (size_t id = 0; id < N3; ++id) xnext[id] = omega * (xnext[id] - xlast[id]) + xlast[id];

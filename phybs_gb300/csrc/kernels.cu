@@ -120,6 +120,7 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.status = PBS_OK;
     c.par = 0;
     c.action = ACT_STEP;
+    c.k_restart = 0;
     c.counter_t = 0;
     c.counter_n = 0;
     c.alpha = p.alpha0;
@@ -223,18 +224,26 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         else pk1_neohookean<float>(kin, mu, lambda, P);
         float f[12];
         corner_forces(P, dinv, svol, f);
-        float4 *out = reinterpret_cast<float4 *>(st.tf + 12 * (size_t)t);
-        out[0] = make_float4(f[0], f[1], f[2], f[3]);
-        out[1] = make_float4(f[4], f[5], f[6], f[7]);
-        out[2] = make_float4(f[8], f[9], f[10], f[11]);
+        const int4 sl = m.tslot[t];
+        const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float *o = st.tf + 3 * (size_t)slot[c];
+            o[0] = f[3 * c];
+            o[1] = f[3 * c + 1];
+            o[2] = f[3 * c + 2];
+        }
         if (check) e = (double)clamp_energy(energy_density<float>(kin, mu, lambda) * fabsf(svol), p.clamp_cpu);
         if (do_h) {
             float kd[12];
             hessian_diag(kin, mu, lambda, dinv, svol, kd);
-            float4 *ho = reinterpret_cast<float4 *>(st.hd + 12 * (size_t)t);
-            ho[0] = make_float4(kd[0], kd[1], kd[2], kd[3]);
-            ho[1] = make_float4(kd[4], kd[5], kd[6], kd[7]);
-            ho[2] = make_float4(kd[8], kd[9], kd[10], kd[11]);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float *o = st.hd + 3 * (size_t)slot[c];
+                o[0] = kd[3 * c];
+                o[1] = kd[3 * c + 1];
+                o[2] = kd[3 * c + 2];
+            }
         }
     }
     if (!check) return;
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     const bool do_h = (k % p.hd_every) == 0;
     const float alpha = cp->alpha;
     float rho = cp->rho, omega = cp->omega;
-    chebyshev_schedule(p, k, rho, omega);
+    chebyshev_schedule(p, k - cp->k_restart, rho, omega);
     const size_t cur = (size_t)cp->par * m.Np, nxt = (size_t)(1 - cp->par) * m.Np;
     const int i = b * BLOCK + threadIdx.x;
     const float4 info = m.info[i];
@@ -330,17 +339,20 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
             }
             if (info.z == 0.f) {
                 float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
+                // this node's slots are contiguous and in canonical (tet, corner) order
                 const int a = m.inc_ptr[i], e_ = m.inc_ptr[i + 1];
-                for (int j = a; j < e_; ++j) {
-                    const int ent = m.inc[j];
-                    const size_t o = 12 * (size_t)(ent >> 2) + 3 * (ent & 3);
-                    fx += st.tf[o];
-                    fy += st.tf[o + 1];
-                    fz += st.tf[o + 2];
-                    if (do_h) {
-                        hx += st.hd[o];
-                        hy += st.hd[o + 1];
-                        hz += st.hd[o + 2];
+                const float *tf = st.tf + 3 * (size_t)a;
+                for (int j = 0; j < e_ - a; ++j) {
+                    fx += tf[3 * j];
+                    fy += tf[3 * j + 1];
+                    fz += tf[3 * j + 2];
+                }
+                if (do_h) {
+                    const float *hd = st.hd + 3 * (size_t)a;
+                    for (int j = 0; j < e_ - a; ++j) {
+                        hx += hd[3 * j];
+                        hy += hd[3 * j + 1];
+                        hz += hd[3 * j + 2];
                     }
                 }
                 const float mh = info.x * p.h2inv;
@@ -393,6 +405,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     c.passes += 1;
     if (action == ACT_RESTORE) {
         c.par = 1 - c.par;  // the restored state; k is redone
+        if (p.control == PBS_CONTROL_RESTART) c.k_restart = k;  // rerun the rho schedule from here
     } else {
         const double r = sqrt(R2);
         if (k == 0) c.g0 = r;

@@ -48,7 +48,7 @@ struct pbs_handle {
     std::vector<float> h_rest;  // user layout, for reset
 
     // device mesh
-    DevBuf<int4> tets;
+    DevBuf<int4> tets, tslot;
     DevBuf<float4> row0, row1, row2, info, rest4;
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
     // device state
@@ -71,7 +71,7 @@ struct pbs_handle {
         DevMesh m;
         m.Np = Np; m.Tp = Tp; m.n_inst = B; m.n_tblk = n_tblk; m.n_nblk = n_nblk;
         m.tets = tets.p; m.row0 = row0.p; m.row1 = row1.p; m.row2 = row2.p;
-        m.inc_ptr = inc_ptr.p; m.inc = inc.p; m.info = info.p; m.rest = rest4.p;
+        m.inc_ptr = inc_ptr.p; m.inc = inc.p; m.tslot = tslot.p; m.info = info.p; m.rest = rest4.p;
         m.tblk_inst = tblk_inst.p; m.nblk_inst = nblk_inst.p;
         return m;
     }
@@ -85,7 +85,7 @@ struct pbs_handle {
     void release() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
-        DevBuf<int4> *i4[] = {&tets};
+        DevBuf<int4> *i4[] = {&tets, &tslot};
         for (auto b : i4) b->release();
         DevBuf<float4> *f4[] = {&row0, &row1, &row2, &info, &rest4, &uh, &ul, &dd, &oh, &ol, &u0h, &u0l, &th, &tl,
                                 &v, &vold, &ext, &diag};
@@ -272,6 +272,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
             for (int c = 0; c < 4; ++c) ient[fill[q[c]]++] = 4 * tp + c;
         }
     }
+    std::vector<int4> tslot(Tp, make_int4(-1, -1, -1, -1));
+    for (size_t j = 0; j < ient.size(); ++j) (&tslot[ient[j] >> 2].x)[ient[j] & 3] = (int)j;
     h->h_node_state.assign(Np, 2);
     for (int i = 0; i < N; ++i) h->h_node_state[h->user2pad[i]] = (d->pin_mask && d->pin_mask[i] > 0) ? 1 : 0;
     std::vector<double> rest_pad(3 * (size_t)Np, 0.0);
@@ -297,7 +299,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(cudaEventCreateWithFlags(&h->ev_chunk[1], cudaEventDisableTiming));
     CKC(cudaMallocHost((void **)&h->h_active, 2 * sizeof(int)));
     CKC(cudaMallocHost((void **)&h->h_ctl, B * sizeof(InstCtl)));
-    CKC(h->tets.alloc(Tp)); CKC(h->row0.alloc(Tp)); CKC(h->row1.alloc(Tp)); CKC(h->row2.alloc(Tp));
+    CKC(h->tets.alloc(Tp)); CKC(h->tslot.alloc(Tp)); CKC(h->row0.alloc(Tp)); CKC(h->row1.alloc(Tp)); CKC(h->row2.alloc(Tp));
     CKC(h->info.alloc(Np)); CKC(h->inc_ptr.alloc(Np + 1)); CKC(h->inc.alloc(4 * (size_t)T));
     CKC(h->tblk_inst.alloc(h->n_tblk)); CKC(h->nblk_inst.alloc(h->n_nblk));
     CKC(h->pad2user.alloc(Np)); CKC(h->tet_user.alloc(Tp)); CKC(h->node_state.alloc(Np)); CKC(h->bad.alloc(1));
@@ -305,12 +307,14 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->oh.alloc(Np)); CKC(h->ol.alloc(Np)); CKC(h->u0h.alloc(Np)); CKC(h->u0l.alloc(Np));
     CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
     CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
-    CKC(h->tf.alloc(12 * (size_t)Tp)); CKC(h->hd.alloc(12 * (size_t)Tp));
+    // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
+    CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 12 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 12 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
     cudaStream_t s = h->stream;
     CKC(cudaMemcpyAsync(h->tets.p, tets_pad.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->tslot.p, tslot.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->inc_ptr.p, iptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->inc.p, ient.data(), sizeof(int) * 4 * (size_t)T, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->tblk_inst.p, tblk.data(), sizeof(int) * h->n_tblk, cudaMemcpyHostToDevice, s));

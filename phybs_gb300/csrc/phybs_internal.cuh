@@ -17,7 +17,11 @@
 //                                   state 0 free / 1 pinned / 2 padding, lumped mass}
 //   rest        float4[Np]         rest positions X
 //   inc_ptr     int[Np+1], inc int[4T]   node -> 4*tet+corner gather, canonical order
-//   tf, hd      float[12*Tp]       per-tet corner forces / Jacobi-diagonal terms
+//   tslot       int4[Tp]           for each tet corner, its slot in the gather
+//                                  (its position in inc): the per-tet kernel writes
+//                                  corner forces straight into node-major order
+//   tf, hd      float[3*4T]        corner forces / Jacobi-diagonal terms by slot;
+//                                  node i owns slots inc_ptr[i] .. inc_ptr[i+1]-1
 //   tpart       double2[n_tblk]    per tet-block {sum e, sum e^2} of the energy
 //   npart       double[n_nblk]     per node-block |g|^2
 //   ctl         InstCtl[n_inst]    per-instance descent state
@@ -55,7 +59,7 @@ enum PassAction : int { ACT_STEP = 0, ACT_SAVE_STEP = 1, ACT_RESTORE = 2 };
 struct __align__(16) InstCtl {
     int k, iters, done, passes;
     int rejections, converged, status, par;
-    int action, pad0;
+    int action, k_restart;  // k_restart: first iteration of the current rho schedule (RESTART control)
     unsigned int counter_t, counter_n;
     float alpha, rho, omega, pad1;
     double energy, energy_old, g0, ratio;
@@ -70,6 +74,7 @@ struct DevMesh {
     const int4 *tets;
     const float4 *row0, *row1, *row2;
     const int *inc_ptr, *inc;
+    const int4 *tslot;
     const float4 *info, *rest;
     const int *tblk_inst, *nblk_inst;
 };

@@ -161,3 +161,30 @@ def test_params_validation(lib):
     p = L.default_params()
     p.h = 0.0
     assert lib.pbs_set_params(None, C.byref(p)) == L.PBS_E_INVALID_ARG
+
+
+def build_cpp_demo(tmp_path):
+    import subprocess
+    from phybs_gb300.build import LIB, build
+    build()
+    exe = str(tmp_path / "cuda_interface_demo")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "cuda_interface_demo.cpp"), LIB,
+                    "-Wl,-rpath," + os.path.dirname(LIB), "-o", exe], check=True)
+    return exe
+
+
+def test_cpp_cuda_interface_wrapper_compiles_and_runs(tmp_path):
+    """The header-only CUDAInterface wrapper builds against the C ABI; without
+    a GB300 its constructor throws with PBS_E_NO_DEVICE."""
+    import subprocess
+    exe = build_cpp_demo(tmp_path)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert out[0] == "pattern" and int(out[1]) > 0
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        assert out[2:] == ["error", str(L.PBS_E_NO_DEVICE)]
