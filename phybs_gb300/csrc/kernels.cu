@@ -121,6 +121,7 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.par = 0;
     c.action = ACT_STEP;
     c.k_restart = 0;
+    c.force_check = 0;
     c.counter_t = 0;
     c.counter_n = 0;
     c.alpha = p.alpha0;
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
     InstCtl *cp = st.ctl + m.tblk_inst[b];
     if (cp->done) return;
     const int k = cp->k;
-    const bool check = (k % p.ls_every) == 0;
+    const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const bool do_h = (k % p.hd_every) == 0;
     const size_t cur = (size_t)cp->par * m.Np;
     const float4 *U = st.uh + cur;
@@ -226,24 +227,16 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         corner_forces(P, dinv, svol, f);
         const int4 sl = m.tslot[t];
         const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+        float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            float *o = st.tf + 3 * (size_t)slot[c];
-            o[0] = f[3 * c];
-            o[1] = f[3 * c + 1];
-            o[2] = f[3 * c + 2];
-        }
+        for (int c = 0; c < 4; ++c) tf4[slot[c]] = make_float4(f[3 * c], f[3 * c + 1], f[3 * c + 2], 0.f);
         if (check) e = (double)clamp_energy(energy_density<float>(kin, mu, lambda) * fabsf(svol), p.clamp_cpu);
         if (do_h) {
             float kd[12];
             hessian_diag(kin, mu, lambda, dinv, svol, kd);
+            float4 *hd4 = reinterpret_cast<float4 *>(st.hd);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float *o = st.hd + 3 * (size_t)slot[c];
-                o[0] = kd[3 * c];
-                o[1] = kd[3 * c + 1];
-                o[2] = kd[3 * c + 2];
-            }
+            for (int c = 0; c < 4; ++c) hd4[slot[c]] = make_float4(kd[3 * c], kd[3 * c + 1], kd[3 * c + 2], 0.f);
         }
     }
     if (!check) return;
@@ -286,7 +279,11 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
     // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
     // error of order 2^-24 sqrt(sum e_i^2); slack 0 is the reference's strict test
     const double tau = (double)p.energy_slack * 5.9604644775390625e-8 * sqrt(E2);
-    if (k != 0 && E > c.energy_old + tau) {
+    // RESTART control also treats a non-finite energy (a step that inverted
+    // tets) as a rejection; the reference control accepts it (NaN > E_old is
+    // false), and the step then ends with PBS_E_NONFINITE below
+    const bool bad = !isfinite(E) && p.control == PBS_CONTROL_RESTART;
+    if ((k != 0 && E > c.energy_old + tau) || (bad && k != 0)) {
         c.action = ACT_RESTORE;
         c.alpha = (float)((double)c.alpha * (double)p.alpha_shrink);
         c.rejections += 1;
@@ -295,7 +292,8 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         c.action = ACT_SAVE_STEP;
         c.energy_old = E;
     }
-    if (!isfinite(E)) {
+    c.force_check = 0;
+    if (!isfinite(E) && !(bad && k != 0)) {
         c.status = PBS_E_NONFINITE;
         c.done = 1;
     }
@@ -310,7 +308,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     InstCtl *cp = st.ctl + m.nblk_inst[b];
     if (cp->done) return;
     const int k = cp->k;
-    const bool check = (k % p.ls_every) == 0;
+    const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const int action = check ? cp->action : ACT_STEP;
     const bool do_h = (k % p.hd_every) == 0;
     const float alpha = cp->alpha;
@@ -341,18 +339,20 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
                 float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
                 // this node's slots are contiguous and in canonical (tet, corner) order
                 const int a = m.inc_ptr[i], e_ = m.inc_ptr[i + 1];
-                const float *tf = st.tf + 3 * (size_t)a;
-                for (int j = 0; j < e_ - a; ++j) {
-                    fx += tf[3 * j];
-                    fy += tf[3 * j + 1];
-                    fz += tf[3 * j + 2];
+                const float4 *tf4 = reinterpret_cast<const float4 *>(st.tf);
+                for (int j = a; j < e_; ++j) {
+                    const float4 f = tf4[j];
+                    fx += f.x;
+                    fy += f.y;
+                    fz += f.z;
                 }
                 if (do_h) {
-                    const float *hd = st.hd + 3 * (size_t)a;
-                    for (int j = 0; j < e_ - a; ++j) {
-                        hx += hd[3 * j];
-                        hy += hd[3 * j + 1];
-                        hz += hd[3 * j + 2];
+                    const float4 *hd4 = reinterpret_cast<const float4 *>(st.hd);
+                    for (int j = a; j < e_; ++j) {
+                        const float4 q = hd4[j];
+                        hx += q.x;
+                        hy += q.y;
+                        hz += q.z;
                     }
                 }
                 const float mh = info.x * p.h2inv;
@@ -420,8 +420,14 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
             c.k = k + 1;
         }
         if (!isfinite(R2)) {
-            c.status = PBS_E_NONFINITE;
-            c.done = 1;
+            if (p.control == PBS_CONTROL_RESTART && c.k > 0) {
+                c.force_check = 1;  // the next pass measures the energy and restores
+                c.converged = 0;
+                c.done = 0;
+            } else {
+                c.status = PBS_E_NONFINITE;
+                c.done = 1;
+            }
         }
     }
     if (!c.done) {

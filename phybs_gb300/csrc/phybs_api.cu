@@ -308,7 +308,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
     CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
     // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
-    CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 12 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 12 * (size_t)T)));
+    CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
@@ -328,8 +328,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(cudaMemsetAsync(h->vold.p, 0, sizeof(float4) * Np, s));
     CKC(cudaMemsetAsync(h->diag.p, 0, sizeof(float4) * Np, s));
     CKC(cudaMemsetAsync(h->ext.p, 0, sizeof(float4) * Np, s));
-    CKC(cudaMemsetAsync(h->tf.p, 0, sizeof(float) * 12 * (size_t)Tp, s));
-    CKC(cudaMemsetAsync(h->hd.p, 0, sizeof(float) * 12 * (size_t)Tp, s));
+    CKC(cudaMemsetAsync(h->tf.p, 0, sizeof(float) * std::max(12 * (size_t)Tp, 16 * (size_t)T), s));
+    CKC(cudaMemsetAsync(h->hd.p, 0, sizeof(float) * std::max(12 * (size_t)Tp, 16 * (size_t)T), s));
     {
         DevBuf<float4> *zero[] = {&h->uh, &h->ul, &h->dd};
         for (auto b : zero) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * 2 * (size_t)Np, s));

@@ -20,7 +20,7 @@
 //   tslot       int4[Tp]           for each tet corner, its slot in the gather
 //                                  (its position in inc): the per-tet kernel writes
 //                                  corner forces straight into node-major order
-//   tf, hd      float[3*4T]        corner forces / Jacobi-diagonal terms by slot;
+//   tf, hd      float4[4T]         corner forces / Jacobi-diagonal terms by slot;
 //                                  node i owns slots inc_ptr[i] .. inc_ptr[i+1]-1
 //   tpart       double2[n_tblk]    per tet-block {sum e, sum e^2} of the energy
 //   npart       double[n_nblk]     per node-block |g|^2
@@ -61,7 +61,8 @@ struct __align__(16) InstCtl {
     int rejections, converged, status, par;
     int action, k_restart;  // k_restart: first iteration of the current rho schedule (RESTART control)
     unsigned int counter_t, counter_n;
-    float alpha, rho, omega, pad1;
+    float alpha, rho, omega;
+    int force_check;  // RESTART control: a non-finite residual makes the next pass a line-search pass
     double energy, energy_old, g0, ratio;
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
