@@ -115,6 +115,7 @@ typedef struct pbs_stats {
     double residual_ratio;    /* instance 0 |g_k| / |g_0|                         */
     double device_ms;         /* device time of the last pbs_step (CUDA events)   */
     int graph_launches;       /* captured 16-pass graphs launched by the last step */
+    int warm_start_used;      /* instances whose step started from the learned guess */
 } pbs_stats;
 
 void pbs_default_params(pbs_step_params *p);
@@ -192,6 +193,43 @@ int pbs_get_stream(pbs_handle *h, void **stream);
  * left as it was) and returns the mean milliseconds per launch of the per-tet
  * kernel and of the per-node kernel. */
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms);
+
+/* ------------------------------------------------------------------------
+ * Learned warm start.  A per-node MLP 24 -> 64 -> 64 -> 64 -> 3 (GELU; BF16
+ * weights on the tensor cores, FP32 accumulation; 10,115 FP32 master
+ * parameters: W1 64x24, b1, W2 64x64, b2, W3 64x64, b3, W4 3x64, b4, weights
+ * row-major with one row per output).  It has no counterpart in the
+ * reference: it predicts each step's correction to the inertial guess.
+ * ------------------------------------------------------------------------ */
+typedef struct pbs_mlp pbs_mlp;
+int pbs_mlp_param_count(void);
+/* theta: NPARAM initial values, or NULL for He initialisation from `seed`. */
+int pbs_mlp_create(pbs_mlp **out, const float *theta, unsigned long long seed);
+void pbs_mlp_destroy(pbs_mlp *t);
+int pbs_mlp_get_params(pbs_mlp *t, float *theta);
+int pbs_mlp_set_params(pbs_mlp *t, const float *theta);   /* also resets Adam */
+/* Host arrays: X n x 24, Y n x 3. */
+int pbs_mlp_forward(pbs_mlp *t, const float *X, int n, float *Y);
+/* Gradient of the mean (over rows) squared error of the batch; grad NPARAM floats. */
+int pbs_mlp_gradient(pbs_mlp *t, const float *X, const float *Y, int n, float *grad, float *loss);
+/* Training set (copied to the device) and Adam training on minibatches. */
+int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, int n);
+int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long seed, float *losses);
+
+/* Install (enabled != 0) or switch off the warm start on a solver handle.
+ * theta: pbs_mlp_param_count() values; feat_mean / feat_std: the 24 feature
+ * standardisation constants; out_std: the 3 output scales (the network
+ * predicts correction / (out_std * mean edge length)).  Each pbs_step then
+ * evaluates the network on the plain guess's features, keeps the predicted
+ * guess for an instance only if its energy is not higher than the plain
+ * guess's, and measures the residual tolerance against the plain guess's
+ * gradient either way. */
+int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean, const float *feat_std,
+                       const float *out_std, int enabled);
+/* The 24 raw (unstandardised) features of every node for the next step with
+ * external forces ext (or NULL), and the plain initial guess x~ + warm_start
+ * h (v - v_old) (x_init, 3*N, may be NULL).  The state is not advanced. */
+int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init);
 
 /* Node-node 3N x 3N stiffness pattern of the mesh, bit-identical to
  * IsotropicMaterial::allocateGlobalStiffnessMatrix (IsotropicMaterial.cpp:554-644):

@@ -35,6 +35,9 @@ EXPORTS = (
     "pbs_read_velocities", "pbs_write_velocities", "pbs_reset", "pbs_get_stats", "pbs_get_sizes",
     "pbs_get_incidence", "pbs_get_rest_data", "pbs_eval_tets", "pbs_eval_nodes", "pbs_stiffness_pattern",
     "pbs_set_node_positions", "pbs_get_stream", "pbs_profile_kernels",
+    "pbs_mlp_param_count", "pbs_mlp_create", "pbs_mlp_destroy", "pbs_mlp_get_params", "pbs_mlp_set_params",
+    "pbs_mlp_forward", "pbs_mlp_gradient", "pbs_mlp_set_data", "pbs_mlp_train",
+    "pbs_set_warm_start", "pbs_warm_start_features",
 )
 
 
@@ -58,7 +61,7 @@ class Stats(C.Structure):
     _fields_ = [("passes", C.c_int), ("iterations", C.c_int), ("rejections", C.c_int), ("converged", C.c_int),
                 ("status", C.c_int), ("alpha", C.c_float), ("rho", C.c_float), ("omega", C.c_float),
                 ("energy", C.c_double), ("residual_ratio", C.c_double), ("device_ms", C.c_double),
-                ("graph_launches", C.c_int)]
+                ("graph_launches", C.c_int), ("warm_start_used", C.c_int)]
 
 
 class PhybsError(RuntimeError):

@@ -20,6 +20,7 @@
 //           step needs no host round trip (the reference syncs every 8
 //           iterations, CUDAInterface.cu:886-890).
 #include "../../include/phybs.h"
+#include "pass_math.cuh"
 #include "phybs_internal.cuh"
 #include "tet_math.cuh"
 
@@ -122,6 +123,8 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.action = ACT_STEP;
     c.k_restart = 0;
     c.force_check = 0;
+    c.g0_fixed = 0;
+    c.ws_used = 0;
     c.counter_t = 0;
     c.counter_n = 0;
     c.alpha = p.alpha0;
@@ -179,6 +182,8 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
     st.vold[i] = st.v[i];
     st.v[i] = make_float4(__fdiv_rn(p.damping * dx, p.h), __fdiv_rn(p.damping * dy, p.h), __fdiv_rn(p.damping * dz, p.h),
                           0.f);
+    st.hist2[i] = st.hist1[i];
+    st.hist1[i] = make_float4(dx, dy, dz, 0.f);
     st.u0h[i] = hi;
     st.u0l[i] = lo;
 }
@@ -218,13 +223,8 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         const float svol = r0.w, mu = r1.w, lambda = r2.w;
         Kin<float> kin;
-        disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
-        kinematics(kin);
-        float P[9];
-        if (MATERIAL == PBS_MATERIAL_STRETCH) pk1_stretch(kin, mu, lambda, P);
-        else pk1_neohookean<float>(kin, mu, lambda, P);
         float f[12];
-        corner_forces(P, dinv, svol, f);
+        pass_forces<MATERIAL>(p, U, st.u0h, q, dinv, svol, mu, lambda, kin, f);
         const int4 sl = m.tslot[t];
         const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
         float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
@@ -363,10 +363,12 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
                 } else {
                     D = st.diag[i];
                 }
-                const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
-                const float gx = ((uh.x - th.x) + (ul.x - tl.x)) * mh - fx - p.body_scale * ex.x;
-                const float gy = ((uh.y - th.y) + (ul.y - tl.y)) * mh - fy - p.body_scale * (ex.y + info.y);
-                const float gz = ((uh.z - th.z) + (ul.z - tl.z)) * mh - fz - p.body_scale * ex.z;
+                // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
+                // force (incremental mode) + body_force_scale (external + gravity)
+                const float4 th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
+                const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
+                const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
+                const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
                 r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
                 // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
                 // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
         if (p.control == PBS_CONTROL_RESTART) c.k_restart = k;  // rerun the rho schedule from here
     } else {
         const double r = sqrt(R2);
-        if (k == 0) c.g0 = r;
+        if (k == 0 && !c.g0_fixed) c.g0 = r;
         c.ratio = c.g0 > 0.0 ? r / c.g0 : 0.0;
         if (p.tol > 0.f && k > 0 && r <= (double)p.tol * c.g0) {
             c.converged = 1;  // keep x_k (the current parity)
@@ -436,6 +438,64 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     }
     *cp = c;
     if (c.done) atomicSub(st.active, 1);
+}
+
+// Per-step node constant b = f_el(u0) (incremental mode, FP64) +
+// body_force_scale (external + gravity), split into FP32 (hi, lo).  Each
+// node evaluates its incident tets' full neo-Hookean stress at the step
+// start's FP32 displacement (the base of the passes' increments) in FP64 and
+// sums its corner forces in the canonical order.
+__global__ void k_ref_force(DevMesh m, DevParams p, DevState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const float4 info = m.info[i];
+    if (info.z == 2.f) return;
+    const float4 ex = st.ext[i];
+    double b[3] = {(double)p.body_scale * ex.x, (double)p.body_scale * ((double)ex.y + info.y),
+                   (double)p.body_scale * ex.z};
+    if (p.incremental && info.z == 0.f) {
+        for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+            const int t = m.inc[j] >> 2, c = m.inc[j] & 3;
+            const int4 q = m.tets[t];
+            const int id[4] = {q.x, q.y, q.z, q.w};
+            double u[4][3];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {  // the hi word: the point the pass increments are taken from
+                const float4 hh = st.u0h[id[a]];
+                u[a][0] = hh.x;
+                u[a][1] = hh.y;
+                u[a][2] = hh.z;
+            }
+            const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+            const double dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+            Kin<double> k;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc)
+                    k.G[3 * r + cc] = (u[1][r] - u[0][r]) * dinv[cc] + (u[2][r] - u[0][r]) * dinv[3 + cc] +
+                                      (u[3][r] - u[0][r]) * dinv[6 + cc];
+            kinematics(k);
+            double P[9];
+            pk1_neohookean<double>(k, (double)r1.w, (double)r2.w, P);
+            // corner c: -svol P w_c (w_c = row c-1 of Dm^-1, w_0 = -sum of rows)
+            double w[3];
+#pragma unroll
+            for (int qq = 0; qq < 3; ++qq)
+                w[qq] = c == 0 ? -(dinv[qq] + dinv[3 + qq] + dinv[6 + qq]) : dinv[3 * (c - 1) + qq];
+            const double sv = (double)r0.w;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) b[d] += -sv * (P[3 * d] * w[0] + P[3 * d + 1] * w[1] + P[3 * d + 2] * w[2]);
+        }
+    }
+    float hi[3], lo[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        hi[d] = (float)b[d];
+        lo[d] = (float)(b[d] - (double)hi[d]);
+    }
+    st.bh[i] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    st.bl[i] = make_float4(lo[0], lo[1], lo[2], 0.f);
 }
 
 // ------------------------------------------------------------ helpers
@@ -594,6 +654,10 @@ cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, De
     cudaError_t e = launch_tet_only(s, m, p, st, material);
     if (e != cudaSuccess) return e;
     return launch_node_only(s, m, p, st);
+}
+cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    k_ref_force<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st);
+    return cudaGetLastError();
 }
 cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user) {
     k_epilogue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, pad2user);

@@ -52,7 +52,11 @@ struct pbs_handle {
     DevBuf<float4> row0, row1, row2, info, rest4;
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
     // device state
-    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag;
+    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl;
+    // learned warm start
+    DevBuf<float> ws_theta, ws_stats;  // NPARAM; feat mean 24, feat std 24, out std 3
+    bool ws_enabled = false;
+    int sms = 148;
     DevBuf<float> tf, hd, staging, staging2;
     DevBuf<double2> tpart;
     DevBuf<double> npart;
@@ -79,6 +83,7 @@ struct pbs_handle {
         DevState s;
         s.uh = uh.p; s.ul = ul.p; s.dd = dd.p; s.oh = oh.p; s.ol = ol.p; s.u0h = u0h.p; s.u0l = u0l.p;
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
+        s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
         return s;
     }
@@ -88,11 +93,12 @@ struct pbs_handle {
         DevBuf<int4> *i4[] = {&tets, &tslot};
         for (auto b : i4) b->release();
         DevBuf<float4> *f4[] = {&row0, &row1, &row2, &info, &rest4, &uh, &ul, &dd, &oh, &ol, &u0h, &u0l, &th, &tl,
-                                &v, &vold, &ext, &diag};
+                                &v, &vold, &ext, &diag, &hist1, &hist2, &bh, &bl};
         for (auto b : f4) b->release();
         DevBuf<int> *ii[] = {&inc_ptr, &inc, &tblk_inst, &nblk_inst, &pad2user, &tet_user, &node_state, &bad, &active,
                              &staging_ids};
         for (auto b : ii) b->release();
+        ws_theta.release(); ws_stats.release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
         if (h_active) cudaFreeHost(h_active);
         if (h_ctl) cudaFreeHost(h_ctl);
@@ -126,6 +132,7 @@ static void to_dev_params(const pbs_step_params &p, DevParams &d) {
     d.clamp_cpu = p.energy_clamp == PBS_CLAMP_CPU ? 1 : 0;
     d.pass_cap = p.pass_cap > 0 ? p.pass_cap : p.max_iters + 16;
     d.energy_slack = p.energy_slack;
+    d.incremental = 0;  // set from the material by the handle
 }
 
 extern "C" {
@@ -211,6 +218,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     pbs_handle *h = new (std::nothrow) pbs_handle();
     if (!h) return PBS_E_OUT_OF_MEMORY;
     h->device = dev;
+    h->sms = prop.multiProcessorCount;
     h->N = N; h->T = T; h->B = B;
     h->density = d->density; h->gravity = d->gravity;
     pbs_default_params(&h->params);
@@ -235,6 +243,23 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         for (int i = nptr[b]; i < nptr[b + 1]; ++i) h->user2pad[i] = node_off[b] + (i - nptr[b]);
     }
     const int Np = pn, Tp = pt;
+    for (int b = 0; b < B; ++b) {  // mean edge length: cbrt(6 * mean |vol|)
+        double vs = 0.0;
+        for (int t = tptr[b]; t < tptr[b + 1]; ++t) {
+            const int *q = d->tets + 4 * (size_t)t;
+            double e[3][3];
+            for (int c = 0; c < 3; ++c)
+                for (int k = 0; k < 3; ++k) {
+                    int a = q[c + 1], o = q[0];
+                    if (a < 0 || a >= N || o < 0 || o >= N) { delete h; return PBS_E_BAD_MESH; }
+                    e[c][k] = (double)d->rest[3 * (size_t)a + k] - d->rest[3 * (size_t)o + k];
+                }
+            vs += std::fabs(e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                            e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0])) / 6.0;
+        }
+        const int nt = tptr[b + 1] - tptr[b];
+        ctl[b].ell = nt > 0 ? (float)std::cbrt(6.0 * vs / nt) : 1.0f;
+    }
     h->Np = Np; h->Tp = Tp; h->n_tblk = Tp / BLOCK; h->n_nblk = Np / BLOCK;
     h->h_pad2user.assign(Np, -1);
     for (int i = 0; i < N; ++i) h->h_pad2user[h->user2pad[i]] = i;
@@ -307,6 +332,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->oh.alloc(Np)); CKC(h->ol.alloc(Np)); CKC(h->u0h.alloc(Np)); CKC(h->u0l.alloc(Np));
     CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
     CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
+    CKC(h->hist1.alloc(Np)); CKC(h->hist2.alloc(Np)); CKC(h->bh.alloc(Np)); CKC(h->bl.alloc(Np));
     // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
@@ -333,7 +359,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     {
         DevBuf<float4> *zero[] = {&h->uh, &h->ul, &h->dd};
         for (auto b : zero) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * 2 * (size_t)Np, s));
-        DevBuf<float4> *zero1[] = {&h->oh, &h->ol, &h->u0h, &h->u0l, &h->th, &h->tl};
+        DevBuf<float4> *zero1[] = {&h->oh, &h->ol, &h->u0h, &h->u0l, &h->th, &h->tl, &h->hist1, &h->hist2, &h->bh,
+                                   &h->bl};
         for (auto b : zero1) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * (size_t)Np, s));
     }
     CKC(cudaMemsetAsync(h->bad.p, 0, sizeof(int), s));
@@ -395,6 +422,7 @@ int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lam
     CK(e);
     if (h->material != model) h->graph_valid = false;
     h->material = model;
+    h->dparams.incremental = model == PBS_MATERIAL_NEOHOOKEAN ? 1 : 0;
     return PBS_OK;
 }
 
@@ -404,6 +432,7 @@ int pbs_set_params(pbs_handle *h, const pbs_step_params *p) {
     if (rc != PBS_OK) return rc;
     h->params = *p;
     to_dev_params(h->params, h->dparams);
+    h->dparams.incremental = h->material == PBS_MATERIAL_NEOHOOKEAN ? 1 : 0;
     h->graph_valid = false;
     return PBS_OK;
 }
@@ -445,6 +474,12 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
     CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
+    CK(launch_ref_force(s, m, h->dparams, st));
+    if (h->ws_enabled) {
+        CK(launch_ws_gref(s, m, h->dparams, st, h->material));
+        CK(launch_ws_predict(s, m, h->dparams, st, h->ws_theta.p, h->ws_stats.p, h->ws_stats.p + 24, h->ws_stats.p + 48,
+                             h->hd.p, h->sms));
+    }
     // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
     // of chunk j-1 while chunk j runs, so the device never idles on the poll.
     const int max_chunks = (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES;
@@ -475,6 +510,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
         S.iterations = std::max(S.iterations, c.k);
         S.rejections += c.rejections;
         S.converged += c.converged;
+        S.warm_start_used += c.ws_used;
         if (c.status != PBS_OK && S.status == PBS_OK) S.status = c.status;
         if (c.status == PBS_E_NONFINITE) S.status = PBS_E_NONFINITE;
     }
@@ -548,6 +584,57 @@ int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float
     return PBS_OK;
 }
 
+int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean, const float *feat_std,
+                       const float *out_std, int enabled) {
+    if (!h) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    if (!enabled) {
+        h->ws_enabled = false;
+        return PBS_OK;
+    }
+    const int np = pbs_mlp_param_count();
+    if (!theta || !feat_mean || !feat_std || !out_std) return PBS_E_INVALID_ARG;
+    for (int i = 0; i < np; ++i)
+        if (!std::isfinite(theta[i])) return PBS_E_INVALID_ARG;
+    for (int i = 0; i < 24; ++i)
+        if (!std::isfinite(feat_mean[i]) || !(feat_std[i] > 0.f)) return PBS_E_INVALID_ARG;
+    for (int i = 0; i < 3; ++i)
+        if (!(out_std[i] > 0.f)) return PBS_E_INVALID_ARG;
+    if (!h->ws_theta.p) CK(h->ws_theta.alloc(np));
+    if (!h->ws_stats.p) CK(h->ws_stats.alloc(51));
+    std::vector<float> st(51);
+    std::memcpy(st.data(), feat_mean, 24 * sizeof(float));
+    std::memcpy(st.data() + 24, feat_std, 24 * sizeof(float));
+    std::memcpy(st.data() + 48, out_std, 3 * sizeof(float));
+    CK(cudaMemcpy(h->ws_theta.p, theta, sizeof(float) * np, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->ws_stats.p, st.data(), sizeof(float) * 51, cudaMemcpyHostToDevice));
+    h->ws_enabled = true;
+    return PBS_OK;
+}
+
+int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init) {
+    if (!h || !features) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    DevMesh m = h->mesh();
+    DevState st = h->state();
+    if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
+    CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
+    CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
+    DevBuf<float> out;
+    CK(out.alloc(24 * (size_t)h->N));
+    cudaError_t e = launch_ws_features(s, m, h->dparams, st, h->hd.p, h->pad2user.p, out.p);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(features, out.p, sizeof(float) * 24 * (size_t)h->N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && x_init) e = launch_pack_positions(s, m, h->uh.p, h->ul.p, h->pad2user.p, h->staging.p);
+    if (e == cudaSuccess && x_init)
+        e = cudaMemcpyAsync(x_init, h->staging.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    out.release();
+    CK(e);
+    return PBS_OK;
+}
+
 int pbs_get_stream(pbs_handle *h, void **stream) {
     if (!h || !stream) return PBS_E_INVALID_ARG;
     *stream = (void *)h->stream;
@@ -569,6 +656,7 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
     if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
+    if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
     for (int i = 0; i < passes && e == cudaSuccess; ++i) {
         e = launch_tet_only(s, m, p, st, h->material);

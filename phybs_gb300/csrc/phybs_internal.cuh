@@ -49,6 +49,7 @@ struct DevParams {
     int clamp_cpu;
     int pass_cap;
     float energy_slack;  // reject only if E > E_old + slack * 2^-24 * sqrt(sum e^2)
+    int incremental;     // neo-Hookean: passes evaluate P(F) - P(F0) against an FP64 force at the step start
 };
 
 // What the node kernel does in a pass (decided by the tet kernel's last block
@@ -63,6 +64,10 @@ struct __align__(16) InstCtl {
     unsigned int counter_t, counter_n;
     float alpha, rho, omega;
     int force_check;  // RESTART control: a non-finite residual makes the next pass a line-search pass
+    int g0_fixed;     // g0 was set before iteration 0 (the plain guess's residual, warm start on)
+    int ws_used;      // this step started from the learned guess
+    float ell;        // mean edge length of the instance (feature scale)
+    int pad3;
     double energy, energy_old, g0, ratio;
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
@@ -84,6 +89,9 @@ struct DevState {
     float4 *uh, *ul, *dd;  // [2][Np] each
     float4 *oh, *ol, *u0h, *u0l, *th, *tl;
     float4 *v, *vold, *ext, *diag;
+    float4 *hist1, *hist2;  // displacement of the last step and of the one before
+    float4 *bh, *bl;        // per node (hi, lo): elastic force at the step start (incremental mode)
+                            // plus body_force_scale * (external + gravity)
     float *tf, *hd;
     double2 *tpart;
     double *npart;
@@ -114,7 +122,21 @@ __device__ __host__ __forceinline__ void chebyshev_schedule(const DevParams &p, 
     }
 }
 
-// Launchers (kernels.cu)
+__device__ __forceinline__ float node_ell(const DevMesh &m, const DevState &st, int i) {
+    return st.ctl[m.nblk_inst[i / BLOCK]].ell;
+}
+__device__ __forceinline__ int node_ctl_ws(const DevMesh &m, const DevState &st, int i) {
+    return st.ctl[m.nblk_inst[i / BLOCK]].ws_used;
+}
+
+// Launchers (kernels.cu, warmstart.cu)
+cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
+cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
+cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *theta,
+                              const float *feat_mean, const float *feat_std, const float *out_std, float *tetF,
+                              int sms);
+cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
+                               const int *pad2user, float *out);
 cudaError_t launch_rest(cudaStream_t s, const DevMesh &m, const double *rest_pad, float density, float4 *row0,
                         float4 *row1, float4 *row2, double *tmass, int *bad);
 cudaError_t launch_mass(cudaStream_t s, const DevMesh &m, const double *tmass, const int *state, float gravity,

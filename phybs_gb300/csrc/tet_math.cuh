@@ -127,6 +127,49 @@ template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T
         }
 }
 
+// dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, where the current state
+// k has G = G0 + dG and k0 is the step's start.  With P = mu F + (lambda ln J -
+// mu) F^-T:
+//   dP = mu dG - (lambda ln J - mu) F0^-T dG^T F^-T + lambda (ln J - ln J0) F0^-T
+// (F^-T - F0^-T = -F0^-T dF^T F^-T), ln J - ln J0 = log1p(dJ / J0) and
+//   dJ = cof(F0) : dG + F0 : cof(dG) + det dG
+// -- no term subtracts the two states' O(1) quantities, so dP is accurate to
+// FP32 relative to itself rather than to P.
+template <typename T>
+__device__ __forceinline__ void pk1_neohookean_delta(const Kin<T> &k0, const Kin<T> &k, const T dG[9], T mu, T lambda,
+                                                     T dP[9]) {
+    T F0iT[9], FiT[9], cofdG[9];
+    inv_transpose<T>(k0, F0iT);
+    cofactor3<T>(dG, cofdG);
+    const T J0 = T(1) + k0.d;
+    T dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const T cof0 = ((i == j) ? T(1) + k0.tr : T(0)) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
+            const T F0 = ((i == j) ? T(1) : T(0)) + k0.G[3 * i + j];
+            dJ += cof0 * dG[3 * i + j] + F0 * cofdG[3 * i + j];
+        }
+    const T dl = log1p_t<T>(dJ / J0);
+    const T lnJ = k0.lnJ + dl;
+    inv_transpose<T>(k, FiT);  // F^-T of the current state (k)
+    // M = F0^-T dG^T F^-T
+    T A[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A[3 * i + j] = F0iT[3 * i] * dG[3 * j] + F0iT[3 * i + 1] * dG[3 * j + 1] + F0iT[3 * i + 2] * dG[3 * j + 2];
+    const T c1 = lambda * lnJ - mu, c2 = lambda * dl;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const T M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
+            dP[3 * i + j] = mu * dG[3 * i + j] - c1 * M + c2 * F0iT[3 * i + j];
+        }
+}
+
 // phi(d) = d - log1p(d) >= 0, by its Taylor series where that is exact to FP32.
 template <typename T> __device__ __forceinline__ T phi_log1p(T d) {
     if (fabs(d) < T(0.1)) {

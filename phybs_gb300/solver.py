@@ -145,6 +145,23 @@ class DescentSolver:
         L.check(L.lib().pbs_profile_kernels(self._h, C.c_int(passes), C.byref(a), C.byref(b)), "pbs_profile_kernels")
         return a.value, b.value
 
+    def warm_start_features(self, ext=None):
+        """Raw 24 features per node for the next step, and the plain initial guess."""
+        feats = np.empty((self.n, 24), np.float32)
+        xin = np.empty((self.n, 3), np.float32)
+        e = _f32(ext, (-1, 3)) if ext is not None else None
+        L.check(L.lib().pbs_warm_start_features(self._h, _ptr(e), _ptr(feats), _ptr(xin)), "pbs_warm_start_features")
+        return feats, xin
+
+    def set_warm_start(self, model=None):
+        """Install a WarmStartModel (or switch the warm start off with None)."""
+        if model is None:
+            L.check(L.lib().pbs_set_warm_start(self._h, None, None, None, None, C.c_int(0)), "pbs_set_warm_start")
+            return
+        th, fm, fs, os_ = (_f32(model.theta), _f32(model.feat_mean), _f32(model.feat_std), _f32(model.out_std))
+        L.check(L.lib().pbs_set_warm_start(self._h, _ptr(th), _ptr(fm), _ptr(fs), _ptr(os_), C.c_int(1)),
+                "pbs_set_warm_start")
+
     def velocities(self):
         v = np.empty((self.n, 3), np.float32)
         vo = np.empty((self.n, 3), np.float32)

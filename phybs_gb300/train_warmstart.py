@@ -1,0 +1,143 @@
+"""Generate training frames with the plain GPU descent and train the warm start.
+
+    python -m phybs_gb300.train_warmstart --frames 4000 --out phybs_gb300/warmstart_model.npz
+
+Scenarios (seeded; sizes reduced from the benchmark meshes so that thousands of
+frames solve in minutes):
+  * box: the 1M-tet box's geometry (0.25 x 0.25 x 0.4 m, 5-tet split, +-0.1
+    jitter) at 20x20x32 cubes, E = 10^U(4, 6), Poisson 0.4, top face pinned
+    and the bottom face pulled to a random 1.2-1.8x stretch over 20-40 frames,
+    optional initial twist, gravity;
+  * ellipsoid: the voxelised ellipsoid at half resolution, E = 10^U(4.5, 5.5),
+    Poisson 0.3-0.45, released from a random 30-120 degree twist, bottom 5%
+    pinned, gravity.
+Every frame is solved to |g| <= 1e-4 |g_0| by the plain descent.  A sample of
+free nodes per frame gives (features, (x* - x_init) / l) pairs.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+from . import meshes as M
+from .solver import DescentSolver, make_params
+from .warmstart import MLPTrainer, WarmStartModel
+from . import _lib as L
+
+ALPHA0 = 0.5
+RHO = 0.9998
+
+
+def residual_params(max_iters=8000):
+    return make_params("gpu_reference", h=1 / 30, tol=1e-4, max_iters=max_iters, control=L.PBS_CONTROL_RESTART,
+                       energy_slack=16.0, alpha0=ALPHA0, profile=((10, RHO),))
+
+
+def mean_edge(mesh) -> float:
+    v = np.abs(M.signed_volumes(mesh.rest, mesh.tets))
+    return float(np.cbrt(6.0 * v.mean()))
+
+
+def box_scenario(rng, nx=20, ny=20, nz=32):
+    e = float(10 ** rng.uniform(4.0, 6.0))
+    m = M.box_mesh(nx, ny, nz, edge=0.25 / nx, jitter=0.1, seed=int(rng.integers(1 << 30)), young=e, poisson=0.4,
+                   pin="both")
+    z = m.rest[:, 2]
+    bottom = np.nonzero(z <= z.min() + 1e-9)[0].astype(np.int32)
+    length = float(z.max() - z.min())
+    stretch = float(rng.uniform(0.2, 0.8))
+    ramp = int(rng.integers(20, 41))
+    twist = float(rng.uniform(0.0, np.pi / 4)) if rng.uniform() < 0.5 else 0.0
+    x0 = M.twist_positions(m.rest, twist, axis=2) if twist else None
+    if x0 is not None:
+        x0[m.pins] = m.rest[m.pins]
+
+    def boundary(solver, f):
+        x = m.rest[bottom].copy()
+        x[:, 2] -= np.float32(stretch * length * min((f + 1) / ramp, 1.0))
+        solver.set_node_positions(bottom, x)
+
+    return m, x0, boundary
+
+
+def ellipsoid_scenario(rng):
+    e = float(10 ** rng.uniform(4.5, 5.5))
+    nu = float(rng.uniform(0.3, 0.45))
+    m = M.ellipsoid_mesh(10, 10, 20, cell=0.02, jitter=0.15, seed=int(rng.integers(1 << 30)), young=e, poisson=nu)
+    twist = float(rng.uniform(np.pi / 6, 2 * np.pi / 3))
+    x0 = M.twist_positions(m.rest, twist, axis=2)
+    x0[m.pins] = m.rest[m.pins]
+    return m, x0, None
+
+
+def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int = 60, verbose: bool = True):
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    done = 0
+    t0 = time.time()
+    while done < frames:
+        kind = "box" if rng.uniform() < 0.6 else "ellipsoid"
+        m, x0, boundary = box_scenario(rng) if kind == "box" else ellipsoid_scenario(rng)
+        ell = mean_edge(m)
+        s = DescentSolver(m, positions=x0, params=residual_params())
+        free = np.nonzero(m.pin_mask() == 0)[0]
+        n_frames = min(frames_per_run, frames - done)
+        for f in range(n_frames):
+            if boundary is not None:
+                boundary(s, f)
+            feats, xin = s.warm_start_features()
+            s.step(raise_on_error=False)
+            if s.last_status != 0 or not s.stats()["converged"]:
+                continue
+            xs = s.positions()
+            pick = rng.choice(free, size=min(nodes_per_frame, free.size), replace=False)
+            X.append(feats[pick])
+            Y.append((xs[pick] - xin[pick]) / ell)
+        done += n_frames
+        s.close()
+        if verbose:
+            print(f"  {done}/{frames} frames ({kind}, {m.n_tets} tets), {time.time() - t0:.0f}s", flush=True)
+    return np.concatenate(X).astype(np.float32), np.concatenate(Y).astype(np.float32)
+
+
+def fit(X, Y, steps=3000, batch=8192, lr=1e-3, seed=0, verbose=True) -> WarmStartModel:
+    mean = X.mean(0)
+    std = np.maximum(X.std(0), 1e-6)
+    out_std = np.maximum(Y.std(0), 1e-9)
+    Xs = ((X - mean) / std).astype(np.float32)
+    Ys = (Y / out_std).astype(np.float32)
+    t = MLPTrainer(seed=seed)
+    t.set_data(Xs, Ys)
+    l1 = t.train(int(steps * 0.7), batch=batch, lr=lr, seed=seed)
+    l2 = t.train(steps - int(steps * 0.7), batch=batch, lr=lr * 0.2, seed=seed + 1)
+    if verbose:
+        print(f"  loss {l1[:10].mean():.4f} -> {l1[-10:].mean():.4f} -> {l2[-10:].mean():.4f}", flush=True)
+    model = WarmStartModel(t.params, mean.astype(np.float32), std.astype(np.float32), out_std.astype(np.float32))
+    t.close()
+    return model
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--frames", type=int, default=4000)
+    ap.add_argument("--nodes-per-frame", type=int, default=512)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--data", default=None, help="save the generated (X, Y) here")
+    args = ap.parse_args()
+    t0 = time.time()
+    X, Y = generate(args.frames, args.nodes_per_frame, args.seed)
+    print(f"data: {X.shape[0]} samples in {time.time() - t0:.0f}s", flush=True)
+    if args.data:
+        np.savez_compressed(args.data, X=X, Y=Y)
+    model = fit(X, Y, steps=args.steps, seed=args.seed)
+    from .warmstart import DEFAULT_MODEL
+    model.save(args.out or DEFAULT_MODEL)
+    print(f"saved {args.out or DEFAULT_MODEL} ({time.time() - t0:.0f}s total)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""Learned warm start: the per-node MLP, its trainer, and data generation.
+
+The network (24 -> 64 -> 64 -> 64 -> 3, GELU, BF16 tensor-core kernels with
+FP32 accumulation; phybs_gb300/csrc/mlp*.cu{h}) predicts each node's
+correction to the inertial guess x~ + warm_start h (v - v_old) from local
+features.  The descent solver applies it before the first iteration and keeps
+the plain guess whenever the prediction's energy is higher (the plain descent
+is both the fallback and the judge); every step still iterates to the same
+residual tolerance, measured against the plain guess's gradient.
+
+Features per node (in this order; lengths are divided by the instance's mean
+edge length l and velocities by l / h):
+  0-2   velocity v
+  3-5   last displacement x_n - x_{n-1}
+  6-8   the one before, x_{n-1} - x_{n-2}
+  9-11  inertial-guess offset x_init - x~ = warm_start h (v - v_old)
+  12    log10 E (mean over incident tets)
+  13    Poisson ratio (mean over incident tets)
+  14-22 mean deformation gradient F - I over incident tets at x~
+  23    mean det F - 1 over incident tets at x~
+Target: (x* - x_init) / l, x* the step's converged positions.
+Features and targets are standardised with statistics stored alongside the
+parameters.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+from . import _lib as L
+
+N_FEATURES = 24
+N_OUT = 3
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class MLPTrainer:
+    """GPU trainer / evaluator of the warm-start network (pbs_mlp_* C ABI)."""
+
+    def __init__(self, theta=None, seed: int = 0):
+        self._t = C.c_void_p()
+        th = _f32(theta) if theta is not None else None
+        L.check(L.lib().pbs_mlp_create(C.byref(self._t), _ptr(th), C.c_ulonglong(seed)), "pbs_mlp_create")
+        self.n_params = L.lib().pbs_mlp_param_count()
+
+    def close(self):
+        if self._t:
+            L.lib().pbs_mlp_destroy(self._t)
+            self._t = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        L.check(L.lib().pbs_mlp_get_params(self._t, _ptr(out)), "pbs_mlp_get_params")
+        return out
+
+    @params.setter
+    def params(self, theta):
+        L.check(L.lib().pbs_mlp_set_params(self._t, _ptr(_f32(theta))), "pbs_mlp_set_params")
+
+    def forward(self, X) -> np.ndarray:
+        X = _f32(X).reshape(-1, N_FEATURES)
+        Y = np.empty((X.shape[0], N_OUT), np.float32)
+        L.check(L.lib().pbs_mlp_forward(self._t, _ptr(X), C.c_int(X.shape[0]), _ptr(Y)), "pbs_mlp_forward")
+        return Y
+
+    def gradient(self, X, Y):
+        X = _f32(X).reshape(-1, N_FEATURES)
+        Y = _f32(Y).reshape(-1, N_OUT)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_float()
+        L.check(L.lib().pbs_mlp_gradient(self._t, _ptr(X), _ptr(Y), C.c_int(X.shape[0]), _ptr(g), C.byref(loss)),
+                "pbs_mlp_gradient")
+        return float(loss.value), g
+
+    def set_data(self, X, Y):
+        X = _f32(X).reshape(-1, N_FEATURES)
+        Y = _f32(Y).reshape(-1, N_OUT)
+        L.check(L.lib().pbs_mlp_set_data(self._t, _ptr(X), _ptr(Y), C.c_int(X.shape[0])), "pbs_mlp_set_data")
+
+    def train(self, steps: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        losses = np.empty(max(steps, 1), np.float32)
+        L.check(L.lib().pbs_mlp_train(self._t, C.c_int(steps), C.c_int(batch), C.c_float(lr), C.c_ulonglong(seed),
+                                      _ptr(losses)), "pbs_mlp_train")
+        return losses[:steps]
+
+
+@dataclasses.dataclass
+class WarmStartModel:
+    """Network parameters plus the feature / target standardisation."""
+
+    theta: np.ndarray
+    feat_mean: np.ndarray
+    feat_std: np.ndarray
+    out_std: np.ndarray
+
+    def save(self, path):
+        np.savez(path, theta=self.theta, feat_mean=self.feat_mean, feat_std=self.feat_std, out_std=self.out_std)
+
+    @classmethod
+    def load(cls, path):
+        with np.load(path) as z:
+            return cls(z["theta"].astype(np.float32), z["feat_mean"].astype(np.float32),
+                       z["feat_std"].astype(np.float32), z["out_std"].astype(np.float32))
+
+
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "warmstart_model.npz")

@@ -1,0 +1,119 @@
+"""GPU tests of the learned warm start inside the descent step: features,
+the energy judge / fallback, the unchanged residual bar, and the gain of a
+trained network over the plain inertial guess."""
+import os
+
+import numpy as np
+import pytest
+
+from phybs_gb300 import meshes as M
+from phybs_gb300.solver import DescentSolver
+from phybs_gb300.train_warmstart import box_scenario, residual_params, mean_edge
+from phybs_gb300.warmstart import DEFAULT_MODEL, WarmStartModel, MLPTrainer
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from phybs_gb300.build import build
+    build()
+
+
+def _pull_case(seed=123, n=(10, 10, 16)):
+    rng = np.random.default_rng(seed)
+    return box_scenario(rng, *n)
+
+
+def test_features_match_definition():
+    """Feature columns against a numpy evaluation of their definition."""
+    m, x0, boundary = _pull_case()
+    s = DescentSolver(m, positions=x0, params=residual_params())
+    for f in range(3):
+        boundary(s, f)
+        s.step()
+    feats, xin = s.warm_start_features()
+    v, vo = s.velocities()
+    ell = mean_edge(m)
+    h = 1 / 30
+    free = m.pin_mask() == 0
+    np.testing.assert_allclose(feats[free, 0:3], v[free] * h / ell, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(feats[free, 9:12], 0.2 * h * (v - vo)[free] / ell, rtol=1e-4, atol=1e-6)
+    x = s.positions()
+    np.testing.assert_allclose(xin, x + h * v + 0.2 * h * (v - vo), atol=2e-6)
+    # mean incident J - 1 at x~ = x + h v
+    xt = (x + h * v).astype(np.float64)
+    J = M.signed_volumes(xt, m.tets) / M.signed_volumes(m.rest, m.tets)
+    acc = np.zeros(m.n_nodes)
+    cnt = np.zeros(m.n_nodes)
+    for c in range(4):
+        np.add.at(acc, m.tets[:, c], J - 1)
+        np.add.at(cnt, m.tets[:, c], 1)
+    np.testing.assert_allclose(feats[:, 23], acc / cnt, atol=2e-5)
+    s.close()
+
+
+def test_zero_network_keeps_plain_result():
+    """A network whose output is zero reproduces the plain guess: the step
+    result equals the plain run bit for bit, and the residual reference is the
+    plain guess's either way."""
+    m, x0, boundary = _pull_case()
+    theta = np.zeros(MLPTrainer(seed=0).n_params, np.float32)
+    model = WarmStartModel(theta, np.zeros(24, np.float32), np.ones(24, np.float32), np.ones(3, np.float32))
+    a = DescentSolver(m, positions=x0, params=residual_params())
+    b = DescentSolver(m, positions=x0, params=residual_params())
+    b.set_warm_start(model)
+    for f in range(3):
+        boundary(a, f)
+        boundary(b, f)
+        ia, ib = a.step(), b.step()
+        assert ia == ib
+        assert b.stats()["warm_start_used"] == 1
+    assert np.array_equal(a.positions(), b.positions())
+    a.close()
+    b.close()
+
+
+def test_bad_prediction_falls_back():
+    """A network that predicts a large wrong correction raises the energy; the
+    judge rejects it and the step equals the plain one."""
+    m, x0, boundary = _pull_case()
+    theta = np.zeros(MLPTrainer(seed=0).n_params, np.float32)
+    theta[-3:] = 5.0  # constant output bias: every node moved by 5 edge lengths
+    model = WarmStartModel(theta, np.zeros(24, np.float32), np.ones(24, np.float32), np.ones(3, np.float32))
+    a = DescentSolver(m, positions=x0, params=residual_params())
+    b = DescentSolver(m, positions=x0, params=residual_params())
+    b.set_warm_start(model)
+    for f in range(2):
+        boundary(a, f)
+        boundary(b, f)
+        assert a.step() == b.step()
+        assert b.stats()["warm_start_used"] == 0
+    assert np.array_equal(a.positions(), b.positions())
+    a.close()
+    b.close()
+
+
+@pytest.mark.skipif(not os.path.exists(DEFAULT_MODEL), reason="no trained model committed")
+def test_trained_network_gains_over_plain():
+    """On a held-out pull scenario (seed not used in training) the trained
+    network cuts the iterations to the same residual bar, is used on most
+    frames, and both runs end within 1e-3 of the bbox diagonal of each other."""
+    model = WarmStartModel.load(DEFAULT_MODEL)
+    m, x0, boundary = _pull_case(seed=987654, n=(20, 20, 32))
+    a = DescentSolver(m, positions=x0, params=residual_params())
+    b = DescentSolver(m, positions=x0, params=residual_params())
+    b.set_warm_start(model)
+    ia, ib, used = [], [], 0
+    for f in range(12):
+        boundary(a, f)
+        boundary(b, f)
+        ia.append(a.step())
+        ib.append(b.step())
+        assert a.stats()["converged"] == 1 and b.stats()["converged"] == 1
+        used += b.stats()["warm_start_used"]
+    assert sum(ib[2:]) < sum(ia[2:]), (ia, ib)
+    assert used >= 6
+    assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-3
+    a.close()
+    b.close()
