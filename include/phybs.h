@@ -191,7 +191,8 @@ int pbs_get_stream(pbs_handle *h, void **stream);
 /* Time the two kernels of one descent pass separately with CUDA events on the
  * handle's stream: runs `passes` passes from the current state (the state is
  * left as it was) and returns the mean milliseconds per launch of the per-tet
- * kernel and of the per-node kernel. */
+ * kernel and of the per-node kernel.  Fails with PBS_E_NONFINITE when an
+ * instance stopped before the last pass (its launches would time no work). */
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms);
 
 /* ------------------------------------------------------------------------

@@ -162,6 +162,7 @@ __global__ void k_prologue(DevMesh m, DevParams p, DevState st, const float *ext
     st.tl[i] = make_float4(tl[0], tl[1], tl[2], 0.f);
     st.uh[i] = make_float4(xh[0], xh[1], xh[2], 0.f);
     st.ul[i] = make_float4(xl[0], xl[1], xl[2], 0.f);
+    st.ub[i] = make_float4(xh[0], xh[1], xh[2], 0.f);
     st.dd[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ext_user) e = make_float4(ext_user[3 * (size_t)u], ext_user[3 * (size_t)u + 1], ext_user[3 * (size_t)u + 2], 0.f);
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         const float svol = r0.w, mu = r1.w, lambda = r2.w;
         Kin<float> kin;
         float f[12];
-        pass_forces<MATERIAL>(p, U, st.u0h, q, dinv, svol, mu, lambda, kin, f);
+        pass_forces<MATERIAL>(p, U, st.ub, q, dinv, svol, mu, lambda, kin, f);
         const int4 sl = m.tslot[t];
         const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
         float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
@@ -440,10 +441,10 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     if (c.done) atomicSub(st.active, 1);
 }
 
-// Per-step node constant b = f_el(u0) (incremental mode, FP64) +
+// Per-step node constant b = f_el(u_base) (incremental mode, FP64) +
 // body_force_scale (external + gravity), split into FP32 (hi, lo).  Each
-// node evaluates its incident tets' full neo-Hookean stress at the step
-// start's FP32 displacement (the base of the passes' increments) in FP64 and
+// node evaluates its incident tets' full neo-Hookean stress at the base (the
+// step's initial guess, whose increments the passes evaluate) in FP64 and
 // sums its corner forces in the canonical order.
 __global__ void k_ref_force(DevMesh m, DevParams p, DevState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -460,8 +461,8 @@ __global__ void k_ref_force(DevMesh m, DevParams p, DevState st) {
             const int id[4] = {q.x, q.y, q.z, q.w};
             double u[4][3];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {  // the hi word: the point the pass increments are taken from
-                const float4 hh = st.u0h[id[a]];
+            for (int a = 0; a < 4; ++a) {
+                const float4 hh = st.ub[id[a]];
                 u[a][0] = hh.x;
                 u[a][1] = hh.y;
                 u[a][2] = hh.z;

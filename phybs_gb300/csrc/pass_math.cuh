@@ -7,9 +7,12 @@
 namespace pbs {
 
 // Corner forces of a tet in a descent pass.  Neo-Hookean with p.incremental:
-// the increment dP = P(F) - P(F0) against the step-start displacement U0
-// (the node kernel adds the FP64 force at U0 held in bh/bl); otherwise the
-// full stress.  kin returns the current kinematics (energy, Jacobi diagonal).
+// the increment dP = P(F) - P(F0) against the base displacement U0 (the
+// step's initial guess; the node kernel adds the FP64 force at the base held
+// in bh/bl), so the summed corner terms scale with the guess's error rather
+// than with the stress and the residual has no FP32 floor above ~1e-6 of its
+// initial value; otherwise the full stress.  kin returns the current
+// kinematics (energy, Jacobi diagonal).
 template <int MATERIAL>
 __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U, const float4 *U0, const int4 &q,
                                             const float dinv[9], float svol, float mu, float lambda, Kin<float> &kin,

@@ -52,7 +52,7 @@ struct pbs_handle {
     DevBuf<float4> row0, row1, row2, info, rest4;
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
     // device state
-    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl;
+    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl, ub;
     // learned warm start
     DevBuf<float> ws_theta, ws_stats;  // NPARAM; feat mean 24, feat std 24, out std 3
     bool ws_enabled = false;
@@ -83,7 +83,7 @@ struct pbs_handle {
         DevState s;
         s.uh = uh.p; s.ul = ul.p; s.dd = dd.p; s.oh = oh.p; s.ol = ol.p; s.u0h = u0h.p; s.u0l = u0l.p;
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
-        s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p;
+        s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
         return s;
     }
@@ -93,7 +93,7 @@ struct pbs_handle {
         DevBuf<int4> *i4[] = {&tets, &tslot};
         for (auto b : i4) b->release();
         DevBuf<float4> *f4[] = {&row0, &row1, &row2, &info, &rest4, &uh, &ul, &dd, &oh, &ol, &u0h, &u0l, &th, &tl,
-                                &v, &vold, &ext, &diag, &hist1, &hist2, &bh, &bl};
+                                &v, &vold, &ext, &diag, &hist1, &hist2, &bh, &bl, &ub};
         for (auto b : f4) b->release();
         DevBuf<int> *ii[] = {&inc_ptr, &inc, &tblk_inst, &nblk_inst, &pad2user, &tet_user, &node_state, &bad, &active,
                              &staging_ids};
@@ -333,6 +333,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
     CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
     CKC(h->hist1.alloc(Np)); CKC(h->hist2.alloc(Np)); CKC(h->bh.alloc(Np)); CKC(h->bl.alloc(Np));
+    CKC(h->ub.alloc(Np));
     // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
@@ -360,7 +361,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         DevBuf<float4> *zero[] = {&h->uh, &h->ul, &h->dd};
         for (auto b : zero) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * 2 * (size_t)Np, s));
         DevBuf<float4> *zero1[] = {&h->oh, &h->ol, &h->u0h, &h->u0l, &h->th, &h->tl, &h->hist1, &h->hist2, &h->bh,
-                                   &h->bl};
+                                   &h->bl, &h->ub};
         for (auto b : zero1) CKC(cudaMemsetAsync(b->p, 0, sizeof(float4) * (size_t)Np, s));
     }
     CKC(cudaMemsetAsync(h->bad.p, 0, sizeof(int), s));
@@ -675,6 +676,12 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     }
     for (auto &x : ev) cudaEventDestroy(x);
     CK(e);
+    // every pass must have done real work: an instance that finished early
+    // (non-finite state, line-search stop) would leave no-op launches behind
+    std::vector<InstCtl> c(h->B);
+    CK(cudaMemcpy(c.data(), h->ctl.p, sizeof(InstCtl) * h->B, cudaMemcpyDeviceToHost));
+    for (const InstCtl &x : c)
+        if (x.tet_end > x.tet_begin && (x.passes < passes || x.status != PBS_OK)) return PBS_E_NONFINITE;
     *tet_ms = tt / passes;
     *node_ms = tn / passes;
     return PBS_OK;

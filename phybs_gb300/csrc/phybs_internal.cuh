@@ -49,7 +49,8 @@ struct DevParams {
     int clamp_cpu;
     int pass_cap;
     float energy_slack;  // reject only if E > E_old + slack * 2^-24 * sqrt(sum e^2)
-    int incremental;     // neo-Hookean: passes evaluate P(F) - P(F0) against an FP64 force at the step start
+    int incremental;     // neo-Hookean: passes evaluate P(F) - P(F_base) against an FP64 force at the
+                         // step's initial guess (the base)
 };
 
 // What the node kernel does in a pass (decided by the tet kernel's last block
@@ -90,7 +91,8 @@ struct DevState {
     float4 *oh, *ol, *u0h, *u0l, *th, *tl;
     float4 *v, *vold, *ext, *diag;
     float4 *hist1, *hist2;  // displacement of the last step and of the one before
-    float4 *bh, *bl;        // per node (hi, lo): elastic force at the step start (incremental mode)
+    float4 *ub;             // base displacement of the increments: the step's initial guess (hi word)
+    float4 *bh, *bl;        // per node (hi, lo): elastic force at the base (incremental mode)
                             // plus body_force_scale * (external + gravity)
     float *tf, *hd;
     double2 *tpart;

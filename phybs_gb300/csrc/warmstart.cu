@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(BLOCK) k_ws_force(DevMesh m, DevParams p, DevS
     const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
     Kin<float> kin;
     float f[12];
-    pass_forces<MATERIAL>(p, U, st.u0h, q, dinv, r0.w, r1.w, r2.w, kin, f);
+    pass_forces<MATERIAL>(p, U, st.ub, q, dinv, r0.w, r1.w, r2.w, kin, f);
     const int4 sl = m.tslot[t];
     float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
     tf4[sl.x] = make_float4(f[0], f[1], f[2], 0.f);
@@ -73,13 +73,17 @@ __global__ void __launch_bounds__(BLOCK) k_ws_gref(DevMesh m, DevParams p, DevSt
     const float4 info = m.info[i];
     double r2 = 0.0;
     if (info.z == 0.f) {
+        // incremental mode: the plain guess is the base, so its elastic force is
+        // all in b; otherwise sum the full corner forces of k_ws_force
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        const float4 *tf4 = reinterpret_cast<const float4 *>(st.tf);
-        for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
-            const float4 f = tf4[j];
-            fx += f.x;
-            fy += f.y;
-            fz += f.z;
+        if (!p.incremental) {
+            const float4 *tf4 = reinterpret_cast<const float4 *>(st.tf);
+            for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+                const float4 f = tf4[j];
+                fx += f.x;
+                fy += f.y;
+                fz += f.z;
+            }
         }
         const float4 uh = st.uh[i], ul = st.ul[i], th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
         const float mh = info.x * p.h2inv;
@@ -322,6 +326,7 @@ __global__ void k_ws_select(DevMesh m, DevState st) {
     if (!node_ctl_ws(m, st, i)) return;
     st.uh[i] = st.uh[m.Np + i];
     st.ul[i] = st.ul[m.Np + i];
+    st.ub[i] = st.uh[m.Np + i];
 }
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
@@ -329,8 +334,6 @@ static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
     if (material == PBS_MATERIAL_STRETCH)
         k_ws_force<PBS_MATERIAL_STRETCH><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, st.uh);
-    else
-        k_ws_force<PBS_MATERIAL_NEOHOOKEAN><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, st.uh);
     k_ws_gref<<<m.n_nblk, BLOCK, 0, s>>>(m, p, st);
     return cudaGetLastError();
 }
@@ -345,7 +348,9 @@ cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams 
     k_ws_infer<<<blocks, 128, 0, s>>>(m, p, st, tetF, net);
     k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
     k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_ref_force(s, m, p, st);  // the base moved where the learned guess was kept
 }
 
 cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
