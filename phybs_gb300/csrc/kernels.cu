@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState 
         const float svol = r0.w, mu = r1.w, lambda = r2.w;
         Kin<float> kin;
         float f[12];
-        pass_forces<MATERIAL>(p, U, st.ub, q, dinv, svol, mu, lambda, kin, f);
+        pass_forces<MATERIAL>(p, U, st.ul + cur, st.ub, q, dinv, svol, mu, lambda, kin, f);
         const int4 sl = m.tslot[t];
         const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
         float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
