@@ -185,6 +185,28 @@ int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, f
  * deterministic gather at the given positions (NULL = current). */
 int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag);
 
+/* Elastic forces (3*N, the caller's node order) at the given positions (3*N),
+ * as pbs_eval_nodes computes them, for callers that cannot allocate device
+ * memory in the call: a frame loop that must not stall (cudaMalloc and
+ * cudaFree synchronise the whole device) or a host that keeps all device
+ * memory in its own pool.  No counterpart in the reference.
+ *   - positions and forces are DEVICE pointers on the handle's device; the
+ *     two kernels are enqueued on the handle's stream (pbs_get_stream) and
+ *     the call returns without waiting for them.
+ *   - allocates nothing: the per-tet corner-force scratch is one fixed
+ *     24 MiB array in the library's device image, which bounds the mesh to
+ *     PBS_EVAL_STATIC_MAX_TETS tets after padding (each instance's tet count
+ *     rounded up to 256); larger handles fail with PBS_E_CAPACITY, host
+ *     pointers with PBS_E_INVALID_ARG.
+ *   - the first call on a device looks up that array's address (with the
+ *     device current) and keeps it; make this first call before any stream
+ *     capture.
+ *   - every call on a device shares the array: calls whose kernels overlap
+ *     on the GPU (different streams with no ordering between them) race and
+ *     corrupt each other's forces.  Nothing in it needs to start at zero. */
+#define PBS_EVAL_STATIC_MAX_TETS 524288
+int pbs_eval_nodes_static(pbs_handle *h, const float *positions, float *forces);
+
 /* The CUDA stream (cudaStream_t) every call of this handle launches on, so a
  * caller can order its own work or record timing events on it. */
 int pbs_get_stream(pbs_handle *h, void **stream);

@@ -886,3 +886,11 @@ int pbs_stiffness_pattern(int n_nodes, int n_tets, const int *tets, int *nnz, in
 }
 
 }  // extern "C"
+
+void pbs::handle_view(const pbs_handle *h, HandleView *v) {
+    v->device = h->device;
+    v->stream = h->stream;
+    v->material = h->material;
+    v->mesh = h->mesh();
+    v->pad2user = h->pad2user.p;
+}

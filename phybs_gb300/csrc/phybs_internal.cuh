@@ -167,3 +167,19 @@ cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, con
                           float *force_user, float *hd_user);
 
 }  // namespace pbs
+
+struct pbs_handle;
+
+namespace pbs {
+
+// What an entry point outside the handle's own source file reads of it.
+struct HandleView {
+    int device;
+    cudaStream_t stream;
+    int material;
+    DevMesh mesh;
+    const int *pad2user;  // padded node -> caller's node index, -1 for padding
+};
+void handle_view(const pbs_handle *h, HandleView *v);
+
+}  // namespace pbs
