@@ -163,7 +163,16 @@ int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old);
  * writes TetMesh::getNodes() directly (pinned nodes stay where they are put
  * within a step, DescentOptimize.cpp:109-113 / CUDAInterface.cu:578-585). */
 int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float *xyz);
-/* CUDAInterface::reset (CUDAInterface.cu:776): rest positions, zero velocities. */
+/* Initial guess for the next pbs_step only (3*N positions, caller order;
+ * pinned nodes keep their prescribed positions).  The step treats it as it
+ * treats the learned warm start's prediction: the guess is kept only if its
+ * energy is not higher than the inertial guess's, and the step still iterates
+ * to the same residual bar, measured against the inertial guess's gradient.
+ * No counterpart in the reference, whose first iterate is always the
+ * inertial guess. */
+int pbs_set_guess(pbs_handle *h, const float *positions);
+/* CUDAInterface::reset (CUDAInterface.cu:776): rest positions, zero velocities
+ * (and an empty displacement history for the learned warm start). */
 int pbs_reset(pbs_handle *h);
 int pbs_get_stats(pbs_handle *h, pbs_stats *s);
 
@@ -213,8 +222,10 @@ int pbs_get_stream(pbs_handle *h, void **stream);
 /* Time the two kernels of one descent pass separately with CUDA events on the
  * handle's stream: runs `passes` passes from the current state (the state is
  * left as it was) and returns the mean milliseconds per launch of the per-tet
- * kernel and of the per-node kernel.  Fails with PBS_E_NONFINITE when an
- * instance stopped before the last pass (its launches would time no work). */
+ * kernel and of the per-node kernel.  Fails when an instance stopped before
+ * the last pass (its launches would time no work): with its status
+ * (PBS_E_NONFINITE), or PBS_E_ITER_CAP when it stopped for another reason;
+ * pbs_get_stats then describes that instance. */
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms);
 
 /* ------------------------------------------------------------------------
@@ -242,7 +253,8 @@ int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long
 /* Install (enabled != 0) or switch off the warm start on a solver handle.
  * theta: pbs_mlp_param_count() values; feat_mean / feat_std: the 24 feature
  * standardisation constants; out_std: the 3 output scales (the network
- * predicts correction / (out_std * mean edge length)).  Each pbs_step then
+ * predicts correction / (out_std * s), s the node's motion scale, see
+ * pbs_warm_start_features).  Each pbs_step then
  * evaluates the network on the plain guess's features, keeps the predicted
  * guess for an instance only if its energy is not higher than the plain
  * guess's, and measures the residual tolerance against the plain guess's
@@ -250,9 +262,12 @@ int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long
 int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean, const float *feat_std,
                        const float *out_std, int enabled);
 /* The 24 raw (unstandardised) features of every node for the next step with
- * external forces ext (or NULL), and the plain initial guess x~ + warm_start
- * h (v - v_old) (x_init, 3*N, may be NULL).  The state is not advanced. */
-int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init);
+ * external forces ext (or NULL), the plain initial guess x~ + warm_start
+ * h (v - v_old) (x_init, 3*N, may be NULL) and each node's motion scale
+ * s = |d1| + |d2| + 1e-4 l (scale, N, may be NULL; d1, d2 the node's last two
+ * displacements, l the instance's mean edge length), which divides the
+ * length features.  The state is not advanced. */
+int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init, float *scale);
 
 /* Node-node 3N x 3N stiffness pattern of the mesh, bit-identical to
  * IsotropicMaterial::allocateGlobalStiffnessMatrix (IsotropicMaterial.cpp:554-644):

@@ -1,0 +1,351 @@
+// The per-tet kernel of a descent pass, on chunks of tets.
+//
+// A chunk is a run of at most CHUNK_TETS tets of one instance, consecutive in
+// the Morton order of their centroids, that touches at most CHUNK_NODES
+// nodes.  One CTA per chunk:
+//   1. stages the chunk's nodes (u hi, u lo and the force base) in shared
+//      memory: each node is read once per chunk instead of once per corner;
+//   2. evaluates its tets (one thread per tet, CHUNK_TETS / CHUNK_THREADS tets
+//      a thread), streaming the per-tet rows in chunk order, and writes the 12
+//      corner forces to shared-memory slots, where a node's slots are
+//      contiguous in (tet, corner) order;
+//   3. sums each node's slots in that order into one partial per (node,
+//      chunk), written to part[] at the node's place for this chunk.
+// The node kernel adds a node's partials in chunk order.  No atomics touch a
+// force, so results are bit-reproducible run to run, and instances are
+// chunked on their own, so a packed batch gives each instance the bits it gets
+// alone.  Against one thread per tet writing 4 global slots, this moves the
+// corner forces through shared memory instead of HBM (64 B written and read
+// back per tet per pass) and replaces 4 gathers of 3 node words per tet with
+// one staged read per touched node.
+//
+// On line-search passes the CTA also adds the clamped tet energies and its
+// share of the instance's node energy terms (FP64, fixed order); the
+// instance's last chunk to finish decides accept / reject
+// (DescentOptimize.cpp:162-183) before any node moves.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <utility>
+#include <vector>
+
+#include "../../include/phybs.h"
+#include "pass_math.cuh"
+#include "phybs_internal.cuh"
+#include "tet_math.cuh"
+
+namespace pbs {
+
+// ------------------------------------------------------------ host: layout
+namespace {
+
+uint32_t spread10(uint32_t v) {  // 10 bits -> every third bit of 30
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+}  // namespace
+
+void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<double> &rest, std::vector<InstCtl> &ctl,
+                  ChunkLayout &out) {
+    out = ChunkLayout();
+    std::vector<int> stamp(Np, -1), lidx(Np, 0), n_part(Np, 0);
+    std::vector<std::pair<uint32_t, int>> order;
+    std::vector<int> ctets, lnodes, scount;
+    int tq = 0;
+    for (size_t b = 0; b < ctl.size(); ++b) {
+        InstCtl &C = ctl[b];
+        C.cblk_begin = (int)out.chunk.size();
+        double lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::numeric_limits<double>::max();
+            hi[d] = -std::numeric_limits<double>::max();
+        }
+        auto centroid = [&](int t, double c[3]) {
+            const int *q = &tets[t].x;
+            for (int d = 0; d < 3; ++d)
+                c[d] = 0.25 * (rest[3 * (size_t)q[0] + d] + rest[3 * (size_t)q[1] + d] + rest[3 * (size_t)q[2] + d] +
+                               rest[3 * (size_t)q[3] + d]);
+        };
+        for (int t = C.tet_begin; t < C.tet_end; ++t) {
+            double c[3];
+            centroid(t, c);
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], c[d]);
+                hi[d] = std::max(hi[d], c[d]);
+            }
+        }
+        order.clear();
+        for (int t = C.tet_begin; t < C.tet_end; ++t) {
+            double c[3];
+            centroid(t, c);
+            uint32_t code = 0;
+            for (int d = 0; d < 3; ++d) {
+                const double ext = hi[d] - lo[d];
+                const double f = ext > 0.0 ? (c[d] - lo[d]) / ext : 0.0;
+                const uint32_t v = (uint32_t)std::min(1023.0, std::max(0.0, std::floor(f * 1024.0)));
+                code |= spread10(v) << d;
+            }
+            order.emplace_back(code, t);
+        }
+        std::sort(order.begin(), order.end());
+        if (order.empty()) {  // an instance without tets still needs a CTA for its line-search decisions
+            out.chunk.push_back(make_int4(tq, 0, (int)out.lnode.size(), 0));
+            out.chunk_inst.push_back((int)b);
+        }
+        size_t pos = 0;
+        while (pos < order.size()) {
+            const int cid = (int)out.chunk.size();
+            ctets.clear();
+            lnodes.clear();
+            while (pos < order.size() && (int)ctets.size() < CHUNK_TETS) {
+                const int t = order[pos].second;
+                const int *q = &tets[t].x;
+                int add = 0;
+                for (int c = 0; c < 4; ++c) {
+                    bool seen = stamp[q[c]] == cid;
+                    for (int c2 = 0; c2 < c && !seen; ++c2) seen = q[c2] == q[c];
+                    add += !seen;
+                }
+                if ((int)lnodes.size() + add > CHUNK_NODES) break;
+                for (int c = 0; c < 4; ++c)
+                    if (stamp[q[c]] != cid) {
+                        stamp[q[c]] = cid;
+                        lnodes.push_back(q[c]);
+                    }
+                ctets.push_back(t);
+                ++pos;
+            }
+            std::sort(lnodes.begin(), lnodes.end());
+            const int nl = (int)lnodes.size(), nt = (int)ctets.size();
+            for (int j = 0; j < nl; ++j) lidx[lnodes[j]] = j;
+            scount.assign(nl + 1, 0);
+            for (int t : ctets)
+                for (int c = 0; c < 4; ++c) scount[lidx[(&tets[t].x)[c]] + 1]++;
+            for (int j = 0; j < nl; ++j) scount[j + 1] += scount[j];
+            const int l0 = (int)out.lnode.size();
+            for (int j = 0; j < nl; ++j) {
+                out.lnode.push_back(lnodes[j]);
+                out.lsptr.push_back(scount[j]);
+                n_part[lnodes[j]]++;
+            }
+            for (int lt = 0; lt < nt; ++lt) {
+                const int *q = &tets[ctets[lt]].x;
+                unsigned short loc[4], sl[4];
+                for (int c = 0; c < 4; ++c) {
+                    loc[c] = (unsigned short)lidx[q[c]];
+                    sl[c] = (unsigned short)scount[loc[c]]++;
+                }
+                out.qloc.push_back(make_ushort4(loc[0], loc[1], loc[2], loc[3]));
+                out.qslot.push_back(make_ushort4(sl[0], sl[1], sl[2], sl[3]));
+                out.qperm.push_back(ctets[lt]);
+            }
+            out.chunk.push_back(make_int4(tq, nt, l0, nl));
+            out.chunk_inst.push_back((int)b);
+            out.max_local = std::max(out.max_local, nl);
+            tq += nt;
+        }
+        C.cblk_end = (int)out.chunk.size();
+    }
+    // node -> partials, in chunk order
+    out.pptr.assign(Np + 1, 0);
+    for (int i = 0; i < Np; ++i) out.pptr[i + 1] = out.pptr[i] + n_part[i];
+    std::vector<int> fill(out.pptr.begin(), out.pptr.end() - 1);
+    out.lpidx.resize(out.lnode.size());
+    for (size_t j = 0; j < out.lnode.size(); ++j) out.lpidx[j] = fill[out.lnode[j]]++;
+}
+
+// ------------------------------------------------------------ device
+__global__ void k_pass_rows(int T, const int *qperm, const float4 *row0, const float4 *row1, const float4 *row2,
+                            float4 *q0, float4 *q1, float4 *q2) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= T) return;
+    const int t = qperm[j];
+    q0[j] = row0[t];
+    q1[j] = row1[t];
+    q2[j] = row2[t];
+}
+
+// Sums every local node's slots (in slot order) into its partial for this
+// chunk.
+__device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl, int nt, const float *sx,
+                                               const float *sy, const float *sz, float4 *out) {
+    for (int j = threadIdx.x; j < nl; j += CHUNK_THREADS) {
+        const int s0 = m.lsptr[l0 + j];
+        const int s1 = j + 1 < nl ? m.lsptr[l0 + j + 1] : 4 * nt;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int s = s0; s < s1; ++s) {
+            fx += sx[s];
+            fy += sy[s];
+            fz += sz[s];
+        }
+        out[m.lpidx[l0 + j]] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+template <int MATERIAL>
+__global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
+    extern __shared__ float4 smem4[];
+    float4 *s_uh = smem4, *s_ul = smem4 + CHUNK_NODES, *s_ub = smem4 + 2 * CHUNK_NODES;
+    float *s_x = reinterpret_cast<float *>(smem4 + 3 * CHUNK_NODES);
+    float *s_y = s_x + 4 * CHUNK_TETS, *s_z = s_y + 4 * CHUNK_TETS;
+    __shared__ double sh[CHUNK_THREADS / 32];
+    __shared__ int is_last;
+    const int c = blockIdx.x;
+    InstCtl *cp = st.ctl + m.chunk_inst[c];
+    if (cp->done) return;
+    const int k = cp->k;
+    const bool check = (k % p.ls_every) == 0 || cp->force_check;
+    const bool do_h = (k % p.hd_every) == 0;
+    const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
+    const size_t cur = (size_t)cp->par * m.Np;
+    const int4 cd = m.chunk[c];
+    const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
+    for (int j = threadIdx.x; j < nl; j += CHUNK_THREADS) {
+        const int g = m.lnode[l0 + j];
+        s_uh[j] = st.uh[cur + g];
+        s_ul[j] = st.ul[cur + g];
+        s_ub[j] = inc ? st.ub[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    double e = 0.0;
+    for (int lt = threadIdx.x; lt < nt; lt += CHUNK_THREADS) {
+        const int q = tq0 + lt;
+        const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
+        const ushort4 lc = m.qloc[q], sl = m.qslot[q];
+        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+        Kin<float> kin;
+        float f[12];
+        pass_forces_v<MATERIAL>(p, s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
+                                s_ul[lc.z], s_ul[lc.w], s_ub[lc.x], s_ub[lc.y], s_ub[lc.z], s_ub[lc.w], dinv, r0.w,
+                                r1.w, r2.w, kin, f);
+        const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            s_x[slot[cc]] = f[3 * cc];
+            s_y[slot[cc]] = f[3 * cc + 1];
+            s_z[slot[cc]] = f[3 * cc + 2];
+        }
+        if (check) e += (double)clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu);
+    }
+    __syncthreads();
+    chunk_partials(m, l0, nl, nt, s_x, s_y, s_z, st.part);
+    if (do_h) {  // Jacobi-diagonal refresh: the same slots carry the 12 diagonal terms
+        __syncthreads();
+        for (int lt = threadIdx.x; lt < nt; lt += CHUNK_THREADS) {
+            const int q = tq0 + lt;
+            const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
+            const ushort4 lc = m.qloc[q], sl = m.qslot[q];
+            const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+            Kin<float> kin;
+            float f[12], kd[12];
+            pass_forces_v<MATERIAL>(p, s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
+                                    s_ul[lc.z], s_ul[lc.w], s_ub[lc.x], s_ub[lc.y], s_ub[lc.z], s_ub[lc.w], dinv,
+                                    r0.w, r1.w, r2.w, kin, f);
+            hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
+            const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                s_x[slot[cc]] = kd[3 * cc];
+                s_y[slot[cc]] = kd[3 * cc + 1];
+                s_z[slot[cc]] = kd[3 * cc + 2];
+            }
+        }
+        __syncthreads();
+        chunk_partials(m, l0, nl, nt, s_x, s_y, s_z, st.parth);
+    }
+    if (!check) return;
+    // line-search pass: add this chunk's share of the instance's node terms
+    double e2 = e * e;
+    {
+        const int nb = cp->cblk_end - cp->cblk_begin;
+        const float4 *U = st.uh + cur;
+        for (int i = cp->node_begin + (c - cp->cblk_begin) * CHUNK_THREADS + threadIdx.x; i < cp->node_end;
+             i += nb * CHUNK_THREADS) {
+            const float4 info = m.info[i];
+            if (info.z != 0.f) continue;
+            const double en = node_energy(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+            e += en;
+            e2 += en * en;
+        }
+    }
+    const double se = block_sum(e, sh);
+    const double se2 = block_sum(e2, sh);
+    if (threadIdx.x == 0) {
+        st.cpart[c] = make_double2(se, se2);
+        __threadfence();
+        const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
+        is_last = (prev == (unsigned int)(cp->cblk_end - cp->cblk_begin - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // the instance's last chunk: fixed-order sums, then accept / reject
+    double E = 0.0, E2 = 0.0;
+    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += CHUNK_THREADS) {
+        const double2 v = __ldcg(st.cpart + j);
+        E += v.x;
+        E2 += v.y;
+    }
+    E = block_sum(E, sh);
+    E2 = block_sum(E2, sh);
+    if (threadIdx.x != 0) return;
+    InstCtl ci = *cp;
+    ci.counter_t = 0;
+    ci.energy = E;
+    // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
+    // error of order 2^-24 sqrt(sum e_i^2); slack 0 is the reference's strict test
+    const double tau = (double)p.energy_slack * 5.9604644775390625e-8 * sqrt(E2);
+    // RESTART control also treats a non-finite energy (a step that inverted
+    // tets) as a rejection; the reference control accepts it (NaN > E_old is
+    // false), and the step then ends with PBS_E_NONFINITE below
+    const bool bad = !isfinite(E) && p.control == PBS_CONTROL_RESTART;
+    if ((k != 0 && E > ci.energy_old + tau) || (bad && k != 0)) {
+        ci.action = ACT_RESTORE;
+        ci.alpha = (float)((double)ci.alpha * (double)p.alpha_shrink);
+        ci.rejections += 1;
+        if (p.control == PBS_CONTROL_REFERENCE) ci.iters -= k - p.ls_every;
+    } else {
+        ci.action = ACT_SAVE_STEP;
+        ci.energy_old = E;
+    }
+    ci.force_check = 0;
+    if (!isfinite(E) && !(bad && k != 0)) {
+        ci.status = PBS_E_NONFINITE;
+        ci.done = 1;
+    }
+    *cp = ci;
+    if (ci.done) atomicSub(st.active, 1);
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t prepare_chunk_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_tchunk<PBS_MATERIAL_NEOHOOKEAN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CHUNK_SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_tchunk<PBS_MATERIAL_STRETCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)CHUNK_SMEM);
+}
+
+cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const float4 *row0, const float4 *row1,
+                             const float4 *row2, float4 *q0, float4 *q1, float4 *q2) {
+    if (T <= 0) return cudaSuccess;
+    k_pass_rows<<<(T + 255) / 256, 256, 0, s>>>(T, qperm, row0, row1, row2, q0, q1, q2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
+    if (m.n_chunks <= 0) return cudaSuccess;
+    if (material == PBS_MATERIAL_STRETCH)
+        k_tchunk<PBS_MATERIAL_STRETCH><<<m.n_chunks, CHUNK_THREADS, CHUNK_SMEM, s>>>(m, p, st);
+    else
+        k_tchunk<PBS_MATERIAL_NEOHOOKEAN><<<m.n_chunks, CHUNK_THREADS, CHUNK_SMEM, s>>>(m, p, st);
+    return cudaGetLastError();
+}
+
+}  // namespace pbs

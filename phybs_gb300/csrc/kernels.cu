@@ -1,17 +1,18 @@
 // Device kernels of the descent time step (sm_103a).
 //
 // One descent iteration ("pass") is two launches:
-//   k_tet   one thread per tet: gathers the 4 corner displacements (float4),
-//           forms G, the first Piola-Kirchhoff stress and the 12 corner
-//           forces; on Hessian-refresh passes the 12 Jacobi-diagonal terms; on
+//   k_tchunk (chunks.cu) one CTA per chunk of tets: forms G, the first
+//           Piola-Kirchhoff stress and the 12 corner forces of every tet; on
+//           Hessian-refresh passes the 12 Jacobi-diagonal terms; on
 //           line-search passes the clamped tet energies plus the node energy
-//           terms, reduced in FP64.  The instance's last block to finish
-//           decides accept / reject (DescentOptimize.cpp:162-183) before any
-//           node moves.  Replaces computeForceKd (CUDAInterface.cu:495-568)
-//           and its 13-25 atomics per tet.
-//   k_node  one thread per node: sums its incident corner forces in the
-//           canonical (tet, corner) order -- no atomics, so forces are
-//           bit-reproducible -- forms the gradient, takes the Jacobi step with
+//           terms, reduced in FP64.  Corner terms are summed per node in
+//           shared memory into one partial per (node, chunk).  The instance's
+//           last chunk to finish decides accept / reject
+//           (DescentOptimize.cpp:162-183) before any node moves.  Replaces
+//           computeForceKd (CUDAInterface.cu:495-568) and its 13-25 atomics
+//           per tet.
+//   k_node  one thread per node: adds its partials in chunk order -- no
+//           atomics, so forces are bit-reproducible -- forms the gradient, takes the Jacobi step with
 //           Chebyshev extrapolation (updateNodesNextIter + updateChebyshev,
 //           CUDAInterface.cu:572-623) in step form, d' = (omega-1) d +
 //           omega alpha delta, u' = u + d' in compensated FP32, or restores the
@@ -25,29 +26,6 @@
 #include "tet_math.cuh"
 
 namespace pbs {
-
-// ------------------------------------------------------------ reductions
-// Deterministic block sum: fixed shuffle tree per warp, then warp 0 sums the
-// warp totals in warp order.  Result valid in thread 0.
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ double block_sum(double v, double *sh) {
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (w == 0) {
-        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-        r = warp_sum(r);
-    }
-    return r;
-}
 
 // ------------------------------------------------------------ rest state
 // Dm^-1 and det Dm / 6 in FP64 from the rest positions (TetMesh.cpp:190-204,
@@ -190,118 +168,6 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-// Energy terms of one free node: 1/2 m |u - u~|^2 / h^2 - g_y u_y - f_ext . u
-// (DescentOptimize.cpp:128-142 / CUDAInterface.cu:589-597), measured from the
-// rest shape so that no large constant rides along in the sum.
-__device__ __forceinline__ double node_energy(const DevState &st, const float4 &info, const float4 &uh,
-                                              const float4 &ul, int i, float h2inv) {
-    const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
-    const float dx = (uh.x - th.x) + (ul.x - tl.x);
-    const float dy = (uh.y - th.y) + (ul.y - tl.y);
-    const float dz = (uh.z - th.z) + (ul.z - tl.z);
-    const double uy = (double)uh.y + ul.y;
-    return 0.5 * (double)info.x * ((double)dx * dx + (double)dy * dy + (double)dz * dz) * (double)h2inv -
-           (double)info.y * uy - ((double)ex.x * ((double)uh.x + ul.x) + (double)ex.y * uy + (double)ex.z * ((double)uh.z + ul.z));
-}
-
-template <int MATERIAL>
-__global__ void __launch_bounds__(BLOCK) k_tet(DevMesh m, DevParams p, DevState st) {
-    __shared__ double sh[BLOCK / 32];
-    __shared__ int is_last;
-    const int b = blockIdx.x;
-    InstCtl *cp = st.ctl + m.tblk_inst[b];
-    if (cp->done) return;
-    const int k = cp->k;
-    const bool check = (k % p.ls_every) == 0 || cp->force_check;
-    const bool do_h = (k % p.hd_every) == 0;
-    const size_t cur = (size_t)cp->par * m.Np;
-    const float4 *U = st.uh + cur;
-    const int t = b * BLOCK + threadIdx.x;
-    double e = 0.0;
-    const int4 q = m.tets[t];
-    if (q.x >= 0) {
-        const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
-        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-        const float svol = r0.w, mu = r1.w, lambda = r2.w;
-        Kin<float> kin;
-        float f[12];
-        pass_forces<MATERIAL>(p, U, st.ul + cur, st.ub, q, dinv, svol, mu, lambda, kin, f);
-        const int4 sl = m.tslot[t];
-        const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
-        float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) tf4[slot[c]] = make_float4(f[3 * c], f[3 * c + 1], f[3 * c + 2], 0.f);
-        if (check) e = (double)clamp_energy(energy_density<float>(kin, mu, lambda) * fabsf(svol), p.clamp_cpu);
-        if (do_h) {
-            float kd[12];
-            hessian_diag(kin, mu, lambda, dinv, svol, kd);
-            float4 *hd4 = reinterpret_cast<float4 *>(st.hd);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) hd4[slot[c]] = make_float4(kd[3 * c], kd[3 * c + 1], kd[3 * c + 2], 0.f);
-        }
-    }
-    if (!check) return;
-    // line-search pass: add this block's share of the instance's node terms
-    double e2 = e * e;
-    {
-        const int nb = cp->tblk_end - cp->tblk_begin;
-        for (int i = cp->node_begin + (b - cp->tblk_begin) * BLOCK + threadIdx.x; i < cp->node_end; i += nb * BLOCK) {
-            const float4 info = m.info[i];
-            if (info.z != 0.f) continue;
-            const double en = node_energy(st, info, U[i], st.ul[cur + i], i, p.h2inv);
-            e += en;
-            e2 += en * en;
-        }
-    }
-    const double se = block_sum(e, sh);
-    const double se2 = block_sum(e2, sh);
-    if (threadIdx.x == 0) {
-        st.tpart[b] = make_double2(se, se2);
-        __threadfence();
-        const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
-        is_last = (prev == (unsigned int)(cp->tblk_end - cp->tblk_begin - 1));
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    // the instance's last block: fixed-order sums, then accept / reject
-    double E = 0.0, E2 = 0.0;
-    for (int j = cp->tblk_begin + threadIdx.x; j < cp->tblk_end; j += BLOCK) {
-        const double2 v = __ldcg(st.tpart + j);
-        E += v.x;
-        E2 += v.y;
-    }
-    E = block_sum(E, sh);
-    E2 = block_sum(E2, sh);
-    if (threadIdx.x != 0) return;
-    InstCtl c = *cp;
-    c.counter_t = 0;
-    c.energy = E;
-    // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
-    // error of order 2^-24 sqrt(sum e_i^2); slack 0 is the reference's strict test
-    const double tau = (double)p.energy_slack * 5.9604644775390625e-8 * sqrt(E2);
-    // RESTART control also treats a non-finite energy (a step that inverted
-    // tets) as a rejection; the reference control accepts it (NaN > E_old is
-    // false), and the step then ends with PBS_E_NONFINITE below
-    const bool bad = !isfinite(E) && p.control == PBS_CONTROL_RESTART;
-    if ((k != 0 && E > c.energy_old + tau) || (bad && k != 0)) {
-        c.action = ACT_RESTORE;
-        c.alpha = (float)((double)c.alpha * (double)p.alpha_shrink);
-        c.rejections += 1;
-        if (p.control == PBS_CONTROL_REFERENCE) c.iters -= k - p.ls_every;
-    } else {
-        c.action = ACT_SAVE_STEP;
-        c.energy_old = E;
-    }
-    c.force_check = 0;
-    if (!isfinite(E) && !(bad && k != 0)) {
-        c.status = PBS_E_NONFINITE;
-        c.done = 1;
-    }
-    *cp = c;
-    if (c.done) atomicSub(st.active, 1);
-}
-
 __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState st) {
     __shared__ double sh[BLOCK / 32];
     __shared__ int is_last;
@@ -338,19 +204,17 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
             }
             if (info.z == 0.f) {
                 float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
-                // this node's slots are contiguous and in canonical (tet, corner) order
-                const int a = m.inc_ptr[i], e_ = m.inc_ptr[i + 1];
-                const float4 *tf4 = reinterpret_cast<const float4 *>(st.tf);
+                // this node's per-chunk partial sums, in chunk order
+                const int a = m.pptr[i], e_ = m.pptr[i + 1];
                 for (int j = a; j < e_; ++j) {
-                    const float4 f = tf4[j];
+                    const float4 f = st.part[j];
                     fx += f.x;
                     fy += f.y;
                     fz += f.z;
                 }
                 if (do_h) {
-                    const float4 *hd4 = reinterpret_cast<const float4 *>(st.hd);
                     for (int j = a; j < e_; ++j) {
-                        const float4 q = hd4[j];
+                        const float4 q = st.parth[j];
                         hx += q.x;
                         hy += q.y;
                         hz += q.z;
@@ -638,13 +502,6 @@ cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, Inst
 cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
                             const int *pad2user) {
     k_prologue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, ext_user, pad2user);
-    return cudaGetLastError();
-}
-cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
-    if (material == PBS_MATERIAL_STRETCH)
-        k_tet<PBS_MATERIAL_STRETCH><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
-    else
-        k_tet<PBS_MATERIAL_NEOHOOKEAN><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
     return cudaGetLastError();
 }
 cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {

@@ -6,6 +6,43 @@
 
 namespace pbs {
 
+// Deterministic block sum: fixed shuffle tree per warp, then warp 0 sums the
+// warp totals in warp order.  Result valid in thread 0; sh holds one double
+// per warp.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// Energy terms of one free node: 1/2 m |u - u~|^2 / h^2 - g_y u_y - f_ext . u
+// (DescentOptimize.cpp:128-142 / CUDAInterface.cu:589-597), measured from the
+// rest shape so that no large constant rides along in the sum.
+__device__ __forceinline__ double node_energy(const DevState &st, const float4 &info, const float4 &uh,
+                                              const float4 &ul, int i, float h2inv) {
+    const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
+    const float dx = (uh.x - th.x) + (ul.x - tl.x);
+    const float dy = (uh.y - th.y) + (ul.y - tl.y);
+    const float dz = (uh.z - th.z) + (ul.z - tl.z);
+    const double uy = (double)uh.y + ul.y;
+    return 0.5 * (double)info.x * ((double)dx * dx + (double)dy * dy + (double)dz * dz) * (double)h2inv -
+           (double)info.y * uy - ((double)ex.x * ((double)uh.x + ul.x) + (double)ex.y * uy + (double)ex.z * ((double)uh.z + ul.z));
+}
+
 // Corner forces of a tet in a descent pass.  Neo-Hookean with p.incremental:
 // the increment dP = P(F) - P(F0) against the base displacement U0 (the
 // step's initial guess; the node kernel adds the FP64 force at the base held
@@ -26,17 +63,17 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, 0.f);
 }
 
+// Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
 template <int MATERIAL>
-__device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U, const float4 *UL, const float4 *U0,
-                                            const int4 &q, const float dinv[9], float svol, float mu, float lambda,
-                                            Kin<float> &kin, float f[12]) {
-    const float4 x0 = U[q.x], x1 = U[q.y], x2 = U[q.z], x3 = U[q.w];
-    const float4 l0 = UL[q.x], l1 = UL[q.y], l2 = UL[q.z], l3 = UL[q.w];
+__device__ __forceinline__ void pass_forces_v(const DevParams &p, const float4 &x0, const float4 &x1, const float4 &x2,
+                                              const float4 &x3, const float4 &l0, const float4 &l1, const float4 &l2,
+                                              const float4 &l3, const float4 &a0, const float4 &a1, const float4 &a2,
+                                              const float4 &a3, const float dinv[9], float svol, float mu,
+                                              float lambda, Kin<float> &kin, float f[12]) {
     float P[9];
     if (MATERIAL != PBS_MATERIAL_STRETCH && p.incremental) {
         disp_gradient<float>(x0, x1, x2, x3, dinv, kin.G);
         kinematics(kin);
-        const float4 a0 = U0[q.x], a1 = U0[q.y], a2 = U0[q.z], a3 = U0[q.w];
         Kin<float> k0;
         disp_gradient<float>(a0, a1, a2, a3, dinv, k0.G);
         kinematics(k0);
@@ -55,6 +92,17 @@ __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U,
         else pk1_neohookean<float>(kin, mu, lambda, P);
     }
     corner_forces(P, dinv, svol, f);
+}
+
+template <int MATERIAL>
+__device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U, const float4 *UL, const float4 *U0,
+                                            const int4 &q, const float dinv[9], float svol, float mu, float lambda,
+                                            Kin<float> &kin, float f[12]) {
+    const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    pass_forces_v<MATERIAL>(p, U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w],
+                            inc ? U0[q.x] : z, inc ? U0[q.y] : z, inc ? U0[q.z] : z, inc ? U0[q.w] : z, dinv, svol,
+                            mu, lambda, kin, f);
 }
 
 }  // namespace pbs

@@ -51,11 +51,19 @@ struct pbs_handle {
     DevBuf<int4> tets, tslot;
     DevBuf<float4> row0, row1, row2, info, rest4;
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
+    // pass layout (chunks of tets)
+    int n_chunks = 0;
+    DevBuf<int4> chunk;
+    DevBuf<int> chunk_inst, qperm, lnode, lsptr, lpidx, pptr;
+    DevBuf<ushort4> qloc, qslot;
+    DevBuf<float4> qrow0, qrow1, qrow2, part, parth;
+    DevBuf<double2> cpart;
     // device state
     DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl, ub;
     // learned warm start
     DevBuf<float> ws_theta, ws_stats;  // NPARAM; feat mean 24, feat std 24, out std 3
     bool ws_enabled = false;
+    bool guess_pending = false;  // parity 1 holds a caller guess for the next step
     int sms = 148;
     DevBuf<float> tf, hd, staging, staging2;
     DevBuf<double2> tpart;
@@ -77,6 +85,9 @@ struct pbs_handle {
         m.tets = tets.p; m.row0 = row0.p; m.row1 = row1.p; m.row2 = row2.p;
         m.inc_ptr = inc_ptr.p; m.inc = inc.p; m.tslot = tslot.p; m.info = info.p; m.rest = rest4.p;
         m.tblk_inst = tblk_inst.p; m.nblk_inst = nblk_inst.p;
+        m.n_chunks = n_chunks; m.chunk = chunk.p; m.chunk_inst = chunk_inst.p;
+        m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qloc = qloc.p; m.qslot = qslot.p;
+        m.lnode = lnode.p; m.lsptr = lsptr.p; m.lpidx = lpidx.p; m.pptr = pptr.p;
         return m;
     }
     DevState state() const {
@@ -85,6 +96,7 @@ struct pbs_handle {
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
         s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
+        s.cpart = cpart.p; s.part = part.p; s.parth = parth.p;
         return s;
     }
     void release() {
@@ -99,6 +111,11 @@ struct pbs_handle {
                              &staging_ids};
         for (auto b : ii) b->release();
         ws_theta.release(); ws_stats.release();
+        chunk.release(); qloc.release(); qslot.release(); cpart.release();
+        DevBuf<int> *ci[] = {&chunk_inst, &qperm, &lnode, &lsptr, &lpidx, &pptr};
+        for (auto b : ci) b->release();
+        DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
+        for (auto b : cf) b->release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
         if (h_active) cudaFreeHost(h_active);
         if (h_ctl) cudaFreeHost(h_ctl);
@@ -314,6 +331,10 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         rest4[ip] = make_float4(d->rest[3 * (size_t)i], d->rest[3 * (size_t)i + 1], d->rest[3 * (size_t)i + 2], 0.f);
     }
     h->h_rest.assign(d->rest, d->rest + 3 * (size_t)N);
+    ChunkLayout cl;
+    build_chunks(Np, tets_pad, rest_pad, ctl, cl);
+    h->n_chunks = (int)cl.chunk.size();
+    const size_t L = cl.lnode.size();
 
     auto fail = [&](int code) { h->release(); delete h; return code; };
 #define CKC(x) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) return fail(e__ == cudaErrorMemoryAllocation ? PBS_E_OUT_OF_MEMORY : PBS_E_CUDA); } while (0)
@@ -339,7 +360,24 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
+    CKC(h->chunk.alloc(h->n_chunks)); CKC(h->chunk_inst.alloc(h->n_chunks)); CKC(h->cpart.alloc(h->n_chunks));
+    CKC(h->qperm.alloc(T)); CKC(h->qloc.alloc(T)); CKC(h->qslot.alloc(T));
+    CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T));
+    CKC(h->lnode.alloc(L)); CKC(h->lsptr.alloc(L)); CKC(h->lpidx.alloc(L)); CKC(h->pptr.alloc(Np + 1));
+    CKC(h->part.alloc(L)); CKC(h->parth.alloc(L));
+    CKC(prepare_chunk_kernels());
     cudaStream_t s = h->stream;
+    CKC(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * h->n_chunks, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->chunk_inst.p, cl.chunk_inst.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->qperm.p, cl.qperm.data(), sizeof(int) * T, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->qloc.p, cl.qloc.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->qslot.p, cl.qslot.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->lnode.p, cl.lnode.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->lsptr.p, cl.lsptr.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->lpidx.p, cl.lpidx.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CKC(cudaMemcpyAsync(h->pptr.p, cl.pptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
+    CKC(cudaMemsetAsync(h->part.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
+    CKC(cudaMemsetAsync(h->parth.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
     CKC(cudaMemcpyAsync(h->tets.p, tets_pad.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->tslot.p, tslot.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->inc_ptr.p, iptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
@@ -418,6 +456,9 @@ int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lam
     cudaError_t e = cudaMemcpyAsync(buf.p, mu, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(buf.p + count, lambda, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = launch_set_lame(h->stream, h->Tp, h->tets.p, buf.p, buf.p + count, count, h->row1.p, h->row2.p, h->tet_user.p);
+    if (e == cudaSuccess)  // the pass kernel's copy of the rows, in chunk order
+        e = launch_pass_rows(h->stream, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0.p, h->qrow1.p,
+                             h->qrow2.p);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     buf.release();
     CK(e);
@@ -476,10 +517,14 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     CK(launch_ref_force(s, m, h->dparams, st));
-    if (h->ws_enabled) {
+    if (h->ws_enabled || h->guess_pending) {
         CK(launch_ws_gref(s, m, h->dparams, st, h->material));
-        CK(launch_ws_predict(s, m, h->dparams, st, h->ws_theta.p, h->ws_stats.p, h->ws_stats.p + 24, h->ws_stats.p + 48,
-                             h->hd.p, h->sms));
+        if (h->guess_pending)
+            CK(launch_ws_choose(s, m, h->dparams, st));
+        else
+            CK(launch_ws_predict(s, m, h->dparams, st, h->ws_theta.p, h->ws_stats.p, h->ws_stats.p + 24,
+                                 h->ws_stats.p + 48, h->hd.p, h->sms));
+        h->guess_pending = false;
     }
     // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
     // of chunk j-1 while chunk j runs, so the device never idles on the poll.
@@ -613,7 +658,7 @@ int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean
     return PBS_OK;
 }
 
-int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init) {
+int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init, float *scale) {
     if (!h || !features) return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
     cudaStream_t s = h->stream;
@@ -624,15 +669,26 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
     CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     DevBuf<float> out;
-    CK(out.alloc(24 * (size_t)h->N));
-    cudaError_t e = launch_ws_features(s, m, h->dparams, st, h->hd.p, h->pad2user.p, out.p);
+    CK(out.alloc(25 * (size_t)h->N));
+    float *sc = out.p + 24 * (size_t)h->N;
+    cudaError_t e = launch_ws_features(s, m, h->dparams, st, h->hd.p, h->pad2user.p, out.p, sc);
     if (e == cudaSuccess) e = cudaMemcpyAsync(features, out.p, sizeof(float) * 24 * (size_t)h->N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && scale) e = cudaMemcpyAsync(scale, sc, sizeof(float) * h->N, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && x_init) e = launch_pack_positions(s, m, h->uh.p, h->ul.p, h->pad2user.p, h->staging.p);
     if (e == cudaSuccess && x_init)
         e = cudaMemcpyAsync(x_init, h->staging.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     out.release();
     CK(e);
+    return PBS_OK;
+}
+
+int pbs_set_guess(pbs_handle *h, const float *positions) {
+    if (!h || !positions) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = upload_positions(h, positions, h->uh.p + h->Np, h->ul.p + h->Np);
+    if (rc != PBS_OK) return rc;
+    h->guess_pending = true;
     return PBS_OK;
 }
 
@@ -680,8 +736,17 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     // (non-finite state, line-search stop) would leave no-op launches behind
     std::vector<InstCtl> c(h->B);
     CK(cudaMemcpy(c.data(), h->ctl.p, sizeof(InstCtl) * h->B, cudaMemcpyDeviceToHost));
-    for (const InstCtl &x : c)
-        if (x.tet_end > x.tet_begin && (x.passes < passes || x.status != PBS_OK)) return PBS_E_NONFINITE;
+    for (const InstCtl &x : c) {
+        if (x.tet_end == x.tet_begin) continue;
+        if (x.status != PBS_OK || x.passes < passes) {  // pbs_get_stats then describes the stopped instance
+            pbs_stats S{};
+            S.passes = x.passes; S.iterations = x.k; S.rejections = x.rejections; S.converged = x.converged;
+            S.status = x.status; S.alpha = x.alpha; S.rho = x.rho; S.omega = x.omega; S.energy = x.energy;
+            S.residual_ratio = x.ratio;
+            h->stats = S;
+            return x.status != PBS_OK ? x.status : PBS_E_ITER_CAP;
+        }
+    }
     *tet_ms = tt / passes;
     *node_ms = tn / passes;
     return PBS_OK;
@@ -712,6 +777,9 @@ int pbs_reset(pbs_handle *h) {
     CK(cudaMemsetAsync(h->u0l.p, 0, sizeof(float4) * h->Np, h->stream));
     CK(cudaMemsetAsync(h->v.p, 0, sizeof(float4) * h->Np, h->stream));
     CK(cudaMemsetAsync(h->vold.p, 0, sizeof(float4) * h->Np, h->stream));
+    // the warm start's displacement history starts over with the motion
+    CK(cudaMemsetAsync(h->hist1.p, 0, sizeof(float4) * h->Np, h->stream));
+    CK(cudaMemsetAsync(h->hist2.p, 0, sizeof(float4) * h->Np, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return PBS_OK;
 }

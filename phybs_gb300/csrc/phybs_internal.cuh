@@ -23,16 +23,36 @@
 //   tf, hd      float4[4T]         corner forces / Jacobi-diagonal terms by slot;
 //                                  node i owns slots inc_ptr[i] .. inc_ptr[i+1]-1
 //   tpart       double2[n_tblk]    per tet-block {sum e, sum e^2} of the energy
+// Pass layout (the per-tet kernel of a descent pass works on chunks: runs of
+// at most CHUNK_TETS tets of one instance, in Morton order of their centroids,
+// touching at most CHUNK_NODES nodes):
+//   chunk       int4[n_chunks]     {first pass tet, tet count, first local entry, local count}
+//   qrow0..2    float4[T] each     row0..2 of the pass tets, in pass (chunk) order
+//   qloc        ushort4[T]         corner -> local node of the tet's chunk
+//   qslot       ushort4[T]         corner -> shared-memory slot: a local node's slots
+//                                  are contiguous, in (tet, corner) order
+//   lnode       int[L]             local node -> padded node id (ascending per chunk)
+//   lsptr       int[L]             first slot of the local node (chunk-relative)
+//   lpidx       int[L]             where the chunk's partial sum for that node goes
+//   pptr        int[Np+1]          node i's partials: part[pptr[i] .. pptr[i+1]-1], by chunk
+//   part, parth float4[L]          per (node, chunk) partial force / Jacobi-diagonal sums
+//   cpart       double2[n_chunks]  per chunk {sum e, sum e^2}
 //   npart       double[n_nblk]     per node-block |g|^2
 //   ctl         InstCtl[n_inst]    per-instance descent state
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace pbs {
 
 constexpr int PAD = 256;    // instance alignment (tets and nodes)
 constexpr int BLOCK = 256;  // threads per block of the step kernels
+constexpr int CHUNK_TETS = 1024;    // tets per chunk at most
+constexpr int CHUNK_NODES = 448;    // nodes a chunk may touch
+constexpr int CHUNK_THREADS = 256;  // threads of the chunked per-tet kernel
+constexpr size_t CHUNK_SMEM = 3 * sizeof(float4) * CHUNK_NODES + 3 * sizeof(float) * 4 * CHUNK_TETS;
 
 // Step parameters as the kernels see them (a by-value kernel argument).
 struct DevParams {
@@ -73,6 +93,7 @@ struct __align__(16) InstCtl {
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
     int tblk_begin, tblk_end, nblk_begin, nblk_end;
+    int cblk_begin, cblk_end, pad4, pad5;  // the instance's chunks
 };
 
 struct DevMesh {
@@ -84,6 +105,13 @@ struct DevMesh {
     const int4 *tslot;
     const float4 *info, *rest;
     const int *tblk_inst, *nblk_inst;
+    // pass layout
+    int n_chunks;
+    const int4 *chunk;
+    const int *chunk_inst;
+    const float4 *qrow0, *qrow1, *qrow2;
+    const ushort4 *qloc, *qslot;
+    const int *lnode, *lsptr, *lpidx, *pptr;
 };
 
 struct DevState {
@@ -95,8 +123,9 @@ struct DevState {
     float4 *bh, *bl;        // per node (hi, lo): elastic force at the base (incremental mode)
                             // plus body_force_scale * (external + gravity)
     float *tf, *hd;
-    double2 *tpart;
+    double2 *tpart, *cpart;
     double *npart;
+    float4 *part, *parth;
     InstCtl *ctl;
     int *active;  // instances not yet done
 };
@@ -131,14 +160,30 @@ __device__ __forceinline__ int node_ctl_ws(const DevMesh &m, const DevState &st,
     return st.ctl[m.nblk_inst[i / BLOCK]].ws_used;
 }
 
+// Host: the pass layout of a packed mesh (chunks.cu).  tets: padded corner ids
+// (-1 rows are padding); rest: padded rest positions (3 per node); ctl: the
+// instances' node / tet ranges, whose cblk ranges are filled in.
+struct ChunkLayout {
+    std::vector<int4> chunk;
+    std::vector<int> chunk_inst, qperm, lnode, lsptr, lpidx, pptr;
+    std::vector<ushort4> qloc, qslot;
+    int max_local = 0;
+};
+void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<double> &rest, std::vector<InstCtl> &ctl,
+                  ChunkLayout &out);
+cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const float4 *row0, const float4 *row1,
+                             const float4 *row2, float4 *q0, float4 *q1, float4 *q2);
+cudaError_t prepare_chunk_kernels();
+
 // Launchers (kernels.cu, warmstart.cu)
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
 cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *theta,
                               const float *feat_mean, const float *feat_std, const float *out_std, float *tetF,
                               int sms);
+cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
-                               const int *pad2user, float *out);
+                               const int *pad2user, float *out, float *scale_out);
 cudaError_t launch_rest(cudaStream_t s, const DevMesh &m, const double *rest_pad, float density, float4 *row0,
                         float4 *row1, float4 *row2, double *tmass, int *bad);
 cudaError_t launch_mass(cudaStream_t s, const DevMesh &m, const double *tmass, const int *state, float gravity,

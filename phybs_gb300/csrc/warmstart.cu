@@ -8,7 +8,8 @@
 //   k_ws_infer     per 16-node tile and warp: node features (velocity history,
 //                  inertial offset, material, mean incident F and J), the
 //                  standardised 24-vector, the tensor-core MLP, and the
-//                  candidate guess u_plain + correction (free nodes)
+//                  candidate guess u_plain + s * out_std * output (free nodes;
+//                  s the node's motion scale)
 //   k_ws_judge     energies of both guesses (tets + node terms, FP64 sums);
 //                  the instance keeps the candidate only if its energy is not
 //                  higher (the plain descent is the fallback and the judge)
@@ -22,25 +23,6 @@
 #include "tet_math.cuh"
 
 namespace pbs {
-
-__device__ __forceinline__ double ws_warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ double ws_block_sum(double v, double *sh) {
-    v = ws_warp_sum(v);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (w == 0) {
-        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-        r = ws_warp_sum(r);
-    }
-    return r;
-}
 
 // Corner forces at displacement U into the gather slots (as k_tet, no energy).
 template <int MATERIAL>
@@ -92,7 +74,7 @@ __global__ void __launch_bounds__(BLOCK) k_ws_gref(DevMesh m, DevParams p, DevSt
         const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
         r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
     }
-    const double s = ws_block_sum(r2, sh);
+    const double s = block_sum(r2, sh);
     if (threadIdx.x == 0) {
         st.npart[b] = s;
         __threadfence();
@@ -104,7 +86,7 @@ __global__ void __launch_bounds__(BLOCK) k_ws_gref(DevMesh m, DevParams p, DevSt
     __threadfence();
     double R2 = 0.0;
     for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += BLOCK) R2 += __ldcg(st.npart + j);
-    R2 = ws_block_sum(R2, sh);
+    R2 = block_sum(R2, sh);
     if (threadIdx.x == 0) {
         cp->counter_n = 0;
         cp->g0 = sqrt(R2);
@@ -130,11 +112,16 @@ __global__ void k_ws_tet_F(DevMesh m, DevState st, float *tetF) {
     o[9] = kin.d;
 }
 
-// The 24 raw features of node i (see phybs_gb300/warmstart.py for the list).
+// The 24 raw features of node i (see phybs_gb300/warmstart.py for the list)
+// and its motion scale s = |d1| + |d2| + 1e-4 l (d1, d2: the last two
+// displacements, l: the mean edge length), which divides every length
+// feature and the predicted correction.
 __device__ __forceinline__ void node_features(const DevMesh &m, const DevState &st, const DevParams &p,
-                                              const float *tetF, float ell, int i, float f[24]) {
+                                              const float *tetF, float ell, int i, float f[24], float &scale) {
     const float4 v = st.v[i], vo = st.vold[i], h1 = st.hist1[i], h2 = st.hist2[i];
-    const float il = 1.0f / ell, ivl = p.h / ell, wo = p.warm_start * p.h / ell;
+    scale = sqrtf(h1.x * h1.x + h1.y * h1.y + h1.z * h1.z) + sqrtf(h2.x * h2.x + h2.y * h2.y + h2.z * h2.z) +
+            1e-4f * ell;
+    const float il = 1.0f / scale, ivl = p.h / scale, wo = p.warm_start * p.h / scale;
     f[0] = v.x * ivl; f[1] = v.y * ivl; f[2] = v.z * ivl;
     f[3] = h1.x * il; f[4] = h1.y * il; f[5] = h1.z * il;
     f[6] = h2.x * il; f[7] = h2.y * il; f[8] = h2.z * il;
@@ -158,14 +145,16 @@ __device__ __forceinline__ void node_features(const DevMesh &m, const DevState &
     for (int k = 0; k < 10; ++k) f[14 + k] = acc[k] * inv;
 }
 
-__global__ void k_ws_features(DevMesh m, DevParams p, DevState st, const float *tetF, const int *pad2user, float *out) {
+__global__ void k_ws_features(DevMesh m, DevParams p, DevState st, const float *tetF, const int *pad2user, float *out,
+                              float *scale_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
     const int u = pad2user[i];
     if (u < 0) return;
-    float f[24];
-    node_features(m, st, p, tetF, node_ell(m, st, i), i, f);
+    float f[24], sc;
+    node_features(m, st, p, tetF, node_ell(m, st, i), i, f, sc);
     for (int k = 0; k < 24; ++k) out[24 * (size_t)u + k] = f[k];
+    if (scale_out) scale_out[u] = sc;
 }
 
 struct WsNet {
@@ -178,6 +167,7 @@ struct WsNet {
 __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevState st, const float *tetF, WsNet net) {
     __shared__ mlp::SmemWeights sw;
     __shared__ float tile[4][16][25];
+    __shared__ float tscale[4][16];
     __shared__ float fm[24], fs[24], os[3];
     mlp::stage_weights(net.theta, sw);
     if (threadIdx.x < 24) {
@@ -191,10 +181,10 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
     for (int row0 = (blockIdx.x * 4 + w) * 16; row0 < m.Np; row0 += nwarps * 16) {
         if (lane < 16) {
             const int i = row0 + lane;
-            float f[24];
+            float f[24], sc = 0.f;
             const float4 info = m.info[i];
             if (info.z == 0.f) {
-                node_features(m, st, p, tetF, node_ell(m, st, i), i, f);
+                node_features(m, st, p, tetF, node_ell(m, st, i), i, f, sc);
 #pragma unroll
                 for (int k = 0; k < 24; ++k) f[k] = (f[k] - fm[k]) * fs[k];
             } else {
@@ -203,6 +193,7 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
             }
 #pragma unroll
             for (int k = 0; k < 24; ++k) tile[w][lane][k] = f[k];
+            tscale[w][lane] = sc;
         }
         __syncwarp();
         uint32_t x[2][4];
@@ -242,10 +233,10 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
                 float hx = st.uh[i].x, hy = st.uh[i].y, hz = st.uh[i].z;
                 float lx = st.ul[i].x, ly = st.ul[i].y, lz = st.ul[i].z;
                 if (info.z == 0.f) {
-                    const float ell = node_ell(m, st, i);
-                    add_comp(hx, lx, tile[w][lane][0] * os[0] * ell);
-                    add_comp(hy, ly, tile[w][lane][1] * os[1] * ell);
-                    add_comp(hz, lz, tile[w][lane][2] * os[2] * ell);
+                    const float sc = tscale[w][lane];
+                    add_comp(hx, lx, tile[w][lane][0] * os[0] * sc);
+                    add_comp(hy, ly, tile[w][lane][1] * os[1] * sc);
+                    add_comp(hz, lz, tile[w][lane][2] * os[2] * sc);
                 }
                 st.uh[m.Np + i] = make_float4(hx, hy, hz, 0.f);
                 st.ul[m.Np + i] = make_float4(lx, ly, lz, 0.f);
@@ -253,17 +244,6 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
         }
         __syncwarp();
     }
-}
-
-__device__ __forceinline__ double ws_node_energy(const DevState &st, const float4 &info, const float4 &uh,
-                                                 const float4 &ul, int i, float h2inv) {
-    const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
-    const float dx = (uh.x - th.x) + (ul.x - tl.x);
-    const float dy = (uh.y - th.y) + (ul.y - tl.y);
-    const float dz = (uh.z - th.z) + (ul.z - tl.z);
-    const double uy = (double)uh.y + ul.y;
-    return 0.5 * (double)info.x * ((double)dx * dx + (double)dy * dy + (double)dz * dz) * (double)h2inv -
-           (double)info.y * uy - ((double)ex.x * ((double)uh.x + ul.x) + (double)ex.y * uy + (double)ex.z * ((double)uh.z + ul.z));
 }
 
 // Energies of the plain guess (parity 0) and the candidate (parity 1).
@@ -292,11 +272,11 @@ __global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevS
     for (int i = cp->node_begin + (b - cp->tblk_begin) * BLOCK + threadIdx.x; i < cp->node_end; i += nb * BLOCK) {
         const float4 info = m.info[i];
         if (info.z != 0.f) continue;
-        e0 += ws_node_energy(st, info, st.uh[i], st.ul[i], i, p.h2inv);
-        e1 += ws_node_energy(st, info, st.uh[m.Np + i], st.ul[m.Np + i], i, p.h2inv);
+        e0 += node_energy(st, info, st.uh[i], st.ul[i], i, p.h2inv);
+        e1 += node_energy(st, info, st.uh[m.Np + i], st.ul[m.Np + i], i, p.h2inv);
     }
-    const double s0 = ws_block_sum(e0, sh);
-    const double s1 = ws_block_sum(e1, sh);
+    const double s0 = block_sum(e0, sh);
+    const double s1 = block_sum(e1, sh);
     if (threadIdx.x == 0) {
         st.tpart[b] = make_double2(s0, s1);
         __threadfence();
@@ -312,8 +292,8 @@ __global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevS
         E0 += v.x;
         E1 += v.y;
     }
-    E0 = ws_block_sum(E0, sh);
-    E1 = ws_block_sum(E1, sh);
+    E0 = block_sum(E0, sh);
+    E1 = block_sum(E1, sh);
     if (threadIdx.x == 0) {
         cp->counter_t = 0;
         cp->ws_used = (isfinite(E1) && E1 <= E0) ? 1 : 0;
@@ -329,7 +309,26 @@ __global__ void k_ws_select(DevMesh m, DevState st) {
     st.ub[i] = st.uh[m.Np + i];
 }
 
+// A caller-supplied candidate (parity 1) keeps the prescribed positions of
+// pinned nodes, as the plain guess (parity 0) has them.
+__global__ void k_ws_guess_pins(DevMesh m, DevState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    if (m.info[i].z == 0.f) return;
+    st.uh[m.Np + i] = st.uh[i];
+    st.ul[m.Np + i] = st.ul[i];
+}
+
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    k_ws_guess_pins<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
+    k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
+    k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_ref_force(s, m, p, st);
+}
 
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
     if (material == PBS_MATERIAL_STRETCH)
@@ -354,9 +353,9 @@ cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams 
 }
 
 cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
-                               const int *pad2user, float *out) {
+                               const int *pad2user, float *out, float *scale_out) {
     k_ws_tet_F<<<nblk(m.Tp, 256), 256, 0, s>>>(m, st, tetF);
-    k_ws_features<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st, tetF, pad2user, out);
+    k_ws_features<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st, tetF, pad2user, out, scale_out);
     return cudaGetLastError();
 }
 

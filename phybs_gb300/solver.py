@@ -129,6 +129,10 @@ class DescentSolver:
     def update_positions(self, x):
         L.check(L.lib().pbs_update_positions(self._h, _ptr(_f32(x, (-1, 3)))), "pbs_update_positions")
 
+    def set_guess(self, x):
+        """Initial guess for the next step (kept only if its energy is lower)."""
+        L.check(L.lib().pbs_set_guess(self._h, _ptr(_f32(x, (-1, 3)))), "pbs_set_guess")
+
     def set_node_positions(self, ids, xyz):
         ids = np.ascontiguousarray(ids, np.int32)
         xyz = _f32(xyz, (-1, 3))
@@ -146,12 +150,15 @@ class DescentSolver:
         return a.value, b.value
 
     def warm_start_features(self, ext=None):
-        """Raw 24 features per node for the next step, and the plain initial guess."""
+        """Raw 24 features per node for the next step, the plain initial
+        guess, and each node's motion scale (features, x_init, scale)."""
         feats = np.empty((self.n, 24), np.float32)
         xin = np.empty((self.n, 3), np.float32)
+        scale = np.empty(self.n, np.float32)
         e = _f32(ext, (-1, 3)) if ext is not None else None
-        L.check(L.lib().pbs_warm_start_features(self._h, _ptr(e), _ptr(feats), _ptr(xin)), "pbs_warm_start_features")
-        return feats, xin
+        L.check(L.lib().pbs_warm_start_features(self._h, _ptr(e), _ptr(feats), _ptr(xin), _ptr(scale)),
+                "pbs_warm_start_features")
+        return feats, xin, scale
 
     def set_warm_start(self, model=None):
         """Install a WarmStartModel (or switch the warm start off with None)."""

@@ -2,17 +2,19 @@
 
     python -m phybs_gb300.train_warmstart --frames 4000 --out phybs_gb300/warmstart_model.npz
 
-Scenarios (seeded; sizes reduced from the benchmark meshes so that thousands of
-frames solve in minutes):
-  * box: the 1M-tet box's geometry (0.25 x 0.25 x 0.4 m, 5-tet split, +-0.1
-    jitter) at 20x20x32 cubes, E = 10^U(4, 6), Poisson 0.4, top face pinned
-    and the bottom face pulled to a random 1.2-1.8x stretch over 20-40 frames,
-    optional initial twist, gravity;
-  * ellipsoid: the voxelised ellipsoid at half resolution, E = 10^U(4.5, 5.5),
-    Poisson 0.3-0.45, released from a random 30-120 degree twist, bottom 5%
-    pinned, gravity.
-Every frame is solved to |g| <= 1e-4 |g_0| by the plain descent.  A sample of
-free nodes per frame gives (features, (x* - x_init) / l) pairs.
+Scenarios (seeded; every run draws its own mesh seed, material and loading):
+  * box1m: the 1M-tet box (50 x 50 x 80 cubes of 0.005 m, 5-tet split, +-0.1
+    jitter) with mesh seeds from 1000 up (the benchmark evaluates seed 0),
+    E = 10^U(4, 6), Poisson 0.4, top face pinned and the bottom face pulled
+    to a random 1.3-1.7x stretch over 20-40 frames, then held;
+  * box: the same geometry at 20 x 20 x 32 cubes, stretch 1.2-1.8x, half of
+    the runs with an initial twist of up to 45 degrees;
+  * ellipsoid: the 42K-tet voxelised ellipsoid (20 x 20 x 40 cells of 0.01 m),
+    E = 10^U(4.5, 5.5), Poisson 0.3-0.45, released from a random 30-120
+    degree twist, bottom 5% pinned.
+All run with gravity at h = 1/30 s.  Every frame is solved to
+|g| <= 1e-4 |g_0| by the plain descent.  A sample of free nodes per frame
+gives (features, (x* - x_init) / s) pairs, s the node's motion scale.
 """
 from __future__ import annotations
 
@@ -26,11 +28,13 @@ from .solver import DescentSolver, make_params
 from .warmstart import MLPTrainer, WarmStartModel
 from . import _lib as L
 
-ALPHA0 = 0.5
-RHO = 0.9998
+# The residual-target settings of the benchmark (alpha0 = 0.5 diverges on
+# the 1M-tet box; rho = 0.9999 needs the fewest iterations there).
+ALPHA0 = 0.3
+RHO = 0.9999
 
 
-def residual_params(max_iters=8000):
+def residual_params(max_iters=20000):
     return make_params("gpu_reference", h=1 / 30, tol=1e-4, max_iters=max_iters, control=L.PBS_CONTROL_RESTART,
                        energy_slack=16.0, alpha0=ALPHA0, profile=((10, RHO),))
 
@@ -40,16 +44,16 @@ def mean_edge(mesh) -> float:
     return float(np.cbrt(6.0 * v.mean()))
 
 
-def box_scenario(rng, nx=20, ny=20, nz=32):
+def box_scenario(rng, nx=20, ny=20, nz=32, stretch_range=(0.2, 0.8), twist_prob=0.5, mesh_seed=None):
     e = float(10 ** rng.uniform(4.0, 6.0))
-    m = M.box_mesh(nx, ny, nz, edge=0.25 / nx, jitter=0.1, seed=int(rng.integers(1 << 30)), young=e, poisson=0.4,
-                   pin="both")
+    seed = int(rng.integers(1 << 30)) if mesh_seed is None else mesh_seed
+    m = M.box_mesh(nx, ny, nz, edge=0.25 / nx, jitter=0.1, seed=seed, young=e, poisson=0.4, pin="both")
     z = m.rest[:, 2]
     bottom = np.nonzero(z <= z.min() + 1e-9)[0].astype(np.int32)
     length = float(z.max() - z.min())
-    stretch = float(rng.uniform(0.2, 0.8))
+    stretch = float(rng.uniform(*stretch_range))
     ramp = int(rng.integers(20, 41))
-    twist = float(rng.uniform(0.0, np.pi / 4)) if rng.uniform() < 0.5 else 0.0
+    twist = float(rng.uniform(0.0, np.pi / 4)) if rng.uniform() < twist_prob else 0.0
     x0 = M.twist_positions(m.rest, twist, axis=2) if twist else None
     if x0 is not None:
         x0[m.pins] = m.rest[m.pins]
@@ -65,40 +69,54 @@ def box_scenario(rng, nx=20, ny=20, nz=32):
 def ellipsoid_scenario(rng):
     e = float(10 ** rng.uniform(4.5, 5.5))
     nu = float(rng.uniform(0.3, 0.45))
-    m = M.ellipsoid_mesh(10, 10, 20, cell=0.02, jitter=0.15, seed=int(rng.integers(1 << 30)), young=e, poisson=nu)
+    m = M.ellipsoid_mesh(20, 20, 40, cell=0.01, jitter=0.15, seed=int(rng.integers(1 << 30)), young=e, poisson=nu)
     twist = float(rng.uniform(np.pi / 6, 2 * np.pi / 3))
     x0 = M.twist_positions(m.rest, twist, axis=2)
     x0[m.pins] = m.rest[m.pins]
     return m, x0, None
 
 
-def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int = 60, verbose: bool = True):
+def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int = 60, verbose: bool = True,
+             mix=(0.4, 0.3, 0.3)):
+    """Solve frames of randomly drawn scenarios; mix = the fractions of runs
+    that are box1m, box and ellipsoid."""
     rng = np.random.default_rng(seed)
     X, Y = [], []
     done = 0
+    n_1m = 0
     t0 = time.time()
     while done < frames:
-        kind = "box" if rng.uniform() < 0.6 else "ellipsoid"
-        m, x0, boundary = box_scenario(rng) if kind == "box" else ellipsoid_scenario(rng)
+        u = rng.uniform()
+        kind = "box1m" if u < mix[0] else ("box" if u < mix[0] + mix[1] else "ellipsoid")
+        if kind == "box1m":
+            m, x0, boundary = box_scenario(rng, 50, 50, 80, stretch_range=(0.3, 0.7), twist_prob=0.0,
+                                           mesh_seed=1000 + seed * 1000 + n_1m)
+            n_1m += 1
+        elif kind == "box":
+            m, x0, boundary = box_scenario(rng)
+        else:
+            m, x0, boundary = ellipsoid_scenario(rng)
         ell = mean_edge(m)
         s = DescentSolver(m, positions=x0, params=residual_params())
         free = np.nonzero(m.pin_mask() == 0)[0]
-        n_frames = min(frames_per_run, frames - done)
+        n_frames = min(40 if kind == "box1m" else frames_per_run, frames - done)
+        its = []
         for f in range(n_frames):
             if boundary is not None:
                 boundary(s, f)
-            feats, xin = s.warm_start_features()
-            s.step(raise_on_error=False)
+            feats, xin, scale = s.warm_start_features()
+            its.append(s.step(raise_on_error=False))
             if s.last_status != 0 or not s.stats()["converged"]:
                 continue
             xs = s.positions()
             pick = rng.choice(free, size=min(nodes_per_frame, free.size), replace=False)
             X.append(feats[pick])
-            Y.append((xs[pick] - xin[pick]) / ell)
+            Y.append((xs[pick] - xin[pick]) / scale[pick, None])
         done += n_frames
         s.close()
         if verbose:
-            print(f"  {done}/{frames} frames ({kind}, {m.n_tets} tets), {time.time() - t0:.0f}s", flush=True)
+            print(f"  {done}/{frames} frames ({kind}, {m.n_tets} tets, {np.mean(its):.0f} iterations/frame), "
+                  f"{time.time() - t0:.0f}s", flush=True)
     return np.concatenate(X).astype(np.float32), np.concatenate(Y).astype(np.float32)
 
 
@@ -127,12 +145,16 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--data", default=None, help="save the generated (X, Y) here")
+    ap.add_argument("--data-max", type=int, default=0, help="save at most this many samples (0 = all)")
     args = ap.parse_args()
     t0 = time.time()
     X, Y = generate(args.frames, args.nodes_per_frame, args.seed)
     print(f"data: {X.shape[0]} samples in {time.time() - t0:.0f}s", flush=True)
     if args.data:
-        np.savez_compressed(args.data, X=X, Y=Y)
+        keep = np.arange(X.shape[0])
+        if args.data_max and X.shape[0] > args.data_max:
+            keep = np.sort(np.random.default_rng(args.seed).choice(X.shape[0], args.data_max, replace=False))
+        np.savez_compressed(args.data, X=X[keep], Y=Y[keep])
     model = fit(X, Y, steps=args.steps, seed=args.seed)
     from .warmstart import DEFAULT_MODEL
     model.save(args.out or DEFAULT_MODEL)

@@ -29,16 +29,26 @@ def test_features_match_definition():
     """Feature columns against a numpy evaluation of their definition."""
     m, x0, boundary = _pull_case()
     s = DescentSolver(m, positions=x0, params=residual_params())
+    xs = [s.positions().astype(np.float64)]
     for f in range(3):
         boundary(s, f)
         s.step()
-    feats, xin = s.warm_start_features()
+        xs.append(s.positions().astype(np.float64))
+    feats, xin, scale = s.warm_start_features()
     v, vo = s.velocities()
     ell = mean_edge(m)
     h = 1 / 30
     free = m.pin_mask() == 0
-    np.testing.assert_allclose(feats[free, 0:3], v[free] * h / ell, rtol=1e-5, atol=1e-6)
-    np.testing.assert_allclose(feats[free, 9:12], 0.2 * h * (v - vo)[free] / ell, rtol=1e-4, atol=1e-6)
+    # s = |d1| + |d2| + 1e-4 l from the last two displacements (pinned nodes are
+    # prescribed between steps, so only free nodes follow the recorded history)
+    d1, d2 = xs[3] - xs[2], xs[2] - xs[1]
+    ref_scale = np.linalg.norm(d1, axis=1) + np.linalg.norm(d2, axis=1) + 1e-4 * ell
+    np.testing.assert_allclose(scale[free], ref_scale[free], rtol=1e-3, atol=1e-6 * ell)
+    sc = scale[:, None]
+    np.testing.assert_allclose(feats[free, 0:3], (v * h / sc)[free], rtol=1e-4, atol=1e-4)
+    np.testing.assert_allclose(feats[free, 3:6], (d1 / sc)[free], rtol=1e-3, atol=1e-3)
+    np.testing.assert_allclose(feats[free, 6:9], (d2 / sc)[free], rtol=1e-3, atol=1e-3)
+    np.testing.assert_allclose(feats[free, 9:12], (0.2 * h * (v - vo) / sc)[free], rtol=1e-3, atol=1e-4)
     x = s.positions()
     np.testing.assert_allclose(xin, x + h * v + 0.2 * h * (v - vo), atol=2e-6)
     # mean incident J - 1 at x~ = x + h v
