@@ -25,7 +25,11 @@ def build(reference: bool = True, verbose: bool = False) -> None:
     src = os.path.join(HERE, "phybs_oracle.cpp")
     if (not os.path.exists(ORACLE_SO)) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", ORACLE_SO, src]
-        subprocess.run(cmd, check=True, capture_output=not verbose)
+        # OpenMP only parallelises the per-tet loops (results are identical);
+        # without it the oracle builds serial
+        r = subprocess.run(cmd[:1] + ["-fopenmp"] + cmd[1:], capture_output=True)
+        if r.returncode != 0:
+            subprocess.run(cmd, check=True, capture_output=not verbose)
     if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "FVM")):
         subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={REFERENCE_TREE}", "-j8"],
                        check=True, capture_output=not verbose)

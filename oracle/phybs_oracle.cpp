@@ -32,6 +32,9 @@
 #include <vector>
 #include <algorithm>
 #include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -364,6 +367,7 @@ template <typename R> struct Mesh {
     std::vector<TetIn<R>> tin;
     std::vector<R> mass, grav_y;   // mass: pinned = 1e8; grav_y = -9.8 * lumped mass (pre-pin)
     std::vector<int> pinned;
+    std::vector<int> iptr, ient;   // node -> 4 * tet + corner, ascending tet
 };
 
 template <typename R> Mesh<R> load_mesh(int n, int t, const int *tets, const double *dinv9, const double *an9,
@@ -380,40 +384,91 @@ template <typename R> Mesh<R> load_mesh(int n, int t, const int *tets, const dou
     m.mass.assign(mass, mass + n);
     m.grav_y.assign(grav_y, grav_y + n);
     m.pinned.assign(pin_mask, pin_mask + n);
+    m.iptr.assign(n + 1, 0);
+    for (int i = 0; i < 4 * t; ++i) m.iptr[tets[i] + 1]++;
+    for (int i = 0; i < n; ++i) m.iptr[i + 1] += m.iptr[i];
+    m.ient.resize(4 * (size_t)t);
+    std::vector<int> fill(m.iptr.begin(), m.iptr.end() - 1);
+    for (int i = 0; i < 4 * t; ++i) m.ient[fill[tets[i]]++] = i;
     return m;
 }
+
+// Per-node sums of per-tet 12-vectors, each node adding its incident (tet,
+// corner) terms in ascending tet order: the order in which a serial scatter
+// over tets adds them, so the result is the scatter's, bit for bit.
+template <typename R> void gather_nodes(const Mesh<R> &m, const std::vector<R> &all, std::vector<R> &out) {
+    out.assign(3 * (size_t)m.n, R(0));
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < m.n; ++v) {
+        R s[3] = {0, 0, 0};
+        for (int j = m.iptr[v]; j < m.iptr[v + 1]; ++j) {
+            const R *c = &all[3 * (size_t)m.ient[j]];
+            for (int d = 0; d < 3; ++d) s[d] += c[d];
+        }
+        for (int d = 0; d < 3; ++d) out[3 * (size_t)v + d] = s[d];
+    }
+}
+
+// Per-tet terms are evaluated in parallel (OpenMP, when built with it) into a
+// per-tet buffer, then gathered per node in tet order: the sums are the
+// serial scatter's, bit for bit, whatever the thread count.
 
 // Per-node elastic force in tet order (the reference's scatter order).
 template <typename R> void elastic_forces(const Mesh<R> &m, const std::vector<R> &x, int material, std::vector<R> &f) {
     f.assign(3 * (size_t)m.n, R(0));
-    R cf[12];
+    std::vector<R> all(12 * (size_t)m.t);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         const int *t = m.tets + 4 * i;
         M3<R> F = deformation_gradient(x.data(), t, m.tin[i].Dinv);
         M3<R> P = material == 1 ? pk1_stretch(F, m.tin[i].mu, m.tin[i].lambda) : pk1_nh(F, m.tin[i].mu, m.tin[i].lambda);
-        corner_forces(P, m.tin[i].AN, cf);
-        for (int c = 1; c < 4; ++c)
-            for (int d = 0; d < 3; ++d) f[3 * t[c] + d] += cf[3 * c + d];
-        for (int d = 0; d < 3; ++d) f[3 * t[0] + d] += cf[d];
+        corner_forces(P, m.tin[i].AN, &all[12 * (size_t)i]);
     }
+    gather_nodes(m, all, f);
 }
 
 template <typename R> void hessian_diag_nodes(const Mesh<R> &m, const std::vector<R> &x, int closed, std::vector<R> &hd) {
     hd.assign(3 * (size_t)m.n, R(0));
-    R k[12];
+    std::vector<R> all(12 * (size_t)m.t);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         const int *t = m.tets + 4 * i;
         M3<R> F = deformation_gradient(x.data(), t, m.tin[i].Dinv);
-        if (closed) hessian_diag_closed(F, m.tin[i], k); else hessian_diag_svd(F, m.tin[i], k);
-        for (int c = 0; c < 4; ++c)
-            for (int d = 0; d < 3; ++d) hd[3 * t[c] + d] += k[3 * c + d];
+        if (closed) hessian_diag_closed(F, m.tin[i], &all[12 * (size_t)i]);
+        else hessian_diag_svd(F, m.tin[i], &all[12 * (size_t)i]);
     }
+    gather_nodes(m, all, hd);
+}
+
+// Sum of the clamped tet energies, added in tet order.
+template <typename R> R elastic_energy(const Mesh<R> &m, const std::vector<R> &x, int clamp) {
+    std::vector<R> e(m.t);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < m.t; ++i) {
+        M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
+        e[i] = tet_energy(F, m.tin[i].mu, m.tin[i].lambda, m.tin[i].vol, clamp);
+    }
+    R Ee = 0;
+    for (int i = 0; i < m.t; ++i) Ee += e[i];
+    return Ee;
 }
 
 }  // namespace
 
 // ============================================================== C ABI
 extern "C" {
+
+// Threads of the per-tet loops (1 = serial; ignored without OpenMP).  Returns
+// the count in effect.
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
 
 // Step parameters (mirrors pbs_step_params of include/phybs.h field by field).
 typedef struct orc_params {
@@ -573,11 +628,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                 // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:118-144): the
                 // gravity term 0.5 m 2 g y is -gravity_y . y; plus the external work
                 // -f_ext . x over free nodes.
-                R Ee = 0;
-                for (int i = 0; i < m.t; ++i) {
-                    M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
-                    Ee += tet_energy(F, m.tin[i].mu, m.tin[i].lambda, m.tin[i].vol, p->energy_clamp);
-                }
+                const R Ee = elastic_energy(m, x, p->energy_clamp);
                 R En = 0;
                 for (int i = 0; i < n; ++i) {
                     if (m.pinned[i]) continue;

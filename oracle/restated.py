@@ -7,6 +7,7 @@ C++ side evaluates in.  Layouts: positions (N, 3); tets (T, 4) int32; per-tet
 from __future__ import annotations
 
 import ctypes as C
+import os
 import dataclasses
 
 import numpy as np
@@ -37,6 +38,14 @@ class OrcStats(C.Structure):
     _fields_ = [("passes", C.c_int), ("k_final", C.c_int), ("rejections", C.c_int), ("converged", C.c_int),
                 ("alpha", C.c_double), ("energy", C.c_double), ("energy_old", C.c_double), ("rho", C.c_double),
                 ("omega", C.c_double), ("residual_ratio", C.c_double), ("residual0", C.c_double)]
+
+
+def set_threads(n: int = 0) -> int:
+    """Threads of the per-tet loops (0 = all host cores); returns the count in
+    effect.  Results do not depend on it."""
+    if n <= 0:
+        n = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    return int(lib().orc_set_threads(C.c_int(n)))
 
 
 def make_params(h=0.03, max_iters=96, tol=0.0, control=0, alpha0=0.1, alpha_min=0.01, alpha_shrink=0.7,
