@@ -246,8 +246,11 @@ int pbs_mlp_set_params(pbs_mlp *t, const float *theta);   /* also resets Adam */
 int pbs_mlp_forward(pbs_mlp *t, const float *X, int n, float *Y);
 /* Gradient of the mean (over rows) squared error of the batch; grad NPARAM floats. */
 int pbs_mlp_gradient(pbs_mlp *t, const float *X, const float *Y, int n, float *grad, float *loss);
-/* Training set (copied to the device) and Adam training on minibatches. */
-int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, int n);
+/* Training set (copied to the device): X n x 24, Y n x 3, W n non-negative
+ * sample weights or NULL (all 1; the loss is then the mean squared error,
+ * otherwise sum_i W_i |y_i - Y_i|^2 / n over the minibatch).  Adam training
+ * on minibatches. */
+int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, const float *W, int n);
 int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long seed, float *losses);
 
 /* Install (enabled != 0) or switch off the warm start on a solver handle.

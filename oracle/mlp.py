@@ -68,15 +68,16 @@ def forward(theta, X, round_bf16=False):
     return h, cache
 
 
-def loss_and_grad(theta, X, Y, round_bf16=False):
-    """Mean over rows of the squared error summed over the 3 outputs, and its
-    gradient with respect to theta."""
+def loss_and_grad(theta, X, Y, round_bf16=False, W=None):
+    """Mean over rows of the squared error summed over the 3 outputs (each row
+    weighted by W when given), and its gradient with respect to theta."""
     layers = unpack(theta)
     out, cache = forward(theta, X, round_bf16)
     n = X.shape[0]
     diff = out - np.asarray(Y, np.float64)
-    loss = float((diff ** 2).sum() / n)
-    delta = 2.0 * diff / n
+    w = np.ones((n, 1)) if W is None else np.asarray(W, np.float64).reshape(n, 1)
+    loss = float((w * diff ** 2).sum() / n)
+    delta = 2.0 * w * diff / n
     grads = [None] * 4
     for li in range(3, -1, -1):
         hin, z = cache[li]

@@ -172,6 +172,14 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     __shared__ double sh[BLOCK / 32];
     __shared__ int is_last;
     const int b = blockIdx.x;
+    const int i = b * BLOCK + threadIdx.x;  // < Np: the grid covers the padded nodes exactly
+    // loads that do not depend on the instance's state go out before it is read
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 info = m.info[i];
+    const float4 th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
+    const int pa = m.pptr[i], pe = m.pptr[i + 1];
+    const float4 f0 = pa < pe ? st.part[pa] : z4;
+    const float4 f1 = pa + 1 < pe ? st.part[pa + 1] : z4;
     InstCtl *cp = st.ctl + m.nblk_inst[b];
     if (cp->done) return;
     const int k = cp->k;
@@ -182,8 +190,6 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     float rho = cp->rho, omega = cp->omega;
     chebyshev_schedule(p, k - cp->k_restart, rho, omega);
     const size_t cur = (size_t)cp->par * m.Np, nxt = (size_t)(1 - cp->par) * m.Np;
-    const int i = b * BLOCK + threadIdx.x;
-    const float4 info = m.info[i];
     double r2 = 0.0;
     if (info.z != 2.f) {
         const float4 uh = st.uh[cur + i], ul = st.ul[cur + i], dd = st.dd[cur + i];
@@ -205,15 +211,20 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
             if (info.z == 0.f) {
                 float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
                 // this node's per-chunk partial sums, in chunk order
-                const int a = m.pptr[i], e_ = m.pptr[i + 1];
-                for (int j = a; j < e_; ++j) {
+                fx += f0.x;
+                fy += f0.y;
+                fz += f0.z;
+                fx += f1.x;
+                fy += f1.y;
+                fz += f1.z;
+                for (int j = pa + 2; j < pe; ++j) {
                     const float4 f = st.part[j];
                     fx += f.x;
                     fy += f.y;
                     fz += f.z;
                 }
                 if (do_h) {
-                    for (int j = a; j < e_; ++j) {
+                    for (int j = pa; j < pe; ++j) {
                         const float4 q = st.parth[j];
                         hx += q.x;
                         hy += q.y;
@@ -230,7 +241,6 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
                 }
                 // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
                 // force (incremental mode) + body_force_scale (external + gravity)
-                const float4 th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
                 const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
                 const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
                 const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
@@ -306,11 +316,54 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
 }
 
 // Per-step node constant b = f_el(u_base) (incremental mode, FP64) +
-// body_force_scale (external + gravity), split into FP32 (hi, lo).  Each
-// node evaluates its incident tets' full neo-Hookean stress at the base (the
-// step's initial guess, whose increments the passes evaluate) in FP64 and
-// sums its corner forces in the canonical order.
-__global__ void k_ref_force(DevMesh m, DevParams p, DevState st) {
+// body_force_scale (external + gravity), split into FP32 (hi, lo).
+// k_ref_tet evaluates each tet's full neo-Hookean stress at the base (the
+// step's initial guess, whose increments the passes evaluate) in FP64 once and
+// writes its 4 corner forces into FP64 gather slots; k_ref_gather sums each
+// node's slots in the canonical (tet, corner) order.
+__global__ void k_ref_tet(DevMesh m, DevParams p, DevState st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.Tp) return;
+    const int4 q = m.tets[t];
+    if (q.x < 0) return;
+    const int id[4] = {q.x, q.y, q.z, q.w};
+    double u[4][3];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float4 hh = st.ub[id[a]];
+        u[a][0] = hh.x;
+        u[a][1] = hh.y;
+        u[a][2] = hh.z;
+    }
+    const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+    const double dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    Kin<double> k;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+            k.G[3 * r + cc] = (u[1][r] - u[0][r]) * dinv[cc] + (u[2][r] - u[0][r]) * dinv[3 + cc] +
+                              (u[3][r] - u[0][r]) * dinv[6 + cc];
+    kinematics(k);
+    double P[9];
+    pk1_neohookean<double>(k, (double)r1.w, (double)r2.w, P);
+    const double sv = (double)r0.w;
+    const int4 sl = m.tslot[t];
+    const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        // corner c: -svol P w_c (w_c = row c-1 of Dm^-1, w_0 = -sum of rows)
+        double w[3];
+#pragma unroll
+        for (int qq = 0; qq < 3; ++qq)
+            w[qq] = c == 0 ? -(dinv[qq] + dinv[3 + qq] + dinv[6 + qq]) : dinv[3 * (c - 1) + qq];
+        double *o = st.rslot + 3 * (size_t)slot[c];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[d] = -sv * (P[3 * d] * w[0] + P[3 * d + 1] * w[1] + P[3 * d + 2] * w[2]);
+    }
+}
+
+__global__ void k_ref_gather(DevMesh m, DevParams p, DevState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
     const float4 info = m.info[i];
@@ -320,37 +373,9 @@ __global__ void k_ref_force(DevMesh m, DevParams p, DevState st) {
                    (double)p.body_scale * ex.z};
     if (p.incremental && info.z == 0.f) {
         for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
-            const int t = m.inc[j] >> 2, c = m.inc[j] & 3;
-            const int4 q = m.tets[t];
-            const int id[4] = {q.x, q.y, q.z, q.w};
-            double u[4][3];
+            const double *o = st.rslot + 3 * (size_t)j;
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const float4 hh = st.ub[id[a]];
-                u[a][0] = hh.x;
-                u[a][1] = hh.y;
-                u[a][2] = hh.z;
-            }
-            const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
-            const double dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-            Kin<double> k;
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-#pragma unroll
-                for (int cc = 0; cc < 3; ++cc)
-                    k.G[3 * r + cc] = (u[1][r] - u[0][r]) * dinv[cc] + (u[2][r] - u[0][r]) * dinv[3 + cc] +
-                                      (u[3][r] - u[0][r]) * dinv[6 + cc];
-            kinematics(k);
-            double P[9];
-            pk1_neohookean<double>(k, (double)r1.w, (double)r2.w, P);
-            // corner c: -svol P w_c (w_c = row c-1 of Dm^-1, w_0 = -sum of rows)
-            double w[3];
-#pragma unroll
-            for (int qq = 0; qq < 3; ++qq)
-                w[qq] = c == 0 ? -(dinv[qq] + dinv[3 + qq] + dinv[6 + qq]) : dinv[3 * (c - 1) + qq];
-            const double sv = (double)r0.w;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) b[d] += -sv * (P[3 * d] * w[0] + P[3 * d + 1] * w[1] + P[3 * d + 2] * w[2]);
+            for (int d = 0; d < 3; ++d) b[d] += o[d];
         }
     }
     float hi[3], lo[3];
@@ -514,7 +539,8 @@ cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, De
     return launch_node_only(s, m, p, st);
 }
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
-    k_ref_force<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st);
+    if (p.incremental) k_ref_tet<<<nblk(m.Tp, 128), 128, 0, s>>>(m, p, st);
+    k_ref_gather<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st);
     return cudaGetLastError();
 }
 cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user) {

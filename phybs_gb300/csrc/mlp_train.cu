@@ -140,8 +140,8 @@ __device__ __forceinline__ void weight_grad(const __nv_bfloat16 *delta, const __
     }
 }
 
-__global__ void __launch_bounds__(128) k_mlp_grad(const float *theta, const float *X, const float *Y, const int *idx,
-                                                  int batch, float *part) {
+__global__ void __launch_bounds__(128) k_mlp_grad(const float *theta, const float *X, const float *Y, const float *W,
+                                                  const int *idx, int batch, float *part) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem &s = *reinterpret_cast<TrainSmem *>(smem_raw);
     stage_weights(theta, s.w);
@@ -191,15 +191,17 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const float *theta, const floa
         store_act(acc, r0, s.h3, s.gd3, a);
         float o[1][4];
         layer<4, 1>(a, s.w.w4, s.w.b4, o);
-        // output deltas 2 (y - t) / B
+        // output deltas 2 w (y - t) / B (w = 1 without sample weights)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int rl = r0 + g + (q >= 2 ? 8 : 0), c = 2 * t + (q & 1);
             float dlt = 0.f;
             if (c < OUT && base + rl < batch) {
-                const float diff = o[0][q] - Y[(size_t)idx[base + rl] * OUT + c];
-                loss += diff * diff;
-                dlt = 2.0f * diff * inv_b;
+                const int row = idx[base + rl];
+                const float diff = o[0][q] - Y[(size_t)row * OUT + c];
+                const float wd = W ? W[row] * diff : diff;
+                loss += wd * diff;
+                dlt = 2.0f * wd * inv_b;
             }
             if (c < 4) s.d4[rl * 4 + c] = dlt;
         }
@@ -313,7 +315,7 @@ struct pbs_mlp {
     cudaStream_t stream = nullptr;
     int sms = 148;
     float *theta = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *part = nullptr;
-    float *X = nullptr, *Y = nullptr, *io = nullptr;
+    float *X = nullptr, *Y = nullptr, *W = nullptr, *io = nullptr;
     int *idx = nullptr;
     int n = 0, cap_part = 0, cap_io = 0, step = 0;
 };
@@ -344,13 +346,13 @@ static int ensure_part(pbs_mlp *t, int nparts) {
     return PBS_OK;
 }
 
-static int run_grad(pbs_mlp *t, const float *X, const float *Y, const int *idx, int batch) {
+static int run_grad(pbs_mlp *t, const float *X, const float *Y, const float *W, const int *idx, int batch) {
     const int ctas = grad_ctas(batch, t->sms);
     int rc = ensure_part(t, ctas);
     if (rc != PBS_OK) return rc;
     const size_t smem = sizeof(TrainSmem);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_mlp_grad<<<ctas, 128, smem, t->stream>>>(t->theta, X, Y, idx, batch, t->part);
+    k_mlp_grad<<<ctas, 128, smem, t->stream>>>(t->theta, X, Y, W, idx, batch, t->part);
     MCK(cudaGetLastError());
     k_mlp_reduce<<<(NPART + 255) / 256, 256, 0, t->stream>>>(t->part, ctas, t->grad);
     MCK(cudaGetLastError());
@@ -397,7 +399,7 @@ int pbs_mlp_create(pbs_mlp **out, const float *theta, unsigned long long seed) {
 void pbs_mlp_destroy(pbs_mlp *t) {
     if (!t) return;
     if (t->stream) cudaStreamSynchronize(t->stream);
-    float *bufs[] = {t->theta, t->m, t->v, t->grad, t->part, t->X, t->Y, t->io};
+    float *bufs[] = {t->theta, t->m, t->v, t->grad, t->part, t->X, t->Y, t->W, t->io};
     for (float *b : bufs)
         if (b) cudaFree(b);
     if (t->idx) cudaFree(t->idx);
@@ -447,7 +449,7 @@ int pbs_mlp_gradient(pbs_mlp *t, const float *X, const float *Y, int n, float *g
     if (e == cudaSuccess) e = cudaMemcpyAsync(dY, Y, sizeof(float) * (size_t)n * OUT, cudaMemcpyHostToDevice, t->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(didx, iota.data(), sizeof(int) * n, cudaMemcpyHostToDevice, t->stream);
     if (e != cudaSuccess) { cudaFree(didx); return PBS_E_CUDA; }
-    rc = run_grad(t, dX, dY, didx, n);
+    rc = run_grad(t, dX, dY, nullptr, didx, n);
     std::vector<float> g(NPART);
     if (rc == PBS_OK && cudaMemcpyAsync(g.data(), t->grad, sizeof(float) * NPART, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess)
         rc = PBS_E_CUDA;
@@ -459,19 +461,25 @@ int pbs_mlp_gradient(pbs_mlp *t, const float *X, const float *Y, int n, float *g
     return PBS_OK;
 }
 
-int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, int n) {
+int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, const float *W, int n) {
     if (!t || !X || !Y || n <= 0) return PBS_E_INVALID_ARG;
+    if (W)
+        for (int i = 0; i < n; ++i)
+            if (!(W[i] >= 0.f) || !std::isfinite(W[i])) return PBS_E_INVALID_ARG;
     if (t->X) cudaFree(t->X);
     if (t->Y) cudaFree(t->Y);
+    if (t->W) cudaFree(t->W);
     if (t->idx) cudaFree(t->idx);
-    t->X = t->Y = nullptr;
+    t->X = t->Y = t->W = nullptr;
     t->idx = nullptr;
     t->n = 0;
     MCK(cudaMalloc(&t->X, sizeof(float) * (size_t)n * IN));
     MCK(cudaMalloc(&t->Y, sizeof(float) * (size_t)n * OUT));
+    if (W) MCK(cudaMalloc(&t->W, sizeof(float) * (size_t)n));
     MCK(cudaMalloc(&t->idx, sizeof(int) * (size_t)n));
     MCK(cudaMemcpyAsync(t->X, X, sizeof(float) * (size_t)n * IN, cudaMemcpyHostToDevice, t->stream));
     MCK(cudaMemcpyAsync(t->Y, Y, sizeof(float) * (size_t)n * OUT, cudaMemcpyHostToDevice, t->stream));
+    if (W) MCK(cudaMemcpyAsync(t->W, W, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, t->stream));
     MCK(cudaStreamSynchronize(t->stream));
     t->n = n;
     return PBS_OK;
@@ -495,7 +503,7 @@ int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long
             MCK(cudaMemcpyAsync(t->idx, perm.data(), sizeof(int) * t->n, cudaMemcpyHostToDevice, t->stream));
             pos = 0;
         }
-        int rc = run_grad(t, t->X, t->Y, t->idx + pos, batch);
+        int rc = run_grad(t, t->X, t->Y, t->W, t->idx + pos, batch);
         if (rc != PBS_OK) return rc;
         pos += batch;
         t->step += 1;

@@ -58,6 +58,7 @@ struct pbs_handle {
     DevBuf<ushort4> qloc, qslot;
     DevBuf<float4> qrow0, qrow1, qrow2, part, parth;
     DevBuf<double2> cpart;
+    DevBuf<double> rslot;
     // device state
     DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl, ub;
     // learned warm start
@@ -96,7 +97,7 @@ struct pbs_handle {
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
         s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
-        s.cpart = cpart.p; s.part = part.p; s.parth = parth.p;
+        s.cpart = cpart.p; s.part = part.p; s.parth = parth.p; s.rslot = rslot.p;
         return s;
     }
     void release() {
@@ -111,7 +112,7 @@ struct pbs_handle {
                              &staging_ids};
         for (auto b : ii) b->release();
         ws_theta.release(); ws_stats.release();
-        chunk.release(); qloc.release(); qslot.release(); cpart.release();
+        chunk.release(); qloc.release(); qslot.release(); cpart.release(); rslot.release();
         DevBuf<int> *ci[] = {&chunk_inst, &qperm, &lnode, &lsptr, &lpidx, &pptr};
         for (auto b : ci) b->release();
         DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
@@ -364,7 +365,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->qperm.alloc(T)); CKC(h->qloc.alloc(T)); CKC(h->qslot.alloc(T));
     CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T));
     CKC(h->lnode.alloc(L)); CKC(h->lsptr.alloc(L)); CKC(h->lpidx.alloc(L)); CKC(h->pptr.alloc(Np + 1));
-    CKC(h->part.alloc(L)); CKC(h->parth.alloc(L));
+    CKC(h->part.alloc(L)); CKC(h->parth.alloc(L)); CKC(h->rslot.alloc(12 * (size_t)T));
     CKC(prepare_chunk_kernels());
     cudaStream_t s = h->stream;
     CKC(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * h->n_chunks, cudaMemcpyHostToDevice, s));

@@ -37,6 +37,7 @@
 //   pptr        int[Np+1]          node i's partials: part[pptr[i] .. pptr[i+1]-1], by chunk
 //   part, parth float4[L]          per (node, chunk) partial force / Jacobi-diagonal sums
 //   cpart       double2[n_chunks]  per chunk {sum e, sum e^2}
+//   rslot       double[3][4T]      per-step FP64 corner forces at the base, by gather slot
 //   npart       double[n_nblk]     per node-block |g|^2
 //   ctl         InstCtl[n_inst]    per-instance descent state
 #pragma once
@@ -126,6 +127,7 @@ struct DevState {
     double2 *tpart, *cpart;
     double *npart;
     float4 *part, *parth;
+    double *rslot;  // 3 * 4T: FP64 corner forces at the base, by gather slot
     InstCtl *ctl;
     int *active;  // instances not yet done
 };

@@ -95,10 +95,13 @@ class MLPTrainer:
                 "pbs_mlp_gradient")
         return float(loss.value), g
 
-    def set_data(self, X, Y):
+    def set_data(self, X, Y, W=None):
+        """Training set; W: optional per-sample loss weights."""
         X = _f32(X).reshape(-1, N_FEATURES)
         Y = _f32(Y).reshape(-1, N_OUT)
-        L.check(L.lib().pbs_mlp_set_data(self._t, _ptr(X), _ptr(Y), C.c_int(X.shape[0])), "pbs_mlp_set_data")
+        W = _f32(W).reshape(-1) if W is not None else None
+        L.check(L.lib().pbs_mlp_set_data(self._t, _ptr(X), _ptr(Y), _ptr(W), C.c_int(X.shape[0])),
+                "pbs_mlp_set_data")
 
     def train(self, steps: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
         losses = np.empty(max(steps, 1), np.float32)

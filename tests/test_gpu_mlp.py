@@ -78,6 +78,27 @@ def test_adam_step_matches_oracle():
     t.close()
 
 
+def test_weighted_adam_step_matches_oracle():
+    """With per-sample loss weights, one full-batch Adam step moves every
+    parameter by -lr * sign of the FP64 weighted gradient (Adam's first step),
+    wherever that gradient is clearly non-zero."""
+    theta = OM.init_params(9).astype(np.float32)
+    t = MLPTrainer(theta)
+    X, Y = _data(512, 5)
+    W = np.random.default_rng(6).uniform(0.0, 4.0, 512).astype(np.float32)
+    t.set_data(X, Y, W)
+    lr = 1e-3
+    t.train(1, batch=512, lr=lr, seed=0)
+    step = t.params.astype(np.float64) - theta
+    _, g = OM.loss_and_grad(theta, X, Y, round_bf16=True, W=W)
+    clear = np.abs(g) > 1e-2 * np.abs(g).max()
+    assert clear.sum() > 1000
+    np.testing.assert_allclose(step[clear], -lr * np.sign(g[clear]), rtol=1e-2, atol=1e-6)
+    _, g_unw = OM.loss_and_grad(theta, X, Y, round_bf16=True)
+    assert (np.sign(g_unw[clear]) != np.sign(g[clear])).any()  # the weights changed the step
+    t.close()
+
+
 def test_training_reduces_loss():
     t = MLPTrainer(seed=11)
     X, Y = _data(20000, 4)

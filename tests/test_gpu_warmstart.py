@@ -89,7 +89,9 @@ def test_bad_prediction_falls_back():
     judge rejects it and the step equals the plain one."""
     m, x0, boundary = _pull_case()
     theta = np.zeros(MLPTrainer(seed=0).n_params, np.float32)
-    theta[-3:] = 5.0  # constant output bias: every node moved by 5 edge lengths
+    # constant output bias: every free node moved by 2e4 motion scales (at least
+    # two edge lengths, the scale being >= 1e-4 edge)
+    theta[-3:] = 2e4
     model = WarmStartModel(theta, np.zeros(24, np.float32), np.ones(24, np.float32), np.ones(3, np.float32))
     a = DescentSolver(m, positions=x0, params=residual_params())
     b = DescentSolver(m, positions=x0, params=residual_params())
