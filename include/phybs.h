@@ -101,6 +101,10 @@ typedef struct pbs_step_params {
     float energy_slack;       /* line-search rounding allowance: reject only if
                                  E > E_old + energy_slack * 2^-24 * sqrt(sum of squared
                                  energy terms); 0 = the reference's strict E > E_old */
+    int incremental_stress;   /* neo-Hookean passes: 1 = evaluate P(F) - P(F_base) against
+                                 an FP64 force at the step's initial guess (residual
+                                 accurate far below 1e-6 of its initial value),
+                                 0 = the full FP32 stress each pass (fewer operations) */
 } pbs_step_params;
 
 typedef struct pbs_stats {
@@ -267,9 +271,10 @@ int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean
 /* The 24 raw (unstandardised) features of every node for the next step with
  * external forces ext (or NULL), the plain initial guess x~ + warm_start
  * h (v - v_old) (x_init, 3*N, may be NULL) and each node's motion scale
- * s = |d1| + |d2| + 1e-4 l (scale, N, may be NULL; d1, d2 the node's last two
- * displacements, l the instance's mean edge length), which divides the
- * length features.  The state is not advanced. */
+ * s = (1 - damping) |d1| + |d1 - d2| + 1e-4 l (scale, N, may be NULL; d1, d2
+ * the node's last two displacements, l the instance's mean edge length: the
+ * plain guess's error under constant acceleration), which divides the length
+ * features.  The state is not advanced. */
 int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init, float *scale);
 
 /* Node-node 3N x 3N stiffness pattern of the mesh, bit-identical to

@@ -150,7 +150,7 @@ static void to_dev_params(const pbs_step_params &p, DevParams &d) {
     d.clamp_cpu = p.energy_clamp == PBS_CLAMP_CPU ? 1 : 0;
     d.pass_cap = p.pass_cap > 0 ? p.pass_cap : p.max_iters + 16;
     d.energy_slack = p.energy_slack;
-    d.incremental = 0;  // set from the material by the handle
+    d.incremental = 0;  // set from the material and incremental_stress by the handle
 }
 
 extern "C" {
@@ -174,6 +174,7 @@ void pbs_default_params(pbs_step_params *p) {
     p->energy_clamp = PBS_CLAMP_CPU;
     p->pass_cap = 0;
     p->energy_slack = 0.0f;
+    p->incremental_stress = 1;
 }
 
 const char *pbs_error_string(int code) {
@@ -204,7 +205,8 @@ static int validate_params(const pbs_step_params *p) {
     if (!(p->h > 0.f) || p->max_iters < 0 || p->line_search_every <= 0 || p->hessian_every <= 0 ||
         p->n_profile < 0 || p->n_profile > 4 || !(p->alpha0 > 0.f) || !(p->alpha_shrink > 0.f) ||
         p->alpha_shrink >= 1.f || (p->control != PBS_CONTROL_REFERENCE && p->control != PBS_CONTROL_RESTART) ||
-        p->tol < 0.f || p->pass_cap < 0 || !(p->energy_slack >= 0.f))
+        p->tol < 0.f || p->pass_cap < 0 || !(p->energy_slack >= 0.f) ||
+        (p->incremental_stress != 0 && p->incremental_stress != 1))
         return PBS_E_INVALID_ARG;
     return PBS_OK;
 }
@@ -465,7 +467,7 @@ int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lam
     CK(e);
     if (h->material != model) h->graph_valid = false;
     h->material = model;
-    h->dparams.incremental = model == PBS_MATERIAL_NEOHOOKEAN ? 1 : 0;
+    h->dparams.incremental = model == PBS_MATERIAL_NEOHOOKEAN && h->params.incremental_stress ? 1 : 0;
     return PBS_OK;
 }
 
@@ -475,7 +477,7 @@ int pbs_set_params(pbs_handle *h, const pbs_step_params *p) {
     if (rc != PBS_OK) return rc;
     h->params = *p;
     to_dev_params(h->params, h->dparams);
-    h->dparams.incremental = h->material == PBS_MATERIAL_NEOHOOKEAN ? 1 : 0;
+    h->dparams.incremental = h->material == PBS_MATERIAL_NEOHOOKEAN && h->params.incremental_stress ? 1 : 0;
     h->graph_valid = false;
     return PBS_OK;
 }

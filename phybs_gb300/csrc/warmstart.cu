@@ -113,13 +113,16 @@ __global__ void k_ws_tet_F(DevMesh m, DevState st, float *tetF) {
 }
 
 // The 24 raw features of node i (see phybs_gb300/warmstart.py for the list)
-// and its motion scale s = |d1| + |d2| + 1e-4 l (d1, d2: the last two
-// displacements, l: the mean edge length), which divides every length
-// feature and the predicted correction.
+// and its motion scale s = (1 - damping) |d1| + |d1 - d2| + 1e-4 l (d1, d2:
+// the last two displacements, l: the mean edge length): the size of the plain
+// guess's error when the node moves with constant acceleration.  It divides
+// every length feature and the predicted correction, so the network's target
+// is O(1) in smooth motion, where the guess is worth most.
 __device__ __forceinline__ void node_features(const DevMesh &m, const DevState &st, const DevParams &p,
                                               const float *tetF, float ell, int i, float f[24], float &scale) {
     const float4 v = st.v[i], vo = st.vold[i], h1 = st.hist1[i], h2 = st.hist2[i];
-    scale = sqrtf(h1.x * h1.x + h1.y * h1.y + h1.z * h1.z) + sqrtf(h2.x * h2.x + h2.y * h2.y + h2.z * h2.z) +
+    const float ax = h1.x - h2.x, ay = h1.y - h2.y, az = h1.z - h2.z;
+    scale = (1.0f - p.damping) * sqrtf(h1.x * h1.x + h1.y * h1.y + h1.z * h1.z) + sqrtf(ax * ax + ay * ay + az * az) +
             1e-4f * ell;
     const float il = 1.0f / scale, ivl = p.h / scale, wo = p.warm_start * p.h / scale;
     f[0] = v.x * ivl; f[1] = v.y * ivl; f[2] = v.z * ivl;
@@ -331,8 +334,11 @@ cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &
 }
 
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
+    // without incremental stress the elastic force at the plain guess is not in b
     if (material == PBS_MATERIAL_STRETCH)
         k_ws_force<PBS_MATERIAL_STRETCH><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, st.uh);
+    else if (!p.incremental)
+        k_ws_force<PBS_MATERIAL_NEOHOOKEAN><<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, st.uh);
     k_ws_gref<<<m.n_nblk, BLOCK, 0, s>>>(m, p, st);
     return cudaGetLastError();
 }

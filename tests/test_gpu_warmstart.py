@@ -39,11 +39,13 @@ def test_features_match_definition():
     ell = mean_edge(m)
     h = 1 / 30
     free = m.pin_mask() == 0
-    # s = |d1| + |d2| + 1e-4 l from the last two displacements (pinned nodes are
-    # prescribed between steps, so only free nodes follow the recorded history)
+    # s = (1 - damping) |d1| + |d1 - d2| + 1e-4 l from the last two displacements
+    # (pinned nodes are prescribed between steps, so only free nodes follow the
+    # recorded history)
     d1, d2 = xs[3] - xs[2], xs[2] - xs[1]
-    ref_scale = np.linalg.norm(d1, axis=1) + np.linalg.norm(d2, axis=1) + 1e-4 * ell
-    np.testing.assert_allclose(scale[free], ref_scale[free], rtol=1e-3, atol=1e-6 * ell)
+    ref_scale = 0.01 * np.linalg.norm(d1, axis=1) + np.linalg.norm(d1 - d2, axis=1) + 1e-4 * ell
+    # |d1 - d2| from read-back FP32 positions carries their rounding (~1e-8 m)
+    np.testing.assert_allclose(scale[free], ref_scale[free], rtol=1e-2, atol=1e-7 + 1e-6 * ell)
     sc = scale[:, None]
     np.testing.assert_allclose(feats[free, 0:3], (v * h / sc)[free], rtol=1e-4, atol=1e-4)
     np.testing.assert_allclose(feats[free, 3:6], (d1 / sc)[free], rtol=1e-3, atol=1e-3)
