@@ -232,6 +232,25 @@ int pbs_get_stream(pbs_handle *h, void **stream);
  * pbs_get_stats then describes that instance. */
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms);
 
+/* Chunk shape of the per-tet pass kernel picked by pbs_autotune. */
+typedef struct pbs_tune_result {
+    int chunk_threads;       /* threads per CTA                                   */
+    int chunk_tets;          /* tets per chunk at most                            */
+    int chunk_nodes;         /* nodes a chunk may touch at most                   */
+    int n_tried;             /* shapes timed                                      */
+    double pass_ms;          /* per-tet + per-node kernel time of one pass, kept shape */
+    double default_pass_ms;  /* the same for the default shape (256, 1024, 448)   */
+} pbs_tune_result;
+/* Autotuner of the pass kernels' block and tile shape: rebuilds the pass
+ * layout for each candidate chunk shape (threads per CTA, tets per chunk,
+ * nodes per chunk), times `passes` passes of it from the current state with
+ * CUDA events and keeps the fastest.  Forces stay deterministic for a given
+ * shape; another shape changes the order the corner forces are summed in, so
+ * results can differ in the last bits.  Call between steps (it recaptures the
+ * step graph).  No counterpart in the reference, whose launch shapes are
+ * fixed. */
+int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
+
 /* ------------------------------------------------------------------------
  * Learned warm start.  A per-node MLP 24 -> 64 -> 64 -> 64 -> 3 (GELU; BF16
  * weights on the tensor cores, FP32 accumulation; 10,115 FP32 master

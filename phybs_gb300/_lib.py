@@ -38,7 +38,7 @@ EXPORTS = (
     "pbs_mlp_param_count", "pbs_mlp_create", "pbs_mlp_destroy", "pbs_mlp_get_params", "pbs_mlp_set_params",
     "pbs_mlp_forward", "pbs_mlp_gradient", "pbs_mlp_set_data", "pbs_mlp_train",
     "pbs_set_warm_start", "pbs_warm_start_features", "pbs_eval_nodes_static",
-    "pbs_set_guess",
+    "pbs_set_guess", "pbs_autotune",
 )
 
 PBS_EVAL_STATIC_MAX_TETS = 524288
@@ -65,6 +65,11 @@ class Stats(C.Structure):
                 ("status", C.c_int), ("alpha", C.c_float), ("rho", C.c_float), ("omega", C.c_float),
                 ("energy", C.c_double), ("residual_ratio", C.c_double), ("device_ms", C.c_double),
                 ("graph_launches", C.c_int), ("warm_start_used", C.c_int)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("chunk_threads", C.c_int), ("chunk_tets", C.c_int), ("chunk_nodes", C.c_int), ("n_tried", C.c_int),
+                ("pass_ms", C.c_double), ("default_pass_ms", C.c_double)]
 
 
 class PhybsError(RuntimeError):

@@ -1,11 +1,12 @@
 // The per-tet kernel of a descent pass, on chunks of tets.
 //
-// A chunk is a run of at most CHUNK_TETS tets of one instance, consecutive in
-// the Morton order of their centroids, that touches at most CHUNK_NODES
-// nodes.  One CTA per chunk:
+// A chunk is a run of at most chunk_tets tets of one instance, consecutive in
+// the Morton order of their centroids, that touches at most chunk_nodes nodes
+// (the handle's chunk shape: CHUNK_TETS / CHUNK_NODES / CHUNK_THREADS, or what
+// pbs_autotune picked).  One CTA per chunk:
 //   1. stages the chunk's nodes (u hi, u lo and the force base) in shared
 //      memory: each node is read once per chunk instead of once per corner;
-//   2. evaluates its tets (one thread per tet, CHUNK_TETS / CHUNK_THREADS tets
+//   2. evaluates its tets (one thread per tet, chunk tets / CTA threads tets
 //      a thread), streaming the per-tet rows in chunk order, and writes the 12
 //      corner forces to shared-memory slots, where a node's slots are
 //      contiguous in (tet, corner) order;
@@ -52,7 +53,7 @@ uint32_t spread10(uint32_t v) {  // 10 bits -> every third bit of 30
 }  // namespace
 
 void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<double> &rest, std::vector<InstCtl> &ctl,
-                  ChunkLayout &out) {
+                  int chunk_tets, int chunk_nodes, ChunkLayout &out) {
     out = ChunkLayout();
     std::vector<int> stamp(Np, -1), lidx(Np, 0), n_part(Np, 0);
     std::vector<std::pair<uint32_t, int>> order;
@@ -103,7 +104,7 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
             const int cid = (int)out.chunk.size();
             ctets.clear();
             lnodes.clear();
-            while (pos < order.size() && (int)ctets.size() < CHUNK_TETS) {
+            while (pos < order.size() && (int)ctets.size() < chunk_tets) {
                 const int t = order[pos].second;
                 const int *q = &tets[t].x;
                 int add = 0;
@@ -112,7 +113,7 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
                     for (int c2 = 0; c2 < c && !seen; ++c2) seen = q[c2] == q[c];
                     add += !seen;
                 }
-                if ((int)lnodes.size() + add > CHUNK_NODES) break;
+                if ((int)lnodes.size() + add > chunk_nodes) break;
                 for (int c = 0; c < 4; ++c)
                     if (stamp[q[c]] != cid) {
                         stamp[q[c]] = cid;
@@ -173,9 +174,10 @@ __global__ void k_pass_rows(int T, const int *qperm, const float4 *row0, const f
 
 // Sums every local node's slots (in slot order) into its partial for this
 // chunk.
+template <int THREADS>
 __device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl, int nt, const float *sx,
                                                const float *sy, const float *sz, float4 *out) {
-    for (int j = threadIdx.x; j < nl; j += CHUNK_THREADS) {
+    for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int s0 = m.lsptr[l0 + j];
         const int s1 = j + 1 < nl ? m.lsptr[l0 + j + 1] : 4 * nt;
         float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -188,13 +190,14 @@ __device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl,
     }
 }
 
-template <int MATERIAL>
-__global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
+template <int MATERIAL, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
     extern __shared__ float4 smem4[];
-    float4 *s_uh = smem4, *s_ul = smem4 + CHUNK_NODES, *s_ub = smem4 + 2 * CHUNK_NODES;
-    float *s_x = reinterpret_cast<float *>(smem4 + 3 * CHUNK_NODES);
-    float *s_y = s_x + 4 * CHUNK_TETS, *s_z = s_y + 4 * CHUNK_TETS;
-    __shared__ double sh[CHUNK_THREADS / 32];
+    const int CN = m.chunk_nodes, CT = m.chunk_tets;
+    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;
+    float *s_x = reinterpret_cast<float *>(smem4 + 3 * CN);
+    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
+    __shared__ double sh[THREADS / 32];
     __shared__ int is_last;
     const int c = blockIdx.x;
     InstCtl *cp = st.ctl + m.chunk_inst[c];
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
     const size_t cur = (size_t)cp->par * m.Np;
     const int4 cd = m.chunk[c];
     const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
-    for (int j = threadIdx.x; j < nl; j += CHUNK_THREADS) {
+    for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int g = m.lnode[l0 + j];
         s_uh[j] = st.uh[cur + g];
         s_ul[j] = st.ul[cur + g];
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
     }
     __syncthreads();
     double e = 0.0;
-    for (int lt = threadIdx.x; lt < nt; lt += CHUNK_THREADS) {
+    for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const int q = tq0 + lt;
         const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
         const ushort4 lc = m.qloc[q], sl = m.qslot[q];
@@ -234,10 +237,10 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
         if (check) e += (double)clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu);
     }
     __syncthreads();
-    chunk_partials(m, l0, nl, nt, s_x, s_y, s_z, st.part);
+    chunk_partials<THREADS>(m, l0, nl, nt, s_x, s_y, s_z, st.part);
     if (do_h) {  // Jacobi-diagonal refresh: the same slots carry the 12 diagonal terms
         __syncthreads();
-        for (int lt = threadIdx.x; lt < nt; lt += CHUNK_THREADS) {
+        for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
             const int q = tq0 + lt;
             const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
             const ushort4 lc = m.qloc[q], sl = m.qslot[q];
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
             }
         }
         __syncthreads();
-        chunk_partials(m, l0, nl, nt, s_x, s_y, s_z, st.parth);
+        chunk_partials<THREADS>(m, l0, nl, nt, s_x, s_y, s_z, st.parth);
     }
     if (!check) return;
     // line-search pass: add this chunk's share of the instance's node terms
@@ -265,8 +268,8 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
     {
         const int nb = cp->cblk_end - cp->cblk_begin;
         const float4 *U = st.uh + cur;
-        for (int i = cp->node_begin + (c - cp->cblk_begin) * CHUNK_THREADS + threadIdx.x; i < cp->node_end;
-             i += nb * CHUNK_THREADS) {
+        for (int i = cp->node_begin + (c - cp->cblk_begin) * THREADS + threadIdx.x; i < cp->node_end;
+             i += nb * THREADS) {
             const float4 info = m.info[i];
             if (info.z != 0.f) continue;
             const double en = node_energy(st, info, U[i], st.ul[cur + i], i, p.h2inv);
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
     __threadfence();
     // the instance's last chunk: fixed-order sums, then accept / reject
     double E = 0.0, E2 = 0.0;
-    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += CHUNK_THREADS) {
+    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += THREADS) {
         const double2 v = __ldcg(st.cpart + j);
         E += v.x;
         E2 += v.y;
@@ -324,12 +327,18 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_tchunk(DevMesh m, DevParams p
 }
 
 // ------------------------------------------------------------ launchers
+template <int MATERIAL, int THREADS> static cudaError_t allow_smem() {
+    return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                CHUNK_MAX_SMEM);
+}
+
 cudaError_t prepare_chunk_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_tchunk<PBS_MATERIAL_NEOHOOKEAN>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CHUNK_SMEM);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_tchunk<PBS_MATERIAL_STRETCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)CHUNK_SMEM);
+    const cudaError_t e[] = {allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128>(), allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256>(),
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 512>(), allow_smem<PBS_MATERIAL_STRETCH, 128>(),
+                             allow_smem<PBS_MATERIAL_STRETCH, 256>(), allow_smem<PBS_MATERIAL_STRETCH, 512>()};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const float4 *row0, const float4 *row1,
@@ -339,12 +348,23 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
+template <int MATERIAL>
+static void launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st) {
+    const size_t smem = chunk_smem(m.chunk_tets, m.chunk_nodes);
+    if (m.chunk_threads == 128)
+        k_tchunk<MATERIAL, 128><<<m.n_chunks, 128, smem, s>>>(m, p, st);
+    else if (m.chunk_threads == 512)
+        k_tchunk<MATERIAL, 512><<<m.n_chunks, 512, smem, s>>>(m, p, st);
+    else
+        k_tchunk<MATERIAL, 256><<<m.n_chunks, 256, smem, s>>>(m, p, st);
+}
+
 cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
     if (m.n_chunks <= 0) return cudaSuccess;
     if (material == PBS_MATERIAL_STRETCH)
-        k_tchunk<PBS_MATERIAL_STRETCH><<<m.n_chunks, CHUNK_THREADS, CHUNK_SMEM, s>>>(m, p, st);
+        launch_tchunk<PBS_MATERIAL_STRETCH>(s, m, p, st);
     else
-        k_tchunk<PBS_MATERIAL_NEOHOOKEAN><<<m.n_chunks, CHUNK_THREADS, CHUNK_SMEM, s>>>(m, p, st);
+        launch_tchunk<PBS_MATERIAL_NEOHOOKEAN>(s, m, p, st);
     return cudaGetLastError();
 }
 

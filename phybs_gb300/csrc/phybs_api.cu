@@ -51,8 +51,10 @@ struct pbs_handle {
     DevBuf<int4> tets, tslot;
     DevBuf<float4> row0, row1, row2, info, rest4;
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
-    // pass layout (chunks of tets)
-    int n_chunks = 0;
+    // pass layout (chunks of tets) and the host copies it is rebuilt from
+    int n_chunks = 0, chunk_tets = CHUNK_TETS, chunk_nodes = CHUNK_NODES, chunk_threads = CHUNK_THREADS;
+    std::vector<int4> h_tets_pad;
+    std::vector<double> h_rest_pad;
     DevBuf<int4> chunk;
     DevBuf<int> chunk_inst, qperm, lnode, lsptr, lpidx, pptr;
     DevBuf<ushort4> qloc, qslot;
@@ -87,6 +89,7 @@ struct pbs_handle {
         m.inc_ptr = inc_ptr.p; m.inc = inc.p; m.tslot = tslot.p; m.info = info.p; m.rest = rest4.p;
         m.tblk_inst = tblk_inst.p; m.nblk_inst = nblk_inst.p;
         m.n_chunks = n_chunks; m.chunk = chunk.p; m.chunk_inst = chunk_inst.p;
+        m.chunk_tets = chunk_tets; m.chunk_nodes = chunk_nodes; m.chunk_threads = chunk_threads;
         m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qloc = qloc.p; m.qslot = qslot.p;
         m.lnode = lnode.p; m.lsptr = lsptr.p; m.lpidx = lpidx.p; m.pptr = pptr.p;
         return m;
@@ -135,6 +138,57 @@ struct pbs_handle {
             return e__ == cudaErrorMemoryAllocation ? PBS_E_OUT_OF_MEMORY : PBS_E_CUDA; \
         }                                                       \
     } while (0)
+
+// (Re)builds the pass layout with the given chunk shape: host chunking of the
+// padded mesh, the device arrays, the chunk-ordered copy of the per-tet rows
+// (when they exist) and the instances' chunk ranges.  host_ctl: the control
+// blocks still on the host (creation), else those on the device are updated.
+static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, std::vector<InstCtl> *host_ctl) {
+    std::vector<InstCtl> ctl;
+    if (host_ctl) {
+        ctl = *host_ctl;
+    } else {
+        ctl.resize(h->B);
+        CK(cudaMemcpy(ctl.data(), h->ctl.p, sizeof(InstCtl) * h->B, cudaMemcpyDeviceToHost));
+    }
+    ChunkLayout cl;
+    build_chunks(h->Np, h->h_tets_pad, h->h_rest_pad, ctl, ct, cn, cl);
+    const int nc = (int)cl.chunk.size();
+    const size_t L = cl.lnode.size(), T = (size_t)h->T;
+    h->chunk.release(); h->chunk_inst.release(); h->cpart.release(); h->qperm.release(); h->qloc.release();
+    h->qslot.release(); h->lnode.release(); h->lsptr.release(); h->lpidx.release(); h->pptr.release();
+    h->part.release(); h->parth.release();
+    CK(h->chunk.alloc(nc)); CK(h->chunk_inst.alloc(nc)); CK(h->cpart.alloc(nc));
+    CK(h->qperm.alloc(T)); CK(h->qloc.alloc(T)); CK(h->qslot.alloc(T));
+    CK(h->lnode.alloc(L)); CK(h->lsptr.alloc(L)); CK(h->lpidx.alloc(L)); CK(h->pptr.alloc(h->Np + 1));
+    CK(h->part.alloc(L)); CK(h->parth.alloc(L));
+    cudaStream_t s = h->stream;
+    CK(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * nc, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->chunk_inst.p, cl.chunk_inst.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->qperm.p, cl.qperm.data(), sizeof(int) * T, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->qloc.p, cl.qloc.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->qslot.p, cl.qslot.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->lnode.p, cl.lnode.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->lsptr.p, cl.lsptr.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->lpidx.p, cl.lpidx.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->pptr.p, cl.pptr.data(), sizeof(int) * (h->Np + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(h->part.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
+    CK(cudaMemsetAsync(h->parth.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
+    h->n_chunks = nc;
+    h->chunk_threads = threads;
+    h->chunk_tets = ct;
+    h->chunk_nodes = cn;
+    if (host_ctl) {
+        *host_ctl = ctl;
+    } else {
+        CK(cudaMemcpyAsync(h->ctl.p, ctl.data(), sizeof(InstCtl) * h->B, cudaMemcpyHostToDevice, s));
+        CK(launch_pass_rows(s, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0.p, h->qrow1.p,
+                            h->qrow2.p));
+    }
+    CK(cudaStreamSynchronize(s));
+    h->graph_valid = false;
+    return PBS_OK;
+}
 
 static void to_dev_params(const pbs_step_params &p, DevParams &d) {
     d.h = p.h;
@@ -334,10 +388,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         rest4[ip] = make_float4(d->rest[3 * (size_t)i], d->rest[3 * (size_t)i + 1], d->rest[3 * (size_t)i + 2], 0.f);
     }
     h->h_rest.assign(d->rest, d->rest + 3 * (size_t)N);
-    ChunkLayout cl;
-    build_chunks(Np, tets_pad, rest_pad, ctl, cl);
-    h->n_chunks = (int)cl.chunk.size();
-    const size_t L = cl.lnode.size();
+    h->h_tets_pad = tets_pad;
+    h->h_rest_pad = rest_pad;
 
     auto fail = [&](int code) { h->release(); delete h; return code; };
 #define CKC(x) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) return fail(e__ == cudaErrorMemoryAllocation ? PBS_E_OUT_OF_MEMORY : PBS_E_CUDA); } while (0)
@@ -363,24 +415,13 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
-    CKC(h->chunk.alloc(h->n_chunks)); CKC(h->chunk_inst.alloc(h->n_chunks)); CKC(h->cpart.alloc(h->n_chunks));
-    CKC(h->qperm.alloc(T)); CKC(h->qloc.alloc(T)); CKC(h->qslot.alloc(T));
-    CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T));
-    CKC(h->lnode.alloc(L)); CKC(h->lsptr.alloc(L)); CKC(h->lpidx.alloc(L)); CKC(h->pptr.alloc(Np + 1));
-    CKC(h->part.alloc(L)); CKC(h->parth.alloc(L)); CKC(h->rslot.alloc(12 * (size_t)T));
+    CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T)); CKC(h->rslot.alloc(12 * (size_t)T));
     CKC(prepare_chunk_kernels());
     cudaStream_t s = h->stream;
-    CKC(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * h->n_chunks, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->chunk_inst.p, cl.chunk_inst.data(), sizeof(int) * h->n_chunks, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->qperm.p, cl.qperm.data(), sizeof(int) * T, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->qloc.p, cl.qloc.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->qslot.p, cl.qslot.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->lnode.p, cl.lnode.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->lsptr.p, cl.lsptr.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->lpidx.p, cl.lpidx.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
-    CKC(cudaMemcpyAsync(h->pptr.p, cl.pptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
-    CKC(cudaMemsetAsync(h->part.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
-    CKC(cudaMemsetAsync(h->parth.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
+    {
+        const int rc = set_pass_layout(h, CHUNK_THREADS, CHUNK_TETS, CHUNK_NODES, &ctl);
+        if (rc != PBS_OK) return fail(rc);
+    }
     CKC(cudaMemcpyAsync(h->tets.p, tets_pad.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->tslot.p, tslot.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
     CKC(cudaMemcpyAsync(h->inc_ptr.p, iptr.data(), sizeof(int) * (Np + 1), cudaMemcpyHostToDevice, s));
@@ -701,9 +742,13 @@ int pbs_get_stream(pbs_handle *h, void **stream) {
     return PBS_OK;
 }
 
-int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
-    if (!h || passes <= 0 || !tet_ms || !node_ms) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+}  // extern "C"
+
+// Times `passes` passes from the current state (CUDA events around each
+// kernel on the handle's stream); the state the next step starts from (u0,
+// velocities) is untouched.  Fails when an instance stopped before the last
+// pass, leaving its counters in h->stats.
+static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
     cudaStream_t s = h->stream;
     DevParams p = h->dparams;
     p.max_iters = passes + 1;
@@ -752,6 +797,56 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     }
     *tet_ms = tt / passes;
     *node_ms = tn / passes;
+    return PBS_OK;
+}
+
+extern "C" {
+
+int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
+    if (!h || passes <= 0 || !tet_ms || !node_ms) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    return time_passes(h, passes, tet_ms, node_ms);
+}
+
+int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
+    if (!h || passes <= 0) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch
+    static const int shapes[][3] = {{256, 1024, 448}, {256, 768, 352}, {256, 512, 256}, {128, 512, 256},
+                                    {128, 256, 160}, {512, 1024, 448}, {512, 2048, 832}};
+    const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
+    const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes;
+    double best = 1e300, first = -1.0;
+    int bi = -1, tried = 0;
+    for (int i = 0; i < n; ++i) {
+        int rc = set_pass_layout(h, shapes[i][0], shapes[i][1], shapes[i][2], nullptr);
+        if (rc != PBS_OK) return rc;
+        double a = 0.0, b = 0.0;
+        rc = time_passes(h, passes, &a, &b);  // warm-up run, then the timed one
+        if (rc == PBS_OK) rc = time_passes(h, passes, &a, &b);
+        if (rc != PBS_OK) {
+            // the state cannot be timed: restore the shape the handle had
+            const int rc2 = set_pass_layout(h, t0, c0, n0, nullptr);
+            return rc2 != PBS_OK ? rc2 : rc;
+        }
+        const double t = a + b;
+        ++tried;
+        if (i == 0) first = t;
+        if (t < best) {
+            best = t;
+            bi = i;
+        }
+    }
+    const int rc = set_pass_layout(h, shapes[bi][0], shapes[bi][1], shapes[bi][2], nullptr);
+    if (rc != PBS_OK) return rc;
+    if (out) {
+        out->chunk_threads = shapes[bi][0];
+        out->chunk_tets = shapes[bi][1];
+        out->chunk_nodes = shapes[bi][2];
+        out->n_tried = tried;
+        out->pass_ms = best;
+        out->default_pass_ms = first;
+    }
     return PBS_OK;
 }
 

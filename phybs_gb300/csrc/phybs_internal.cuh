@@ -50,10 +50,16 @@ namespace pbs {
 
 constexpr int PAD = 256;    // instance alignment (tets and nodes)
 constexpr int BLOCK = 256;  // threads per block of the step kernels
-constexpr int CHUNK_TETS = 1024;    // tets per chunk at most
-constexpr int CHUNK_NODES = 448;    // nodes a chunk may touch
-constexpr int CHUNK_THREADS = 256;  // threads of the chunked per-tet kernel
-constexpr size_t CHUNK_SMEM = 3 * sizeof(float4) * CHUNK_NODES + 3 * sizeof(float) * 4 * CHUNK_TETS;
+// Default chunk shape of the per-tet pass kernel (pbs_autotune may pick
+// another): at most CHUNK_TETS tets touching at most CHUNK_NODES nodes, one
+// CTA of CHUNK_THREADS threads per chunk.
+constexpr int CHUNK_TETS = 1024;
+constexpr int CHUNK_NODES = 448;
+constexpr int CHUNK_THREADS = 256;
+constexpr int CHUNK_MAX_SMEM = 200 * 1024;
+__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes) {
+    return 3 * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets;
+}
 
 // Step parameters as the kernels see them (a by-value kernel argument).
 struct DevParams {
@@ -107,7 +113,7 @@ struct DevMesh {
     const float4 *info, *rest;
     const int *tblk_inst, *nblk_inst;
     // pass layout
-    int n_chunks;
+    int n_chunks, chunk_tets, chunk_nodes, chunk_threads;
     const int4 *chunk;
     const int *chunk_inst;
     const float4 *qrow0, *qrow1, *qrow2;
@@ -172,7 +178,7 @@ struct ChunkLayout {
     int max_local = 0;
 };
 void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<double> &rest, std::vector<InstCtl> &ctl,
-                  ChunkLayout &out);
+                  int chunk_tets, int chunk_nodes, ChunkLayout &out);
 cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const float4 *row0, const float4 *row1,
                              const float4 *row2, float4 *q0, float4 *q1, float4 *q2);
 cudaError_t prepare_chunk_kernels();

@@ -149,6 +149,12 @@ class DescentSolver:
         L.check(L.lib().pbs_profile_kernels(self._h, C.c_int(passes), C.byref(a), C.byref(b)), "pbs_profile_kernels")
         return a.value, b.value
 
+    def autotune(self, passes: int = 32) -> dict:
+        """Pick the pass kernels' chunk shape by timing candidates on this mesh."""
+        r = L.TuneResult()
+        L.check(L.lib().pbs_autotune(self._h, C.c_int(passes), C.byref(r)), "pbs_autotune")
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
     def warm_start_features(self, ext=None):
         """Raw 24 features per node for the next step, the plain initial
         guess, and each node's motion scale (features, x_init, scale)."""

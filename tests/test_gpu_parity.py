@@ -340,3 +340,22 @@ def test_cuda_interface_wrapper():
     ci.doDescentOpt(0.03, 96, np.zeros(3 * n, np.float32), host)
     assert np.isfinite(host).all() and np.abs(host.reshape(-1, 3) - g["rest"]).max() > 0
     ci.reset()
+
+
+def test_autotune_keeps_results():
+    """pbs_autotune picks one of its chunk shapes by timing them on the mesh;
+    a tuned handle steps to the same positions as an untuned one (the shape
+    only changes the order corner forces are summed in)."""
+    m = M.box_mesh(12, 12, 20, edge=0.01, seed=4, young=1e5, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=64)
+    a = DescentSolver(m, params=p)
+    b = DescentSolver(m, params=p)
+    r = b.autotune(8)
+    assert r["n_tried"] == 7 and r["chunk_threads"] in (128, 256, 512)
+    assert 0.0 < r["pass_ms"] <= r["default_pass_ms"]
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-5
+    a.close()
+    b.close()
