@@ -86,11 +86,18 @@ ALPHA0 = 0.3
 RHO = 0.9999
 
 
-def solver_params(h=1 / 30, tol=1e-4, max_iters=20000, alpha0=ALPHA0, rho=RHO):
+# Stress evaluation of the passes: the full FP32 stress reaches |g| <= 1e-4 |g0|
+# on this workload in the same iterations as the incremental form (22,542 vs
+# 22,643 over the first 10 frames) with ~13% less time per pass.
+INCREMENTAL_STRESS = 0
+
+
+def solver_params(h=1 / 30, tol=1e-4, max_iters=20000, alpha0=ALPHA0, rho=RHO, incremental=None):
     from phybs_gb300 import _lib as L
     from phybs_gb300.solver import make_params
+    inc = INCREMENTAL_STRESS if incremental is None else incremental
     return make_params("gpu_reference", h=h, tol=tol, max_iters=max_iters, control=L.PBS_CONTROL_RESTART,
-                       energy_slack=16.0, alpha0=alpha0, profile=((10, rho),))
+                       energy_slack=16.0, alpha0=alpha0, profile=((10, rho),), incremental_stress=inc)
 
 
 class ClockSampler:
@@ -209,10 +216,14 @@ def run_reference(args):
 
 
 def launches_per_frame(graph_launches: int, warm: bool) -> int:
-    """Kernels of one frame: the boundary scatter; init_ctl, prologue,
-    ref_force, epilogue; with the warm start the reference-gradient kernel, tet F,
-    inference, judge, select and a second ref_force; 2 x 16 per graph launch."""
-    return 1 + 4 + (6 if warm else 0) + 2 * 16 * graph_launches
+    """Kernels of one frame: the boundary scatter; init_ctl, prologue, the
+    base force (per-tet FP64 + gather with incremental stress, the gather
+    alone otherwise), epilogue; with the warm start the plain guess's corner
+    forces (full stress only), reference gradient, tet F, inference, judge,
+    select and the base force again; 2 x 16 per graph launch."""
+    ref = 2 if INCREMENTAL_STRESS else 1
+    warm_extra = (0 if INCREMENTAL_STRESS else 1) + 5 + ref if warm else 0
+    return 1 + 3 + ref + warm_extra + 2 * 16 * graph_launches
 
 
 def run_arm(args, m, bottom, length, model, world, e2e: bool):
@@ -437,9 +448,14 @@ def main():
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain descent only")
+    ap.add_argument("--stress", choices=["full", "incremental"], default=None,
+                    help="pass stress evaluation (default: full FP32 stress)")
     ap.add_argument("--workload", choices=["box1m", "batch"], default="box1m",
                     help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances")
     args = ap.parse_args()
+    if args.stress is not None:
+        global INCREMENTAL_STRESS
+        INCREMENTAL_STRESS = 1 if args.stress == "incremental" else 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -253,12 +253,15 @@ template <typename R> void corner_forces(const M3<R> &P, const M3<R> &AN, R out[
 
 // IsotropicNeohookeanMaterial.cpp:164-171; clamp 0: e > 1e-6 ? e : 0 (CPU),
 // clamp 1: max(e, 0) (CUDAInterface.cu:549).
-template <typename R> R tet_energy(const M3<R> &F, R mu, R lambda, R vol, int clamp) {
+// keep_nan: an inverted tet's NaN energy stays NaN (RESTART control) instead of
+// the reference clamps' 0.
+template <typename R> R tet_energy(const M3<R> &F, R mu, R lambda, R vol, int clamp, int keep_nan = 0) {
     R I1 = 0;
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) I1 += F(i, j) * F(i, j);
     R lj = std::log(det3(F));
     R e = (R(0.5) * mu * (I1 - 3) - mu * lj + R(0.5) * lambda * lj * lj) * vol;
+    if (keep_nan && e != e) return e;
     if (clamp == 0) return e > R(1e-6) ? e : R(0);
     return e > R(0) ? e : R(0);
 }
@@ -441,12 +444,12 @@ template <typename R> void hessian_diag_nodes(const Mesh<R> &m, const std::vecto
 }
 
 // Sum of the clamped tet energies, added in tet order.
-template <typename R> R elastic_energy(const Mesh<R> &m, const std::vector<R> &x, int clamp) {
+template <typename R> R elastic_energy(const Mesh<R> &m, const std::vector<R> &x, int clamp, int keep_nan) {
     std::vector<R> e(m.t);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
-        e[i] = tet_energy(F, m.tin[i].mu, m.tin[i].lambda, m.tin[i].vol, clamp);
+        e[i] = tet_energy(F, m.tin[i].mu, m.tin[i].lambda, m.tin[i].vol, clamp, keep_nan);
     }
     R Ee = 0;
     for (int i = 0; i < m.t; ++i) Ee += e[i];
@@ -621,14 +624,19 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
         int passes = 0, rejections = 0, converged = 0;
         double g0 = -1, ratio = -1;
         int k, k_restart = 0;  // RESTART control runs the rho schedule from the last restart
+        // RESTART control: a non-finite residual makes the next iteration a
+        // line-search check, and a non-finite energy is a rejection
+        bool force_check = false;
+        const bool restart = p->control == 1;
         for (k = 0; k < iters; ++k) {
             if (alpha < (R)p->alpha_min) break;
             ++passes;
-            if (k % p->line_search_every == 0) {
+            if (k % p->line_search_every == 0 || force_check) {
+                force_check = false;
                 // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:118-144): the
                 // gravity term 0.5 m 2 g y is -gravity_y . y; plus the external work
                 // -f_ext . x over free nodes.
-                const R Ee = elastic_energy(m, x, p->energy_clamp);
+                const R Ee = elastic_energy(m, x, p->energy_clamp, restart ? 1 : 0);
                 R En = 0;
                 for (int i = 0; i < n; ++i) {
                     if (m.pinned[i]) continue;
@@ -637,7 +645,8 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     En += R(0.5) * m.mass[i] * d2 * h2inv - m.grav_y[i] * x[3 * i + 1] - w;
                 }
                 E = Ee + En;
-                if (k != 0 && E > Eold) {
+                if (!std::isfinite(E) && (k == 0 || !restart)) break;  // a non-finite step start: give up
+                if (k != 0 && (E > Eold || !std::isfinite(E))) {
                     alpha *= (R)p->alpha_shrink;
                     ++rejections;
                     if (p->control == 0) iters -= k - p->line_search_every;
@@ -666,6 +675,10 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     g[id] = gv;
                     r2 += (double)gv * (double)gv;
                 }
+            if (!std::isfinite(r2)) {
+                if (!restart) break;  // the device stops with PBS_E_NONFINITE
+                force_check = true;   // the next iteration measures the energy and restores
+            }
             double r = std::sqrt(r2);
             if (k == 0) g0 = r;
             ratio = g0 > 0 ? r / g0 : 0.0;

@@ -234,7 +234,9 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
             s_y[slot[cc]] = f[3 * cc + 1];
             s_z[slot[cc]] = f[3 * cc + 2];
         }
-        if (check) e += (double)clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu);
+        if (check)
+            e += (double)search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
+                                       p.control == PBS_CONTROL_RESTART);
     }
     __syncthreads();
     chunk_partials<THREADS>(m, l0, nl, nt, s_x, s_y, s_z, st.part);
@@ -317,7 +319,8 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         ci.action = ACT_SAVE_STEP;
         ci.energy_old = E;
     }
-    ci.force_check = 0;
+    // force_check stays set: the node kernel of this pass reads it to apply the
+    // decision, and clears it
     if (!isfinite(E) && !(bad && k != 0)) {
         ci.status = PBS_E_NONFINITE;
         ci.done = 1;

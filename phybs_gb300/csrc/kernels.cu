@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     InstCtl c = *cp;
     c.counter_n = 0;
     c.passes += 1;
+    c.force_check = 0;  // a forced line-search check was applied in this pass
     if (action == ACT_RESTORE) {
         c.par = 1 - c.par;  // the restored state; k is redone
         if (p.control == PBS_CONTROL_RESTART) c.k_restart = k;  // rerun the rho schedule from here

@@ -198,6 +198,14 @@ __device__ __forceinline__ float clamp_energy(float e, int clamp_cpu) {
     return fmaxf(e, 0.0f);                       // CUDAInterface.cu:549
 }
 
+// Tet energy as a line search compares it.  Both reference clamps map the NaN
+// energy of an inverted tet (log J of J <= 0) to 0, which makes an inverted
+// state look cheaper; with keep_nan (RESTART control, the warm-start judge) a
+// NaN stays NaN so that the state is rejected.
+__device__ __forceinline__ float search_energy(float e, int clamp_cpu, bool keep_nan) {
+    return (keep_nan && e != e) ? e : clamp_energy(e, clamp_cpu);
+}
+
 // ---------------------------------------------------------------- SVD
 // One Jacobi rotation annihilating a_pq of a symmetric 3x3 (r = third index),
 // accumulated into V's columns p and q.

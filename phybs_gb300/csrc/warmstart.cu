@@ -267,7 +267,8 @@ __global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevS
             Kin<float> kin;
             disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
             kinematics(kin);
-            const double e = (double)clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu);
+            const double e =
+                (double)search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu, true);
             if (s == 0) e0 = e; else e1 = e;
         }
     }

@@ -129,7 +129,24 @@ def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int =
             np.concatenate(W).astype(np.float64))
 
 
-def fit(X, Y, W=None, steps=3000, batch=8192, lr=1e-3, seed=0, clip=None, verbose=True) -> WarmStartModel:
+def lr_schedule(steps: int, peak: float, chunks: int = 40):
+    """Piecewise-constant one-cycle schedule: (steps, lr) chunks rising linearly
+    to `peak` over the first 10% and falling on a cosine to peak / 300."""
+    out = []
+    per = max(steps // chunks, 1)
+    done = 0
+    for c in range(chunks):
+        n = per if c < chunks - 1 else steps - done
+        if n <= 0:
+            break
+        x = (done + 0.5 * n) / steps
+        lr = peak * x / 0.1 if x < 0.1 else peak * (1 / 300 + (1 - 1 / 300) * 0.5 * (1 + np.cos(np.pi * (x - 0.1) / 0.9)))
+        out.append((n, float(lr)))
+        done += n
+    return out
+
+
+def fit(X, Y, W=None, steps=12000, batch=8192, lr=3e-3, seed=0, clip=None, verbose=True) -> WarmStartModel:
     """Train on (features, scaled corrections, frame weights).  Samples whose
     scaled correction exceeds `clip` (the onset of a motion, where the last
     displacements say nothing about the next one) are left out.  W (from
@@ -151,10 +168,13 @@ def fit(X, Y, W=None, steps=3000, batch=8192, lr=1e-3, seed=0, clip=None, verbos
         print(f"  {keep.sum()} of {keep.size} samples within |y| <= {clip}", flush=True)
     t = MLPTrainer(seed=seed)
     t.set_data(Xs, Ys, W)
-    l1 = t.train(int(steps * 0.7), batch=batch, lr=lr, seed=seed)
-    l2 = t.train(steps - int(steps * 0.7), batch=batch, lr=lr * 0.2, seed=seed + 1)
+    losses = []
+    for i, (n, lr_i) in enumerate(lr_schedule(steps, lr)):
+        losses.append(t.train(n, batch=batch, lr=lr_i, seed=seed + i))
+    losses = np.concatenate(losses)
     if verbose:
-        print(f"  loss {l1[:10].mean():.4f} -> {l1[-10:].mean():.4f} -> {l2[-10:].mean():.4f}", flush=True)
+        print(f"  loss {losses[:10].mean():.4f} -> {losses[len(losses) // 2 - 5:len(losses) // 2 + 5].mean():.4f} "
+              f"-> {losses[-50:].mean():.4f}", flush=True)
     model = WarmStartModel(t.params, mean.astype(np.float32), std.astype(np.float32), out_std.astype(np.float32))
     t.close()
     return model
@@ -164,16 +184,21 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--frames", type=int, default=4000)
     ap.add_argument("--nodes-per-frame", type=int, default=512)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=12000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--data", default=None, help="save the generated (X, Y) here")
     ap.add_argument("--data-max", type=int, default=0, help="save at most this many samples (0 = all)")
+    ap.add_argument("--from-data", default=None, help="fit to (X, Y, W) saved by --data instead of generating")
     args = ap.parse_args()
     t0 = time.time()
-    X, Y, W = generate(args.frames, args.nodes_per_frame, args.seed)
+    if args.from_data:
+        with np.load(args.from_data) as z:
+            X, Y, W = z["X"], z["Y"], z["W"]
+    else:
+        X, Y, W = generate(args.frames, args.nodes_per_frame, args.seed)
     print(f"data: {X.shape[0]} samples in {time.time() - t0:.0f}s", flush=True)
-    if args.data:
+    if args.data and not args.from_data:
         keep = np.arange(X.shape[0])
         if args.data_max and X.shape[0] > args.data_max:
             keep = np.sort(np.random.default_rng(args.seed).choice(X.shape[0], args.data_max, replace=False))

@@ -359,3 +359,31 @@ def test_autotune_keeps_results():
     assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-5
     a.close()
     b.close()
+
+
+def test_restart_control_recovers_from_nonfinite_iterates():
+    """A step size far beyond the stable one (alpha0 = 3) inverts tets within
+    six passes: the residual turns non-finite before the first scheduled
+    energy check.  RESTART control then checks the energy at once (an inverted
+    tet's energy counts as non-finite, not as the reference clamps' 0),
+    rejects, restores the last accepted iterate with a smaller step, and the
+    step still converges -- as the FP64 restatement does."""
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=20000, tol=1e-4, control=L.PBS_CONTROL_RESTART,
+                    alpha0=3.0, energy_slack=16.0, profile=((10, 0.995),))
+    s = DescentSolver(m, params=p)
+    s.step()
+    st = s.stats()
+    assert st["status"] == 0 and st["converged"] == 1 and st["rejections"] >= 1, st
+    x = s.positions()
+    assert np.isfinite(x).all()
+    mu, lam = O.lame(m.young, m.poisson)
+    r = O.rest(m.rest, m.tets, m.pin_mask(), prec=64)
+    ref = O.StepState(m.rest)
+    po = O.make_params(h=1 / 30, max_iters=20000, tol=1e-4, control=1, alpha0=3.0, body_force_scale=1.0,
+                       energy_clamp=1, profile=((10, 0.995),), hessian_closed=1)
+    so = O.step(ref, po, m.tets, r, mu, lam, m.pin_mask(), prec=64)
+    assert so.converged == 1 and so.rejections >= 1
+    # both stop at |g| <= 1e-4 |g0|: positions agree to well within the step
+    assert np.abs(x - ref.x0).max() / m.bbox_diagonal() < 1e-4
+    s.close()
