@@ -200,15 +200,19 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
     __shared__ double sh[THREADS / 32];
     __shared__ int is_last;
     const int c = blockIdx.x;
-    InstCtl *cp = st.ctl + m.chunk_inst[c];
+    // the chunk table is constant: read it before waiting for the node kernel
+    const int4 cd = m.chunk[c];
+    const int inst = m.chunk_inst[c];
+    const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
+    pdl_launch_dependents();
+    pdl_wait();
+    InstCtl *cp = st.ctl + inst;
     if (cp->done) return;
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const bool do_h = (k % p.hd_every) == 0;
     const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
     const size_t cur = (size_t)cp->par * m.Np;
-    const int4 cd = m.chunk[c];
-    const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
     for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int g = m.lnode[l0 + j];
         s_uh[j] = st.uh[cur + g];
@@ -351,24 +355,32 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
-template <int MATERIAL>
-static void launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st) {
-    const size_t smem = chunk_smem(m.chunk_tets, m.chunk_nodes);
-    if (m.chunk_threads == 128)
-        k_tchunk<MATERIAL, 128><<<m.n_chunks, 128, smem, s>>>(m, p, st);
-    else if (m.chunk_threads == 512)
-        k_tchunk<MATERIAL, 512><<<m.n_chunks, 512, smem, s>>>(m, p, st);
-    else
-        k_tchunk<MATERIAL, 256><<<m.n_chunks, 256, smem, s>>>(m, p, st);
+template <int MATERIAL, int THREADS>
+static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(m.n_chunks);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS>, m, p, st);
 }
 
-cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
+template <int MATERIAL>
+static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
+    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128>(s, m, p, st, pdl);
+    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512>(s, m, p, st, pdl);
+    return launch_tchunk_t<MATERIAL, 256>(s, m, p, st, pdl);
+}
+
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, bool pdl) {
     if (m.n_chunks <= 0) return cudaSuccess;
-    if (material == PBS_MATERIAL_STRETCH)
-        launch_tchunk<PBS_MATERIAL_STRETCH>(s, m, p, st);
-    else
-        launch_tchunk<PBS_MATERIAL_NEOHOOKEAN>(s, m, p, st);
-    return cudaGetLastError();
+    if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH>(s, m, p, st, pdl);
+    return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN>(s, m, p, st, pdl);
 }
 
 }  // namespace pbs

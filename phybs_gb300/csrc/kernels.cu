@@ -178,9 +178,12 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     const float4 info = m.info[i];
     const float4 th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
     const int pa = m.pptr[i], pe = m.pptr[i + 1];
+    const int inst = m.nblk_inst[b];
+    pdl_launch_dependents();
+    pdl_wait();  // the chunk kernel's partials and decisions are visible from here
     const float4 f0 = pa < pe ? st.part[pa] : z4;
     const float4 f1 = pa + 1 < pe ? st.part[pa + 1] : z4;
-    InstCtl *cp = st.ctl + m.nblk_inst[b];
+    InstCtl *cp = st.ctl + inst;
     if (cp->done) return;
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
@@ -530,14 +533,23 @@ cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p
     k_prologue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, ext_user, pad2user);
     return cudaGetLastError();
 }
-cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
-    k_node<<<m.n_nblk, BLOCK, 0, s>>>(m, p, st);
-    return cudaGetLastError();
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(m.n_nblk);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_node, m, p, st);
 }
+// One pass of the step graph: both kernels with programmatic dependent launch.
 cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
-    cudaError_t e = launch_tet_only(s, m, p, st, material);
+    cudaError_t e = launch_tet_only(s, m, p, st, material, true);
     if (e != cudaSuccess) return e;
-    return launch_node_only(s, m, p, st);
+    return launch_node_only(s, m, p, st, true);
 }
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
     if (p.incremental) k_ref_tet<<<nblk(m.Tp, 128), 128, 0, s>>>(m, p, st);

@@ -6,6 +6,16 @@
 
 namespace pbs {
 
+// Programmatic dependent launch between the two kernels of a pass (and from
+// one pass to the next) inside the step graph.  A kernel lets its successor
+// launch as soon as all of its own CTAs are running, so the successor's CTAs
+// fill the SMs the tail wave leaves idle and issue their state-independent
+// loads; pdl_wait() then blocks until this grid's predecessor has completed and
+// its writes are visible.  Every read of the predecessor's outputs and every
+// write comes after pdl_wait().  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Deterministic block sum: fixed shuffle tree per warp, then warp 0 sums the
 // warp totals in warp order.  Result valid in thread 0; sh holds one double
 // per warp.

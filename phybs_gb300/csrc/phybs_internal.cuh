@@ -202,8 +202,10 @@ cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, Inst
 cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
                             const int *pad2user);
 cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
-cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
-cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
+// pdl: launch with programmatic stream serialization (the step graph's passes)
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material,
+                            bool pdl = false);
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl = false);
 cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user);
 // positions (user layout) <-> displacement pairs
 cudaError_t launch_pack_positions(cudaStream_t s, const DevMesh &m, const float4 *uh, const float4 *ul,

@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevS
     E1 = block_sum(E1, sh);
     if (threadIdx.x == 0) {
         cp->counter_t = 0;
-        cp->ws_used = (isfinite(E1) && E1 <= E0) ? 1 : 0;
+        // a finite candidate also wins over a plain guess whose energy is not finite
+        cp->ws_used = (isfinite(E1) && (E1 <= E0 || !isfinite(E0))) ? 1 : 0;
     }
 }
 

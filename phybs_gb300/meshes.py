@@ -281,14 +281,17 @@ def batch_of_boxes(n_instances: int = 256, seed: int = 0, edge: float = 0.01, sp
                        instance_tet_ptr=np.array(tet_ptr, np.int32), name=name)
 
 
-def twist_positions(rest: np.ndarray, angle: float, axis: int = 2) -> np.ndarray:
+def twist_positions(rest: np.ndarray, angle: float, axis: int = 2, profile: str = "linear") -> np.ndarray:
     """Rotate each node about the long axis through the mesh centre by an angle
-    growing linearly from 0 at the lowest coordinate to ``angle`` at the top."""
+    growing linearly from 0 at the lowest coordinate to ``angle`` at the top
+    (``profile="sine"``: angle * sin(pi s), s in [0, 1] along the axis, zero at
+    both ends, for meshes pinned at both ends)."""
     p = np.asarray(rest, np.float64).reshape(-1, 3)
     a, b = [d for d in range(3) if d != axis]
     c = 0.5 * (p.min(0) + p.max(0))
     z = p[:, axis]
-    t = (z - z.min()) / max(z.max() - z.min(), 1e-30) * angle
+    s = (z - z.min()) / max(z.max() - z.min(), 1e-30)
+    t = (np.sin(np.pi * s) if profile == "sine" else s) * angle
     x, y = p[:, a] - c[a], p[:, b] - c[b]
     out = p.copy()
     out[:, a] = c[a] + np.cos(t) * x - np.sin(t) * y

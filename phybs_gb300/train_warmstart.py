@@ -55,7 +55,9 @@ def box_scenario(rng, nx=20, ny=20, nz=32, stretch_range=(0.2, 0.8), twist_prob=
     stretch = float(rng.uniform(*stretch_range))
     ramp = int(rng.integers(20, 41))
     twist = float(rng.uniform(0.0, np.pi / 4)) if rng.uniform() < twist_prob else 0.0
-    x0 = M.twist_positions(m.rest, twist, axis=2) if twist else None
+    # both ends are pinned: a twist that vanishes at both ends, so that no tet
+    # next to a pinned face starts inverted
+    x0 = M.twist_positions(m.rest, twist, axis=2, profile="sine") if twist else None
     if x0 is not None:
         x0[m.pins] = m.rest[m.pins]
 
