@@ -179,6 +179,11 @@ int pbs_set_guess(pbs_handle *h, const float *positions);
  * (and an empty displacement history for the learned warm start). */
 int pbs_reset(pbs_handle *h);
 int pbs_get_stats(pbs_handle *h, pbs_stats *s);
+/* The last step's figures of one packed instance (0 .. n_instances-1): its
+ * own passes, iterations, rejections, convergence, status and residual ratio
+ * (device_ms and graph_launches are the whole step's).  No counterpart in the
+ * reference, which steps one mesh. */
+int pbs_get_instance_stats(pbs_handle *h, int instance, pbs_stats *s);
 
 /* Mesh sizes and the device-side gather structure, for parity checks.
  * row_ptr: n_nodes+1; entries: 4*n_tets, entry = 4*tet + corner, ordered per

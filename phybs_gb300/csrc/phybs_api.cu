@@ -400,6 +400,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(cudaEventCreateWithFlags(&h->ev_chunk[1], cudaEventDisableTiming));
     CKC(cudaMallocHost((void **)&h->h_active, 2 * sizeof(int)));
     CKC(cudaMallocHost((void **)&h->h_ctl, B * sizeof(InstCtl)));
+    std::memset(h->h_ctl, 0, B * sizeof(InstCtl));
     CKC(h->tets.alloc(Tp)); CKC(h->tslot.alloc(Tp)); CKC(h->row0.alloc(Tp)); CKC(h->row1.alloc(Tp)); CKC(h->row2.alloc(Tp));
     CKC(h->info.alloc(Np)); CKC(h->inc_ptr.alloc(Np + 1)); CKC(h->inc.alloc(4 * (size_t)T));
     CKC(h->tblk_inst.alloc(h->n_tblk)); CKC(h->nblk_inst.alloc(h->n_nblk));
@@ -885,6 +886,18 @@ int pbs_reset(pbs_handle *h) {
 int pbs_get_stats(pbs_handle *h, pbs_stats *s) {
     if (!h || !s) return PBS_E_INVALID_ARG;
     *s = h->stats;
+    return PBS_OK;
+}
+
+int pbs_get_instance_stats(pbs_handle *h, int instance, pbs_stats *s) {
+    if (!h || !s || instance < 0 || instance >= h->B) return PBS_E_INVALID_ARG;
+    const InstCtl &c = h->h_ctl[instance];  // copied back at the end of every pbs_step
+    pbs_stats S{};
+    S.passes = c.passes; S.iterations = c.k; S.rejections = c.rejections; S.converged = c.converged;
+    S.status = c.status; S.alpha = c.alpha; S.rho = c.rho; S.omega = c.omega; S.energy = c.energy;
+    S.residual_ratio = c.ratio; S.device_ms = h->stats.device_ms; S.graph_launches = h->stats.graph_launches;
+    S.warm_start_used = c.ws_used;
+    *s = S;
     return PBS_OK;
 }
 

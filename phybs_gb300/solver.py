@@ -189,6 +189,12 @@ class DescentSolver:
     def reset(self):
         L.check(L.lib().pbs_reset(self._h), "pbs_reset")
 
+    def instance_stats(self, instance: int) -> dict:
+        """The last step's figures of one packed instance."""
+        s = L.Stats()
+        L.check(L.lib().pbs_get_instance_stats(self._h, C.c_int(instance), C.byref(s)), "pbs_get_instance_stats")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
     def stats(self) -> dict:
         s = L.Stats()
         L.check(L.lib().pbs_get_stats(self._h, C.byref(s)), "pbs_get_stats")

@@ -179,6 +179,10 @@ def test_batched_instances_equal_single_runs():
         for _ in range(2):
             s.step()
         assert np.array_equal(s.positions(), xb[nptr[i]:nptr[i + 1]]), i
+        # the batch reports each instance's own control state
+        si, sa = sb.instance_stats(i), s.stats()
+        for key in ("passes", "iterations", "rejections", "converged", "status", "alpha", "residual_ratio"):
+            assert si[key] == sa[key], (i, key, si[key], sa[key])
         s.close()
     sb.close()
 
