@@ -120,6 +120,8 @@ typedef struct pbs_stats {
     double device_ms;         /* device time of the last pbs_step (CUDA events)   */
     int graph_launches;       /* captured 16-pass graphs launched by the last step */
     int warm_start_used;      /* instances whose step started from the learned guess */
+    int guess_fallbacks;      /* RESTART control: instances whose inertial guess inverted a
+                                 tet, started from the step's start positions instead */
 } pbs_stats;
 
 void pbs_default_params(pbs_step_params *p);

@@ -616,6 +616,16 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             xt[i] = x0[i] + h * v[i];
             x[i] = xt[i] + (R)p->warm_start * h * (v[i] - vold[i]);
         }
+        // RESTART control: a guess that inverts a tet (det F <= 0) starts the
+        // step from x0 instead, as the device's k_guess_check / k_guess_fallback do
+        if (p->control == 1) {
+            bool bad = false;
+            for (int i = 0; i < m.t && !bad; ++i) {
+                M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
+                if (!(det3(F) > R(0))) bad = true;
+            }
+            if (bad) x = x0;
+        }
         xlast = x;  // only read once omega != 1, i.e. after it was set below
         R rho = (R)cheb[0], omega = (R)cheb[1];
         R alpha = (R)p->alpha0;

@@ -64,7 +64,7 @@ class Stats(C.Structure):
     _fields_ = [("passes", C.c_int), ("iterations", C.c_int), ("rejections", C.c_int), ("converged", C.c_int),
                 ("status", C.c_int), ("alpha", C.c_float), ("rho", C.c_float), ("omega", C.c_float),
                 ("energy", C.c_double), ("residual_ratio", C.c_double), ("device_ms", C.c_double),
-                ("graph_launches", C.c_int), ("warm_start_used", C.c_int)]
+                ("graph_launches", C.c_int), ("warm_start_used", C.c_int), ("guess_fallbacks", C.c_int)]
 
 
 class TuneResult(C.Structure):

@@ -103,6 +103,7 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.force_check = 0;
     c.g0_fixed = 0;
     c.ws_used = 0;
+    c.guess_bad = 0;
     c.counter_t = 0;
     c.counter_n = 0;
     c.alpha = p.alpha0;
@@ -145,6 +146,35 @@ __global__ void k_prologue(DevMesh m, DevParams p, DevState st, const float *ext
     float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ext_user) e = make_float4(ext_user[3 * (size_t)u], ext_user[3 * (size_t)u + 1], ext_user[3 * (size_t)u + 2], 0.f);
     st.ext[i] = e;
+}
+
+// RESTART control: a guess that inverts a tet.  When prescribed nodes stop or
+// reverse, x~ = x0 + h v carries the free nodes' momentum into the held layer
+// and can turn tets inside out before the solve starts; the reference then
+// iterates on NaN forces (its energy clamps hide the NaN).  k_guess_check
+// flags an instance whose guess has a tet with det F <= 0 (or a non-finite
+// one), k_guess_fallback starts it from the step's start positions instead --
+// the last accepted state -- with the same residual bar.
+__global__ void k_guess_check(DevMesh m, DevState st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;  // one instance per 256-tet block
+    const int4 q = m.tets[t];
+    if (q.x < 0) return;
+    const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+    const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    Kin<float> kin;
+    disp_gradient<float>(st.uh[q.x], st.uh[q.y], st.uh[q.z], st.uh[q.w], dinv, kin.G);
+    kinematics(kin);
+    if (!(1.0f + kin.d > 0.0f)) atomicOr(&st.ctl[m.tblk_inst[blockIdx.x]].guess_bad, 1);
+}
+
+__global__ void k_guess_fallback(DevMesh m, DevState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    if (!node_ctl(m, st, i).guess_bad) return;
+    const float4 h0 = st.u0h[i], l0 = st.u0l[i];
+    st.uh[i] = h0;
+    st.ul[i] = l0;
+    st.ub[i] = h0;
 }
 
 // v_old <- v; v = damping (u - u0) / h; u0 <- u  (DescentOptimize.cpp:238-240)
@@ -554,6 +584,12 @@ cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, De
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
     if (p.incremental) k_ref_tet<<<nblk(m.Tp, 128), 128, 0, s>>>(m, p, st);
     k_ref_gather<<<nblk(m.Np, 128), 128, 0, s>>>(m, p, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_guess_check(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    if (p.control != PBS_CONTROL_RESTART) return cudaSuccess;
+    k_guess_check<<<m.n_tblk, BLOCK, 0, s>>>(m, st);
+    k_guess_fallback<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, st);
     return cudaGetLastError();
 }
 cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user) {

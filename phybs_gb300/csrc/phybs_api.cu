@@ -561,6 +561,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
     CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
+    CK(launch_guess_check(s, m, h->dparams, st));
     CK(launch_ref_force(s, m, h->dparams, st));
     if (h->ws_enabled || h->guess_pending) {
         CK(launch_ws_gref(s, m, h->dparams, st, h->material));
@@ -602,6 +603,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
         S.rejections += c.rejections;
         S.converged += c.converged;
         S.warm_start_used += c.ws_used;
+        S.guess_fallbacks += c.guess_bad;
         if (c.status != PBS_OK && S.status == PBS_OK) S.status = c.status;
         if (c.status == PBS_E_NONFINITE) S.status = PBS_E_NONFINITE;
     }
@@ -762,6 +764,7 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
     if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
+    if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
     for (int i = 0; i < passes && e == cudaSuccess; ++i) {
@@ -897,6 +900,7 @@ int pbs_get_instance_stats(pbs_handle *h, int instance, pbs_stats *s) {
     S.status = c.status; S.alpha = c.alpha; S.rho = c.rho; S.omega = c.omega; S.energy = c.energy;
     S.residual_ratio = c.ratio; S.device_ms = h->stats.device_ms; S.graph_launches = h->stats.graph_launches;
     S.warm_start_used = c.ws_used;
+    S.guess_fallbacks = c.guess_bad;
     *s = S;
     return PBS_OK;
 }

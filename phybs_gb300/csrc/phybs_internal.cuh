@@ -95,7 +95,7 @@ struct __align__(16) InstCtl {
     int g0_fixed;     // g0 was set before iteration 0 (the plain guess's residual, warm start on)
     int ws_used;      // this step started from the learned guess
     float ell;        // mean edge length of the instance (feature scale)
-    int pad3;
+    int guess_bad;    // RESTART control: the inertial guess inverts a tet; the step starts from u0
     double energy, energy_old, g0, ratio;
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
@@ -206,6 +206,9 @@ cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, De
 cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material,
                             bool pdl = false);
 cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl = false);
+// RESTART control: replaces an instance's inertial guess by the step's start
+// positions when the guess inverts a tet (kernels.cu)
+cudaError_t launch_guess_check(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_epilogue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const int *pad2user);
 // positions (user layout) <-> displacement pairs
 cudaError_t launch_pack_positions(cudaStream_t s, const DevMesh &m, const float4 *uh, const float4 *ul,

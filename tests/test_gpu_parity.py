@@ -391,3 +391,41 @@ def test_restart_control_recovers_from_nonfinite_iterates():
     # both stop at |g| <= 1e-4 |g0|: positions agree to well within the step
     assert np.abs(x - ref.x0).max() / m.bbox_diagonal() < 1e-4
     s.close()
+
+
+def test_inverting_guess_falls_back_to_start_positions():
+    """A bar pinned at both ends, its far face pulled 4 cm (1.6 cells) a frame
+    for four frames, then held: in the first held frame the inertial guess
+    carries the free nodes' momentum through the held face and inverts tets.
+    RESTART control starts that step from the start positions instead; every
+    frame converges, and positions follow the FP64 restatement, which does the
+    same."""
+    b = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    x = b.rest[:, 0]
+    pins = np.nonzero((x <= x.min() + 1e-9) | (x >= x.max() - 1e-9))[0].astype(np.int32)
+    far = np.nonzero(x >= x.max() - 1e-9)[0].astype(np.int32)
+    m = M.TetMeshData(b.rest, b.tets, pins, 5e4, 0.4)
+    h = 1 / 30
+    p = make_params("gpu_reference", h=h, max_iters=20000, tol=1e-4, control=L.PBS_CONTROL_RESTART, alpha0=0.5,
+                    energy_slack=16.0, profile=((10, 0.995),))
+    s = DescentSolver(m, params=p)
+    mu, lam = O.lame(m.young, m.poisson)
+    r = O.rest(m.rest, m.tets, m.pin_mask(), prec=64)
+    ref = O.StepState(m.rest)
+    po = O.make_params(h=h, max_iters=20000, tol=1e-4, control=1, alpha0=0.5, body_force_scale=1.0, energy_clamp=1,
+                       profile=((10, 0.995),), hessian_closed=1)
+    fallbacks = []
+    for f in range(7):
+        tgt = m.rest[far].astype(np.float64).copy()
+        tgt[:, 0] += 0.04 * min(f + 1, 4)
+        s.set_node_positions(far, tgt.astype(np.float32))
+        s.step()
+        st = s.stats()
+        assert st["status"] == 0 and st["converged"] == 1, (f, st)
+        fallbacks.append(st["guess_fallbacks"])
+        ref.x0[far] = tgt
+        so = O.step(ref, po, m.tets, r, mu, lam, m.pin_mask(), prec=64)
+        assert so.converged == 1, f
+        assert np.abs(s.positions() - ref.x0).max() / m.bbox_diagonal() < 2e-4, f
+    assert fallbacks[4] == 1 and sum(fallbacks) >= 1, fallbacks
+    s.close()
