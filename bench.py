@@ -50,10 +50,11 @@ UNIT = "frames/s"
 # x_next 12 B written, amortised over tets): 56 + 64 N / T.
 STATIC_BYTES_PER_TET = 56.0
 BYTES_PER_NODE = 64.0
-# Iterations one frame of the box workload takes (mean over frames 1-8 of
-# the GPU solve, seed 0); used only by the CPU reference arm, which times a
-# bounded sample of iterations and cannot afford whole frames at 1M tets.
-REFERENCE_ITERS_PER_FRAME = 2000.0
+# Iterations a frame of the box workload takes with the plain descent (mean
+# over the timed frames 3..29 of the GPU solve, seed 0, full FP32 stress:
+# 1,412); used only by the CPU reference arm, which times a bounded sample of
+# iterations and cannot afford whole frames at 1M tets.
+REFERENCE_ITERS_PER_FRAME = 1412.0
 CPU_SAMPLE_ITERS = 32
 BATCH_ITERS = 96  # doDescentOpt(h, iterations) as fvm.cpp:187 calls it
 
@@ -227,7 +228,20 @@ def launches_per_frame(graph_launches: int, warm: bool) -> int:
     return 1 + 3 + ref + warm_extra + 2 * 16 * graph_launches
 
 
-def run_arm(args, m, bottom, length, model, world, e2e: bool):
+def tune_shape(args, m):
+    """The pass kernels' chunk shape for this mesh (pbs_autotune on a fresh
+    handle at the workload's first frame), applied to every arm."""
+    from phybs_gb300.solver import DescentSolver
+    s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
+    try:
+        return s.autotune(16)
+    except Exception:  # keep the default shape
+        return None
+    finally:
+        s.close()
+
+
+def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
     """One arm over frames 0 .. W+K-1 on a fresh handle.  Returns the timed
     K frames' results: device time (CUDA events on the library's stream) or,
     with e2e, host wall time including each frame's position read-back."""
@@ -236,6 +250,8 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool):
     from phybs_gb300.solver import DescentSolver
 
     s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
+    if tune is not None:
+        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"])
     if model is not None:
         s.set_warm_start(model)
     stream = torch.cuda.ExternalStream(s.stream())
@@ -285,11 +301,13 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool):
     return res
 
 
-def profile_pass(args, m):
+def profile_pass(args, m, tune=None):
     """Per-kernel times of one descent pass (CUDA events on the library's
     stream, mean of 20 passes from the workload's first frame)."""
     from phybs_gb300.solver import DescentSolver
     s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
+    if tune is not None:
+        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"])
     try:
         return s.profile_kernels(20), None
     except Exception as exc:  # an instance stopped early: no valid per-kernel time
@@ -307,11 +325,12 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     m, bottom, length, young = box_workload(args.seed, args.scale)
     model = WarmStartModel.load(DEFAULT_MODEL) if os.path.exists(DEFAULT_MODEL) and not args.plain_only else None
-    plain = run_arm(args, m, bottom, length, None, world, e2e=False)
-    warm = run_arm(args, m, bottom, length, model, world, e2e=False) if model is not None else None
+    tune = tune_shape(args, m)
+    plain = run_arm(args, m, bottom, length, None, world, e2e=False, tune=tune)
+    warm = run_arm(args, m, bottom, length, model, world, e2e=False, tune=tune) if model is not None else None
     head = warm if warm is not None else plain
-    head_e2e = run_arm(args, m, bottom, length, model, world, e2e=True)
-    prof, prof_err = profile_pass(args, m)
+    head_e2e = run_arm(args, m, bottom, length, model, world, e2e=True, tune=tune)
+    prof, prof_err = profile_pass(args, m, tune)
     if rank != 0:
         return
     peak, peak_kind = measured_peak()
@@ -345,7 +364,8 @@ def run_ours(args, rank, world):
                                f"1.5x over 30 frames; {mode}; every frame to |g|<=1e-4|g0|; frames "
                                f"{args.warmup}..{args.warmup + args.steps - 1} timed",
                    "seed": args.seed, "young": young, "h": 1 / 30, "tol": 1e-4, "alpha0": ALPHA0, "rho": RHO,
-                   "l2": "working set larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+                   "l2": "working set larger than L2 (no flush)", "parallelism": f"replicas x{world}",
+                   "stress": "incremental" if INCREMENTAL_STRESS else "full", "autotune": tune},
         "iterations_per_frame": float(np.mean(head["iters"])), "iterations_per_s": head["passes"] / head["seconds"],
         "plain": summary(plain),
         "roofline": roof,
@@ -389,7 +409,8 @@ def run_batch(args, rank, world):
     torch.cuda.set_device(dev)
     from phybs_gb300.solver import make_params
     m = M.batch_of_boxes(256, seed=args.seed)
-    s = DescentSolver(m, params=make_params("gpu_reference", h=1 / 30, max_iters=BATCH_ITERS))
+    s = DescentSolver(m, params=make_params("gpu_reference", h=1 / 30, max_iters=BATCH_ITERS,
+                                            incremental_stress=INCREMENTAL_STRESS))
     tune = s.autotune(16)
     stream = torch.cuda.ExternalStream(s.stream())
     for _ in range(args.warmup):

@@ -257,6 +257,11 @@ typedef struct pbs_tune_result {
  * step graph).  No counterpart in the reference, whose launch shapes are
  * fixed. */
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
+/* Sets a chunk shape directly (for instance one pbs_autotune picked on another
+ * handle of the same mesh): threads per CTA 128, 256 or 512; tets per chunk
+ * 1 .. 16384; nodes per chunk >= 4; the shared memory it needs at most
+ * 200 KB.  Call between steps. */
+int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes);
 
 /* ------------------------------------------------------------------------
  * Learned warm start.  A per-node MLP 24 -> 64 -> 64 -> 64 -> 3 (GELU; BF16

@@ -190,12 +190,12 @@ __device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl,
     }
 }
 
-template <int MATERIAL, int THREADS>
+template <int MATERIAL, int THREADS, bool INC>
 __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
     extern __shared__ float4 smem4[];
     const int CN = m.chunk_nodes, CT = m.chunk_tets;
-    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;
-    float *s_x = reinterpret_cast<float *>(smem4 + 3 * CN);
+    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;  // s_ub only with INC
+    float *s_x = reinterpret_cast<float *>(smem4 + (INC ? 3 : 2) * CN);
     float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
     __shared__ double sh[THREADS / 32];
     __shared__ int is_last;
@@ -211,13 +211,12 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const bool do_h = (k % p.hd_every) == 0;
-    const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
     const size_t cur = (size_t)cp->par * m.Np;
     for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int g = m.lnode[l0 + j];
         s_uh[j] = st.uh[cur + g];
         s_ul[j] = st.ul[cur + g];
-        s_ub[j] = inc ? st.ub[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (INC) s_ub[j] = st.ub[g];
     }
     __syncthreads();
     double e = 0.0;
@@ -228,9 +227,10 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         Kin<float> kin;
         float f[12];
-        pass_forces_v<MATERIAL>(p, s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
-                                s_ul[lc.z], s_ul[lc.w], s_ub[lc.x], s_ub[lc.y], s_ub[lc.z], s_ub[lc.w], dinv, r0.w,
-                                r1.w, r2.w, kin, f);
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        pass_forces_c<MATERIAL, INC>(s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
+                                     s_ul[lc.z], s_ul[lc.w], INC ? s_ub[lc.x] : z4, INC ? s_ub[lc.y] : z4,
+                                     INC ? s_ub[lc.z] : z4, INC ? s_ub[lc.w] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
         const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
@@ -253,9 +253,11 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
             const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
             Kin<float> kin;
             float f[12], kd[12];
-            pass_forces_v<MATERIAL>(p, s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
-                                    s_ul[lc.z], s_ul[lc.w], s_ub[lc.x], s_ub[lc.y], s_ub[lc.z], s_ub[lc.w], dinv,
-                                    r0.w, r1.w, r2.w, kin, f);
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            pass_forces_c<MATERIAL, INC>(s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
+                                         s_ul[lc.z], s_ul[lc.w], INC ? s_ub[lc.x] : z4, INC ? s_ub[lc.y] : z4,
+                                         INC ? s_ub[lc.z] : z4, INC ? s_ub[lc.w] : z4, dinv, r0.w, r1.w, r2.w, kin,
+                                         f);
             hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
             const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
@@ -334,15 +336,23 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
 }
 
 // ------------------------------------------------------------ launchers
-template <int MATERIAL, int THREADS> static cudaError_t allow_smem() {
-    return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int MATERIAL, int THREADS, bool INC> static cudaError_t allow_smem() {
+    return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS, INC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 CHUNK_MAX_SMEM);
 }
 
+template <int MATERIAL, bool INC> static cudaError_t allow_smem_all() {
+    const cudaError_t e[] = {allow_smem<MATERIAL, 128, INC>(), allow_smem<MATERIAL, 256, INC>(),
+                             allow_smem<MATERIAL, 512, INC>()};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
+}
+
 cudaError_t prepare_chunk_kernels() {
-    const cudaError_t e[] = {allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128>(), allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256>(),
-                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 512>(), allow_smem<PBS_MATERIAL_STRETCH, 128>(),
-                             allow_smem<PBS_MATERIAL_STRETCH, 256>(), allow_smem<PBS_MATERIAL_STRETCH, 512>()};
+    const cudaError_t e[] = {allow_smem_all<PBS_MATERIAL_NEOHOOKEAN, true>(),
+                             allow_smem_all<PBS_MATERIAL_NEOHOOKEAN, false>(),
+                             allow_smem_all<PBS_MATERIAL_STRETCH, false>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -355,32 +365,33 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
-template <int MATERIAL, int THREADS>
+template <int MATERIAL, int THREADS, bool INC>
 static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m.n_chunks);
     cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes);
+    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes, INC);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS>, m, p, st);
+    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC>, m, p, st);
 }
 
-template <int MATERIAL>
+template <int MATERIAL, bool INC>
 static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
-    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128>(s, m, p, st, pdl);
-    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512>(s, m, p, st, pdl);
-    return launch_tchunk_t<MATERIAL, 256>(s, m, p, st, pdl);
+    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128, INC>(s, m, p, st, pdl);
+    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512, INC>(s, m, p, st, pdl);
+    return launch_tchunk_t<MATERIAL, 256, INC>(s, m, p, st, pdl);
 }
 
 cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, bool pdl) {
     if (m.n_chunks <= 0) return cudaSuccess;
-    if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH>(s, m, p, st, pdl);
-    return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN>(s, m, p, st, pdl);
+    if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH, false>(s, m, p, st, pdl);
+    if (p.incremental) return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, pdl);
+    return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, false>(s, m, p, st, pdl);
 }
 
 }  // namespace pbs

@@ -74,14 +74,16 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 }
 
 // Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
-template <int MATERIAL>
-__device__ __forceinline__ void pass_forces_v(const DevParams &p, const float4 &x0, const float4 &x1, const float4 &x2,
-                                              const float4 &x3, const float4 &l0, const float4 &l1, const float4 &l2,
-                                              const float4 &l3, const float4 &a0, const float4 &a1, const float4 &a2,
-                                              const float4 &a3, const float dinv[9], float svol, float mu,
-                                              float lambda, Kin<float> &kin, float f[12]) {
+// INC (compile time): the incremental neo-Hookean form; a0..a3 are unused
+// without it.
+template <int MATERIAL, bool INC>
+__device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
+                                              const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
+                                              const float4 &a0, const float4 &a1, const float4 &a2, const float4 &a3,
+                                              const float dinv[9], float svol, float mu, float lambda, Kin<float> &kin,
+                                              float f[12]) {
     float P[9];
-    if (MATERIAL != PBS_MATERIAL_STRETCH && p.incremental) {
+    if (MATERIAL != PBS_MATERIAL_STRETCH && INC) {
         disp_gradient<float>(x0, x1, x2, x3, dinv, kin.G);
         kinematics(kin);
         Kin<float> k0;
@@ -102,6 +104,18 @@ __device__ __forceinline__ void pass_forces_v(const DevParams &p, const float4 &
         else pk1_neohookean<float>(kin, mu, lambda, P);
     }
     corner_forces(P, dinv, svol, f);
+}
+
+template <int MATERIAL>
+__device__ __forceinline__ void pass_forces_v(const DevParams &p, const float4 &x0, const float4 &x1, const float4 &x2,
+                                              const float4 &x3, const float4 &l0, const float4 &l1, const float4 &l2,
+                                              const float4 &l3, const float4 &a0, const float4 &a1, const float4 &a2,
+                                              const float4 &a3, const float dinv[9], float svol, float mu,
+                                              float lambda, Kin<float> &kin, float f[12]) {
+    if (MATERIAL != PBS_MATERIAL_STRETCH && p.incremental)
+        pass_forces_c<MATERIAL, true>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
+    else
+        pass_forces_c<MATERIAL, false>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
 }
 
 template <int MATERIAL>

@@ -812,12 +812,21 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     return time_passes(h, passes, tet_ms, node_ms);
 }
 
+int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes) {
+    if (!h || (threads != 128 && threads != 256 && threads != 512) || chunk_tets < 1 || chunk_nodes < 4 ||
+        4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 ||
+        chunk_smem(chunk_tets, chunk_nodes, true) > (size_t)CHUNK_MAX_SMEM)
+        return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    return set_pass_layout(h, threads, chunk_tets, chunk_nodes, nullptr);
+}
+
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
     if (!h || passes <= 0) return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
     // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch
     static const int shapes[][3] = {{256, 1024, 448}, {256, 768, 352}, {256, 512, 256}, {128, 512, 256},
-                                    {128, 256, 160}, {512, 1024, 448}, {512, 2048, 832}};
+                                    {128, 256, 160}, {512, 1024, 448}, {512, 2048, 832}, {256, 640, 320}};
     const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
     const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes;
     double best = 1e300, first = -1.0;

@@ -57,8 +57,10 @@ constexpr int CHUNK_TETS = 1024;
 constexpr int CHUNK_NODES = 448;
 constexpr int CHUNK_THREADS = 256;
 constexpr int CHUNK_MAX_SMEM = 200 * 1024;
-__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes) {
-    return 3 * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets;
+// Dynamic shared memory of the per-tet pass kernel: staged node words (u hi,
+// u lo, and the force base with incremental stress) and 3 floats per corner slot.
+__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc) {
+    return (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets;
 }
 
 // Step parameters as the kernels see them (a by-value kernel argument).

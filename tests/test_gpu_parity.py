@@ -355,7 +355,7 @@ def test_autotune_keeps_results():
     a = DescentSolver(m, params=p)
     b = DescentSolver(m, params=p)
     r = b.autotune(8)
-    assert r["n_tried"] == 7 and r["chunk_threads"] in (128, 256, 512)
+    assert r["n_tried"] == 8 and r["chunk_threads"] in (128, 256, 512)
     assert 0.0 < r["pass_ms"] <= r["default_pass_ms"]
     for _ in range(3):
         a.step()
