@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
     E = block_sum(E, sh);
     E2 = block_sum(E2, sh);
     if (threadIdx.x != 0) return;
-    InstCtl ci = *cp;
+    InstCtl &ci = *cp;  // in place, as in the node kernel
     ci.counter_t = 0;
     ci.energy = E;
     // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
@@ -331,7 +331,6 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         ci.status = PBS_E_NONFINITE;
         ci.done = 1;
     }
-    *cp = ci;
     if (ci.done) atomicSub(st.active, 1);
 }
 

@@ -198,7 +198,7 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-__global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState st) {
+__global__ void __launch_bounds__(BLOCK, 4) k_node(DevMesh m, DevParams p, DevState st) {
     __shared__ double sh[BLOCK / 32];
     __shared__ int is_last;
     const int b = blockIdx.x;
@@ -310,7 +310,9 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += BLOCK) R2 += __ldcg(st.npart + j);
     R2 = block_sum(R2, sh);
     if (threadIdx.x != 0) return;
-    InstCtl c = *cp;
+    // updated in place: every other block has read it, and the next kernel
+    // reads it only after its grid-dependency wait
+    InstCtl &c = *cp;
     c.counter_n = 0;
     c.passes += 1;
     c.force_check = 0;  // a forced line-search check was applied in this pass
@@ -345,7 +347,6 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
         if (c.k >= c.iters || c.alpha < p.alpha_min) c.done = 1;
         else if (c.passes >= p.pass_cap) { c.done = 1; c.status = PBS_E_ITER_CAP; }
     }
-    *cp = c;
     if (c.done) atomicSub(st.active, 1);
 }
 
