@@ -198,7 +198,7 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-__global__ void __launch_bounds__(BLOCK, 4) k_node(DevMesh m, DevParams p, DevState st) {
+__global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState st) {
     __shared__ double sh[BLOCK / 32];
     __shared__ int is_last;
     const int b = blockIdx.x;
