@@ -101,6 +101,10 @@ typedef struct pbs_step_params {
     float energy_slack;       /* line-search rounding allowance: reject only if
                                  E > E_old + energy_slack * 2^-24 * sqrt(sum of squared
                                  energy terms); 0 = the reference's strict E > E_old */
+    float alpha_grow;         /* RESTART control: alpha <- min(alpha * alpha_grow, alpha0) at
+                                 every accepted line-search check, so that one early rejection
+                                 does not slow the whole step; 1 = the reference's alpha,
+                                 which only shrinks */
     int incremental_stress;   /* neo-Hookean passes: 1 = evaluate P(F) - P(F_base) against
                                  an FP64 force at the step's initial guess (residual
                                  accurate far below 1e-6 of its initial value),

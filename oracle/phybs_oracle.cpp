@@ -490,6 +490,7 @@ typedef struct orc_params {
     int energy_clamp;
     int material;           // 0 NH invariants, 1 stretch-based
     int hessian_closed;     // 1: closed-form diagonal, 0: SVD (Xu et al.) path
+    float alpha_grow;        // RESTART: alpha <- min(alpha * alpha_grow, alpha0) on an accepted check
 } orc_params;
 
 typedef struct orc_stats {
@@ -666,6 +667,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     continue;
                 }
                 Eold = E;
+                if (restart && k != 0 && k > k_restart) alpha = std::min(alpha * (R)p->alpha_grow, (R)p->alpha0);
                 xold = x;
             }
             if (k % p->hessian_every == 0) {

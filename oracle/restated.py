@@ -31,7 +31,8 @@ class OrcParams(C.Structure):
                 ("line_search_every", C.c_int), ("hessian_every", C.c_int), ("n_profile", C.c_int),
                 ("profile_k", C.c_int * 4), ("profile_rho", C.c_float * 4), ("damping", C.c_float),
                 ("warm_start", C.c_float), ("body_force_scale", C.c_float),
-                ("energy_clamp", C.c_int), ("material", C.c_int), ("hessian_closed", C.c_int)]
+                ("energy_clamp", C.c_int), ("material", C.c_int), ("hessian_closed", C.c_int),
+                ("alpha_grow", C.c_float)]
 
 
 class OrcStats(C.Structure):
@@ -51,7 +52,7 @@ def set_threads(n: int = 0) -> int:
 def make_params(h=0.03, max_iters=96, tol=0.0, control=0, alpha0=0.1, alpha_min=0.01, alpha_shrink=0.7,
                 line_search_every=8, hessian_every=32, profile=((1, 0.96), (7, 0.991), (10, 0.999)),
                 damping=0.99, warm_start=0.2, body_force_scale=2.0, energy_clamp=0, material=0,
-                hessian_closed=0) -> OrcParams:
+                hessian_closed=0, alpha_grow=1.0) -> OrcParams:
     p = OrcParams()
     p.h, p.max_iters, p.tol, p.control = h, max_iters, tol, control
     p.alpha0, p.alpha_min, p.alpha_shrink = alpha0, alpha_min, alpha_shrink
@@ -62,6 +63,7 @@ def make_params(h=0.03, max_iters=96, tol=0.0, control=0, alpha0=0.1, alpha_min=
         p.profile_rho[i] = r
     p.damping, p.warm_start, p.body_force_scale = damping, warm_start, body_force_scale
     p.energy_clamp, p.material, p.hessian_closed = energy_clamp, material, hessian_closed
+    p.alpha_grow = alpha_grow
     return p
 
 

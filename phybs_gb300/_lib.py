@@ -57,7 +57,8 @@ class StepParams(C.Structure):
                 ("line_search_every", C.c_int), ("hessian_every", C.c_int), ("n_profile", C.c_int),
                 ("profile_k", C.c_int * 4), ("profile_rho", C.c_float * 4), ("damping", C.c_float),
                 ("warm_start", C.c_float), ("body_force_scale", C.c_float), ("energy_clamp", C.c_int),
-                ("pass_cap", C.c_int), ("energy_slack", C.c_float), ("incremental_stress", C.c_int)]
+                ("pass_cap", C.c_int), ("energy_slack", C.c_float), ("alpha_grow", C.c_float),
+                ("incremental_stress", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -324,6 +324,10 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
     } else {
         ci.action = ACT_SAVE_STEP;
         ci.energy_old = E;
+        // grow only after real steps since the last restore (not on the re-check
+        // of a restored iterate, whose energy is the accepted one)
+        if (p.control == PBS_CONTROL_RESTART && k != 0 && k > ci.k_restart)
+            ci.alpha = fminf(ci.alpha * p.alpha_grow, p.alpha0);
     }
     // force_check stays set: the node kernel of this pass reads it to apply the
     // decision, and clears it

@@ -204,6 +204,7 @@ static void to_dev_params(const pbs_step_params &p, DevParams &d) {
     d.clamp_cpu = p.energy_clamp == PBS_CLAMP_CPU ? 1 : 0;
     d.pass_cap = p.pass_cap > 0 ? p.pass_cap : p.max_iters + 16;
     d.energy_slack = p.energy_slack;
+    d.alpha_grow = p.alpha_grow;
     d.incremental = 0;  // set from the material and incremental_stress by the handle
 }
 
@@ -228,6 +229,7 @@ void pbs_default_params(pbs_step_params *p) {
     p->energy_clamp = PBS_CLAMP_CPU;
     p->pass_cap = 0;
     p->energy_slack = 0.0f;
+    p->alpha_grow = 1.0f;
     p->incremental_stress = 1;
 }
 
@@ -260,7 +262,8 @@ static int validate_params(const pbs_step_params *p) {
         p->n_profile < 0 || p->n_profile > 4 || !(p->alpha0 > 0.f) || !(p->alpha_shrink > 0.f) ||
         p->alpha_shrink >= 1.f || (p->control != PBS_CONTROL_REFERENCE && p->control != PBS_CONTROL_RESTART) ||
         p->tol < 0.f || p->pass_cap < 0 || !(p->energy_slack >= 0.f) ||
-        (p->incremental_stress != 0 && p->incremental_stress != 1))
+        (p->incremental_stress != 0 && p->incremental_stress != 1) || !(p->alpha_grow >= 1.0f) ||
+        !std::isfinite(p->alpha_grow))
         return PBS_E_INVALID_ARG;
     return PBS_OK;
 }

@@ -78,6 +78,7 @@ struct DevParams {
     int clamp_cpu;
     int pass_cap;
     float energy_slack;  // reject only if E > E_old + slack * 2^-24 * sqrt(sum e^2)
+    float alpha_grow;    // RESTART: alpha <- min(alpha * alpha_grow, alpha0) on an accepted check
     int incremental;     // neo-Hookean: passes evaluate P(F) - P(F_base) against an FP64 force at the
                          // step's initial guess (the base)
 };
