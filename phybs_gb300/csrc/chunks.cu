@@ -190,40 +190,69 @@ __device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl,
     }
 }
 
-template <int MATERIAL, int THREADS, bool INC>
+// STAGE: the row-staged variant.  Every thread first issues asynchronous
+// copies of its tets' rows and corner ids into shared memory -- before the
+// grid-dependency wait, since they are constant -- and of the chunk's node
+// words after it; one wait then covers all of them, instead of one global
+// round trip per tet inside the loop.
+template <int MATERIAL, int THREADS, bool INC, bool STAGE>
 __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
     extern __shared__ float4 smem4[];
     const int CN = m.chunk_nodes, CT = m.chunk_tets;
     float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;  // s_ub only with INC
     float *s_x = reinterpret_cast<float *>(smem4 + (INC ? 3 : 2) * CN);
     float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
+    float4 *s_r0 = reinterpret_cast<float4 *>(s_z + 4 * CT), *s_r1 = s_r0 + CT, *s_r2 = s_r1 + CT;  // STAGE only
+    ushort4 *s_lc = reinterpret_cast<ushort4 *>(s_r2 + CT), *s_sl = s_lc + CT;
     __shared__ double sh[THREADS / 32];
     __shared__ int is_last;
     const int c = blockIdx.x;
-    // the chunk table is constant: read it before waiting for the node kernel
+    // the chunk table and the per-tet rows are constant: read them before
+    // waiting for the node kernel
     const int4 cd = m.chunk[c];
     const int inst = m.chunk_inst[c];
     const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
+    if (STAGE) {
+        for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
+            const int q = tq0 + lt;
+            cp_async16(s_r0 + lt, m.qrow0 + q);
+            cp_async16(s_r1 + lt, m.qrow1 + q);
+            cp_async16(s_r2 + lt, m.qrow2 + q);
+            cp_async8(s_lc + lt, m.qloc + q);
+            cp_async8(s_sl + lt, m.qslot + q);
+        }
+        cp_async_commit();
+    }
     pdl_launch_dependents();
     pdl_wait();
     InstCtl *cp = st.ctl + inst;
-    if (cp->done) return;
+    if (cp->done) {
+        if (STAGE) cp_async_wait_all();
+        return;
+    }
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const bool do_h = (k % p.hd_every) == 0;
     const size_t cur = (size_t)cp->par * m.Np;
     for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int g = m.lnode[l0 + j];
-        s_uh[j] = st.uh[cur + g];
-        s_ul[j] = st.ul[cur + g];
-        if (INC) s_ub[j] = st.ub[g];
+        if (STAGE) {
+            cp_async16(s_uh + j, st.uh + cur + g);
+            cp_async16(s_ul + j, st.ul + cur + g);
+        } else {
+            s_uh[j] = st.uh[cur + g];
+            s_ul[j] = st.ul[cur + g];
+            if (INC) s_ub[j] = st.ub[g];
+        }
     }
+    if (STAGE) cp_async_wait_all();
     __syncthreads();
     double e = 0.0;
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const int q = tq0 + lt;
-        const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
-        const ushort4 lc = m.qloc[q], sl = m.qslot[q];
+        const float4 r0 = STAGE ? s_r0[lt] : m.qrow0[q], r1 = STAGE ? s_r1[lt] : m.qrow1[q],
+                     r2 = STAGE ? s_r2[lt] : m.qrow2[q];
+        const ushort4 lc = STAGE ? s_lc[lt] : m.qloc[q], sl = STAGE ? s_sl[lt] : m.qslot[q];
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         Kin<float> kin;
         float f[12];
@@ -248,8 +277,9 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         __syncthreads();
         for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
             const int q = tq0 + lt;
-            const float4 r0 = m.qrow0[q], r1 = m.qrow1[q], r2 = m.qrow2[q];
-            const ushort4 lc = m.qloc[q], sl = m.qslot[q];
+            const float4 r0 = STAGE ? s_r0[lt] : m.qrow0[q], r1 = STAGE ? s_r1[lt] : m.qrow1[q],
+                         r2 = STAGE ? s_r2[lt] : m.qrow2[q];
+            const ushort4 lc = STAGE ? s_lc[lt] : m.qloc[q], sl = STAGE ? s_sl[lt] : m.qslot[q];
             const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
             Kin<float> kin;
             float f[12], kd[12];
@@ -339,14 +369,14 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
 }
 
 // ------------------------------------------------------------ launchers
-template <int MATERIAL, int THREADS, bool INC> static cudaError_t allow_smem() {
-    return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS, INC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int MATERIAL, int THREADS, bool INC, bool STAGE> static cudaError_t allow_smem() {
+    return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS, INC, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 CHUNK_MAX_SMEM);
 }
 
 template <int MATERIAL, bool INC> static cudaError_t allow_smem_all() {
-    const cudaError_t e[] = {allow_smem<MATERIAL, 128, INC>(), allow_smem<MATERIAL, 256, INC>(),
-                             allow_smem<MATERIAL, 512, INC>()};
+    const cudaError_t e[] = {allow_smem<MATERIAL, 128, INC, false>(), allow_smem<MATERIAL, 256, INC, false>(),
+                             allow_smem<MATERIAL, 512, INC, false>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -355,7 +385,9 @@ template <int MATERIAL, bool INC> static cudaError_t allow_smem_all() {
 cudaError_t prepare_chunk_kernels() {
     const cudaError_t e[] = {allow_smem_all<PBS_MATERIAL_NEOHOOKEAN, true>(),
                              allow_smem_all<PBS_MATERIAL_NEOHOOKEAN, false>(),
-                             allow_smem_all<PBS_MATERIAL_STRETCH, false>()};
+                             allow_smem_all<PBS_MATERIAL_STRETCH, false>(),
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(),
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -368,32 +400,36 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
-template <int MATERIAL, int THREADS, bool INC>
+template <int MATERIAL, int THREADS, bool INC, bool STAGE>
 static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m.n_chunks);
     cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes, INC);
+    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes, INC, STAGE);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC>, m, p, st);
+    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC, STAGE>, m, p, st);
 }
 
 template <int MATERIAL, bool INC>
 static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
-    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128, INC>(s, m, p, st, pdl);
-    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512, INC>(s, m, p, st, pdl);
-    return launch_tchunk_t<MATERIAL, 256, INC>(s, m, p, st, pdl);
+    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128, INC, false>(s, m, p, st, pdl);
+    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512, INC, false>(s, m, p, st, pdl);
+    return launch_tchunk_t<MATERIAL, 256, INC, false>(s, m, p, st, pdl);
 }
 
 cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, bool pdl) {
     if (m.n_chunks <= 0) return cudaSuccess;
     if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH, false>(s, m, p, st, pdl);
     if (p.incremental) return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, pdl);
+    if (m.chunk_stage && m.chunk_threads == 128)  // row-staged shapes: full-stress neo-Hookean only
+        return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(s, m, p, st, pdl);
+    if (m.chunk_stage && m.chunk_threads == 256)
+        return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(s, m, p, st, pdl);
     return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, false>(s, m, p, st, pdl);
 }
 

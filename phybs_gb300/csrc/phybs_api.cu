@@ -53,6 +53,7 @@ struct pbs_handle {
     DevBuf<int> inc_ptr, inc, tblk_inst, nblk_inst, pad2user, tet_user, node_state, bad, staging_ids;
     // pass layout (chunks of tets) and the host copies it is rebuilt from
     int n_chunks = 0, chunk_tets = CHUNK_TETS, chunk_nodes = CHUNK_NODES, chunk_threads = CHUNK_THREADS;
+    int chunk_stage = 0;
     std::vector<int4> h_tets_pad;
     std::vector<double> h_rest_pad;
     DevBuf<int4> chunk;
@@ -90,6 +91,7 @@ struct pbs_handle {
         m.tblk_inst = tblk_inst.p; m.nblk_inst = nblk_inst.p;
         m.n_chunks = n_chunks; m.chunk = chunk.p; m.chunk_inst = chunk_inst.p;
         m.chunk_tets = chunk_tets; m.chunk_nodes = chunk_nodes; m.chunk_threads = chunk_threads;
+        m.chunk_stage = chunk_stage;
         m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qloc = qloc.p; m.qslot = qslot.p;
         m.lnode = lnode.p; m.lsptr = lsptr.p; m.lpidx = lpidx.p; m.pptr = pptr.p;
         return m;
@@ -143,7 +145,7 @@ struct pbs_handle {
 // padded mesh, the device arrays, the chunk-ordered copy of the per-tet rows
 // (when they exist) and the instances' chunk ranges.  host_ctl: the control
 // blocks still on the host (creation), else those on the device are updated.
-static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, std::vector<InstCtl> *host_ctl) {
+static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, int stage, std::vector<InstCtl> *host_ctl) {
     std::vector<InstCtl> ctl;
     if (host_ctl) {
         ctl = *host_ctl;
@@ -178,6 +180,7 @@ static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, std::vect
     h->chunk_threads = threads;
     h->chunk_tets = ct;
     h->chunk_nodes = cn;
+    h->chunk_stage = stage;
     if (host_ctl) {
         *host_ctl = ctl;
     } else {
@@ -423,7 +426,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(prepare_chunk_kernels());
     cudaStream_t s = h->stream;
     {
-        const int rc = set_pass_layout(h, CHUNK_THREADS, CHUNK_TETS, CHUNK_NODES, &ctl);
+        const int rc = set_pass_layout(h, CHUNK_THREADS, CHUNK_TETS, CHUNK_NODES, 0, &ctl);
         if (rc != PBS_OK) return fail(rc);
     }
     CKC(cudaMemcpyAsync(h->tets.p, tets_pad.data(), sizeof(int4) * Tp, cudaMemcpyHostToDevice, s));
@@ -815,34 +818,40 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     return time_passes(h, passes, tet_ms, node_ms);
 }
 
-int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes) {
+int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged) {
     if (!h || (threads != 128 && threads != 256 && threads != 512) || chunk_tets < 1 || chunk_nodes < 4 ||
-        4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 ||
-        chunk_smem(chunk_tets, chunk_nodes, true) > (size_t)CHUNK_MAX_SMEM)
+        4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 || (staged != 0 && staged != 1) ||
+        (staged && threads == 512) ||
+        chunk_smem(chunk_tets, chunk_nodes, true, staged != 0) > (size_t)CHUNK_MAX_SMEM)
         return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
-    return set_pass_layout(h, threads, chunk_tets, chunk_nodes, nullptr);
+    return set_pass_layout(h, threads, chunk_tets, chunk_nodes, staged, nullptr);
 }
 
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
     if (!h || passes <= 0) return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
-    // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch
-    static const int shapes[][3] = {{256, 1024, 448}, {256, 768, 352}, {256, 512, 256}, {128, 512, 256},
-                                    {128, 256, 160}, {512, 1024, 448}, {512, 2048, 832}, {256, 640, 320}};
+    // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch, rows
+    // staged in shared memory (full-stress neo-Hookean only)
+    static const int shapes[][4] = {{256, 1024, 448, 0}, {256, 768, 352, 0}, {256, 512, 256, 0},
+                                    {128, 512, 256, 0},  {128, 256, 160, 0}, {512, 1024, 448, 0},
+                                    {512, 2048, 832, 0}, {256, 640, 320, 0}, {256, 512, 256, 1},
+                                    {256, 384, 208, 1},  {128, 256, 160, 1}, {128, 384, 208, 1}};
     const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
-    const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes;
+    const bool can_stage = h->material == PBS_MATERIAL_NEOHOOKEAN && !h->dparams.incremental;
+    const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes, s0 = h->chunk_stage;
     double best = 1e300, first = -1.0;
     int bi = -1, tried = 0;
     for (int i = 0; i < n; ++i) {
-        int rc = set_pass_layout(h, shapes[i][0], shapes[i][1], shapes[i][2], nullptr);
+        if (shapes[i][3] && !can_stage) continue;
+        int rc = set_pass_layout(h, shapes[i][0], shapes[i][1], shapes[i][2], shapes[i][3], nullptr);
         if (rc != PBS_OK) return rc;
         double a = 0.0, b = 0.0;
         rc = time_passes(h, passes, &a, &b);  // warm-up run, then the timed one
         if (rc == PBS_OK) rc = time_passes(h, passes, &a, &b);
         if (rc != PBS_OK) {
             // the state cannot be timed: restore the shape the handle had
-            const int rc2 = set_pass_layout(h, t0, c0, n0, nullptr);
+            const int rc2 = set_pass_layout(h, t0, c0, n0, s0, nullptr);
             return rc2 != PBS_OK ? rc2 : rc;
         }
         const double t = a + b;
@@ -853,12 +862,13 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
             bi = i;
         }
     }
-    const int rc = set_pass_layout(h, shapes[bi][0], shapes[bi][1], shapes[bi][2], nullptr);
+    const int rc = set_pass_layout(h, shapes[bi][0], shapes[bi][1], shapes[bi][2], shapes[bi][3], nullptr);
     if (rc != PBS_OK) return rc;
     if (out) {
         out->chunk_threads = shapes[bi][0];
         out->chunk_tets = shapes[bi][1];
         out->chunk_nodes = shapes[bi][2];
+        out->chunk_staged = shapes[bi][3];
         out->n_tried = tried;
         out->pass_ms = best;
         out->default_pass_ms = first;

@@ -58,9 +58,12 @@ constexpr int CHUNK_NODES = 448;
 constexpr int CHUNK_THREADS = 256;
 constexpr int CHUNK_MAX_SMEM = 200 * 1024;
 // Dynamic shared memory of the per-tet pass kernel: staged node words (u hi,
-// u lo, and the force base with incremental stress) and 3 floats per corner slot.
-__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc) {
-    return (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets;
+// u lo, and the force base with incremental stress), 3 floats per corner slot
+// and, in the row-staged variant, the chunk's per-tet rows and corner ids
+// (64 B per tet).
+__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc, bool stage = false) {
+    return (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets +
+           (stage ? 64 * (size_t)tets : 0);
 }
 
 // Step parameters as the kernels see them (a by-value kernel argument).
@@ -116,7 +119,7 @@ struct DevMesh {
     const float4 *info, *rest;
     const int *tblk_inst, *nblk_inst;
     // pass layout
-    int n_chunks, chunk_tets, chunk_nodes, chunk_threads;
+    int n_chunks, chunk_tets, chunk_nodes, chunk_threads, chunk_stage;
     const int4 *chunk;
     const int *chunk_inst;
     const float4 *qrow0, *qrow1, *qrow2;

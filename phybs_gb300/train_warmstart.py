@@ -37,7 +37,7 @@ CLIP = 4.0  # scaled corrections beyond this are motion onsets: not learnable fr
 
 def residual_params(max_iters=20000):
     return make_params("gpu_reference", h=1 / 30, tol=1e-4, max_iters=max_iters, control=L.PBS_CONTROL_RESTART,
-                       energy_slack=16.0, alpha0=ALPHA0, profile=((10, RHO),))
+                       energy_slack=16.0, alpha0=ALPHA0, profile=((10, RHO),), alpha_grow=1.2)
 
 
 def mean_edge(mesh) -> float:

@@ -429,3 +429,24 @@ def test_inverting_guess_falls_back_to_start_positions():
         assert np.abs(s.positions() - ref.x0).max() / m.bbox_diagonal() < 2e-4, f
     assert fallbacks[4] == 1 and sum(fallbacks) >= 1, fallbacks
     s.close()
+
+
+def test_row_staged_chunk_kernel_matches_unstaged():
+    """The row-staged pass kernel (per-tet rows copied into shared memory
+    asynchronously) computes exactly what the unstaged one computes for the same
+    chunk shape: same corner forces, same order of summation."""
+    m = M.box_mesh(12, 12, 20, edge=0.01, seed=4, young=1e5, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=64, incremental_stress=0)
+    a = DescentSolver(m, params=p)
+    b = DescentSolver(m, params=p)
+    a.set_chunk_shape(256, 512, 256, 0)
+    b.set_chunk_shape(256, 512, 256, 1)
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert np.array_equal(a.positions(), b.positions())
+    assert a.stats()["iterations"] == b.stats()["iterations"]
+    with pytest.raises(L.PhybsError):
+        b.set_chunk_shape(512, 512, 256, 1)  # no staged variant with 512 threads
+    a.close()
+    b.close()
