@@ -94,10 +94,12 @@ RHO = 0.9999
 ALPHA_GROW = 1.2
 
 
-# Stress evaluation of the passes: the full FP32 stress reaches |g| <= 1e-4 |g0|
-# on this workload in the same iterations as the incremental form (22,542 vs
-# 22,643 over the first 10 frames) with ~13% less time per pass.
-INCREMENTAL_STRESS = 0
+# Stress evaluation of the passes: incremental (P(F) - P(F0) against an FP64
+# force at the step's initial guess).  The full FP32 stress is ~13% faster per
+# pass, but with alpha_grow its residual floor stalls the last, most stretched
+# frames of this pull just above 1e-4 |g0| (frame 29 ran into the iteration
+# cap in both arms); the incremental form has no floor there.
+INCREMENTAL_STRESS = 1
 
 
 def solver_params(h=1 / 30, tol=1e-4, max_iters=20000, alpha0=ALPHA0, rho=RHO, incremental=None):
@@ -482,7 +484,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="time the plain descent only")
     ap.add_argument("--stress", choices=["full", "incremental"], default=None,
-                    help="pass stress evaluation (default: full FP32 stress)")
+                    help="pass stress evaluation (default: incremental)")
     ap.add_argument("--workload", choices=["box1m", "batch"], default="box1m",
                     help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances")
     args = ap.parse_args()

@@ -450,3 +450,26 @@ def test_row_staged_chunk_kernel_matches_unstaged():
         b.set_chunk_shape(512, 512, 256, 1)  # no staged variant with 512 threads
     a.close()
     b.close()
+
+
+def test_alpha_growth_matches_oracle():
+    """RESTART control with alpha_grow: the step size shrinks on a rejection and
+    recovers by the growth factor on later accepted checks (never above
+    alpha0); GPU and the FP64 restatement both converge to the same positions."""
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=20000, tol=1e-4, control=L.PBS_CONTROL_RESTART,
+                    alpha0=1.0, energy_slack=16.0, profile=((10, 0.995),), alpha_grow=1.2)
+    s = DescentSolver(m, params=p)
+    mu, lam = O.lame(m.young, m.poisson)
+    r = O.rest(m.rest, m.tets, m.pin_mask(), prec=64)
+    ref = O.StepState(m.rest)
+    po = O.make_params(h=1 / 30, max_iters=20000, tol=1e-4, control=1, alpha0=1.0, body_force_scale=1.0,
+                       energy_clamp=1, profile=((10, 0.995),), hessian_closed=1, alpha_grow=1.2)
+    for f in range(3):
+        s.step()
+        st = s.stats()
+        so = O.step(ref, po, m.tets, r, mu, lam, m.pin_mask(), prec=64)
+        assert st["converged"] == 1 and so.converged == 1, (f, st)
+        assert 0.0 < st["alpha"] <= 1.0
+        assert np.abs(s.positions() - ref.x0).max() / m.bbox_diagonal() < 2e-4, f
+    s.close()
