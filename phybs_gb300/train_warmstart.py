@@ -148,14 +148,20 @@ def lr_schedule(steps: int, peak: float, chunks: int = 40):
     return out
 
 
-def fit(X, Y, W=None, steps=12000, batch=8192, lr=3e-3, seed=0, clip=None, verbose=True) -> WarmStartModel:
+def fit(X, Y, W=None, steps=12000, batch=8192, lr=3e-3, seed=0, clip=None, huber=0.05, verbose=True) -> WarmStartModel:
     """Train on (features, scaled corrections, frame weights).  Samples whose
     scaled correction exceeds `clip` (the onset of a motion, where the last
     displacements say nothing about the next one) are left out.  W (from
     generate) weighs each frame by the inverse of its mean squared correction,
     so that the loss measures every frame's relative error: the small
     corrections of smooth frames, where a percent-level prediction saves most
-    iterations, count as much as the large corrections of a released twist."""
+    iterations, count as much as the large corrections of a released twist.
+
+    huber: the loss is made robust by one round of iteratively reweighted
+    least squares -- after half the steps every sample's weight is scaled by
+    min(1, sqrt(huber / r2)), r2 its weighted squared error -- so that frames
+    the history cannot predict (the errors beyond ~sqrt(huber) of the
+    correction) stop dominating the fit of the predictable ones."""
     clip = CLIP if clip is None else clip
     keep = np.abs(Y).max(1) <= clip
     X, Y = X[keep], Y[keep]
@@ -171,7 +177,15 @@ def fit(X, Y, W=None, steps=12000, batch=8192, lr=3e-3, seed=0, clip=None, verbo
     t = MLPTrainer(seed=seed)
     t.set_data(Xs, Ys, W)
     losses = []
-    for i, (n, lr_i) in enumerate(lr_schedule(steps, lr)):
+    sched = lr_schedule(steps, lr)
+    for i, (n, lr_i) in enumerate(sched):
+        if huber and i == len(sched) // 2:  # reweight once, halfway
+            pred = np.concatenate([t.forward(Xs[j:j + 262144]) for j in range(0, len(Xs), 262144)])
+            r2 = W.astype(np.float64) * ((pred - Ys) ** 2).sum(1)
+            Wh = W * np.minimum(1.0, np.sqrt(huber / np.maximum(r2, 1e-30))).astype(np.float32)
+            t.set_data(Xs, Ys, (Wh / Wh.mean()).astype(np.float32))
+            if verbose:
+                print(f"  reweighted: {np.mean(r2 > huber):.3f} of the samples beyond the Huber threshold", flush=True)
         losses.append(t.train(n, batch=batch, lr=lr_i, seed=seed + i))
     losses = np.concatenate(losses)
     if verbose:
