@@ -249,8 +249,7 @@ typedef struct pbs_tune_result {
     int chunk_tets;          /* tets per chunk at most                            */
     int chunk_nodes;         /* nodes a chunk may touch at most                   */
     int chunk_staged;        /* 1: the chunk's per-tet rows are staged in shared
-                                memory by asynchronous copies (full-stress
-                                neo-Hookean only)                                 */
+                                memory by asynchronous copies (neo-Hookean only)  */
     int n_tried;             /* shapes timed                                      */
     double pass_ms;          /* per-tet + per-node kernel time of one pass, kept shape */
     double default_pass_ms;  /* the same for the default shape (256, 1024, 448)   */
@@ -268,8 +267,8 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
 /* Sets a chunk shape directly (for instance one pbs_autotune picked on another
  * handle of the same mesh): threads per CTA 128, 256 or 512; tets per chunk
  * 1 .. 16384; nodes per chunk >= 4; staged 0 or 1 (not with 512 threads;
- * used by full-stress neo-Hookean handles only); the shared memory it needs
- * at most 200 KB.  Call between steps. */
+ * used by neo-Hookean handles only); the shared memory it needs at most
+ * 200 KB.  Call between steps. */
 int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged);
 
 /* ------------------------------------------------------------------------

@@ -239,6 +239,7 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         if (STAGE) {
             cp_async16(s_uh + j, st.uh + cur + g);
             cp_async16(s_ul + j, st.ul + cur + g);
+            if (INC) cp_async16(s_ub + j, st.ub + g);
         } else {
             s_uh[j] = st.uh[cur + g];
             s_ul[j] = st.ul[cur + g];
@@ -387,7 +388,9 @@ cudaError_t prepare_chunk_kernels() {
                              allow_smem_all<PBS_MATERIAL_NEOHOOKEAN, false>(),
                              allow_smem_all<PBS_MATERIAL_STRETCH, false>(),
                              allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(),
-                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>()};
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(),
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128, true, true>(),
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -425,11 +428,15 @@ static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevPara
 cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, bool pdl) {
     if (m.n_chunks <= 0) return cudaSuccess;
     if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH, false>(s, m, p, st, pdl);
-    if (p.incremental) return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, pdl);
-    if (m.chunk_stage && m.chunk_threads == 128)  // row-staged shapes: full-stress neo-Hookean only
-        return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(s, m, p, st, pdl);
-    if (m.chunk_stage && m.chunk_threads == 256)
-        return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(s, m, p, st, pdl);
+    // row-staged shapes: neo-Hookean, 128 or 256 threads
+    const bool st128 = m.chunk_stage && m.chunk_threads == 128, st256 = m.chunk_stage && m.chunk_threads == 256;
+    if (p.incremental) {
+        if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, true, true>(s, m, p, st, pdl);
+        if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>(s, m, p, st, pdl);
+        return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, pdl);
+    }
+    if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(s, m, p, st, pdl);
+    if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(s, m, p, st, pdl);
     return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, false>(s, m, p, st, pdl);
 }
 

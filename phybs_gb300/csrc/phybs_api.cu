@@ -832,13 +832,13 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
     if (!h || passes <= 0) return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
     // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch, rows
-    // staged in shared memory (full-stress neo-Hookean only)
+    // staged in shared memory (neo-Hookean only)
     static const int shapes[][4] = {{256, 1024, 448, 0}, {256, 768, 352, 0}, {256, 512, 256, 0},
                                     {128, 512, 256, 0},  {128, 256, 160, 0}, {512, 1024, 448, 0},
                                     {512, 2048, 832, 0}, {256, 640, 320, 0}, {256, 512, 256, 1},
                                     {256, 384, 208, 1},  {128, 256, 160, 1}, {128, 384, 208, 1}};
     const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
-    const bool can_stage = h->material == PBS_MATERIAL_NEOHOOKEAN && !h->dparams.incremental;
+    const bool can_stage = h->material == PBS_MATERIAL_NEOHOOKEAN;
     const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes, s0 = h->chunk_stage;
     double best = 1e300, first = -1.0;
     int bi = -1, tried = 0;

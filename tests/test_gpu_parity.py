@@ -355,7 +355,7 @@ def test_autotune_keeps_results():
     a = DescentSolver(m, params=p)
     b = DescentSolver(m, params=p)
     r = b.autotune(8)
-    assert r["n_tried"] == 8 and r["chunk_threads"] in (128, 256, 512)
+    assert r["n_tried"] == 12 and r["chunk_threads"] in (128, 256, 512)
     assert 0.0 < r["pass_ms"] <= r["default_pass_ms"]
     for _ in range(3):
         a.step()
@@ -431,12 +431,13 @@ def test_inverting_guess_falls_back_to_start_positions():
     s.close()
 
 
-def test_row_staged_chunk_kernel_matches_unstaged():
+@pytest.mark.parametrize("incremental", [0, 1])
+def test_row_staged_chunk_kernel_matches_unstaged(incremental):
     """The row-staged pass kernel (per-tet rows copied into shared memory
     asynchronously) computes exactly what the unstaged one computes for the same
     chunk shape: same corner forces, same order of summation."""
     m = M.box_mesh(12, 12, 20, edge=0.01, seed=4, young=1e5, poisson=0.4)
-    p = make_params("gpu_reference", h=1 / 30, max_iters=64, incremental_stress=0)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=64, incremental_stress=incremental)
     a = DescentSolver(m, params=p)
     b = DescentSolver(m, params=p)
     a.set_chunk_shape(256, 512, 256, 0)
