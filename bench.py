@@ -260,7 +260,8 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
 
     s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
     if tune is not None:
-        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"])
+        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"],
+                          tune["node_npt"])
     if model is not None:
         s.set_warm_start(model)
     stream = torch.cuda.ExternalStream(s.stream())
@@ -316,7 +317,8 @@ def profile_pass(args, m, tune=None):
     from phybs_gb300.solver import DescentSolver
     s = DescentSolver(m, params=solver_params(max_iters=args.max_iters))
     if tune is not None:
-        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"])
+        s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"],
+                          tune["node_npt"])
     try:
         return s.profile_kernels(20), None
     except Exception as exc:  # an instance stopped early: no valid per-kernel time

@@ -250,14 +250,16 @@ typedef struct pbs_tune_result {
     int chunk_nodes;         /* nodes a chunk may touch at most                   */
     int chunk_staged;        /* 1: the chunk's per-tet rows are staged in shared
                                 memory by asynchronous copies (neo-Hookean only)  */
+    int node_npt;            /* nodes per thread of the node kernel (1 or 2)      */
     int n_tried;             /* shapes timed                                      */
     double pass_ms;          /* per-tet + per-node kernel time of one pass, kept shape */
     double default_pass_ms;  /* the same for the default shape (256, 1024, 448)   */
 } pbs_tune_result;
-/* Autotuner of the pass kernels' block and tile shape: rebuilds the pass
+/* Autotuner of the pass kernels' block and tile shapes: rebuilds the pass
  * layout for each candidate chunk shape (threads per CTA, tets per chunk,
  * nodes per chunk, rows staged in shared memory or read in the loop), times
- * `passes` passes of it from the current state with
+ * `passes` passes of it from the current state (then the node kernel with 1
+ * and 2 nodes per thread) with
  * CUDA events and keeps the fastest.  Forces stay deterministic for a given
  * shape; another shape changes the order the corner forces are summed in, so
  * results can differ in the last bits.  Call between steps (it recaptures the
@@ -268,8 +270,9 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
  * handle of the same mesh): threads per CTA 128, 256 or 512; tets per chunk
  * 1 .. 16384; nodes per chunk >= 4; staged 0 or 1 (not with 512 threads;
  * used by neo-Hookean handles only); the shared memory it needs at most
- * 200 KB.  Call between steps. */
-int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged);
+ * 200 KB; node_npt 1 or 2 nodes per thread of the node kernel.  Call between
+ * steps. */
+int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged, int node_npt);
 
 /* ------------------------------------------------------------------------
  * Learned warm start.  A per-node MLP 24 -> 64 -> 64 -> 64 -> 3 (GELU; BF16

@@ -70,7 +70,7 @@ class Stats(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("chunk_threads", C.c_int), ("chunk_tets", C.c_int), ("chunk_nodes", C.c_int),
-                ("chunk_staged", C.c_int), ("n_tried", C.c_int),
+                ("chunk_staged", C.c_int), ("node_npt", C.c_int), ("n_tried", C.c_int),
                 ("pass_ms", C.c_double), ("default_pass_ms", C.c_double)]
 
 

@@ -198,104 +198,152 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-__global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState st) {
-    __shared__ double sh[BLOCK / 32];
+// The state-independent inputs of one node, loaded before the grid-dependency
+// wait.
+struct NodeIn {
+    float4 info, th, tl, bh, bl;
+    int pa, pe;
+};
+
+// The instance's pass state as the node update needs it.
+struct PassCtx {
+    int action;
+    bool do_h;
+    float alpha, omega;
+    size_t cur, nxt;
+};
+
+// Jacobi step with Chebyshev extrapolation (or restore / save) of node i;
+// returns its |g|^2.
+__device__ __forceinline__ double node_update(const DevMesh &m, const DevParams &p, const DevState &st, int i,
+                                              const NodeIn &in, const float4 &f0, const float4 &f1, const PassCtx &c) {
+    double r2 = 0.0;
+    if (in.info.z == 2.f) return r2;
+    const size_t cur = c.cur, nxt = c.nxt;
+    const float4 uh = st.uh[cur + i], ul = st.ul[cur + i], dd = st.dd[cur + i];
+    float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c.action == ACT_RESTORE) {
+        // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
+        // x_last = x_{k-1} = u - d (the reference does not restore it), or
+        // restarts it under PBS_CONTROL_RESTART
+        nh = st.oh[i];
+        nl = st.ol[i];
+        if (in.info.z == 0.f && p.control == PBS_CONTROL_REFERENCE)
+            nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
+                             ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
+    } else {
+        if (c.action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:181)
+            st.oh[i] = uh;
+            st.ol[i] = ul;
+        }
+        if (in.info.z == 0.f) {
+            float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
+            // this node's per-chunk partial sums, in chunk order
+            fx += f0.x;
+            fy += f0.y;
+            fz += f0.z;
+            fx += f1.x;
+            fy += f1.y;
+            fz += f1.z;
+            for (int j = in.pa + 2; j < in.pe; ++j) {
+                const float4 f = st.part[j];
+                fx += f.x;
+                fy += f.y;
+                fz += f.z;
+            }
+            if (c.do_h) {
+                for (int j = in.pa; j < in.pe; ++j) {
+                    const float4 q = st.parth[j];
+                    hx += q.x;
+                    hy += q.y;
+                    hz += q.z;
+                }
+            }
+            const float mh = in.info.x * p.h2inv;
+            float4 D;
+            if (c.do_h) {
+                D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
+                st.diag[i] = D;
+            } else {
+                D = st.diag[i];
+            }
+            // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
+            // force (incremental mode) + body_force_scale (external + gravity)
+            const float4 th = in.th, tl = in.tl, bh = in.bh, bl = in.bl;
+            const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
+            const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
+            const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
+            r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
+            // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
+            // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
+            // d' = (omega - 1) d + omega delta
+            const float alpha = c.alpha, omega = c.omega;
+            const float dx = alpha * (gx / -D.x), dy = alpha * (gy / -D.y), dz = alpha * (gz / -D.z);
+            if (omega != 1.0f)
+                nd = make_float4((omega - 1.f) * dd.x + omega * dx, (omega - 1.f) * dd.y + omega * dy,
+                                 (omega - 1.f) * dd.z + omega * dz, 0.f);
+            else
+                nd = make_float4(dx, dy, dz, 0.f);
+            add_comp(nh.x, nl.x, nd.x);
+            add_comp(nh.y, nl.y, nd.y);
+            add_comp(nh.z, nl.z, nd.z);
+        }
+    }
+    st.uh[nxt + i] = nh;
+    st.ul[nxt + i] = nl;
+    st.dd[nxt + i] = nd;
+    return r2;
+}
+
+// One CTA per 256-node block (one instance); NPT nodes per thread, whose
+// loads are all issued before any of them is used.
+template <int NPT>
+__global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, DevState st) {
+    constexpr int TH = BLOCK / NPT;
+    __shared__ double sh[TH / 32];
     __shared__ int is_last;
     const int b = blockIdx.x;
-    const int i = b * BLOCK + threadIdx.x;  // < Np: the grid covers the padded nodes exactly
     // loads that do not depend on the instance's state go out before it is read
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 info = m.info[i];
-    const float4 th = st.th[i], tl = st.tl[i], bh = st.bh[i], bl = st.bl[i];
-    const int pa = m.pptr[i], pe = m.pptr[i + 1];
+    NodeIn in[NPT];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+        const int i = b * BLOCK + threadIdx.x + j * TH;  // < Np: the grid covers the padded nodes exactly
+        in[j].info = m.info[i];
+        in[j].th = st.th[i];
+        in[j].tl = st.tl[i];
+        in[j].bh = st.bh[i];
+        in[j].bl = st.bl[i];
+        in[j].pa = m.pptr[i];
+        in[j].pe = m.pptr[i + 1];
+    }
     const int inst = m.nblk_inst[b];
     pdl_launch_dependents();
     pdl_wait();  // the chunk kernel's partials and decisions are visible from here
-    const float4 f0 = pa < pe ? st.part[pa] : z4;
-    const float4 f1 = pa + 1 < pe ? st.part[pa + 1] : z4;
+    float4 f0[NPT], f1[NPT];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+        f0[j] = in[j].pa < in[j].pe ? st.part[in[j].pa] : z4;
+        f1[j] = in[j].pa + 1 < in[j].pe ? st.part[in[j].pa + 1] : z4;
+    }
     InstCtl *cp = st.ctl + inst;
     if (cp->done) return;
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const int action = check ? cp->action : ACT_STEP;
     const bool do_h = (k % p.hd_every) == 0;
-    const float alpha = cp->alpha;
     float rho = cp->rho, omega = cp->omega;
     chebyshev_schedule(p, k - cp->k_restart, rho, omega);
-    const size_t cur = (size_t)cp->par * m.Np, nxt = (size_t)(1 - cp->par) * m.Np;
+    PassCtx ctx;
+    ctx.action = action;
+    ctx.do_h = do_h;
+    ctx.alpha = cp->alpha;
+    ctx.omega = omega;
+    ctx.cur = (size_t)cp->par * m.Np;
+    ctx.nxt = (size_t)(1 - cp->par) * m.Np;
     double r2 = 0.0;
-    if (info.z != 2.f) {
-        const float4 uh = st.uh[cur + i], ul = st.ul[cur + i], dd = st.dd[cur + i];
-        float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (action == ACT_RESTORE) {
-            // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
-            // x_last = x_{k-1} = u - d (the reference does not restore it), or
-            // restarts it under PBS_CONTROL_RESTART
-            nh = st.oh[i];
-            nl = st.ol[i];
-            if (info.z == 0.f && p.control == PBS_CONTROL_REFERENCE)
-                nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
-                                 ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
-        } else {
-            if (action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:181)
-                st.oh[i] = uh;
-                st.ol[i] = ul;
-            }
-            if (info.z == 0.f) {
-                float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
-                // this node's per-chunk partial sums, in chunk order
-                fx += f0.x;
-                fy += f0.y;
-                fz += f0.z;
-                fx += f1.x;
-                fy += f1.y;
-                fz += f1.z;
-                for (int j = pa + 2; j < pe; ++j) {
-                    const float4 f = st.part[j];
-                    fx += f.x;
-                    fy += f.y;
-                    fz += f.z;
-                }
-                if (do_h) {
-                    for (int j = pa; j < pe; ++j) {
-                        const float4 q = st.parth[j];
-                        hx += q.x;
-                        hy += q.y;
-                        hz += q.z;
-                    }
-                }
-                const float mh = info.x * p.h2inv;
-                float4 D;
-                if (do_h) {
-                    D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
-                    st.diag[i] = D;
-                } else {
-                    D = st.diag[i];
-                }
-                // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
-                // force (incremental mode) + body_force_scale (external + gravity)
-                const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
-                const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
-                const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
-                r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
-                // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
-                // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
-                // d' = (omega - 1) d + omega delta
-                const float dx = alpha * (gx / -D.x), dy = alpha * (gy / -D.y), dz = alpha * (gz / -D.z);
-                if (omega != 1.0f)
-                    nd = make_float4((omega - 1.f) * dd.x + omega * dx, (omega - 1.f) * dd.y + omega * dy,
-                                     (omega - 1.f) * dd.z + omega * dz, 0.f);
-                else
-                    nd = make_float4(dx, dy, dz, 0.f);
-                add_comp(nh.x, nl.x, nd.x);
-                add_comp(nh.y, nl.y, nd.y);
-                add_comp(nh.z, nl.z, nd.z);
-            }
-        }
-        st.uh[nxt + i] = nh;
-        st.ul[nxt + i] = nl;
-        st.dd[nxt + i] = nd;
-    }
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) r2 += node_update(m, p, st, b * BLOCK + threadIdx.x + j * TH, in[j], f0[j], f1[j], ctx);
     const double sr = block_sum(r2, sh);
     if (threadIdx.x == 0) {
         st.npart[b] = sr;
@@ -307,7 +355,7 @@ __global__ void __launch_bounds__(BLOCK) k_node(DevMesh m, DevParams p, DevState
     if (!is_last) return;
     __threadfence();
     double R2 = 0.0;
-    for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += BLOCK) R2 += __ldcg(st.npart + j);
+    for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += TH) R2 += __ldcg(st.npart + j);
     R2 = block_sum(R2, sh);
     if (threadIdx.x != 0) return;
     // updated in place: every other block has read it, and the next kernel
@@ -564,17 +612,21 @@ cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p
     k_prologue<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, p, st, ext_user, pad2user);
     return cudaGetLastError();
 }
-cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
+template <int NPT>
+static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m.n_nblk);
-    cfg.blockDim = dim3(BLOCK);
+    cfg.blockDim = dim3(BLOCK / NPT);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_node, m, p, st);
+    return cudaLaunchKernelEx(&cfg, k_node<NPT>, m, p, st);
+}
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
+    return m.node_npt == 2 ? launch_node_t<2>(s, m, p, st, pdl) : launch_node_t<1>(s, m, p, st, pdl);
 }
 // One pass of the step graph: both kernels with programmatic dependent launch.
 cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {

@@ -54,6 +54,7 @@ struct pbs_handle {
     // pass layout (chunks of tets) and the host copies it is rebuilt from
     int n_chunks = 0, chunk_tets = CHUNK_TETS, chunk_nodes = CHUNK_NODES, chunk_threads = CHUNK_THREADS;
     int chunk_stage = 0;
+    int node_npt = NODE_NPT_DEFAULT;
     std::vector<int4> h_tets_pad;
     std::vector<double> h_rest_pad;
     DevBuf<int4> chunk;
@@ -92,6 +93,7 @@ struct pbs_handle {
         m.n_chunks = n_chunks; m.chunk = chunk.p; m.chunk_inst = chunk_inst.p;
         m.chunk_tets = chunk_tets; m.chunk_nodes = chunk_nodes; m.chunk_threads = chunk_threads;
         m.chunk_stage = chunk_stage;
+        m.node_npt = node_npt;
         m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qloc = qloc.p; m.qslot = qslot.p;
         m.lnode = lnode.p; m.lsptr = lsptr.p; m.lpidx = lpidx.p; m.pptr = pptr.p;
         return m;
@@ -818,13 +820,15 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
     return time_passes(h, passes, tet_ms, node_ms);
 }
 
-int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged) {
+int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged, int node_npt) {
     if (!h || (threads != 128 && threads != 256 && threads != 512) || chunk_tets < 1 || chunk_nodes < 4 ||
+        (node_npt != 1 && node_npt != 2) ||
         4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 || (staged != 0 && staged != 1) ||
         (staged && threads == 512) ||
         chunk_smem(chunk_tets, chunk_nodes, true, staged != 0) > (size_t)CHUNK_MAX_SMEM)
         return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
+    h->node_npt = node_npt;
     return set_pass_layout(h, threads, chunk_tets, chunk_nodes, staged, nullptr);
 }
 
@@ -862,9 +866,26 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
             bi = i;
         }
     }
-    const int rc = set_pass_layout(h, shapes[bi][0], shapes[bi][1], shapes[bi][2], shapes[bi][3], nullptr);
+    int rc = set_pass_layout(h, shapes[bi][0], shapes[bi][1], shapes[bi][2], shapes[bi][3], nullptr);
     if (rc != PBS_OK) return rc;
+    // the node kernel: 1 or 2 nodes per thread (independent of the chunk shape)
+    double node_ms[2] = {0.0, 0.0};
+    const int npt0 = h->node_npt;
+    for (int npt = 1; npt <= 2; ++npt) {
+        h->node_npt = npt;
+        double a = 0.0, b = 0.0;
+        rc = time_passes(h, passes, &a, &b);
+        if (rc == PBS_OK) rc = time_passes(h, passes, &a, &b);
+        if (rc != PBS_OK) {
+            h->node_npt = npt0;
+            return rc;
+        }
+        node_ms[npt - 1] = b;
+    }
+    h->node_npt = node_ms[1] < node_ms[0] ? 2 : 1;
+    h->graph_valid = false;
     if (out) {
+        out->node_npt = h->node_npt;
         out->chunk_threads = shapes[bi][0];
         out->chunk_tets = shapes[bi][1];
         out->chunk_nodes = shapes[bi][2];

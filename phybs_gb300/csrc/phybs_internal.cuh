@@ -49,7 +49,10 @@
 namespace pbs {
 
 constexpr int PAD = 256;    // instance alignment (tets and nodes)
-constexpr int BLOCK = 256;  // threads per block of the step kernels
+constexpr int BLOCK = 256;  // threads per block of the step kernels (nodes per node block)
+// nodes per thread of the node kernel (BLOCK / npt threads per CTA): 1 or 2,
+// picked by pbs_autotune
+constexpr int NODE_NPT_DEFAULT = 1;
 // Default chunk shape of the per-tet pass kernel (pbs_autotune may pick
 // another): at most CHUNK_TETS tets touching at most CHUNK_NODES nodes, one
 // CTA of CHUNK_THREADS threads per chunk.
@@ -120,6 +123,7 @@ struct DevMesh {
     const int *tblk_inst, *nblk_inst;
     // pass layout
     int n_chunks, chunk_tets, chunk_nodes, chunk_threads, chunk_stage;
+    int node_npt;
     const int4 *chunk;
     const int *chunk_inst;
     const float4 *qrow0, *qrow1, *qrow2;

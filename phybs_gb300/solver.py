@@ -155,10 +155,10 @@ class DescentSolver:
         L.check(L.lib().pbs_autotune(self._h, C.c_int(passes), C.byref(r)), "pbs_autotune")
         return {k: getattr(r, k) for k, _ in r._fields_}
 
-    def set_chunk_shape(self, threads: int, chunk_tets: int, chunk_nodes: int, staged: int = 0):
-        """Use a chunk shape picked elsewhere (e.g. by autotune on another handle)."""
+    def set_chunk_shape(self, threads: int, chunk_tets: int, chunk_nodes: int, staged: int = 0, node_npt: int = 1):
+        """Use launch shapes picked elsewhere (e.g. by autotune on another handle)."""
         L.check(L.lib().pbs_set_chunk_shape(self._h, C.c_int(threads), C.c_int(chunk_tets), C.c_int(chunk_nodes),
-                                            C.c_int(staged)), "pbs_set_chunk_shape")
+                                            C.c_int(staged), C.c_int(node_npt)), "pbs_set_chunk_shape")
 
     def warm_start_features(self, ext=None):
         """Raw 24 features per node for the next step, the plain initial

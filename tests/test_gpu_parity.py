@@ -440,15 +440,16 @@ def test_row_staged_chunk_kernel_matches_unstaged(incremental):
     p = make_params("gpu_reference", h=1 / 30, max_iters=64, incremental_stress=incremental)
     a = DescentSolver(m, params=p)
     b = DescentSolver(m, params=p)
-    a.set_chunk_shape(256, 512, 256, 0)
-    b.set_chunk_shape(256, 512, 256, 1)
+    a.set_chunk_shape(256, 512, 256, 0, 1)
+    b.set_chunk_shape(256, 512, 256, 1, 2)
     for _ in range(3):
         a.step()
         b.step()
-    assert np.array_equal(a.positions(), b.positions())
-    assert a.stats()["iterations"] == b.stats()["iterations"]
+    # same corner forces; the node kernel's two-nodes-per-thread variant changes
+    # only the order of the |g|^2 reduction
+    assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-6
     with pytest.raises(L.PhybsError):
-        b.set_chunk_shape(512, 512, 256, 1)  # no staged variant with 512 threads
+        b.set_chunk_shape(512, 512, 256, 1, 1)  # no staged variant with 512 threads
     a.close()
     b.close()
 
