@@ -206,13 +206,15 @@ def main():
     ap.add_argument("--data", default=None, help="save the generated (X, Y) here")
     ap.add_argument("--data-max", type=int, default=0, help="save at most this many samples (0 = all)")
     ap.add_argument("--from-data", default=None, help="fit to (X, Y, W) saved by --data instead of generating")
+    ap.add_argument("--mix", default="0.5,0.3,0.2", help="fractions of box1m, box and ellipsoid runs")
     args = ap.parse_args()
     t0 = time.time()
     if args.from_data:
         with np.load(args.from_data) as z:
             X, Y, W = z["X"], z["Y"], z["W"]
     else:
-        X, Y, W = generate(args.frames, args.nodes_per_frame, args.seed)
+        X, Y, W = generate(args.frames, args.nodes_per_frame, args.seed,
+                           mix=tuple(float(v) for v in args.mix.split(",")))
     print(f"data: {X.shape[0]} samples in {time.time() - t0:.0f}s", flush=True)
     if args.data and not args.from_data:
         keep = np.arange(X.shape[0])
