@@ -336,7 +336,11 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     m, bottom, length, young = box_workload(args.seed, args.scale)
     model = WarmStartModel.load(DEFAULT_MODEL) if os.path.exists(DEFAULT_MODEL) and not args.plain_only else None
-    tune = tune_shape(args, m)
+    if args.shape:
+        v = [int(x) for x in args.shape.split(",")]
+        tune = {"chunk_threads": v[0], "chunk_tets": v[1], "chunk_nodes": v[2], "chunk_staged": v[3], "node_npt": v[4]}
+    else:
+        tune = tune_shape(args, m)
     plain = run_arm(args, m, bottom, length, None, world, e2e=False, tune=tune)
     warm = run_arm(args, m, bottom, length, model, world, e2e=False, tune=tune) if model is not None else None
     head = warm if warm is not None else plain
@@ -487,6 +491,8 @@ def main():
     ap.add_argument("--plain-only", action="store_true", help="time the plain descent only")
     ap.add_argument("--stress", choices=["full", "incremental"], default=None,
                     help="pass stress evaluation (default: incremental)")
+    ap.add_argument("--shape", default=None,
+                    help="launch shapes 'threads,tets,nodes,staged,node_npt' instead of autotuning (profiling runs)")
     ap.add_argument("--workload", choices=["box1m", "batch"], default="box1m",
                     help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances")
     args = ap.parse_args()
