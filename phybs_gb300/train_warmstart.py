@@ -199,14 +199,14 @@ def fit(X, Y, W=None, steps=12000, batch=8192, lr=3e-3, seed=0, clip=None, huber
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--frames", type=int, default=4000)
-    ap.add_argument("--nodes-per-frame", type=int, default=512)
+    ap.add_argument("--nodes-per-frame", type=int, default=1024)
     ap.add_argument("--steps", type=int, default=12000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--data", default=None, help="save the generated (X, Y) here")
     ap.add_argument("--data-max", type=int, default=0, help="save at most this many samples (0 = all)")
     ap.add_argument("--from-data", default=None, help="fit to (X, Y, W) saved by --data instead of generating")
-    ap.add_argument("--mix", default="0.5,0.3,0.2", help="fractions of box1m, box and ellipsoid runs")
+    ap.add_argument("--mix", default="0.7,0.2,0.1", help="fractions of box1m, box and ellipsoid runs")
     args = ap.parse_args()
     t0 = time.time()
     if args.from_data:
