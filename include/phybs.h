@@ -39,6 +39,8 @@ extern "C" {
 #define PBS_E_NO_DEVICE (-6)   /* no CUDA device, or not compute capability 10.3 */
 #define PBS_E_OUT_OF_MEMORY (-7)
 #define PBS_E_CAPACITY (-8)    /* a size beyond a documented fixed maximum      */
+#define PBS_E_DEVICE_TIMEOUT (-9) /* a kernel's bounded wait on its own copies
+                                     ran out (the step's results are invalid)   */
 
 /* Materials.  Both are the neo-Hookean energy
  *   Psi = mu/2 (I1 - 3) - mu ln J + lambda/2 (ln J)^2,
@@ -249,7 +251,9 @@ typedef struct pbs_tune_result {
     int chunk_tets;          /* tets per chunk at most                            */
     int chunk_nodes;         /* nodes a chunk may touch at most                   */
     int chunk_staged;        /* 1: the chunk's per-tet rows are staged in shared
-                                memory by asynchronous copies (neo-Hookean only)  */
+                                memory by asynchronous copies; 2: persistent CTAs
+                                walk the chunks through two staging buffers fed by
+                                bulk (TMA) copies (neo-Hookean only)              */
     int node_npt;            /* nodes per thread of the node kernel (1 or 2)      */
     int n_tried;             /* shapes timed                                      */
     double pass_ms;          /* per-tet + per-node kernel time of one pass, kept shape */
@@ -257,7 +261,8 @@ typedef struct pbs_tune_result {
 } pbs_tune_result;
 /* Autotuner of the pass kernels' block and tile shapes: rebuilds the pass
  * layout for each candidate chunk shape (threads per CTA, tets per chunk,
- * nodes per chunk, rows staged in shared memory or read in the loop), times
+ * nodes per chunk, staging: rows read in the loop, staged in shared memory, or
+ * the persistent double-buffered kernel), times
  * `passes` passes of it from the current state (then the node kernel with 1
  * and 2 nodes per thread) with
  * CUDA events and keeps the fastest.  Forces stay deterministic for a given
@@ -268,7 +273,7 @@ typedef struct pbs_tune_result {
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
 /* Sets a chunk shape directly (for instance one pbs_autotune picked on another
  * handle of the same mesh): threads per CTA 128, 256 or 512; tets per chunk
- * 1 .. 16384; nodes per chunk >= 4; staged 0 or 1 (not with 512 threads;
+ * 1 .. 16384; nodes per chunk >= 4; staged 0, 1 or 2 (not with 512 threads;
  * used by neo-Hookean handles only); the shared memory it needs at most
  * 200 KB; node_npt 1 or 2 nodes per thread of the node kernel.  Call between
  * steps. */

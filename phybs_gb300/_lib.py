@@ -20,6 +20,7 @@ PBS_E_BAD_MESH = -5
 PBS_E_NO_DEVICE = -6
 PBS_E_OUT_OF_MEMORY = -7
 PBS_E_CAPACITY = -8
+PBS_E_DEVICE_TIMEOUT = -9
 
 PBS_MATERIAL_NEOHOOKEAN = 0
 PBS_MATERIAL_STRETCH = 1

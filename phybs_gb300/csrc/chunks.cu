@@ -57,7 +57,7 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
     out = ChunkLayout();
     std::vector<int> stamp(Np, -1), lidx(Np, 0), n_part(Np, 0);
     std::vector<std::pair<uint32_t, int>> order;
-    std::vector<int> ctets, lnodes, scount;
+    std::vector<int> ctets, lnodes, scount, lnode_all, lsptr_all, lsend_all;
     int tq = 0;
     for (size_t b = 0; b < ctl.size(); ++b) {
         InstCtl &C = ctl[b];
@@ -96,7 +96,7 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
         }
         std::sort(order.begin(), order.end());
         if (order.empty()) {  // an instance without tets still needs a CTA for its line-search decisions
-            out.chunk.push_back(make_int4(tq, 0, (int)out.lnode.size(), 0));
+            out.chunk.push_back(make_int4(tq, 0, (int)lnode_all.size(), 0));
             out.chunk_inst.push_back((int)b);
         }
         size_t pos = 0;
@@ -122,6 +122,9 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
                 ctets.push_back(t);
                 ++pos;
             }
+            // local nodes in ascending id order: a warp's node gathers then
+            // share sectors (ordering them by corner count, which evens out the
+            // partial-sum loops, measured slower)
             std::sort(lnodes.begin(), lnodes.end());
             const int nl = (int)lnodes.size(), nt = (int)ctets.size();
             for (int j = 0; j < nl; ++j) lidx[lnodes[j]] = j;
@@ -129,21 +132,22 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
             for (int t : ctets)
                 for (int c = 0; c < 4; ++c) scount[lidx[(&tets[t].x)[c]] + 1]++;
             for (int j = 0; j < nl; ++j) scount[j + 1] += scount[j];
-            const int l0 = (int)out.lnode.size();
+            const int l0 = (int)lnode_all.size();
             for (int j = 0; j < nl; ++j) {
-                out.lnode.push_back(lnodes[j]);
-                out.lsptr.push_back(scount[j]);
+                lnode_all.push_back(lnodes[j]);
+                lsptr_all.push_back(scount[j]);
+                lsend_all.push_back(scount[j + 1]);
                 n_part[lnodes[j]]++;
             }
             for (int lt = 0; lt < nt; ++lt) {
                 const int *q = &tets[ctets[lt]].x;
-                unsigned short loc[4], sl[4];
+                unsigned loc[4], sl[4];
                 for (int c = 0; c < 4; ++c) {
-                    loc[c] = (unsigned short)lidx[q[c]];
-                    sl[c] = (unsigned short)scount[loc[c]]++;
+                    loc[c] = (unsigned)lidx[q[c]];
+                    sl[c] = (unsigned)scount[loc[c]]++;
                 }
-                out.qloc.push_back(make_ushort4(loc[0], loc[1], loc[2], loc[3]));
-                out.qslot.push_back(make_ushort4(sl[0], sl[1], sl[2], sl[3]));
+                out.qcor.push_back(make_uint4(loc[0] | loc[1] << 16, loc[2] | loc[3] << 16, sl[0] | sl[1] << 16,
+                                              sl[2] | sl[3] << 16));
                 out.qperm.push_back(ctets[lt]);
             }
             out.chunk.push_back(make_int4(tq, nt, l0, nl));
@@ -157,8 +161,9 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
     out.pptr.assign(Np + 1, 0);
     for (int i = 0; i < Np; ++i) out.pptr[i + 1] = out.pptr[i] + n_part[i];
     std::vector<int> fill(out.pptr.begin(), out.pptr.end() - 1);
-    out.lpidx.resize(out.lnode.size());
-    for (size_t j = 0; j < out.lnode.size(); ++j) out.lpidx[j] = fill[out.lnode[j]]++;
+    out.lmeta.resize(lnode_all.size());
+    for (size_t j = 0; j < lnode_all.size(); ++j)
+        out.lmeta[j] = make_int4(lnode_all[j], lsptr_all[j], lsend_all[j], fill[lnode_all[j]]++);
 }
 
 // ------------------------------------------------------------ device
@@ -172,137 +177,109 @@ __global__ void k_pass_rows(int T, const int *qperm, const float4 *row0, const f
     q2[j] = row2[t];
 }
 
-// Sums every local node's slots (in slot order) into its partial for this
-// chunk.
-template <int THREADS>
-__device__ __forceinline__ void chunk_partials(const DevMesh &m, int l0, int nl, int nt, const float *sx,
-                                               const float *sy, const float *sz, float4 *out) {
-    for (int j = threadIdx.x; j < nl; j += THREADS) {
-        const int s0 = m.lsptr[l0 + j];
-        const int s1 = j + 1 < nl ? m.lsptr[l0 + j + 1] : 4 * nt;
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (int s = s0; s < s1; ++s) {
-            fx += sx[s];
-            fy += sy[s];
-            fz += sz[s];
-        }
-        out[m.lpidx[l0 + j]] = make_float4(fx, fy, fz, 0.f);
-    }
+// Corner ids of a pass tet from its packed record.
+__device__ __forceinline__ void unpack_cor(const uint4 &w, int loc[4], int slot[4]) {
+    loc[0] = (int)(w.x & 0xffffu);
+    loc[1] = (int)(w.x >> 16);
+    loc[2] = (int)(w.y & 0xffffu);
+    loc[3] = (int)(w.y >> 16);
+    slot[0] = (int)(w.z & 0xffffu);
+    slot[1] = (int)(w.z >> 16);
+    slot[2] = (int)(w.w & 0xffffu);
+    slot[3] = (int)(w.w >> 16);
 }
 
-// STAGE: the row-staged variant.  Every thread first issues asynchronous
-// copies of its tets' rows and corner ids into shared memory -- before the
-// grid-dependency wait, since they are constant -- and of the chunk's node
-// words after it; one wait then covers all of them, instead of one global
-// round trip per tet inside the loop.
-template <int MATERIAL, int THREADS, bool INC, bool STAGE>
-__global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevState st) {
-    extern __shared__ float4 smem4[];
-    const int CN = m.chunk_nodes, CT = m.chunk_tets;
-    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;  // s_ub only with INC
-    float *s_x = reinterpret_cast<float *>(smem4 + (INC ? 3 : 2) * CN);
-    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
-    float4 *s_r0 = reinterpret_cast<float4 *>(s_z + 4 * CT), *s_r1 = s_r0 + CT, *s_r2 = s_r1 + CT;  // STAGE only
-    ushort4 *s_lc = reinterpret_cast<ushort4 *>(s_r2 + CT), *s_sl = s_lc + CT;
-    __shared__ double sh[THREADS / 32];
-    __shared__ int is_last;
-    const int c = blockIdx.x;
-    // the chunk table and the per-tet rows are constant: read them before
-    // waiting for the node kernel
-    const int4 cd = m.chunk[c];
-    const int inst = m.chunk_inst[c];
-    const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
-    if (STAGE) {
-        for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
-            const int q = tq0 + lt;
-            cp_async16(s_r0 + lt, m.qrow0 + q);
-            cp_async16(s_r1 + lt, m.qrow1 + q);
-            cp_async16(s_r2 + lt, m.qrow2 + q);
-            cp_async8(s_lc + lt, m.qloc + q);
-            cp_async8(s_sl + lt, m.qslot + q);
-        }
-        cp_async_commit();
-    }
-    pdl_launch_dependents();
-    pdl_wait();
-    InstCtl *cp = st.ctl + inst;
-    if (cp->done) {
-        if (STAGE) cp_async_wait_all();
-        return;
-    }
-    const int k = cp->k;
-    const bool check = (k % p.ls_every) == 0 || cp->force_check;
-    const bool do_h = (k % p.hd_every) == 0;
-    const size_t cur = (size_t)cp->par * m.Np;
-    for (int j = threadIdx.x; j < nl; j += THREADS) {
-        const int g = m.lnode[l0 + j];
-        if (STAGE) {
-            cp_async16(s_uh + j, st.uh + cur + g);
-            cp_async16(s_ul + j, st.ul + cur + g);
-            if (INC) cp_async16(s_ub + j, st.ub + g);
-        } else {
-            s_uh[j] = st.uh[cur + g];
-            s_ul[j] = st.ul[cur + g];
-            if (INC) s_ub[j] = st.ub[g];
-        }
-    }
-    if (STAGE) cp_async_wait_all();
-    __syncthreads();
+// One chunk as its tet loop reads it: node words staged in shared memory;
+// per-tet rows and corner records in shared memory or at the chunk's place in
+// the pass arrays.
+struct ChunkView {
+    const float4 *uh, *ul, *ub;
+    const float4 *r0, *r1, *r2;
+    const uint4 *cor;
+};
+
+// Corner forces of the chunk's tets into the slots; on line-search passes
+// returns the thread's sum of clamped tet energies.
+template <int MATERIAL, int THREADS, bool INC>
+__device__ __forceinline__ double chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check, float *sx,
+                                               float *sy, float *sz) {
     double e = 0.0;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
-        const int q = tq0 + lt;
-        const float4 r0 = STAGE ? s_r0[lt] : m.qrow0[q], r1 = STAGE ? s_r1[lt] : m.qrow1[q],
-                     r2 = STAGE ? s_r2[lt] : m.qrow2[q];
-        const ushort4 lc = STAGE ? s_lc[lt] : m.qloc[q], sl = STAGE ? s_sl[lt] : m.qslot[q];
+        const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
+        int lc[4], sl[4];
+        unpack_cor(v.cor[lt], lc, sl);
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         Kin<float> kin;
         float f[12];
-        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        pass_forces_c<MATERIAL, INC>(s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
-                                     s_ul[lc.z], s_ul[lc.w], INC ? s_ub[lc.x] : z4, INC ? s_ub[lc.y] : z4,
-                                     INC ? s_ub[lc.z] : z4, INC ? s_ub[lc.w] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
-        const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+        pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
+                                     INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
+                                     INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
+                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
-            s_x[slot[cc]] = f[3 * cc];
-            s_y[slot[cc]] = f[3 * cc + 1];
-            s_z[slot[cc]] = f[3 * cc + 2];
+            sx[sl[cc]] = f[3 * cc];
+            sy[sl[cc]] = f[3 * cc + 1];
+            sz[sl[cc]] = f[3 * cc + 2];
         }
         if (check)
             e += (double)search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
                                        p.control == PBS_CONTROL_RESTART);
     }
-    __syncthreads();
-    chunk_partials<THREADS>(m, l0, nl, nt, s_x, s_y, s_z, st.part);
-    if (do_h) {  // Jacobi-diagonal refresh: the same slots carry the 12 diagonal terms
-        __syncthreads();
-        for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
-            const int q = tq0 + lt;
-            const float4 r0 = STAGE ? s_r0[lt] : m.qrow0[q], r1 = STAGE ? s_r1[lt] : m.qrow1[q],
-                         r2 = STAGE ? s_r2[lt] : m.qrow2[q];
-            const ushort4 lc = STAGE ? s_lc[lt] : m.qloc[q], sl = STAGE ? s_sl[lt] : m.qslot[q];
-            const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-            Kin<float> kin;
-            float f[12], kd[12];
-            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-            pass_forces_c<MATERIAL, INC>(s_uh[lc.x], s_uh[lc.y], s_uh[lc.z], s_uh[lc.w], s_ul[lc.x], s_ul[lc.y],
-                                         s_ul[lc.z], s_ul[lc.w], INC ? s_ub[lc.x] : z4, INC ? s_ub[lc.y] : z4,
-                                         INC ? s_ub[lc.z] : z4, INC ? s_ub[lc.w] : z4, dinv, r0.w, r1.w, r2.w, kin,
-                                         f);
-            hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
-            const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
+    return e;
+}
+
+// Jacobi-diagonal refresh: the same slots carry the 12 diagonal terms.
+template <int MATERIAL, int THREADS, bool INC>
+__device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float *sx, float *sy, float *sz) {
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
+        const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
+        int lc[4], sl[4];
+        unpack_cor(v.cor[lt], lc, sl);
+        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+        Kin<float> kin;
+        float f[12], kd[12];
+        pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
+                                     INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
+                                     INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
+                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
+        hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                s_x[slot[cc]] = kd[3 * cc];
-                s_y[slot[cc]] = kd[3 * cc + 1];
-                s_z[slot[cc]] = kd[3 * cc + 2];
-            }
+        for (int cc = 0; cc < 4; ++cc) {
+            sx[sl[cc]] = kd[3 * cc];
+            sy[sl[cc]] = kd[3 * cc + 1];
+            sz[sl[cc]] = kd[3 * cc + 2];
         }
-        __syncthreads();
-        chunk_partials<THREADS>(m, l0, nl, nt, s_x, s_y, s_z, st.parth);
     }
-    if (!check) return;
-    // line-search pass: add this chunk's share of the instance's node terms
+}
+
+// Sums every local node's slots (in slot order) into its partial for this
+// chunk.  meta: the chunk's local-node records (shared or global memory).
+template <int THREADS>
+__device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const float *sx, const float *sy,
+                                               const float *sz, float4 *out) {
+    for (int j = threadIdx.x; j < nl; j += THREADS) {
+        const int4 md = meta[j];
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int s = md.y; s < md.z; ++s) {
+            fx += sx[s];
+            fy += sy[s];
+            fz += sz[s];
+        }
+        out[md.w] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+// Line-search pass: adds the chunk's share of the instance's node energy terms
+// to the thread's tet energies e, stores the chunk's {sum e, sum e^2}, and in
+// the instance's last chunk to finish sums the chunks in order and decides
+// accept / reject (DescentOptimize.cpp:162-183).  Called by every thread of
+// the CTA; *is_last is a shared word.
+template <int THREADS>
+__device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevParams &p, const DevState &st, int c,
+                                                  InstCtl *cp, int k, size_t cur, double e, double *sh,
+                                                  int *is_last) {
     double e2 = e * e;
     {
         const int nb = cp->cblk_end - cp->cblk_begin;
@@ -322,10 +299,10 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
         st.cpart[c] = make_double2(se, se2);
         __threadfence();
         const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
-        is_last = (prev == (unsigned int)(cp->cblk_end - cp->cblk_begin - 1));
+        *is_last = (prev == (unsigned int)(cp->cblk_end - cp->cblk_begin - 1));
     }
     __syncthreads();
-    if (!is_last) return;
+    if (!*is_last) return;
     __threadfence();
     // the instance's last chunk: fixed-order sums, then accept / reject
     double E = 0.0, E2 = 0.0;
@@ -369,9 +346,344 @@ __global__ void __launch_bounds__(THREADS) k_tchunk(DevMesh m, DevParams p, DevS
     if (ci.done) atomicSub(st.active, 1);
 }
 
+// The whole of one chunk once its node words (and, with STAGE, its rows and
+// records) are in shared memory: forces, partials, the Jacobi diagonal every
+// hd_every passes, and the line-search tail.
+template <int MATERIAL, int THREADS, bool INC>
+__device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p, const DevState &st, int c,
+                                           InstCtl *cp, int k, bool check, bool do_h, size_t cur, const ChunkView &v,
+                                           const int4 *meta, int nt, int nl, float *sx, float *sy, float *sz,
+                                           double *sh, int *is_last) {
+    const double e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sx, sy, sz);
+    __syncthreads();
+    chunk_partials<THREADS>(meta, nl, sx, sy, sz, st.part);
+    if (do_h) {
+        __syncthreads();
+        chunk_hdiag<MATERIAL, THREADS, INC>(v, nt, sx, sy, sz);
+        __syncthreads();
+        chunk_partials<THREADS>(meta, nl, sx, sy, sz, st.parth);
+    }
+    if (check) chunk_line_search<THREADS>(m, p, st, c, cp, k, cur, e, sh, is_last);
+}
+
+// One CTA per chunk.  STAGE: every thread first issues asynchronous copies of
+// its tets' rows and corner records and of the chunk's local-node records into
+// shared memory -- before the grid-dependency wait, since they are constant --
+// and of the chunk's node words after it; one wait then covers all of them,
+// instead of one global round trip per tet inside the loop.
+// Register budget of the incremental variants: 85 a thread (768 threads a SM).
+template <int MATERIAL, int THREADS, bool INC, bool STAGE>
+__global__ void __launch_bounds__(THREADS, INC ? 768 / THREADS : 0)
+    k_tchunk(DevMesh m, DevParams p, DevState st, int par) {
+    extern __shared__ float4 smem4[];
+    const int CN = m.chunk_nodes, CT = m.chunk_tets;
+    // node words: u hi, u lo (without INC) or the increment (with INC), base
+    // (INC only); corner slots; with STAGE the rows and records
+    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;
+    float *s_x = reinterpret_cast<float *>(smem4 + (INC ? 3 : 2) * CN);
+    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
+    float4 *s_r0 = reinterpret_cast<float4 *>(s_z + 4 * CT), *s_r1 = s_r0 + CT, *s_r2 = s_r1 + CT;  // STAGE only
+    uint4 *s_cor = reinterpret_cast<uint4 *>(s_r2 + CT);
+    int4 *s_meta = reinterpret_cast<int4 *>(s_cor + CT);
+    __shared__ double sh[THREADS / 32];
+    __shared__ int is_last;
+    const int c = blockIdx.x;
+    // the chunk table and the per-tet rows are constant: read them before
+    // waiting for the node kernel
+    const int4 cd = m.chunk[c];
+    const int inst = m.chunk_inst[c];
+    const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
+    if (STAGE) {
+        for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
+            const int q = tq0 + lt;
+            cp_async16(s_r0 + lt, m.qrow0 + q);
+            cp_async16(s_r1 + lt, m.qrow1 + q);
+            cp_async16(s_r2 + lt, m.qrow2 + q);
+            cp_async16(s_cor + lt, m.qcor + q);
+        }
+        for (int j = threadIdx.x; j < nl; j += THREADS) cp_async16(s_meta + j, m.lmeta + l0 + j);
+        cp_async_commit();
+    }
+    const size_t cur = (size_t)par * m.Np;
+    pdl_launch_dependents();
+    pdl_wait();
+    InstCtl *cp = st.ctl + inst;
+    const int4 *meta = STAGE ? s_meta : m.lmeta + l0;
+    if (STAGE) {
+        // each thread stages the node words of the records it copied itself;
+        // the gathers need no control word (the pass's parity is known at
+        // launch) and run while it is read
+        cp_async_wait_all();
+        for (int j = threadIdx.x; j < nl; j += THREADS) {
+            const int g = s_meta[j].x;
+            cp_async16(s_uh + j, st.uh + cur + g);
+            cp_async16(s_ul + j, st.ul + cur + g);
+            if (INC) cp_async16(s_ub + j, st.ub + g);
+        }
+        cp_async_commit();
+    }
+    if (cp->done) {
+        if (STAGE) cp_async_wait_all();
+        return;
+    }
+    const int k = cp->k;
+    const bool check = (k % p.ls_every) == 0 || cp->force_check;
+    const bool do_h = (k % p.hd_every) == 0;
+    if (STAGE) {
+        cp_async_wait_all();
+        if (INC)  // the increments of the nodes this thread staged
+            for (int j = threadIdx.x; j < nl; j += THREADS) s_ul[j] = node_increment(s_uh[j], s_ul[j], s_ub[j]);
+    } else {
+        for (int j = threadIdx.x; j < nl; j += THREADS) {
+            const int g = meta[j].x;
+            const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
+            if (INC) {
+                const float4 ub = st.ub[g];
+                s_ul[j] = node_increment(uh, ul, ub);
+                s_ub[j] = ub;
+            } else {
+                s_uh[j] = uh;
+                s_ul[j] = ul;
+            }
+        }
+    }
+    __syncthreads();
+    ChunkView v;
+    v.uh = s_uh;
+    v.ul = s_ul;
+    v.ub = s_ub;
+    v.r0 = STAGE ? s_r0 : m.qrow0 + tq0;
+    v.r1 = STAGE ? s_r1 : m.qrow1 + tq0;
+    v.r2 = STAGE ? s_r2 : m.qrow2 + tq0;
+    v.cor = STAGE ? s_cor : m.qcor + tq0;
+    chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cp, k, check, do_h, cur, v, meta, nt, nl, s_x, s_y, s_z, sh,
+                                       &is_last);
+}
+
+// ------------------------------------------------------------ persistent, TMA-fed variant
+// mbarrier and bulk-copy (TMA) primitives.  A bulk copy moves a contiguous
+// global range into shared memory and reports its bytes to an mbarrier; the
+// phase completes when the expected byte count has arrived.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for phase `parity` of *bar for at most limit_ns; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, unsigned long long limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+// A wait on a bulk copy that has not completed in a second means the copy
+// engine or the pipeline bookkeeping is broken: the kernel records
+// PBS_E_DEVICE_TIMEOUT in the instance and returns instead of spinning on.
+constexpr unsigned long long STREAM_WAIT_NS = 1000000000ull;
+
+// One staging buffer of the persistent kernel.
+struct StageBuf {
+    float4 *r0, *r1, *r2;
+    uint4 *cor;
+    int4 *meta;
+    float4 *uh, *ul, *ub;
+};
+
+// Buffer b of the persistent kernel's shared memory: [buffer 0][buffer 1]
+// [slots]; a buffer holds rows 0..2 and corner records (16 B a tet each),
+// then local-node records and node words (16 B a node each).
+__device__ __forceinline__ StageBuf stage_buf(float4 *smem4, int b, int CT, int CN, int stride) {
+    float4 *q = smem4 + b * stride;
+    StageBuf s;
+    s.r0 = q;
+    s.r1 = q + CT;
+    s.r2 = q + 2 * CT;
+    s.cor = reinterpret_cast<uint4 *>(q + 3 * CT);
+    s.meta = reinterpret_cast<int4 *>(q + 4 * CT);
+    s.uh = q + 4 * CT + CN;
+    s.ul = q + 4 * CT + 2 * CN;
+    s.ub = q + 4 * CT + 3 * CN;  // with incremental stress only
+    return s;
+}
+
+// Thread 0: the chunk's rows, corner records and local-node records by bulk
+// copies, completing on *bar.
+__device__ __forceinline__ void stage_chunk_bulk(const DevMesh &m, int c, const StageBuf &b, uint64_t *bar) {
+    const int4 cd = m.chunk[c];
+    const unsigned nt = (unsigned)cd.y, nl = (unsigned)cd.w;
+    mbar_expect_tx(bar, 64u * nt + 16u * nl);
+    if (nt) {
+        bulk_g2s(b.r0, m.qrow0 + cd.x, 16u * nt, bar);
+        bulk_g2s(b.r1, m.qrow1 + cd.x, 16u * nt, bar);
+        bulk_g2s(b.r2, m.qrow2 + cd.x, 16u * nt, bar);
+        bulk_g2s(b.cor, m.qcor + cd.x, 16u * nt, bar);
+    }
+    if (nl) bulk_g2s(b.meta, m.lmeta + cd.z, 16u * nl, bar);
+}
+
+// What a chunk's pass needs from its instance's control block.
+struct StreamCtx {
+    InstCtl *cp;
+    int k, nt, nl;
+    bool skip, check, do_h;
+    size_t cur;
+};
+
+__device__ __forceinline__ StreamCtx stream_ctx(const DevMesh &m, const DevParams &p, const DevState &st, int c,
+                                                size_t cur) {
+    StreamCtx x;
+    const int4 cd = m.chunk[c];
+    x.nt = cd.y;
+    x.nl = cd.w;
+    x.cp = st.ctl + m.chunk_inst[c];
+    x.skip = x.cp->done != 0;
+    x.k = x.cp->k;
+    x.check = (x.k % p.ls_every) == 0 || x.cp->force_check;
+    x.do_h = (x.k % p.hd_every) == 0;
+    x.cur = cur;
+    return x;
+}
+
+// Node words of a chunk (local-node records already in b.meta) by cp.async.
+template <int THREADS, bool INC>
+__device__ __forceinline__ void stage_nodes(const DevState &st, const StageBuf &b, int nl, size_t cur) {
+    for (int j = threadIdx.x; j < nl; j += THREADS) {
+        const int g = b.meta[j].x;
+        cp_async16(b.uh + j, st.uh + cur + g);
+        cp_async16(b.ul + j, st.ul + cur + g);
+        if (INC) cp_async16(b.ub + j, st.ub + g);
+    }
+}
+
+// Persistent chunk kernel: CTA b walks chunks b, b + G, b + 2G, ... (G =
+// gridDim.x, a whole number of resident CTAs per SM) through two staging
+// buffers.  While chunk j computes, chunk j+1's node words are in flight by
+// cp.async and chunk j+2's rows and records by bulk copies, so the global
+// round trips of the one-CTA-per-chunk kernel (control block, records, node
+// gather) leave the critical path.  Chunk for chunk, the arithmetic and its
+// order are those of k_tchunk with the same shape: results are bit-identical.
+template <int MATERIAL, int THREADS, bool INC>
+__global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, DevParams p, DevState st, int par) {
+    extern __shared__ float4 smem4[];
+    const int CN = m.chunk_nodes, CT = m.chunk_tets;
+    const int stride = 4 * CT + (INC ? 4 : 3) * CN;  // float4 words of one staging buffer
+    float *s_x = reinterpret_cast<float *>(smem4 + 2 * stride);
+    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ double sh[THREADS / 32];
+    __shared__ int is_last;
+    const int G = gridDim.x, c0 = blockIdx.x;
+    const int nj = c0 < m.n_chunks ? (m.n_chunks - c0 + G - 1) / G : 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    // the first two chunks' rows and records are constant: they go out before
+    // the grid-dependency wait
+    if (threadIdx.x == 0) {
+        if (nj > 0) stage_chunk_bulk(m, c0, stage_buf(smem4, 0, CT, CN, stride), &bar[0]);
+        if (nj > 1) stage_chunk_bulk(m, c0 + G, stage_buf(smem4, 1, CT, CN, stride), &bar[1]);
+    }
+    pdl_launch_dependents();
+    pdl_wait();
+    if (nj == 0) return;
+    StreamCtx cur, nxt;
+    nxt.skip = true;
+    // chunk 0: its records, then its node words
+    bool ok = mbar_wait_bounded(&bar[0], 0u, STREAM_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(&st.ctl[m.chunk_inst[c0]].status, PBS_E_DEVICE_TIMEOUT);
+        if (nj > 1) mbar_wait_bounded(&bar[1], 0u, STREAM_WAIT_NS);
+        return;
+    }
+    const size_t pcur = (size_t)par * m.Np;
+    cur = stream_ctx(m, p, st, c0, pcur);
+    if (!cur.skip) stage_nodes<THREADS, INC>(st, stage_buf(smem4, 0, CT, CN, stride), cur.nl, cur.cur);
+    cp_async_commit();
+    for (int j = 0; j < nj; ++j) {
+        const int b = j & 1, c = c0 + j * G;
+        if (j + 1 < nj) {
+            // chunk j+1: wait for its records, start its node words
+            ok = mbar_wait_bounded(&bar[b ^ 1], (unsigned)((j + 1) >> 1) & 1u, STREAM_WAIT_NS);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicExch(&st.ctl[m.chunk_inst[c + G]].status, PBS_E_DEVICE_TIMEOUT);
+                cp_async_wait_all();
+                mbar_wait_bounded(&bar[b ^ 1], (unsigned)((j + 1) >> 1) & 1u, STREAM_WAIT_NS);
+                return;
+            }
+            nxt = stream_ctx(m, p, st, c + G, pcur);
+            if (!nxt.skip) stage_nodes<THREADS, INC>(st, stage_buf(smem4, b ^ 1, CT, CN, stride), nxt.nl, nxt.cur);
+            cp_async_commit();
+            asm volatile("cp.async.wait_group 1;" ::: "memory");  // chunk j's node words (this thread's)
+        } else {
+            cp_async_wait_all();
+        }
+        const StageBuf sb = stage_buf(smem4, b, CT, CN, stride);
+        if (INC && !cur.skip)  // the increments of the nodes this thread staged
+            for (int i = threadIdx.x; i < cur.nl; i += THREADS) sb.ul[i] = node_increment(sb.uh[i], sb.ul[i], sb.ub[i]);
+        __syncthreads();
+        if (!cur.skip) {
+            ChunkView v;
+            v.uh = sb.uh;
+            v.ul = sb.ul;
+            v.ub = sb.ub;
+            v.r0 = sb.r0;
+            v.r1 = sb.r1;
+            v.r2 = sb.r2;
+            v.cor = sb.cor;
+            chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cur.cp, cur.k, cur.check, cur.do_h, cur.cur, v, sb.meta,
+                                               cur.nt, cur.nl, s_x, s_y, s_z, sh, &is_last);
+        }
+        __syncthreads();  // buffer b and the slots are free again
+        if (threadIdx.x == 0 && j + 2 < nj) stage_chunk_bulk(m, c + 2 * G, sb, &bar[b]);
+        cur = nxt;
+    }
+}
+
 // ------------------------------------------------------------ launchers
 template <int MATERIAL, int THREADS, bool INC, bool STAGE> static cudaError_t allow_smem() {
     return cudaFuncSetAttribute(k_tchunk<MATERIAL, THREADS, INC, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                CHUNK_MAX_SMEM);
+}
+
+template <int MATERIAL, int THREADS, bool INC> static cudaError_t allow_smem_stream() {
+    return cudaFuncSetAttribute(k_tstream<MATERIAL, THREADS, INC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 CHUNK_MAX_SMEM);
 }
 
@@ -390,7 +702,11 @@ cudaError_t prepare_chunk_kernels() {
                              allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(),
                              allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(),
                              allow_smem<PBS_MATERIAL_NEOHOOKEAN, 128, true, true>(),
-                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>()};
+                             allow_smem<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>(),
+                             allow_smem_stream<PBS_MATERIAL_NEOHOOKEAN, 128, false>(),
+                             allow_smem_stream<PBS_MATERIAL_NEOHOOKEAN, 256, false>(),
+                             allow_smem_stream<PBS_MATERIAL_NEOHOOKEAN, 128, true>(),
+                             allow_smem_stream<PBS_MATERIAL_NEOHOOKEAN, 256, true>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -403,41 +719,93 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
-template <int MATERIAL, int THREADS, bool INC, bool STAGE>
-static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
+static cudaLaunchConfig_t chunk_config(cudaStream_t s, int grid, int threads, size_t smem, bool pdl,
+                                       cudaLaunchAttribute *at) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(m.n_chunks);
-    cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes, INC, STAGE);
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC, STAGE>, m, p, st);
+    return cfg;
+}
+
+template <int MATERIAL, int THREADS, bool INC, bool STAGE>
+static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, int par,
+                                   bool pdl) {
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg = chunk_config(s, m.n_chunks, THREADS,
+                                          chunk_smem(m.chunk_tets, m.chunk_nodes, INC, STAGE ? 1 : 0), pdl, at);
+    return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC, STAGE>, m, p, st, par);
+}
+
+template <int MATERIAL, int THREADS, bool INC>
+static cudaError_t launch_tstream_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, int par,
+                                    bool pdl) {
+    if (m.stream_grid <= 0) return cudaErrorInvalidConfiguration;
+    cudaLaunchAttribute at[1];
+    cudaLaunchConfig_t cfg =
+        chunk_config(s, m.stream_grid, THREADS, chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 2), pdl, at);
+    return cudaLaunchKernelEx(&cfg, k_tstream<MATERIAL, THREADS, INC>, m, p, st, par);
 }
 
 template <int MATERIAL, bool INC>
-static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, bool pdl) {
-    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128, INC, false>(s, m, p, st, pdl);
-    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512, INC, false>(s, m, p, st, pdl);
-    return launch_tchunk_t<MATERIAL, 256, INC, false>(s, m, p, st, pdl);
+static cudaError_t launch_tchunk(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, int par,
+                                 bool pdl) {
+    if (m.chunk_threads == 128) return launch_tchunk_t<MATERIAL, 128, INC, false>(s, m, p, st, par, pdl);
+    if (m.chunk_threads == 512) return launch_tchunk_t<MATERIAL, 512, INC, false>(s, m, p, st, par, pdl);
+    return launch_tchunk_t<MATERIAL, 256, INC, false>(s, m, p, st, par, pdl);
 }
 
-cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, bool pdl) {
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par,
+                            bool pdl) {
     if (m.n_chunks <= 0) return cudaSuccess;
-    if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH, false>(s, m, p, st, pdl);
-    // row-staged shapes: neo-Hookean, 128 or 256 threads
-    const bool st128 = m.chunk_stage && m.chunk_threads == 128, st256 = m.chunk_stage && m.chunk_threads == 256;
-    if (p.incremental) {
-        if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, true, true>(s, m, p, st, pdl);
-        if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>(s, m, p, st, pdl);
-        return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, pdl);
+    if (material == PBS_MATERIAL_STRETCH) return launch_tchunk<PBS_MATERIAL_STRETCH, false>(s, m, p, st, par, pdl);
+    // staged shapes: neo-Hookean, 128 or 256 threads
+    const bool t128 = m.chunk_threads == 128, t256 = m.chunk_threads == 256;
+    if (m.chunk_stage == 2) {
+        if (p.incremental) {
+            if (t128) return launch_tstream_t<PBS_MATERIAL_NEOHOOKEAN, 128, true>(s, m, p, st, par, pdl);
+            if (t256) return launch_tstream_t<PBS_MATERIAL_NEOHOOKEAN, 256, true>(s, m, p, st, par, pdl);
+        } else {
+            if (t128) return launch_tstream_t<PBS_MATERIAL_NEOHOOKEAN, 128, false>(s, m, p, st, par, pdl);
+            if (t256) return launch_tstream_t<PBS_MATERIAL_NEOHOOKEAN, 256, false>(s, m, p, st, par, pdl);
+        }
     }
-    if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(s, m, p, st, pdl);
-    if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(s, m, p, st, pdl);
-    return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, false>(s, m, p, st, pdl);
+    const bool st128 = m.chunk_stage == 1 && t128, st256 = m.chunk_stage == 1 && t256;
+    if (p.incremental) {
+        if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, true, true>(s, m, p, st, par, pdl);
+        if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, true, true>(s, m, p, st, par, pdl);
+        return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, true>(s, m, p, st, par, pdl);
+    }
+    if (st128) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 128, false, true>(s, m, p, st, par, pdl);
+    if (st256) return launch_tchunk_t<PBS_MATERIAL_NEOHOOKEAN, 256, false, true>(s, m, p, st, par, pdl);
+    return launch_tchunk<PBS_MATERIAL_NEOHOOKEAN, false>(s, m, p, st, par, pdl);
+}
+
+// CTAs of the persistent chunk kernel for the mesh's shape: as many as fit on
+// the device at once, at most one per chunk.  0 when the shape has no
+// persistent variant.
+template <int MATERIAL, int THREADS, bool INC> static int stream_fit(const DevMesh &m, int sms) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tstream<MATERIAL, THREADS, INC>, THREADS,
+                                                      chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 2)) != cudaSuccess)
+        return 0;
+    return std::min(m.n_chunks, per_sm * sms);
+}
+
+int stream_grid(const DevMesh &m, int material, bool inc, int sms) {
+    if (m.chunk_stage != 2 || material != PBS_MATERIAL_NEOHOOKEAN || m.n_chunks <= 0) return 0;
+    if (m.chunk_threads == 128)
+        return inc ? stream_fit<PBS_MATERIAL_NEOHOOKEAN, 128, true>(m, sms)
+                   : stream_fit<PBS_MATERIAL_NEOHOOKEAN, 128, false>(m, sms);
+    if (m.chunk_threads == 256)
+        return inc ? stream_fit<PBS_MATERIAL_NEOHOOKEAN, 256, true>(m, sms)
+                   : stream_fit<PBS_MATERIAL_NEOHOOKEAN, 256, false>(m, sms);
+    return 0;
 }
 
 }  // namespace pbs

@@ -198,11 +198,12 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-// The state-independent inputs of one node, loaded before the grid-dependency
-// wait.
+// The inputs of one node: the state-independent ones loaded before the
+// grid-dependency wait, the state words right after it.
 struct NodeIn {
     float4 info, th, tl, bh, bl;
     int pa, pe;
+    float4 uh, ul, dd, diag;
 };
 
 // The instance's pass state as the node update needs it.
@@ -219,8 +220,8 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
                                               const NodeIn &in, const float4 &f0, const float4 &f1, const PassCtx &c) {
     double r2 = 0.0;
     if (in.info.z == 2.f) return r2;
-    const size_t cur = c.cur, nxt = c.nxt;
-    const float4 uh = st.uh[cur + i], ul = st.ul[cur + i], dd = st.dd[cur + i];
+    const size_t nxt = c.nxt;
+    const float4 uh = in.uh, ul = in.ul, dd = in.dd;
     float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
     if (c.action == ACT_RESTORE) {
         // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
@@ -265,7 +266,7 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
                 D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
                 st.diag[i] = D;
             } else {
-                D = st.diag[i];
+                D = in.diag;
             }
             // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
             // force (incremental mode) + body_force_scale (external + gravity)
@@ -298,7 +299,7 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
 // One CTA per 256-node block (one instance); NPT nodes per thread, whose
 // loads are all issued before any of them is used.
 template <int NPT>
-__global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, DevState st) {
+__global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, DevState st, int par) {
     constexpr int TH = BLOCK / NPT;
     __shared__ double sh[TH / 32];
     __shared__ int is_last;
@@ -318,13 +319,21 @@ __global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, De
         in[j].pe = m.pptr[i + 1];
     }
     const int inst = m.nblk_inst[b];
+    const size_t cur = (size_t)par * m.Np;
     pdl_launch_dependents();
     pdl_wait();  // the chunk kernel's partials and decisions are visible from here
+    // the state words and the first partials go out together with the
+    // instance's control block: the pass's parity is known at launch
     float4 f0[NPT], f1[NPT];
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
+        const int i = b * BLOCK + threadIdx.x + j * TH;
         f0[j] = in[j].pa < in[j].pe ? st.part[in[j].pa] : z4;
         f1[j] = in[j].pa + 1 < in[j].pe ? st.part[in[j].pa + 1] : z4;
+        in[j].uh = st.uh[cur + i];
+        in[j].ul = st.ul[cur + i];
+        in[j].dd = st.dd[cur + i];
+        in[j].diag = st.diag[i];
     }
     InstCtl *cp = st.ctl + inst;
     if (cp->done) return;
@@ -339,8 +348,8 @@ __global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, De
     ctx.do_h = do_h;
     ctx.alpha = cp->alpha;
     ctx.omega = omega;
-    ctx.cur = (size_t)cp->par * m.Np;
-    ctx.nxt = (size_t)(1 - cp->par) * m.Np;
+    ctx.cur = cur;
+    ctx.nxt = (size_t)(1 - par) * m.Np;
     double r2 = 0.0;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) r2 += node_update(m, p, st, b * BLOCK + threadIdx.x + j * TH, in[j], f0[j], f1[j], ctx);
@@ -613,7 +622,7 @@ cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p
     return cudaGetLastError();
 }
 template <int NPT>
-static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
+static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m.n_nblk);
     cfg.blockDim = dim3(BLOCK / NPT);
@@ -623,16 +632,16 @@ static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevPara
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_node<NPT>, m, p, st);
+    return cudaLaunchKernelEx(&cfg, k_node<NPT>, m, p, st, par);
 }
-cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl) {
-    return m.node_npt == 2 ? launch_node_t<2>(s, m, p, st, pdl) : launch_node_t<1>(s, m, p, st, pdl);
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
+    return m.node_npt == 2 ? launch_node_t<2>(s, m, p, st, par, pdl) : launch_node_t<1>(s, m, p, st, par, pdl);
 }
 // One pass of the step graph: both kernels with programmatic dependent launch.
-cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
-    cudaError_t e = launch_tet_only(s, m, p, st, material, true);
+cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par) {
+    cudaError_t e = launch_tet_only(s, m, p, st, material, par, true);
     if (e != cudaSuccess) return e;
-    return launch_node_only(s, m, p, st, true);
+    return launch_node_only(s, m, p, st, par, true);
 }
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
     if (p.incremental) k_ref_tet<<<nblk(m.Tp, 128), 128, 0, s>>>(m, p, st);

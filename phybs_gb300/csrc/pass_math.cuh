@@ -89,8 +89,9 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 }
 
 // Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
-// INC (compile time): the incremental neo-Hookean form; a0..a3 are unused
-// without it.
+// INC (compile time): the incremental neo-Hookean form, where l carries the
+// corner's increment w = (u hi - base) + u lo (formed once per node) and x is
+// unused; without INC, a is unused.
 template <int MATERIAL, bool INC>
 __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
                                               const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
@@ -99,16 +100,12 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
                                               float f[12]) {
     float P[9];
     if (MATERIAL != PBS_MATERIAL_STRETCH && INC) {
-        disp_gradient<float>(x0, x1, x2, x3, dinv, kin.G);
-        kinematics(kin);
         Kin<float> k0;
         disp_gradient<float>(a0, a1, a2, a3, dinv, k0.G);
         kinematics(k0);
-        // increments from the base: (u_hi - base) + u_lo
         float dG[9];
-        disp_gradient<float>(f4add(f4sub(x0, a0), l0), f4add(f4sub(x1, a1), l1), f4add(f4sub(x2, a2), l2),
-                             f4add(f4sub(x3, a3), l3), dinv, dG);
-        pk1_neohookean_delta<float>(k0, kin, dG, mu, lambda, P);
+        disp_gradient<float>(l0, l1, l2, l3, dinv, dG);
+        pk1_neohookean_inc(k0, dG, mu, lambda, kin, P);
     } else {
         // Du = (u_j,hi - u_0,hi) + (u_j,lo - u_0,lo)
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -119,6 +116,11 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
         else pk1_neohookean<float>(kin, mu, lambda, P);
     }
     corner_forces(P, dinv, svol, f);
+}
+
+// The increment of a node for the incremental form: (u hi - base) + u lo.
+__device__ __forceinline__ float4 node_increment(const float4 &uh, const float4 &ul, const float4 &ub) {
+    return f4add(f4sub(uh, ub), ul);
 }
 
 template <int MATERIAL>
@@ -139,9 +141,15 @@ __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U,
                                             Kin<float> &kin, float f[12]) {
     const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    pass_forces_v<MATERIAL>(p, U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w],
-                            inc ? U0[q.x] : z, inc ? U0[q.y] : z, inc ? U0[q.z] : z, inc ? U0[q.w] : z, dinv, svol,
-                            mu, lambda, kin, f);
+    const float4 x0 = U[q.x], x1 = U[q.y], x2 = U[q.z], x3 = U[q.w];
+    const float4 l0 = UL[q.x], l1 = UL[q.y], l2 = UL[q.z], l3 = UL[q.w];
+    const float4 a0 = inc ? U0[q.x] : z, a1 = inc ? U0[q.y] : z, a2 = inc ? U0[q.z] : z, a3 = inc ? U0[q.w] : z;
+    if (inc)
+        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment(x0, l0, a0), node_increment(x1, l1, a1),
+                                node_increment(x2, l2, a2), node_increment(x3, l3, a3), a0, a1, a2, a3, dinv, svol,
+                                mu, lambda, kin, f);
+    else
+        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
 }
 
 }  // namespace pbs

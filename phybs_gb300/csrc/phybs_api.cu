@@ -58,8 +58,9 @@ struct pbs_handle {
     std::vector<int4> h_tets_pad;
     std::vector<double> h_rest_pad;
     DevBuf<int4> chunk;
-    DevBuf<int> chunk_inst, qperm, lnode, lsptr, lpidx, pptr;
-    DevBuf<ushort4> qloc, qslot;
+    DevBuf<int> chunk_inst, qperm, pptr;
+    DevBuf<uint4> qcor;
+    DevBuf<int4> lmeta;
     DevBuf<float4> qrow0, qrow1, qrow2, part, parth;
     DevBuf<double2> cpart;
     DevBuf<double> rslot;
@@ -94,8 +95,9 @@ struct pbs_handle {
         m.chunk_tets = chunk_tets; m.chunk_nodes = chunk_nodes; m.chunk_threads = chunk_threads;
         m.chunk_stage = chunk_stage;
         m.node_npt = node_npt;
-        m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qloc = qloc.p; m.qslot = qslot.p;
-        m.lnode = lnode.p; m.lsptr = lsptr.p; m.lpidx = lpidx.p; m.pptr = pptr.p;
+        m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qcor = qcor.p; m.lmeta = lmeta.p;
+        m.pptr = pptr.p;
+        m.stream_grid = stream_grid(m, material, dparams.incremental != 0, sms);
         return m;
     }
     DevState state() const {
@@ -119,8 +121,8 @@ struct pbs_handle {
                              &staging_ids};
         for (auto b : ii) b->release();
         ws_theta.release(); ws_stats.release();
-        chunk.release(); qloc.release(); qslot.release(); cpart.release(); rslot.release();
-        DevBuf<int> *ci[] = {&chunk_inst, &qperm, &lnode, &lsptr, &lpidx, &pptr};
+        chunk.release(); qcor.release(); lmeta.release(); cpart.release(); rslot.release();
+        DevBuf<int> *ci[] = {&chunk_inst, &qperm, &pptr};
         for (auto b : ci) b->release();
         DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
         for (auto b : cf) b->release();
@@ -158,23 +160,20 @@ static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, int stage
     ChunkLayout cl;
     build_chunks(h->Np, h->h_tets_pad, h->h_rest_pad, ctl, ct, cn, cl);
     const int nc = (int)cl.chunk.size();
-    const size_t L = cl.lnode.size(), T = (size_t)h->T;
-    h->chunk.release(); h->chunk_inst.release(); h->cpart.release(); h->qperm.release(); h->qloc.release();
-    h->qslot.release(); h->lnode.release(); h->lsptr.release(); h->lpidx.release(); h->pptr.release();
+    const size_t L = cl.lmeta.size(), T = (size_t)h->T;
+    h->chunk.release(); h->chunk_inst.release(); h->cpart.release(); h->qperm.release(); h->qcor.release();
+    h->lmeta.release(); h->pptr.release();
     h->part.release(); h->parth.release();
     CK(h->chunk.alloc(nc)); CK(h->chunk_inst.alloc(nc)); CK(h->cpart.alloc(nc));
-    CK(h->qperm.alloc(T)); CK(h->qloc.alloc(T)); CK(h->qslot.alloc(T));
-    CK(h->lnode.alloc(L)); CK(h->lsptr.alloc(L)); CK(h->lpidx.alloc(L)); CK(h->pptr.alloc(h->Np + 1));
+    CK(h->qperm.alloc(T)); CK(h->qcor.alloc(T));
+    CK(h->lmeta.alloc(L)); CK(h->pptr.alloc(h->Np + 1));
     CK(h->part.alloc(L)); CK(h->parth.alloc(L));
     cudaStream_t s = h->stream;
     CK(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->chunk_inst.p, cl.chunk_inst.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->qperm.p, cl.qperm.data(), sizeof(int) * T, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->qloc.p, cl.qloc.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->qslot.p, cl.qslot.data(), sizeof(ushort4) * T, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->lnode.p, cl.lnode.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->lsptr.p, cl.lsptr.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->lpidx.p, cl.lpidx.data(), sizeof(int) * L, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->qcor.p, cl.qcor.data(), sizeof(uint4) * T, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->lmeta.p, cl.lmeta.data(), sizeof(int4) * L, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->pptr.p, cl.pptr.data(), sizeof(int) * (h->Np + 1), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(h->part.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
     CK(cudaMemsetAsync(h->parth.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
@@ -249,6 +248,7 @@ const char *pbs_error_string(int code) {
         case PBS_E_NO_DEVICE: return "no compute capability 10.3 CUDA device";
         case PBS_E_OUT_OF_MEMORY: return "out of device memory";
         case PBS_E_CAPACITY: return "size beyond the fixed maximum";
+        case PBS_E_DEVICE_TIMEOUT: return "a kernel's bounded wait on its own copies ran out";
         default: return "unknown error";
     }
 }
@@ -542,11 +542,12 @@ static int ensure_graph(pbs_handle *h) {
     if (h->graph_valid) return PBS_OK;
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     DevMesh m = h->mesh();
     DevState st = h->state();
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < CHUNK_PASSES && e == cudaSuccess; ++i) e = launch_pass(h->stream, m, h->dparams, st, h->material);
+    for (int i = 0; i < CHUNK_PASSES && e == cudaSuccess; ++i)
+        e = launch_pass(h->stream, m, h->dparams, st, h->material, i & 1);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return PBS_E_CUDA; }
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -776,9 +777,9 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
     for (int i = 0; i < passes && e == cudaSuccess; ++i) {
-        e = launch_tet_only(s, m, p, st, h->material);
+        e = launch_tet_only(s, m, p, st, h->material, i & 1);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 1], s);
-        if (e == cudaSuccess) e = launch_node_only(s, m, p, st);
+        if (e == cudaSuccess) e = launch_node_only(s, m, p, st, i & 1);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 2], s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -823,9 +824,9 @@ int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_
 int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged, int node_npt) {
     if (!h || (threads != 128 && threads != 256 && threads != 512) || chunk_tets < 1 || chunk_nodes < 4 ||
         (node_npt != 1 && node_npt != 2) ||
-        4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 || (staged != 0 && staged != 1) ||
+        4 * (size_t)chunk_tets > 65536 || chunk_nodes > 65536 || staged < 0 || staged > 2 ||
         (staged && threads == 512) ||
-        chunk_smem(chunk_tets, chunk_nodes, true, staged != 0) > (size_t)CHUNK_MAX_SMEM)
+        chunk_smem(chunk_tets, chunk_nodes, true, staged) > (size_t)CHUNK_MAX_SMEM)
         return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
     h->node_npt = node_npt;
@@ -835,12 +836,15 @@ int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_no
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
     if (!h || passes <= 0) return PBS_E_INVALID_ARG;
     CK(cudaSetDevice(h->device));
-    // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch, rows
-    // staged in shared memory (neo-Hookean only)
+    // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch,
+    // staging (neo-Hookean only: 1 = rows staged in shared memory, 2 = the
+    // persistent double-buffered kernel)
     static const int shapes[][4] = {{256, 1024, 448, 0}, {256, 768, 352, 0}, {256, 512, 256, 0},
                                     {128, 512, 256, 0},  {128, 256, 160, 0}, {512, 1024, 448, 0},
                                     {512, 2048, 832, 0}, {256, 640, 320, 0}, {256, 512, 256, 1},
-                                    {256, 384, 208, 1},  {128, 256, 160, 1}, {128, 384, 208, 1}};
+                                    {256, 384, 208, 1},  {128, 256, 160, 1}, {128, 384, 208, 1},
+                                    {256, 256, 160, 2},  {128, 256, 160, 2}, {256, 512, 256, 2},
+                                    {128, 128, 96, 2}};
     const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
     const bool can_stage = h->material == PBS_MATERIAL_NEOHOOKEAN;
     const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes, s0 = h->chunk_stage;

@@ -28,12 +28,13 @@
 // touching at most CHUNK_NODES nodes):
 //   chunk       int4[n_chunks]     {first pass tet, tet count, first local entry, local count}
 //   qrow0..2    float4[T] each     row0..2 of the pass tets, in pass (chunk) order
-//   qloc        ushort4[T]         corner -> local node of the tet's chunk
-//   qslot       ushort4[T]         corner -> shared-memory slot: a local node's slots
-//                                  are contiguous, in (tet, corner) order
-//   lnode       int[L]             local node -> padded node id (ascending per chunk)
-//   lsptr       int[L]             first slot of the local node (chunk-relative)
-//   lpidx       int[L]             where the chunk's partial sum for that node goes
+//   qcor        uint4[T]           corner ids of a pass tet, two 16-bit fields a word:
+//                                  {loc0 | loc1 << 16, loc2 | loc3 << 16, slot0 | slot1 << 16,
+//                                  slot2 | slot3 << 16}; loc = local node of the tet's chunk,
+//                                  slot = its shared-memory slot (a local node's slots are
+//                                  contiguous, in (tet, corner) order)
+//   lmeta       int4[L]            per local node {padded node id (ascending per chunk), first
+//                                  slot, end slot, where the chunk's partial for the node goes}
 //   pptr        int[Np+1]          node i's partials: part[pptr[i] .. pptr[i+1]-1], by chunk
 //   part, parth float4[L]          per (node, chunk) partial force / Jacobi-diagonal sums
 //   cpart       double2[n_chunks]  per chunk {sum e, sum e^2}
@@ -60,13 +61,17 @@ constexpr int CHUNK_TETS = 1024;
 constexpr int CHUNK_NODES = 448;
 constexpr int CHUNK_THREADS = 256;
 constexpr int CHUNK_MAX_SMEM = 200 * 1024;
-// Dynamic shared memory of the per-tet pass kernel: staged node words (u hi,
-// u lo, and the force base with incremental stress), 3 floats per corner slot
-// and, in the row-staged variant, the chunk's per-tet rows and corner ids
-// (64 B per tet).
-__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc, bool stage = false) {
-    return (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets +
-           (stage ? 64 * (size_t)tets : 0);
+// Dynamic shared memory of the per-tet pass kernel for a chunk shape and a
+// staging mode: 0 = node words (u hi, u lo, and the force base with
+// incremental stress, 16 B each) and 3 floats per corner slot; 1 = also the
+// chunk's per-tet rows and corner records (64 B per tet) and local-node
+// records (16 B per node); 2 = the persistent kernel, two buffers of rows,
+// records and node words plus one set of slots.
+__host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc, int stage = 0) {
+    return stage == 2 ? 2 * ((inc ? 4 : 3) * sizeof(float4) * (size_t)nodes + 64 * (size_t)tets) +
+                            3 * sizeof(float) * 4 * (size_t)tets
+                      : (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets +
+                            (stage ? 64 * (size_t)tets + sizeof(int4) * (size_t)nodes : 0);
 }
 
 // Step parameters as the kernels see them (a by-value kernel argument).
@@ -127,8 +132,10 @@ struct DevMesh {
     const int4 *chunk;
     const int *chunk_inst;
     const float4 *qrow0, *qrow1, *qrow2;
-    const ushort4 *qloc, *qslot;
-    const int *lnode, *lsptr, *lpidx, *pptr;
+    const uint4 *qcor;
+    const int4 *lmeta;
+    const int *pptr;
+    int stream_grid;  // CTAs of the persistent chunk kernel (chunk_stage 2)
 };
 
 struct DevState {
@@ -183,8 +190,9 @@ __device__ __forceinline__ int node_ctl_ws(const DevMesh &m, const DevState &st,
 // instances' node / tet ranges, whose cblk ranges are filled in.
 struct ChunkLayout {
     std::vector<int4> chunk;
-    std::vector<int> chunk_inst, qperm, lnode, lsptr, lpidx, pptr;
-    std::vector<ushort4> qloc, qslot;
+    std::vector<int> chunk_inst, qperm, pptr;
+    std::vector<uint4> qcor;
+    std::vector<int4> lmeta;
     int max_local = 0;
 };
 void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<double> &rest, std::vector<InstCtl> &ctl,
@@ -192,6 +200,9 @@ void build_chunks(int Np, const std::vector<int4> &tets, const std::vector<doubl
 cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const float4 *row0, const float4 *row1,
                              const float4 *row2, float4 *q0, float4 *q1, float4 *q2);
 cudaError_t prepare_chunk_kernels();
+// CTAs of the persistent chunk kernel (chunk_stage 2) for this mesh, material
+// and stress mode on a device with `sms` SMs; 0 when it does not apply.
+int stream_grid(const DevMesh &m, int material, bool inc, int sms);
 
 // Launchers (kernels.cu, warmstart.cu)
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
@@ -211,11 +222,15 @@ cudaError_t launch_set_lame(cudaStream_t s, int Tp, const int4 *tets, const floa
 cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, InstCtl *ctl, int *active);
 cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
                             const int *pad2user);
-cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
+// par: the pass's parity, the state buffer (0 or 1) it reads.  A step starts
+// at parity 0 and every pass of a running instance flips it, so pass i of a
+// step (and of the 16-pass step graph) has parity i & 1.
+cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par);
 // pdl: launch with programmatic stream serialization (the step graph's passes)
-cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material,
+cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par,
                             bool pdl = false);
-cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, bool pdl = false);
+cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par,
+                             bool pdl = false);
 // RESTART control: replaces an instance's inertial guess by the step's start
 // positions when the guess inverts a tet (kernels.cu)
 cudaError_t launch_guess_check(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);

@@ -127,45 +127,59 @@ template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T
         }
 }
 
-// dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, where the current state
-// k has G = G0 + dG and k0 is the step's start.  With P = mu F + (lambda ln J -
-// mu) F^-T:
+// dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, from the base kinematics
+// k0 (the step's start, with ln J0) and the increment dG.  With P = mu F +
+// (lambda ln J - mu) F^-T:
 //   dP = mu dG - (lambda ln J - mu) F0^-T dG^T F^-T + lambda (ln J - ln J0) F0^-T
 // (F^-T - F0^-T = -F0^-T dF^T F^-T), ln J - ln J0 = log1p(dJ / J0) and
 //   dJ = cof(F0) : dG + F0 : cof(dG) + det dG
 // -- no term subtracts the two states' O(1) quantities, so dP is accurate to
-// FP32 relative to itself rather than to P.
-template <typename T>
-__device__ __forceinline__ void pk1_neohookean_delta(const Kin<T> &k0, const Kin<T> &k, const T dG[9], T mu, T lambda,
-                                                     T dP[9]) {
-    T F0iT[9], FiT[9], cofdG[9];
-    inv_transpose<T>(k0, F0iT);
-    cofactor3<T>(dG, cofdG);
-    const T J0 = T(1) + k0.d;
-    T dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
+// FP32 relative to itself rather than to P.  The scale factors 1/J0 and 1/J
+// multiply only O(|dG|) terms and use the fast reciprocal (a few ulp).
+// Also returns the current kinematics k: G = G0 + dG, det F - 1 = d0 + dJ and
+// ln J = ln J0 + log1p(dJ / J0).
+__device__ __forceinline__ void pk1_neohookean_inc(const Kin<float> &k0, const float dG[9], float mu, float lambda,
+                                                   Kin<float> &k, float dP[9]) {
+    float F0iT[9], FiT[9], cofdG[9];
+    const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
+    cofactor3<float>(dG, cofdG);
+    float dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const T cof0 = ((i == j) ? T(1) + k0.tr : T(0)) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
-            const T F0 = ((i == j) ? T(1) : T(0)) + k0.G[3 * i + j];
+            const float cof0 = ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
+            const float F0 = ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j];
             dJ += cof0 * dG[3 * i + j] + F0 * cofdG[3 * i + j];
+            F0iT[3 * i + j] = cof0 * rJ0;
         }
-    const T dl = log1p_t<T>(dJ / J0);
-    const T lnJ = k0.lnJ + dl;
-    inv_transpose<T>(k, FiT);  // F^-T of the current state (k)
+    const float dl = log1pf(dJ * rJ0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
+    cofactor3<float>(k.G, k.cofG);
+    k.tr = k.G[0] + k.G[4] + k.G[8];
+    k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
+    k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+    k.d = k0.d + dJ;
+    k.lnJ = k0.lnJ + dl;
+    const float rJ = __fdividef(1.0f, 1.0f + k.d);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            FiT[3 * i + j] = ((i == j ? 1.0f + k.tr : 0.0f) - k.G[3 * j + i] + k.cofG[3 * i + j]) * rJ;
     // M = F0^-T dG^T F^-T
-    T A[9];
+    float A[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) A[3 * i + j] = F0iT[3 * i] * dG[3 * j] + F0iT[3 * i + 1] * dG[3 * j + 1] + F0iT[3 * i + 2] * dG[3 * j + 2];
-    const T c1 = lambda * lnJ - mu, c2 = lambda * dl;
+    const float c1 = lambda * k.lnJ - mu, c2 = lambda * dl;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const T M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
+            const float M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
             dP[3 * i + j] = mu * dG[3 * i + j] - c1 * M + c2 * F0iT[3 * i + j];
         }
 }

@@ -156,7 +156,10 @@ class DescentSolver:
         return {k: getattr(r, k) for k, _ in r._fields_}
 
     def set_chunk_shape(self, threads: int, chunk_tets: int, chunk_nodes: int, staged: int = 0, node_npt: int = 1):
-        """Use launch shapes picked elsewhere (e.g. by autotune on another handle)."""
+        """Use launch shapes picked elsewhere (e.g. by autotune on another handle).
+        staged: 0 = rows read in the tet loop, 1 = rows staged in shared memory,
+        2 = the persistent double-buffered kernel (neo-Hookean, 128 or 256
+        threads)."""
         L.check(L.lib().pbs_set_chunk_shape(self._h, C.c_int(threads), C.c_int(chunk_tets), C.c_int(chunk_nodes),
                                             C.c_int(staged), C.c_int(node_npt)), "pbs_set_chunk_shape")
 

@@ -280,6 +280,46 @@ def test_config1_bar_100_steps_vs_restatement():
     s.close()
 
 
+@pytest.mark.parametrize("material", [L.PBS_MATERIAL_STRETCH, L.PBS_MATERIAL_NEOHOOKEAN])
+def test_ellipsoid_42k_twist_release_vs_restatement(material):
+    """The 42K-tet ellipsoid (20x20x40-cube grid, 5-tet split, interior nodes
+    jittered by +-0.15 cell, E = 1e5, nu = 0.45, lowest 5% of nodes pinned)
+    released from a 90-degree twist about its long axis: h = 1/60, 64
+    iterations per step, stretch-based and neo-Hookean.  Twelve steps compared
+    step by step against the FP32 restatement, each pair starting from the
+    GPU's state, with the tie rule of the bar test."""
+    m = M.ellipsoid_mesh()
+    x = M.twist_positions(m.rest, np.pi / 2, axis=2)
+    mu, lam = O.lame(m.young, m.poisson)
+    s = DescentSolver(m, positions=x, material=material, mu=mu, lam=lam,
+                      params=make_params("cpu_reference", h=1 / 60, max_iters=64))
+    pm = m.pin_mask()
+    r32 = O.rest(m.rest, m.tets, pm, prec=32)
+    p = O.make_params(h=1 / 60, max_iters=64, material=int(material == L.PBS_MATERIAL_STRETCH))
+    diag = bbox_diag(m.rest)
+    v = vo = np.zeros_like(m.rest)
+    flips = []
+    for k in range(12):
+        st = O.StepState(x, v, vo)
+        o = O.step(st, p, m.tets, r32, mu, lam, pm, prec=32)
+        s.step()
+        gs = s.stats()
+        x = s.positions()
+        v, vo = s.velocities()
+        assert np.isfinite(x).all()
+        err = np.abs(x - st.x0).max() / diag
+        if (gs["passes"], gs["rejections"]) == (o.passes, o.rejections):
+            assert err < POS_TOL, (k, err)
+        else:
+            flips.append((k, err))
+            assert err < 1e-3, (k, err, gs, o.passes, o.rejections)
+    assert len(flips) <= 2, flips
+    # the body untwists: the top has turned back from 90 degrees
+    top = m.rest[:, 2] >= m.rest[:, 2].max() - 1e-6
+    assert np.abs(x[top] - M.twist_positions(m.rest, np.pi / 2, axis=2)[top]).max() > 1e-3 * diag
+    s.close()
+
+
 def test_state_roundtrip_and_reset():
     """Positions and velocities read back and written into a fresh handle
     continue the same trajectory (to FP32 rounding: the device carries a
@@ -355,7 +395,7 @@ def test_autotune_keeps_results():
     a = DescentSolver(m, params=p)
     b = DescentSolver(m, params=p)
     r = b.autotune(8)
-    assert r["n_tried"] == 12 and r["chunk_threads"] in (128, 256, 512)
+    assert r["n_tried"] == 16 and r["chunk_threads"] in (128, 256, 512)
     assert 0.0 < r["pass_ms"] <= r["default_pass_ms"]
     for _ in range(3):
         a.step()
@@ -450,6 +490,60 @@ def test_row_staged_chunk_kernel_matches_unstaged(incremental):
     assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-6
     with pytest.raises(L.PhybsError):
         b.set_chunk_shape(512, 512, 256, 1, 1)  # no staged variant with 512 threads
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("incremental", [0, 1])
+@pytest.mark.parametrize("shape", [(256, 256, 160), (128, 128, 96)])
+def test_persistent_chunk_kernel_matches_staged(incremental, shape):
+    """The persistent chunk kernel (each CTA walks a strided list of chunks;
+    rows and records arrive by bulk copies into two staging buffers while the
+    previous chunk computes) is bit-identical to the one-CTA-per-chunk kernel
+    of the same chunk shape.  The 264,000-tet box has more chunks than the
+    device holds CTAs, so every CTA runs the pipeline over several chunks;
+    64 iterations cover line-search checks and Jacobi refreshes."""
+    m = M.box_mesh(30, 40, 44, edge=0.005, seed=6, young=3e5, poisson=0.4)
+    assert m.n_tets == 264000
+    p = make_params("gpu_reference", h=1 / 30, max_iters=64, incremental_stress=incremental)
+    x0 = M.twist_positions(m.rest, 0.6, axis=2)
+    a = DescentSolver(m, positions=x0, params=p)
+    b = DescentSolver(m, positions=x0, params=p)
+    a.set_chunk_shape(*shape, 1, 1)
+    b.set_chunk_shape(*shape, 2, 1)
+    for _ in range(3):
+        a.step()
+        b.step()
+        sa, sb = a.stats(), b.stats()
+        assert (sa["passes"], sa["rejections"], sa["energy"]) == (sb["passes"], sb["rejections"], sb["energy"])
+    assert np.array_equal(a.positions(), b.positions())
+    a.close()
+    b.close()
+
+
+def test_persistent_chunk_kernel_packed_batch():
+    """A packed batch whose instances stop at different passes (residual
+    tolerance, RESTART control with rejections): the persistent kernel skips
+    the chunks of finished instances exactly as the one-CTA-per-chunk kernel
+    does, instance by instance."""
+    packed = M.batch_of_boxes(48, seed=11, nxy=(4, 12), nz=(8, 24))
+    p = make_params("gpu_reference", h=1 / 30, max_iters=3000, tol=1e-3, control=L.PBS_CONTROL_RESTART,
+                    alpha0=0.3, energy_slack=16.0, alpha_grow=1.2, incremental_stress=1)
+    a = DescentSolver(packed, params=p)
+    b = DescentSolver(packed, params=p)
+    a.set_chunk_shape(128, 128, 96, 1, 1)
+    b.set_chunk_shape(128, 128, 96, 2, 1)
+    for _ in range(2):
+        a.step()
+        b.step()
+    passes = set()
+    for i in range(packed.n_instances):
+        sa, sb = a.instance_stats(i), b.instance_stats(i)
+        sa.pop("device_ms"), sb.pop("device_ms")  # wall time, not a result
+        assert sa == sb, i
+        passes.add(sa["passes"])
+    assert len(passes) > 1  # the instances did stop at different passes
+    assert np.array_equal(a.positions(), b.positions())
     a.close()
     b.close()
 
