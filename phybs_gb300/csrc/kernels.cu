@@ -201,9 +201,14 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 // The inputs of one node: the state-independent ones loaded before the
 // grid-dependency wait, the state words right after it.
 struct NodeIn {
-    float4 info, th, tl, bh, bl;
     int pa, pe;
     float4 uh, ul, dd, diag;
+};
+
+// Per-step node constants staged in shared memory before the grid-dependency
+// wait: mass / gravity / state, x~ (hi, lo), b (hi, lo).
+struct NodeConst {
+    float4 info, th, tl, bh, bl;
 };
 
 // The instance's pass state as the node update needs it.
@@ -215,13 +220,14 @@ struct PassCtx {
 };
 
 // Jacobi step with Chebyshev extrapolation (or restore / save) of node i;
-// returns its |g|^2.
-__device__ __forceinline__ double node_update(const DevMesh &m, const DevParams &p, const DevState &st, int i,
-                                              const NodeIn &in, const float4 &f0, const float4 &f1, const PassCtx &c) {
-    double r2 = 0.0;
+// returns its |g|^2 (FP32: three positive squares).
+__device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &p, const DevState &st, int i,
+                                             const NodeConst &in, const NodeIn &nn, const float4 &f0, const float4 &f1,
+                                             const PassCtx &c) {
+    float r2 = 0.f;
     if (in.info.z == 2.f) return r2;
     const size_t nxt = c.nxt;
-    const float4 uh = in.uh, ul = in.ul, dd = in.dd;
+    const float4 uh = nn.uh, ul = nn.ul, dd = nn.dd;
     float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
     if (c.action == ACT_RESTORE) {
         // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
@@ -246,14 +252,14 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
             fx += f1.x;
             fy += f1.y;
             fz += f1.z;
-            for (int j = in.pa + 2; j < in.pe; ++j) {
+            for (int j = nn.pa + 2; j < nn.pe; ++j) {
                 const float4 f = st.part[j];
                 fx += f.x;
                 fy += f.y;
                 fz += f.z;
             }
             if (c.do_h) {
-                for (int j = in.pa; j < in.pe; ++j) {
+                for (int j = nn.pa; j < nn.pe; ++j) {
                     const float4 q = st.parth[j];
                     hx += q.x;
                     hy += q.y;
@@ -266,7 +272,7 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
                 D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
                 st.diag[i] = D;
             } else {
-                D = in.diag;
+                D = nn.diag;
             }
             // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
             // force (incremental mode) + body_force_scale (external + gravity)
@@ -274,7 +280,7 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
             const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
             const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
             const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
-            r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
+            r2 = fmaf(gx, gx, fmaf(gy, gy, gz * gz));
             // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
             // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
             // d' = (omega - 1) d + omega delta
@@ -296,28 +302,53 @@ __device__ __forceinline__ double node_update(const DevMesh &m, const DevParams 
     return r2;
 }
 
-// One CTA per 256-node block (one instance); NPT nodes per thread, whose
-// loads are all issued before any of them is used.
+// Deterministic FP32 block sum (fixed shuffle tree, then warp 0 over the warp
+// totals); result valid in thread 0.
+__device__ __forceinline__ float block_sum_f(float v, float *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    return r;
+}
+
+// One CTA per 256-node block (one instance); NPT nodes per thread.  The
+// per-step constants go to shared memory by cp.async before the
+// grid-dependency wait, so no registers hold them across it.  With two nodes
+// a thread the kernel is held to 85 registers: six 128-thread CTAs fit an SM,
+// and the 1M-tet box's 823 node blocks run as one wave.  |g|^2 is summed in
+// FP32 within the block (256 positive terms: relative error < 1e-6) and in
+// FP64 over the blocks.
 template <int NPT>
-__global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, DevState st, int par) {
+__global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh m, DevParams p, DevState st, int par) {
     constexpr int TH = BLOCK / NPT;
-    __shared__ double sh[TH / 32];
+    __shared__ float sh[TH / 32];
+    __shared__ double shd[TH / 32];
     __shared__ int is_last;
+    __shared__ __align__(16) float4 s_c[5][BLOCK];  // info, th, tl, bh, bl of the block's nodes
     const int b = blockIdx.x;
-    // loads that do not depend on the instance's state go out before it is read
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     NodeIn in[NPT];
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
-        const int i = b * BLOCK + threadIdx.x + j * TH;  // < Np: the grid covers the padded nodes exactly
-        in[j].info = m.info[i];
-        in[j].th = st.th[i];
-        in[j].tl = st.tl[i];
-        in[j].bh = st.bh[i];
-        in[j].bl = st.bl[i];
+        const int l = threadIdx.x + j * TH, i = b * BLOCK + l;  // < Np: the grid covers the padded nodes exactly
+        cp_async16(&s_c[0][l], m.info + i);
+        cp_async16(&s_c[1][l], st.th + i);
+        cp_async16(&s_c[2][l], st.tl + i);
+        cp_async16(&s_c[3][l], st.bh + i);
+        cp_async16(&s_c[4][l], st.bl + i);
         in[j].pa = m.pptr[i];
         in[j].pe = m.pptr[i + 1];
     }
+    cp_async_commit();
     const int inst = m.nblk_inst[b];
     const size_t cur = (size_t)par * m.Np;
     pdl_launch_dependents();
@@ -336,6 +367,7 @@ __global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, De
         in[j].diag = st.diag[i];
     }
     InstCtl *cp = st.ctl + inst;
+    cp_async_wait_all();  // this thread's own constants
     if (cp->done) return;
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
@@ -350,12 +382,21 @@ __global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, De
     ctx.omega = omega;
     ctx.cur = cur;
     ctx.nxt = (size_t)(1 - par) * m.Np;
-    double r2 = 0.0;
+    float r2 = 0.f;
 #pragma unroll
-    for (int j = 0; j < NPT; ++j) r2 += node_update(m, p, st, b * BLOCK + threadIdx.x + j * TH, in[j], f0[j], f1[j], ctx);
-    const double sr = block_sum(r2, sh);
+    for (int j = 0; j < NPT; ++j) {
+        const int l = threadIdx.x + j * TH;
+        NodeConst nc;
+        nc.info = s_c[0][l];
+        nc.th = s_c[1][l];
+        nc.tl = s_c[2][l];
+        nc.bh = s_c[3][l];
+        nc.bl = s_c[4][l];
+        r2 += node_update(m, p, st, b * BLOCK + l, nc, in[j], f0[j], f1[j], ctx);
+    }
+    const float sr = block_sum_f(r2, sh);
     if (threadIdx.x == 0) {
-        st.npart[b] = sr;
+        st.npart[b] = (double)sr;
         __threadfence();
         const unsigned int prev = atomicAdd(&cp->counter_n, 1u);
         is_last = (prev == (unsigned int)(cp->nblk_end - cp->nblk_begin - 1));
@@ -365,7 +406,7 @@ __global__ void __launch_bounds__(BLOCK / NPT) k_node(DevMesh m, DevParams p, De
     __threadfence();
     double R2 = 0.0;
     for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += TH) R2 += __ldcg(st.npart + j);
-    R2 = block_sum(R2, sh);
+    R2 = block_sum(R2, shd);
     if (threadIdx.x != 0) return;
     // updated in place: every other block has read it, and the next kernel
     // reads it only after its grid-dependency wait
