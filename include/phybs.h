@@ -332,6 +332,37 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
 int pbs_stiffness_pattern(int n_nodes, int n_tets, const int *tets, int *nnz, int *row_ptr, int *col,
                           int *diag_idx, int *kid48);
 
+/* ---- Surface picking and drag forces (the viewer's interactive load) ----
+ * The reference's viewer picks a boundary face with a ray and drags it; the
+ * drag becomes the external forces of the next steps (RenderWidget.cpp:154,194
+ * -> TetMesh::pickFacebyRay / dragFaceRing, passed to doDescentOpt by
+ * fvm.cpp:187-188).  These calls compute the same on the device from the
+ * handle's current positions, bit-identical to the reference's FP32. */
+
+/* Boundary triangles (3 * n_faces caller node ids, e.g. a tetgen .face file's,
+ * in the file's orientation) replacing TetMesh::initFacesFromFile
+ * (TetMesh.cpp:130-151).  Builds each face's ring as
+ * TetMesh::computeBoundfaceRingIndices does (TetMesh.cpp:229-277): the face's
+ * three nodes, then every other node that shares a surface edge with one of
+ * them, ascending.  n_faces = 0 clears the surface. */
+int pbs_set_surface(pbs_handle *h, const int *faces, int n_faces);
+/* The ring of one face: its length in *size and up to `capacity` caller node
+ * ids in ring (ring may be NULL to query the length). */
+int pbs_get_face_ring(pbs_handle *h, int face, int *ring, int capacity, int *size);
+/* TetMesh::pickFacebyRay (TetMesh.cpp:395-418) with the normals and centres of
+ * computeBoundfaceNormals (TetMesh.cpp:378-393) at the current positions:
+ * among the faces whose normal (x2 - x0) x (x1 - x0) opposes dir, the first
+ * whose centre lies nearest the ray (orig, dir), within the length of face 0's
+ * first edge; *face = -1 when none does.  orig and dir: 3 floats each. */
+int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face);
+/* TetMesh::dragFaceRing (TetMesh.cpp:446-470): the external forces of a drag
+ * of `face` along drag (3 floats) at the current positions, written to ext
+ * (3 * N floats, caller order; zero off the ring) for the next pbs_step:
+ * factor = min(|drag| / r * 100, 800) with r face 0's first edge, factor * m
+ * * drag / |drag| on the face's nodes and half of it on the rest of the ring
+ * (m: lumped mass, 1e8 for a pinned node). */
+int pbs_drag_face_ring(pbs_handle *h, int face, const float *drag, float *ext);
+
 #ifdef __cplusplus
 }
 #endif

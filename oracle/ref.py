@@ -32,13 +32,16 @@ def lib():
             build(reference=True)
         _lib = C.CDLL(REF_SO)
         _lib.ref_create.restype = C.c_void_p
+        _lib.ref_create_faces.restype = C.c_void_p
         _lib.ref_total_energy.restype = C.c_float
+        _lib.ref_ext_energy.restype = C.c_float
         for name in ["ref_destroy", "ref_set_h", "ref_set_profile", "ref_set_lame", "ref_get_lame", "ref_get_rest",
                      "ref_get_nodes", "ref_set_nodes", "ref_get_vel", "ref_set_vel", "ref_get_vel_old",
                      "ref_set_vel_old", "ref_set_ext", "ref_get_mass", "ref_get_gravity", "ref_get_vol",
                      "ref_get_dminv", "ref_get_an", "ref_force_nh", "ref_force_stretch", "ref_elastic_energy",
                      "ref_hessian_diag", "ref_element_stiffness", "ref_total_energy", "ref_csr_sizes", "ref_csr",
-                     "ref_step", "ref_get_scalars"]:
+                     "ref_step", "ref_get_scalars", "ref_face_ring_size", "ref_face_ring", "ref_pick_face",
+                     "ref_drag_face_ring", "ref_get_ext"]:
             getattr(_lib, name).argtypes = None
     return _lib
 
@@ -54,14 +57,16 @@ def _p(a):
 class RefSim:
     """One reference TetMesh + IsotropicNeohookeanMaterial + DescentOptimize."""
 
-    def __init__(self, rest, tets, pins, young, poisson, density=1000.0):
+    def __init__(self, rest, tets, pins, young, poisson, density=1000.0, faces=None):
         self._tmp = tempfile.TemporaryDirectory(prefix="phybs_ref_")
         rest = _f(rest).reshape(-1, 3)
         tets = np.ascontiguousarray(tets, np.int32).reshape(-1, 4)
         pins = np.ascontiguousarray(pins, np.int32)
-        self.n, self.t = rest.shape[0], tets.shape[0]
-        h = lib().ref_create(self._tmp.name.encode(), C.c_int(self.n), _p(rest), C.c_int(self.t), _p(tets),
-                             C.c_int(pins.size), _p(pins), C.c_float(young), C.c_float(poisson), C.c_float(density))
+        faces = np.zeros((0, 3), np.int32) if faces is None else np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+        self.n, self.t, self.nf = rest.shape[0], tets.shape[0], faces.shape[0]
+        h = lib().ref_create_faces(self._tmp.name.encode(), C.c_int(self.n), _p(rest), C.c_int(self.t), _p(tets),
+                                   C.c_int(pins.size), _p(pins), C.c_float(young), C.c_float(poisson),
+                                   C.c_float(density), C.c_int(self.nf), _p(faces))
         if not h:
             raise RuntimeError("reference harness rejected the mesh")
         self.h = C.c_void_p(h)
@@ -178,6 +183,26 @@ class RefSim:
 
     def step(self, iters):
         lib().ref_step(self.h, C.c_int(iters))
+
+    # -- surface picking and drag (TetMesh.cpp:229-277, 378-418, 446-470, 595-614)
+    def face_ring(self, face):
+        out = np.zeros(lib().ref_face_ring_size(self.h, C.c_int(face)), np.int32)
+        lib().ref_face_ring(self.h, C.c_int(face), _p(out))
+        return out
+
+    def pick_face(self, orig, direction):
+        normals, centers = np.zeros((self.nf, 3), np.float32), np.zeros((self.nf, 3), np.float32)
+        face = lib().ref_pick_face(self.h, _p(_f(orig)), _p(_f(direction)), _p(normals), _p(centers))
+        return face, normals, centers
+
+    def drag_face_ring(self, face, drag):
+        lib().ref_drag_face_ring(self.h, C.c_int(face), _p(_f(drag)))
+
+    def ext(self):
+        return self._get("ref_get_ext", (self.n, 3))
+
+    def ext_energy(self, x):
+        return float(lib().ref_ext_energy(self.h, _p(_f(x).reshape(-1, 3))))
 
     def scalars(self):
         out = np.zeros(5, np.float32)

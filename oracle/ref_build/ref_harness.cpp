@@ -59,9 +59,12 @@ static Eigen::MatrixXf as_pos(const float *p, int n) {
 extern "C" {
 
 // Returns nullptr on failure (unwritable work dir, density other than the
-// loader's 1000, or the loader's own pin rule selecting nodes).
-void *ref_create(const char *workdir, int n_nodes, const float *pos, int n_tets, const int *tets,
-                 int n_pins, const int *pins, float E, float nu, float density) {
+// loader's 1000, or the loader's own pin rule selecting nodes).  faces: the
+// mesh's boundary triangles for TetMesh's .face file (n_faces = 0 writes an
+// empty one); the loader builds their rings (TetMesh.cpp:150).
+void *ref_create_faces(const char *workdir, int n_nodes, const float *pos, int n_tets, const int *tets,
+                       int n_pins, const int *pins, float E, float nu, float density, int n_faces,
+                       const int *faces) {
     if (density != 1000.0f) return nullptr;  // TetMesh.cpp:185 fixes the loader's density
     std::string stem = std::string(workdir) + "/mesh";
     {
@@ -80,7 +83,9 @@ void *ref_create(const char *workdir, int n_nodes, const float *pos, int n_tets,
         std::fclose(f);
         f = std::fopen((stem + ".face").c_str(), "w");
         if (!f) return nullptr;
-        std::fprintf(f, "0  0\n");
+        std::fprintf(f, "%d  0\n", n_faces);
+        for (int i = 0; i < n_faces; ++i)
+            std::fprintf(f, "%d %d %d %d\n", i, faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]);
         std::fclose(f);
     }
     phybs_shim_set_mesh_stem(stem);
@@ -98,6 +103,11 @@ void *ref_create(const char *workdir, int n_nodes, const float *pos, int n_tets,
     s->mat = std::make_shared<IsotropicNeohookeanMaterial>(s->mesh);
     s->opt = std::make_shared<DescentOptimize>(s->mesh, s->mat);
     return s;
+}
+
+void *ref_create(const char *workdir, int n_nodes, const float *pos, int n_tets, const int *tets,
+                 int n_pins, const int *pins, float E, float nu, float density) {
+    return ref_create_faces(workdir, n_nodes, pos, n_tets, tets, n_pins, pins, E, nu, density, 0, nullptr);
 }
 
 void ref_destroy(void *h) { delete static_cast<RefSim *>(h); }
@@ -256,5 +266,32 @@ void ref_get_scalars(void *h, float *out5) {
 }
 
 int ref_num_threads() { return omp_get_max_threads(); }
+
+// Surface picking and drag (TetMesh.cpp:229-277, 378-418, 446-470, 595-614),
+// on the mesh's current nodes (ref_set_nodes).
+int ref_face_ring_size(void *h, int face) { return (int)S(h)->mesh->m_faceRingIndices[face].size(); }
+void ref_face_ring(void *h, int face, int *out) {
+    const auto &r = S(h)->mesh->m_faceRingIndices[face];
+    std::copy(r.begin(), r.end(), out);
+}
+// computeBoundfaceNormals, then pickFacebyRay; normals / centers: 3 x faces
+int ref_pick_face(void *h, const float *orig, const float *dir, float *normals, float *centers) {
+    TetMesh *m = S(h)->mesh.get();
+    m->computeBoundfaceNormals();
+    std::memcpy(normals, m->m_bound_normals.data(), sizeof(float) * m->m_bound_normals.size());
+    std::memcpy(centers, m->m_face_centers.data(), sizeof(float) * m->m_face_centers.size());
+    return m->pickFacebyRay(Eigen::Vector3f(orig[0], orig[1], orig[2]), Eigen::Vector3f(dir[0], dir[1], dir[2]));
+}
+void ref_drag_face_ring(void *h, int face, const float *drag) {
+    S(h)->mesh->dragFaceRing(face, Eigen::Vector3f(drag[0], drag[1], drag[2]));
+}
+void ref_get_ext(void *h, float *out) {
+    auto &m = S(h)->mesh->getExternalForces();
+    std::memcpy(out, m.data(), sizeof(float) * m.size());
+}
+float ref_ext_energy(void *h, const float *pos) {
+    RefSim *s = S(h);
+    return s->mesh->computeExternalForcesEnergy(as_pos(pos, s->mesh->getNodesNum()));
+}
 
 }  // extern "C"

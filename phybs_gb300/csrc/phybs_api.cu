@@ -72,6 +72,14 @@ struct pbs_handle {
     bool guess_pending = false;  // parity 1 holds a caller guess for the next step
     int sms = 148;
     DevBuf<float> tf, hd, staging, staging2;
+    // boundary surface for picking and drag forces: faces and rings in padded
+    // node ids on the device, rings in caller ids on the host
+    int n_faces = 0;
+    std::vector<int> h_ring_ptr, h_ring;
+    DevBuf<int4> faces_pad;
+    DevBuf<int> ring_pad, pick_id;
+    DevBuf<float> pick_d2;
+    DevBuf<float4> drag_ext;
     DevBuf<double2> tpart;
     DevBuf<double> npart;
     DevBuf<InstCtl> ctl;
@@ -127,6 +135,7 @@ struct pbs_handle {
         DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
         for (auto b : cf) b->release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
+        faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         if (h_active) cudaFreeHost(h_active);
         if (h_ctl) cudaFreeHost(h_ctl);
         h_active = nullptr; h_ctl = nullptr;
@@ -958,6 +967,91 @@ int pbs_get_sizes(pbs_handle *h, int *n_nodes, int *n_tets, int *n_instances) {
     if (n_tets) *n_tets = h->T;
     if (n_instances) *n_instances = h->B;
     return PBS_OK;
+}
+
+int pbs_set_surface(pbs_handle *h, const int *faces, int n_faces) {
+    if (!h || n_faces < 0 || (n_faces > 0 && !faces)) return PBS_E_INVALID_ARG;
+    for (size_t i = 0; i < 3 * (size_t)n_faces; ++i)
+        if (faces[i] < 0 || faces[i] >= h->N) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    h->faces_pad.release(); h->ring_pad.release(); h->pick_id.release(); h->pick_d2.release();
+    h->n_faces = 0;
+    h->h_ring_ptr.assign(1, 0);
+    h->h_ring.clear();
+    if (n_faces == 0) return PBS_OK;
+    // TetMesh::computeBoundfaceRingIndices (TetMesh.cpp:229-277): each node's
+    // neighbours through surface edges; a face's ring = its three nodes, then
+    // the union of their neighbours without them, ascending
+    std::vector<std::vector<int>> nbr(h->N);
+    for (int f = 0; f < n_faces; ++f) {
+        const int *q = faces + 3 * (size_t)f;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                if (a != b) nbr[q[a]].push_back(q[b]);
+    }
+    for (auto &v : nbr) {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    std::vector<int4> fpad(n_faces);
+    std::vector<int> tmp;
+    for (int f = 0; f < n_faces; ++f) {
+        const int *q = faces + 3 * (size_t)f;
+        fpad[f] = make_int4(h->user2pad[q[0]], h->user2pad[q[1]], h->user2pad[q[2]], 0);
+        tmp.clear();
+        for (int a = 0; a < 3; ++a) tmp.insert(tmp.end(), nbr[q[a]].begin(), nbr[q[a]].end());
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+        h->h_ring.insert(h->h_ring.end(), q, q + 3);
+        for (int v : tmp)
+            if (v != q[0] && v != q[1] && v != q[2]) h->h_ring.push_back(v);
+        h->h_ring_ptr.push_back((int)h->h_ring.size());
+    }
+    std::vector<int> rpad(h->h_ring.size());
+    for (size_t j = 0; j < rpad.size(); ++j) rpad[j] = h->user2pad[h->h_ring[j]];
+    const int nb = pick_blocks(n_faces, h->sms);
+    CK(h->faces_pad.alloc(n_faces)); CK(h->ring_pad.alloc(rpad.size()));
+    CK(h->pick_id.alloc(nb + 1)); CK(h->pick_d2.alloc(nb));
+    if (!h->drag_ext.p) CK(h->drag_ext.alloc(h->Np));
+    CK(cudaMemcpyAsync(h->faces_pad.p, fpad.data(), sizeof(int4) * n_faces, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->ring_pad.p, rpad.data(), sizeof(int) * rpad.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->n_faces = n_faces;
+    return PBS_OK;
+}
+
+int pbs_get_face_ring(pbs_handle *h, int face, int *ring, int capacity, int *size) {
+    if (!h || !size || face < 0 || face >= h->n_faces || (ring && capacity < 0)) return PBS_E_INVALID_ARG;
+    const int b = h->h_ring_ptr[face], e = h->h_ring_ptr[face + 1];
+    *size = e - b;
+    if (ring)
+        for (int j = 0; j < std::min(e - b, capacity); ++j) ring[j] = h->h_ring[b + j];
+    return PBS_OK;
+}
+
+static bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face) {
+    if (!h || !orig || !dir || !face || h->n_faces == 0 || !finite3(orig) || !finite3(dir)) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    const int nb = pick_blocks(h->n_faces, h->sms);
+    CK(launch_pick_face(h->stream, h->mesh(), h->state(), h->n_faces, h->faces_pad.p,
+                        make_float3(orig[0], orig[1], orig[2]), make_float3(dir[0], dir[1], dir[2]), nb, h->pick_d2.p,
+                        h->pick_id.p, h->pick_id.p + nb));
+    int out = -1;
+    CK(cudaMemcpyAsync(&out, h->pick_id.p + nb, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *face = out;
+    return PBS_OK;
+}
+
+int pbs_drag_face_ring(pbs_handle *h, int face, const float *drag, float *ext) {
+    if (!h || !drag || !ext || face < 0 || face >= h->n_faces || !finite3(drag)) return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    const int b = h->h_ring_ptr[face], len = h->h_ring_ptr[face + 1] - b;
+    CK(launch_drag_ring(h->stream, h->mesh(), h->state(), h->faces_pad.p, h->ring_pad.p, b, len,
+                        make_float3(drag[0], drag[1], drag[2]), h->drag_ext.p));
+    return download_user(h, h->drag_ext.p, ext);
 }
 
 int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {

@@ -256,6 +256,14 @@ struct pbs_handle;
 namespace pbs {
 
 // What an entry point outside the handle's own source file reads of it.
+// Surface picking and drag forces (surface.cu): faces and rings in padded
+// node ids.
+int pick_blocks(int n_faces, int sms);
+cudaError_t launch_pick_face(cudaStream_t s, const DevMesh &m, const DevState &st, int n_faces, const int4 *faces,
+                             float3 orig, float3 dir, int n_blk, float *blk_d2, int *blk_id, int *out);
+cudaError_t launch_drag_ring(cudaStream_t s, const DevMesh &m, const DevState &st, const int4 *faces,
+                             const int *ring, int begin, int len, float3 drag, float4 *ext);
+
 struct HandleView {
     int device;
     cudaStream_t stream;

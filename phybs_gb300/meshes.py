@@ -29,7 +29,7 @@ import os
 import numpy as np
 
 __all__ = [
-    "TetMeshData", "bar_mesh", "box_mesh", "ellipsoid_mesh", "batch_of_boxes",
+    "TetMeshData", "bar_mesh", "box_mesh", "ellipsoid_mesh", "batch_of_boxes", "load_tetgen_faces", "surface_faces",
     "load_tetgen", "write_tetgen_nodes", "orient_positive", "signed_volumes",
     "twist_positions", "incidence_csr",
 ]
@@ -349,6 +349,39 @@ def load_tetgen(stem: str, scale: float = 1.0, young: float = 5e5, poisson: floa
     tets = orient_positive(pos, tets)
     return TetMeshData(pos.astype(np.float32), tets, np.zeros(0, np.int32) if pins is None else pins,
                        young, poisson, name=os.path.basename(stem))
+
+
+def load_tetgen_faces(stem: str) -> np.ndarray:
+    """Boundary triangles of ``<stem>.face`` (tetgen text) as (F, 3) node ids,
+    in the index base of ``<stem>.node`` (the file TetMesh.cpp:130-151 reads)."""
+    head, rows = _read_table(stem + ".node")
+    base = min(int(r[0]) for r in rows[:int(head[0])]) if int(head[0]) else 0
+    head, rows = _read_table(stem + ".face")
+    f = int(head[0])
+    return (np.array([[int(r[1]), int(r[2]), int(r[3])] for r in rows[:f]], np.int64) - base).astype(np.int32)
+
+
+def surface_faces(pos: np.ndarray, tets: np.ndarray) -> np.ndarray:
+    """Boundary triangles of a tet mesh (faces that belong to one tet), in
+    tetgen's orientation: (x1 - x0) x (x2 - x0) points into the mesh, so the
+    picking normal (x2 - x0) x (x1 - x0) points out.  Ordered by tet, then by
+    the corner each face is opposite to."""
+    p = np.asarray(pos, np.float64).reshape(-1, 3)
+    t = np.asarray(tets, np.int64).reshape(-1, 4)
+    tri = np.concatenate([t[:, [1, 2, 3]], t[:, [0, 2, 3]], t[:, [0, 1, 3]], t[:, [0, 1, 2]]], axis=0)
+    opp = np.concatenate([t[:, 0], t[:, 1], t[:, 2], t[:, 3]])
+    order = np.concatenate([np.arange(t.shape[0]) * 4 + k for k in range(4)])
+    key = np.sort(tri, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    inv = inv.reshape(-1)
+    keep = cnt[inv] == 1
+    tri, opp, order = tri[keep], opp[keep], order[keep]
+    tri = tri[np.argsort(order, kind="stable")]
+    opp = opp[np.argsort(order, kind="stable")]
+    n = np.cross(p[tri[:, 1]] - p[tri[:, 0]], p[tri[:, 2]] - p[tri[:, 0]])
+    flip = np.einsum("ij,ij->i", n, p[opp] - p[tri[:, 0]]) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    return tri.astype(np.int32)
 
 
 def write_tetgen_nodes(path: str, pos: np.ndarray) -> None:

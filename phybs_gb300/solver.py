@@ -197,6 +197,34 @@ class DescentSolver:
     def reset(self):
         L.check(L.lib().pbs_reset(self._h), "pbs_reset")
 
+    # -- surface picking and drag forces (TetMesh.cpp:229-277, 378-418, 446-470) --
+    def set_surface(self, faces):
+        """Boundary triangles (F, 3) in caller node ids, e.g. load_tetgen_faces()."""
+        f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        L.check(L.lib().pbs_set_surface(self._h, _ptr(f), C.c_int(f.shape[0])), "pbs_set_surface")
+
+    def face_ring(self, face: int) -> np.ndarray:
+        n = C.c_int()
+        L.check(L.lib().pbs_get_face_ring(self._h, C.c_int(face), None, C.c_int(0), C.byref(n)), "pbs_get_face_ring")
+        out = np.empty(n.value, np.int32)
+        L.check(L.lib().pbs_get_face_ring(self._h, C.c_int(face), _ptr(out), C.c_int(n.value), C.byref(n)),
+                "pbs_get_face_ring")
+        return out
+
+    def pick_face(self, orig, direction) -> int:
+        """The face a ray picks at the current positions (-1: none)."""
+        o, d = _f32(orig, (3,)), _f32(direction, (3,))
+        face = C.c_int()
+        L.check(L.lib().pbs_pick_face(self._h, _ptr(o), _ptr(d), C.byref(face)), "pbs_pick_face")
+        return face.value
+
+    def drag_face_ring(self, face: int, drag) -> np.ndarray:
+        """External forces (N, 3) of dragging `face` along `drag`, for step(ext=...)."""
+        d = _f32(drag, (3,))
+        ext = np.empty((self.n, 3), np.float32)
+        L.check(L.lib().pbs_drag_face_ring(self._h, C.c_int(face), _ptr(d), _ptr(ext)), "pbs_drag_face_ring")
+        return ext
+
     def instance_stats(self, instance: int) -> dict:
         """The last step's figures of one packed instance."""
         s = L.Stats()

@@ -7,8 +7,11 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def golden_names(prefix=""):
+    """Fixture names: the solver fixtures (no prefix), or those starting with
+    `prefix` (e.g. "surface_")."""
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return [n for n in names if n.startswith(prefix)] if prefix else [n for n in names if not n.startswith("surface_")]
 
 
 def load_golden(name):

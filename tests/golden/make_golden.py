@@ -100,7 +100,68 @@ def make(name, cfg, rng):
     print(name, m.n_nodes, m.n_tets, len(m.pins), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def surface_cases():
+    """The reference's shipped meshes with their own .face files."""
+    return {"surface_model_bar": ("model_bar", "bar/bar.1", 0, "min"),
+            "surface_model_dragon": ("model_dragon", "asiandragon/asiandragon.1", 1, "min")}
+
+
+def make_surface(name, spec, rng, n_rays=24, n_drags=12):
+    """Face rings, picks, normals / centres, drag forces and drag energies
+    from TetMesh (TetMesh.cpp:229-277, 378-418, 446-470, 595-614) at the rest
+    shape and at a perturbed shape."""
+    mesh_name, stem, axis, side = spec
+    m = reference_mesh(mesh_name, stem, axis, side)
+    faces = M.load_tetgen_faces(os.path.join(REFERENCE_TREE, "model", stem))
+    sim = REF.RefSim(m.rest, m.tets, m.pins, float(m.young[0]), float(m.poisson[0]), density=m.density, faces=faces)
+    rest = sim.rest()
+    rings = [sim.face_ring(f) for f in range(faces.shape[0])]
+    out = dict(rest=rest, tets=m.tets, pins=m.pins, faces=faces, mass=sim.mass(),
+               ring_ptr=np.cumsum([0] + [len(r) for r in rings]).astype(np.int32),
+               ring=np.concatenate(rings).astype(np.int32))
+    edge = float(np.median(np.linalg.norm(rest[m.tets[:, 1]] - rest[m.tets[:, 0]], axis=1)))
+    states = [rest, (rest + rng.normal(0.0, 0.3 * edge, rest.shape)).astype(np.float32)]
+    states[1][m.pins] = rest[m.pins]
+    for k, x in enumerate(states):
+        sim.set_nodes(x)
+        orig = np.zeros((n_rays, 3), np.float32)
+        dirs = np.zeros((n_rays, 3), np.float32)
+        picks = np.zeros(n_rays, np.int32)
+        extent = float(np.linalg.norm(x.max(0) - x.min(0)))
+        for j in range(n_rays):
+            d = rng.normal(size=3)
+            d = (d / np.linalg.norm(d)).astype(np.float32)
+            dirs[j] = d
+            if j < n_rays - 4:  # aimed at a node
+                target = x[rng.integers(len(x))]
+                orig[j] = (target - 3.0 * edge * d + rng.normal(0.0, 0.2 * edge, 3)).astype(np.float32)
+            else:  # a line far off the mesh: no face is picked
+                side = np.cross(d, [0.0, 0.0, 1.0] if abs(d[2]) < 0.9 else [1.0, 0.0, 0.0])
+                orig[j] = (x.mean(0) + 5.0 * extent * side / np.linalg.norm(side)).astype(np.float32)
+            picks[j], normals, centers = sim.pick_face(orig[j], dirs[j])
+        drag_face = np.array([p if p >= 0 else rng.integers(len(faces)) for p in picks[:n_drags]], np.int32)
+        drags = rng.normal(0.0, 10.0 * edge, (n_drags, 3)).astype(np.float32)
+        ext = np.zeros((n_drags, len(x), 3), np.float32)
+        energy = np.zeros(n_drags, np.float32)
+        for j in range(n_drags):
+            sim.drag_face_ring(int(drag_face[j]), drags[j])
+            ext[j] = sim.ext()
+            energy[j] = sim.ext_energy(x)
+        out.update({f"x{k}": x, f"ray_orig{k}": orig, f"ray_dir{k}": dirs, f"pick{k}": picks,
+                    f"normals{k}": normals, f"centers{k}": centers, f"drag_face{k}": drag_face,
+                    f"drag{k}": drags, f"drag_ext{k}": ext, f"drag_energy{k}": energy})
+    sim.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, len(rest), len(faces), os.path.getsize(os.path.join(HERE, name + ".npz")))
+
+
 if __name__ == "__main__":
+    # `make_golden.py surface` writes only the surface fixtures
+    only_surface = sys.argv[1:] == ["surface"]
     rng = np.random.default_rng(20261203)
-    for n, c in cases().items():
-        make(n, c, rng)
+    if not only_surface:
+        for n, c in cases().items():
+            make(n, c, rng)
+    srng = np.random.default_rng(20261204)
+    for n, spec in surface_cases().items():
+        make_surface(n, spec, srng)
