@@ -332,6 +332,25 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
 int pbs_stiffness_pattern(int n_nodes, int n_tets, const int *tets, int *nnz, int *row_ptr, int *col,
                           int *diag_idx, int *kid48);
 
+/* ---- Linearly implicit (backward) Euler step ----
+ * The reference's second GPU integrator, CUDAInterface::computeInnerforces +
+ * computeGlobalStiffnessMatrix + doBackEuler (CUDAInterface.cu:784-884, driven
+ * by fvm.cpp:179-183):
+ *   (M (1 + alpha dt) + dt (dt + beta) K(x)) v' = M v + dt f(x),  x' = x + dt v'
+ * f = elastic + gravity (+ ext, 3*N floats or NULL); a pinned node's force is
+ * the spring 1e8 (X - x) and its mass 1e8; K = -df/dx (the neo-Hookean
+ * Hessian, which the stretch-based material shares).  The reference uses
+ * dt = 0.03, alpha = beta = 0.02.  K is assembled per 3x3 block row in a
+ * fixed order (no atomics) and the system solved by block-Jacobi
+ * preconditioned conjugate gradients from v, FP64 dot products, until
+ * |r| <= tol |b| (the reference: a cuSOLVER sparse Cholesky).  Returns
+ * PBS_E_ITER_CAP (state advanced with the last iterate) when max_iters did
+ * not reach tol, PBS_E_NONFINITE (state unchanged) on a non-finite residual;
+ * iters_out / residual_out (|r| / |b|) may be NULL.  Shares positions and
+ * velocities with pbs_step. */
+int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, const float *ext, float tol,
+                            int max_iters, int *iters_out, double *residual_out);
+
 /* ---- Surface picking and drag forces (the viewer's interactive load) ----
  * The reference's viewer picks a boundary face with a ray and drags it; the
  * drag becomes the external forces of the next steps (RenderWidget.cpp:154,194

@@ -39,7 +39,7 @@ EXPORTS = (
     "pbs_mlp_param_count", "pbs_mlp_create", "pbs_mlp_destroy", "pbs_mlp_get_params", "pbs_mlp_set_params",
     "pbs_mlp_forward", "pbs_mlp_gradient", "pbs_mlp_set_data", "pbs_mlp_train",
     "pbs_set_warm_start", "pbs_warm_start_features", "pbs_eval_nodes_static",
-    "pbs_set_surface", "pbs_get_face_ring", "pbs_pick_face", "pbs_drag_face_ring",
+    "pbs_set_surface", "pbs_get_face_ring", "pbs_pick_face", "pbs_drag_face_ring", "pbs_backward_euler_step",
     "pbs_set_guess", "pbs_autotune", "pbs_get_instance_stats", "pbs_set_chunk_shape",
 )
 

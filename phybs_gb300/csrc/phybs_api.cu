@@ -80,6 +80,15 @@ struct pbs_handle {
     DevBuf<int> ring_pad, pick_id;
     DevBuf<float> pick_d2;
     DevBuf<float4> drag_ext;
+    // backward-Euler step: block-CSR pattern (built on first use), values,
+    // block-Jacobi inverses, CG vectors and reductions
+    bool bsr_ready = false;
+    DevBuf<int> bsr_ptr, bsr_col;
+    DevBuf<float> bsr_val, cg_dinv;
+    DevBuf<float4> cg_b, cg_x, cg_r, cg_z, cg_p, cg_q;
+    DevBuf<double> cg_part;
+    DevBuf<CgState> cg_state;
+    CgState *h_cg = nullptr;
     DevBuf<double2> tpart;
     DevBuf<double> npart;
     DevBuf<InstCtl> ctl;
@@ -136,6 +145,12 @@ struct pbs_handle {
         for (auto b : cf) b->release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
+        bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
+        DevBuf<float4> *cv[] = {&cg_b, &cg_x, &cg_r, &cg_z, &cg_p, &cg_q};
+        for (auto b : cv) b->release();
+        if (h_cg) cudaFreeHost(h_cg);
+        h_cg = nullptr;
+        bsr_ready = false;
         if (h_active) cudaFreeHost(h_active);
         if (h_ctl) cudaFreeHost(h_ctl);
         h_active = nullptr; h_ctl = nullptr;
@@ -1052,6 +1067,84 @@ int pbs_drag_face_ring(pbs_handle *h, int face, const float *drag, float *ext) {
     CK(launch_drag_ring(h->stream, h->mesh(), h->state(), h->faces_pad.p, h->ring_pad.p, b, len,
                         make_float3(drag[0], drag[1], drag[2]), h->drag_ext.p));
     return download_user(h, h->drag_ext.p, ext);
+}
+
+// Block-CSR pattern of the padded mesh: per padded node, itself and every node
+// sharing a tet with it, ascending; plus the CG buffers.
+static int ensure_bsr(pbs_handle *h) {
+    if (h->bsr_ready) return PBS_OK;
+    std::vector<std::vector<int>> nb(h->Np);
+    for (const int4 &q : h->h_tets_pad) {
+        if (q.x < 0) continue;
+        const int n[4] = {q.x, q.y, q.z, q.w};
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) nb[n[a]].push_back(n[b]);
+    }
+    std::vector<int> ptr(h->Np + 1, 0), col;
+    for (int i = 0; i < h->Np; ++i) {
+        auto &v = nb[i];
+        v.push_back(i);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        col.insert(col.end(), v.begin(), v.end());
+        ptr[i + 1] = (int)col.size();
+        std::vector<int>().swap(v);
+    }
+    const size_t nnzb = col.size(), np = (size_t)h->Np;
+    const int g = cg_blocks(h->Np);
+    CK(h->bsr_ptr.alloc(np + 1)); CK(h->bsr_col.alloc(nnzb)); CK(h->bsr_val.alloc(9 * nnzb));
+    CK(h->cg_dinv.alloc(9 * np)); CK(h->cg_part.alloc(3 * (size_t)g)); CK(h->cg_state.alloc(1));
+    DevBuf<float4> *cv[] = {&h->cg_b, &h->cg_x, &h->cg_r, &h->cg_z, &h->cg_p, &h->cg_q};
+    for (auto b : cv) CK(b->alloc(np));
+    if (!h->h_cg) CK(cudaMallocHost(&h->h_cg, sizeof(CgState)));
+    CK(cudaMemcpyAsync(h->bsr_ptr.p, ptr.data(), sizeof(int) * (np + 1), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->bsr_col.p, col.data(), sizeof(int) * nnzb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->bsr_ready = true;
+    return PBS_OK;
+}
+
+int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, const float *ext, float tol,
+                            int max_iters, int *iters_out, double *residual_out) {
+    if (!h || !(dt > 0.f) || !(alpha >= 0.f) || !(beta >= 0.f) || !(tol > 0.f) || max_iters <= 0)
+        return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_bsr(h);
+    if (rc != PBS_OK) return rc;
+    if (ext) {
+        rc = upload_user(h, ext, h->ext.p);
+        if (rc != PBS_OK) return rc;
+    }
+    cudaStream_t s = h->stream;
+    const DevMesh m = h->mesh();
+    const DevState st = h->state();
+    BsrView A;
+    A.ptr = h->bsr_ptr.p;
+    A.col = h->bsr_col.p;
+    A.val = h->bsr_val.p;
+    const double tol2 = (double)tol * (double)tol;
+    CK(launch_be_assemble(s, m, st, h->material, A, dt, alpha, beta, ext ? h->ext.p : nullptr, h->cg_b.p, h->cg_x.p,
+                          h->cg_dinv.p));
+    CK(launch_cg_init(s, h->Np, A, h->cg_dinv.p, h->cg_b.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
+                      h->cg_part.p, h->cg_state.p, tol2));
+    // iterations in groups of 16; every kernel of a finished solve returns at
+    // once, and the host reads the state once per group
+    for (int it = 0; it < max_iters; it += 16) {
+        for (int k = 0; k < 16 && it + k < max_iters; ++k)
+            CK(launch_cg_iteration(s, h->Np, A, h->cg_dinv.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
+                                   h->cg_q.p, h->cg_part.p, h->cg_state.p, tol2, max_iters));
+        CK(cudaMemcpyAsync(h->h_cg, h->cg_state.p, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h->h_cg->done) break;
+    }
+    const CgState c = *h->h_cg;
+    if (iters_out) *iters_out = c.iters;
+    if (residual_out) *residual_out = c.bb > 0.0 ? std::sqrt(c.rr / c.bb) : 0.0;
+    if (c.status == PBS_E_NONFINITE) return PBS_E_NONFINITE;  // the state is left as it was
+    CK(launch_be_finish(s, m, st, h->cg_x.p, dt));
+    CK(cudaStreamSynchronize(s));
+    h->guess_pending = false;
+    return c.done ? c.status : PBS_E_ITER_CAP;
 }
 
 int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {

@@ -264,6 +264,27 @@ cudaError_t launch_pick_face(cudaStream_t s, const DevMesh &m, const DevState &s
 cudaError_t launch_drag_ring(cudaStream_t s, const DevMesh &m, const DevState &st, const int4 *faces,
                              const int *ring, int begin, int len, float3 drag, float4 *ext);
 
+// Backward-Euler step (implicit.cu): a 3x3 block-CSR matrix over padded
+// nodes (columns ascending per block row) and the conjugate-gradient state.
+struct BsrView {
+    const int *ptr, *col;
+    float *val;  // 9 per block, row-major
+};
+struct CgState {
+    double rz, rr, bb, alpha, beta;
+    int iters, status, done, pad;
+};
+int cg_blocks(int Np);
+cudaError_t launch_be_assemble(cudaStream_t s, const DevMesh &m, const DevState &st, int material, const BsrView &A,
+                               float dt, float alpha, float beta, const float4 *ext, float4 *b, float4 *x,
+                               float *dinv9);
+cudaError_t launch_cg_init(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, const float4 *b,
+                           const float4 *x, float4 *r, float4 *z, float4 *p, double *part, CgState *cs, double tol2);
+cudaError_t launch_cg_iteration(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, float4 *x, float4 *r,
+                                float4 *z, float4 *p, float4 *q, double *part, CgState *cs, double tol2,
+                                int max_iters);
+cudaError_t launch_be_finish(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *x, float dt);
+
 struct HandleView {
     int device;
     cudaStream_t stream;

@@ -197,6 +197,19 @@ class DescentSolver:
     def reset(self):
         L.check(L.lib().pbs_reset(self._h), "pbs_reset")
 
+    def backward_euler_step(self, dt: float = 0.03, alpha: float = 0.02, beta: float = 0.02, ext=None,
+                            tol: float = 1e-6, max_iters: int = 4000, raise_on_cap: bool = True):
+        """One linearly implicit Euler step (CUDAInterface::doBackEuler); returns
+        (CG iterations, |r| / |b|)."""
+        it, res = C.c_int(), C.c_double()
+        e = _f32(ext, (-1, 3)) if ext is not None else None
+        rc = L.lib().pbs_backward_euler_step(self._h, C.c_float(dt), C.c_float(alpha), C.c_float(beta), _ptr(e),
+                                             C.c_float(tol), C.c_int(max_iters), C.byref(it), C.byref(res))
+        if rc != L.PBS_OK and (raise_on_cap or rc != L.PBS_E_ITER_CAP):
+            L.check(rc, "pbs_backward_euler_step")
+        self.last_status = rc
+        return it.value, res.value
+
     # -- surface picking and drag forces (TetMesh.cpp:229-277, 378-418, 446-470) --
     def set_surface(self, faces):
         """Boundary triangles (F, 3) in caller node ids, e.g. load_tetgen_faces()."""

@@ -11,7 +11,9 @@ def golden_names(prefix=""):
     """Fixture names: the solver fixtures (no prefix), or those starting with
     `prefix` (e.g. "surface_")."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    return [n for n in names if n.startswith(prefix)] if prefix else [n for n in names if not n.startswith("surface_")]
+    if prefix:
+        return [n for n in names if n.startswith(prefix)]
+    return [n for n in names if not n.startswith(("surface_", "stiffness_"))]
 
 
 def load_golden(name):

@@ -155,13 +155,41 @@ def make_surface(name, spec, rng, n_rays=24, n_drags=12):
     print(name, len(rest), len(faces), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def make_stiffness(name, cfg, rng, n_sample=64):
+    """Element stiffness matrices K = -df/dx of a sample of tets
+    (IsotropicMaterial::computeStiffnessMatrixFromPos, IsotropicMaterial.cpp:503-552:
+    Xu et al.'s SVD-derivative dP/dF), at a twisted and jittered state, with the
+    reference's rest data; the checker of the backward-Euler step's matrix."""
+    m = cfg["mesh"]
+    sim = REF.RefSim(m.rest, m.tets, m.pins, float(m.young[0]), float(m.poisson[0]), density=m.density)
+    rest = sim.rest()
+    mu, lam = sim.lame()
+    edge = float(np.median(np.linalg.norm(rest[m.tets[:, 1]] - rest[m.tets[:, 0]], axis=1)))
+    x = M.twist_positions(rest, cfg["probe_twist"], axis=twist_axis(rest))
+    x = (x + rng.normal(0.0, 0.05 * edge, x.shape)).astype(np.float32)
+    assert (M.signed_volumes(x, m.tets) > 0).all()
+    sample = np.sort(rng.choice(m.tets.shape[0], size=min(n_sample, m.tets.shape[0]), replace=False)).astype(np.int32)
+    K = np.stack([sim.element_stiffness(int(t), x) for t in sample])
+    out = dict(rest=rest, tets=m.tets, pins=m.pins, mu=mu, lam=lam, dminv=sim.dminv(), vol=sim.vol(),
+               mass=sim.mass(), gravity=sim.gravity(), x=x, sample=sample, K=K)
+    sim.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, len(sample), os.path.getsize(os.path.join(HERE, name + ".npz")))
+
+
 if __name__ == "__main__":
-    # `make_golden.py surface` writes only the surface fixtures
-    only_surface = sys.argv[1:] == ["surface"]
+    # `make_golden.py surface` / `make_golden.py stiffness` write only those fixtures
+    only = sys.argv[1] if len(sys.argv) > 1 else None
     rng = np.random.default_rng(20261203)
-    if not only_surface:
+    if only is None:
         for n, c in cases().items():
             make(n, c, rng)
-    srng = np.random.default_rng(20261204)
-    for n, spec in surface_cases().items():
-        make_surface(n, spec, srng)
+    if only in (None, "surface"):
+        srng = np.random.default_rng(20261204)
+        for n, spec in surface_cases().items():
+            make_surface(n, spec, srng)
+    if only in (None, "stiffness"):
+        krng = np.random.default_rng(20261205)
+        all_cases = cases()
+        for n in ("bar_small", "model_bar", "ellipsoid_small"):
+            make_stiffness("stiffness_" + n, all_cases[n], krng)
