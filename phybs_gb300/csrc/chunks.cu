@@ -304,17 +304,18 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     __syncthreads();
     if (!*is_last) return;
     __threadfence();
-    // the instance's last chunk: fixed-order sums, then accept / reject
-    double E = 0.0, E2 = 0.0;
-    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += THREADS) {
+    // the instance's last chunk: fixed-order sums (two interleaved
+    // accumulators a value), then accept / reject
+    double ea[2] = {0.0, 0.0}, eb[2] = {0.0, 0.0};
+    for (int j = cp->cblk_begin + threadIdx.x, q = 0; j < cp->cblk_end; j += THREADS, q ^= 1) {
         const double2 v = __ldcg(st.cpart + j);
-        E += v.x;
-        E2 += v.y;
+        ea[q] += v.x;
+        eb[q] += v.y;
     }
-    E = block_sum(E, sh);
-    E2 = block_sum(E2, sh);
+    const double E = block_sum(ea[0] + ea[1], sh);
+    const double E2 = block_sum(eb[0] + eb[1], sh);
     if (threadIdx.x != 0) return;
-    InstCtl &ci = *cp;  // in place, as in the node kernel
+    InstCtl ci = *cp;  // one load, updates in registers, one store (as in the node kernel)
     ci.counter_t = 0;
     ci.energy = E;
     // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
@@ -343,6 +344,7 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
         ci.status = PBS_E_NONFINITE;
         ci.done = 1;
     }
+    *cp = ci;
     if (ci.done) atomicSub(st.active, 1);
 }
 

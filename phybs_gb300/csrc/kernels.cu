@@ -110,7 +110,7 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.energy = 0.0;
     c.energy_old = 0.0;
     c.g0 = -1.0;
-    c.ratio = -1.0;
+    c.r2 = -1.0;
     ctl[b] = c;
     if (!c.done) atomicAdd(active, 1);
 }
@@ -404,48 +404,68 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    double R2 = 0.0;
-    for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += TH) R2 += __ldcg(st.npart + j);
-    R2 = block_sum(R2, shd);
+    // the instance's last block: FP64 sum of the block partials in block order
+    // (four interleaved accumulators keep the dependent FP64 chain short)
+    const int nb0 = cp->nblk_begin, nb1 = cp->nblk_end;
+    double a4[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int j = nb0 + threadIdx.x, q = 0; j < nb1; j += TH, q = (q + 1) & 3) a4[q] += __ldcg(st.npart + j);
+    double R2 = block_sum((a4[0] + a4[1]) + (a4[2] + a4[3]), shd);
     if (threadIdx.x != 0) return;
-    // updated in place: every other block has read it, and the next kernel
-    // reads it only after its grid-dependency wait
-    InstCtl &c = *cp;
-    c.counter_n = 0;
-    c.passes += 1;
-    c.force_check = 0;  // a forced line-search check was applied in this pass
+    // The fields this decision reads are loaded together (one round trip),
+    // updated in registers and stored back: every other block has read the
+    // control block, and the next kernel reads it only after its
+    // grid-dependency wait.  No FP64 square root or division per pass: the stop
+    // test compares |g|^2 with (tol g0)^2; the ratio is formed on the host.
+    int passes = cp->passes + 1, par_c = cp->par, kk = k, done = 0, converged = 0, status = cp->status;
+    int force_check = 0, k_restart = cp->k_restart;
+    const int iters = cp->iters, g0_fixed = cp->g0_fixed;
+    const float alpha = cp->alpha;
+    double g0 = cp->g0;
+    float rho_n = cp->rho, omega_n = cp->omega;
     if (action == ACT_RESTORE) {
-        c.par = 1 - c.par;  // the restored state; k is redone
-        if (p.control == PBS_CONTROL_RESTART) c.k_restart = k;  // rerun the rho schedule from here
+        par_c = 1 - par_c;  // the restored state; k is redone
+        if (p.control == PBS_CONTROL_RESTART) k_restart = k;  // rerun the rho schedule from here
     } else {
-        const double r = sqrt(R2);
-        if (k == 0 && !c.g0_fixed) c.g0 = r;
-        c.ratio = c.g0 > 0.0 ? r / c.g0 : 0.0;
-        if (p.tol > 0.f && k > 0 && r <= (double)p.tol * c.g0) {
-            c.converged = 1;  // keep x_k (the current parity)
-            c.done = 1;
+        if (k == 0 && !g0_fixed) g0 = sqrt(R2);
+        cp->r2 = R2;
+        const double lim = (double)p.tol * g0;
+        if (p.tol > 0.f && k > 0 && R2 <= lim * lim) {
+            converged = 1;  // keep x_k (the current parity)
+            done = 1;
         } else {
-            c.rho = rho;
-            c.omega = omega;
-            c.par = 1 - c.par;
-            c.k = k + 1;
+            rho_n = rho;
+            omega_n = omega;
+            par_c = 1 - par_c;
+            kk = k + 1;
         }
         if (!isfinite(R2)) {
-            if (p.control == PBS_CONTROL_RESTART && c.k > 0) {
-                c.force_check = 1;  // the next pass measures the energy and restores
-                c.converged = 0;
-                c.done = 0;
+            if (p.control == PBS_CONTROL_RESTART && kk > 0) {
+                force_check = 1;  // the next pass measures the energy and restores
+                converged = 0;
+                done = 0;
             } else {
-                c.status = PBS_E_NONFINITE;
-                c.done = 1;
+                status = PBS_E_NONFINITE;
+                done = 1;
             }
         }
     }
-    if (!c.done) {
-        if (c.k >= c.iters || c.alpha < p.alpha_min) c.done = 1;
-        else if (c.passes >= p.pass_cap) { c.done = 1; c.status = PBS_E_ITER_CAP; }
+    if (!done) {
+        if (kk >= iters || alpha < p.alpha_min) done = 1;
+        else if (passes >= p.pass_cap) { done = 1; status = PBS_E_ITER_CAP; }
     }
-    if (c.done) atomicSub(st.active, 1);
+    cp->counter_n = 0;
+    cp->passes = passes;
+    cp->force_check = force_check;  // a forced line-search check was applied in this pass
+    cp->par = par_c;
+    cp->k_restart = k_restart;
+    cp->g0 = g0;
+    cp->rho = rho_n;
+    cp->omega = omega_n;
+    cp->k = kk;
+    cp->converged = converged;
+    cp->status = status;
+    cp->done = done;
+    if (done) atomicSub(st.active, 1);
 }
 
 // Per-step node constant b = f_el(u_base) (incremental mode, FP64) +

@@ -644,7 +644,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     S.rho = h->h_ctl[0].rho;
     S.omega = h->h_ctl[0].omega;
     S.energy = h->h_ctl[0].energy;
-    S.residual_ratio = h->h_ctl[0].ratio;
+    S.residual_ratio = residual_ratio(h->h_ctl[0]);
     S.device_ms = ms;
     S.graph_launches = launched;
     h->stats = S;
@@ -787,9 +787,12 @@ int pbs_get_stream(pbs_handle *h, void **stream) {
 static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
     cudaStream_t s = h->stream;
     DevParams p = h->dparams;
-    p.max_iters = passes + 1;
+    // a line-search rejection adds a pass and, under the reference control,
+    // shortens the iteration budget (iterations -= k - 8): neither may end the
+    // timed passes early
+    p.max_iters = 4 * passes + 64;
     p.tol = 0.f;
-    p.pass_cap = passes + 1;
+    p.pass_cap = 4 * passes + 64;
     DevMesh m = h->mesh();
     DevState st = h->state();
     std::vector<cudaEvent_t> ev(2 * passes + 1, nullptr);
@@ -827,7 +830,7 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
             pbs_stats S{};
             S.passes = x.passes; S.iterations = x.k; S.rejections = x.rejections; S.converged = x.converged;
             S.status = x.status; S.alpha = x.alpha; S.rho = x.rho; S.omega = x.omega; S.energy = x.energy;
-            S.residual_ratio = x.ratio;
+            S.residual_ratio = residual_ratio(x);
             h->stats = S;
             return x.status != PBS_OK ? x.status : PBS_E_ITER_CAP;
         }
@@ -969,7 +972,7 @@ int pbs_get_instance_stats(pbs_handle *h, int instance, pbs_stats *s) {
     pbs_stats S{};
     S.passes = c.passes; S.iterations = c.k; S.rejections = c.rejections; S.converged = c.converged;
     S.status = c.status; S.alpha = c.alpha; S.rho = c.rho; S.omega = c.omega; S.energy = c.energy;
-    S.residual_ratio = c.ratio; S.device_ms = h->stats.device_ms; S.graph_launches = h->stats.graph_launches;
+    S.residual_ratio = residual_ratio(c); S.device_ms = h->stats.device_ms; S.graph_launches = h->stats.graph_launches;
     S.warm_start_used = c.ws_used;
     S.guess_fallbacks = c.guess_bad;
     *s = S;

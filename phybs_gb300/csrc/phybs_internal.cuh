@@ -110,12 +110,18 @@ struct __align__(16) InstCtl {
     int ws_used;      // this step started from the learned guess
     float ell;        // mean edge length of the instance (feature scale)
     int guess_bad;    // RESTART control: the inertial guess inverts a tet; the step starts from u0
-    double energy, energy_old, g0, ratio;
+    double energy, energy_old, g0, r2;  // r2: |g|^2 of the last pass (ratio = sqrt(r2) / g0, on the host)
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
     int tblk_begin, tblk_end, nblk_begin, nblk_end;
     int cblk_begin, cblk_end, pad4, pad5;  // the instance's chunks
 };
+
+// |g| / |g0| of an instance's last pass (-1 before the first pass).
+inline double residual_ratio(const InstCtl &c) {
+    if (c.r2 < 0.0 || c.g0 < 0.0) return -1.0;
+    return c.g0 > 0.0 ? __builtin_sqrt(c.r2) / c.g0 : 0.0;
+}
 
 struct DevMesh {
     int Np, Tp, n_inst;
