@@ -201,9 +201,9 @@ struct ChunkView {
 // Corner forces of the chunk's tets into the slots; on line-search passes
 // returns the thread's sum of clamped tet energies.
 template <int MATERIAL, int THREADS, bool INC>
-__device__ __forceinline__ double chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check, float *sx,
+__device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check, float *sx,
                                                float *sy, float *sz) {
-    double e = 0.0;
+    DFloat e{0.f, 0.f};
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
@@ -223,8 +223,8 @@ __device__ __forceinline__ double chunk_forces(const DevParams &p, const ChunkVi
             sz[sl[cc]] = f[3 * cc + 2];
         }
         if (check)
-            e += (double)search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
-                                       p.control == PBS_CONTROL_RESTART);
+            e = df_add(e, search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
+                                        p.control == PBS_CONTROL_RESTART));
     }
     return e;
 }
@@ -274,13 +274,16 @@ __device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const f
 // Line-search pass: adds the chunk's share of the instance's node energy terms
 // to the thread's tet energies e, stores the chunk's {sum e, sum e^2}, and in
 // the instance's last chunk to finish sums the chunks in order and decides
-// accept / reject (DescentOptimize.cpp:162-183).  Called by every thread of
-// the CTA; *is_last is a shared word.
+// accept / reject (DescentOptimize.cpp:162-183).  The sums run in
+// double-float (e) and FP32 (e^2, a noise scale), the chunk totals and their
+// sum in FP64.  Called by every thread of the CTA; *is_last is a shared word.
 template <int THREADS>
 __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevParams &p, const DevState &st, int c,
-                                                  InstCtl *cp, int k, size_t cur, double e, double *sh,
+                                                  InstCtl *cp, int k, size_t cur, DFloat e, double *sh,
                                                   int *is_last) {
-    double e2 = e * e;
+    __shared__ float2 shf[THREADS / 32];
+    __shared__ float shs[THREADS / 32];
+    float e2 = e.hi * e.hi;
     {
         const int nb = cp->cblk_end - cp->cblk_begin;
         const float4 *U = st.uh + cur;
@@ -288,15 +291,15 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
              i += nb * THREADS) {
             const float4 info = m.info[i];
             if (info.z != 0.f) continue;
-            const double en = node_energy(st, info, U[i], st.ul[cur + i], i, p.h2inv);
-            e += en;
-            e2 += en * en;
+            const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+            e = df_add(e, en);
+            e2 = fmaf(en.hi, en.hi, e2);
         }
     }
-    const double se = block_sum(e, sh);
-    const double se2 = block_sum(e2, sh);
+    const DFloat se = block_sum_df(e, shf);
+    const float se2 = block_sum_f(e2, shs);
     if (threadIdx.x == 0) {
-        st.cpart[c] = make_double2(se, se2);
+        st.cpart[c] = make_double2(df_double(se), (double)se2);
         __threadfence();
         const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
         *is_last = (prev == (unsigned int)(cp->cblk_end - cp->cblk_begin - 1));
@@ -356,7 +359,7 @@ __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p,
                                            InstCtl *cp, int k, bool check, bool do_h, size_t cur, const ChunkView &v,
                                            const int4 *meta, int nt, int nl, float *sx, float *sy, float *sz,
                                            double *sh, int *is_last) {
-    const double e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sx, sy, sz);
+    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sx, sy, sz);
     __syncthreads();
     chunk_partials<THREADS>(meta, nl, sx, sy, sz, st.part);
     if (do_h) {
@@ -373,9 +376,14 @@ __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p,
 // shared memory -- before the grid-dependency wait, since they are constant --
 // and of the chunk's node words after it; one wait then covers all of them,
 // instead of one global round trip per tet inside the loop.
-// Register budget of the incremental variants: 85 a thread (768 threads a SM).
+#ifndef PBS_INC_THREADS_PER_SM
+#define PBS_INC_THREADS_PER_SM 1024
+#endif
+// Register budget of the incremental variants: 64 a thread (1024 threads a
+// SM; a few registers spill, and the extra resident warps pay for them: 44.9
+// against 49.7 us a pass on the 1M-tet box at 85 registers).
 template <int MATERIAL, int THREADS, bool INC, bool STAGE>
-__global__ void __launch_bounds__(THREADS, INC ? 768 / THREADS : 0)
+__global__ void __launch_bounds__(THREADS, INC ? PBS_INC_THREADS_PER_SM / THREADS : 0)
     k_tchunk(DevMesh m, DevParams p, DevState st, int par) {
     extern __shared__ float4 smem4[];
     const int CN = m.chunk_nodes, CT = m.chunk_tets;

@@ -302,23 +302,6 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
     return r2;
 }
 
-// Deterministic FP32 block sum (fixed shuffle tree, then warp 0 over the warp
-// totals); result valid in thread 0.
-__device__ __forceinline__ float block_sum_f(float v, float *sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    float r = 0.f;
-    if (w == 0) {
-        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-    }
-    return r;
-}
 
 // One CTA per 256-node block (one instance); NPT nodes per thread.  The
 // per-step constants go to shared memory by cp.async before the

@@ -68,6 +68,68 @@ __device__ __forceinline__ double node_energy(const DevState &st, const float4 &
            (double)info.y * uy - ((double)ex.x * ((double)uh.x + ul.x) + (double)ex.y * uy + (double)ex.z * ((double)uh.z + ul.z));
 }
 
+// Deterministic FP32 block sum (fixed shuffle tree, then warp 0 over the warp
+// totals); result valid in thread 0.
+__device__ __forceinline__ float block_sum_f(float v, float *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    return r;
+}
+
+// Deterministic double-float block sum (fixed shuffle tree, then warp 0 over
+// the warp totals in warp order); result valid in thread 0.  sh: 2 floats a
+// warp.
+__device__ __forceinline__ DFloat block_sum_df(DFloat v, float2 *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_down_sync(0xffffffffu, v.hi, o), l = __shfl_down_sync(0xffffffffu, v.lo, o);
+        v = df_add(v, DFloat{h, l});
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = make_float2(v.hi, v.lo);
+    __syncthreads();
+    DFloat r{0.f, 0.f};
+    if (w == 0) {
+        if (lane < (int)(blockDim.x >> 5)) r = DFloat{sh[lane].x, sh[lane].y};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h = __shfl_down_sync(0xffffffffu, r.hi, o), l = __shfl_down_sync(0xffffffffu, r.lo, o);
+            r = df_add(r, DFloat{h, l});
+        }
+    }
+    return r;
+}
+
+// node_energy in double-float: the same terms, FP32 operations only.
+__device__ __forceinline__ DFloat node_energy_df(const DevState &st, const float4 &info, const float4 &uh,
+                                                 const float4 &ul, int i, float h2inv) {
+    const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
+    const float dx = (uh.x - th.x) + (ul.x - tl.x);
+    const float dy = (uh.y - th.y) + (ul.y - tl.y);
+    const float dz = (uh.z - th.z) + (ul.z - tl.z);
+    const DFloat sq = df_add(df_add(df_prod(dx, dx), df_prod(dy, dy)), df_prod(dz, dz));
+    DFloat k = df_prod(info.x, h2inv);
+    k.hi *= 0.5f;  // exact
+    k.lo *= 0.5f;
+    DFloat e = df_mul(k, sq);
+    e = df_add(e, df_mul(DFloat{uh.y, ul.y}, -info.y));
+    e = df_add(e, df_mul(DFloat{uh.x, ul.x}, -ex.x));
+    e = df_add(e, df_mul(DFloat{uh.y, ul.y}, -ex.y));
+    e = df_add(e, df_mul(DFloat{uh.z, ul.z}, -ex.z));
+    return e;
+}
+
 // Corner forces of a tet in a descent pass.  Neo-Hookean with p.incremental:
 // the increment dP = P(F) - P(F0) against the base displacement U0 (the
 // step's initial guess; the node kernel adds the FP64 force at the base held

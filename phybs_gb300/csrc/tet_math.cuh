@@ -408,4 +408,40 @@ __device__ __forceinline__ void add_comp(float &hi, float &lo, float b) {
     hi = s2;
 }
 
+// Double-float value hi + lo (|lo| <= ulp(hi) / 2) with FP32 operations only:
+// products exact through fma, sums through TwoSum, about 2^-44 relative.  The
+// line search's energy sums use it: in FP64 they ran on GB300's narrow
+// double-precision pipe and made a check pass 60% dearer than a plain one.
+struct DFloat {
+    float hi, lo;
+};
+__device__ __forceinline__ DFloat df_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return DFloat{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ DFloat df_add(DFloat a, float b) {
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    return df_norm(s, __fadd_rn(e, a.lo));
+}
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    return df_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ DFloat df_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return DFloat{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DFloat df_mul(DFloat a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    return df_norm(p, __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p)));
+}
+__device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return df_norm(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ double df_double(DFloat a) { return (double)a.hi + (double)a.lo; }
+
 }  // namespace pbs
