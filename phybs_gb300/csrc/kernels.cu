@@ -314,7 +314,7 @@ template <int NPT>
 __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh m, DevParams p, DevState st, int par) {
     constexpr int TH = BLOCK / NPT;
     __shared__ float sh[TH / 32];
-    __shared__ double shd[TH / 32];
+    __shared__ float2 shf[TH / 32];
     __shared__ int is_last;
     __shared__ __align__(16) float4 s_c[5][BLOCK];  // info, th, tl, bh, bl of the block's nodes
     const int b = blockIdx.x;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     }
     const float sr = block_sum_f(r2, sh);
     if (threadIdx.x == 0) {
-        st.npart[b] = (double)sr;
+        st.npartf[b] = sr;
         __threadfence();
         const unsigned int prev = atomicAdd(&cp->counter_n, 1u);
         is_last = (prev == (unsigned int)(cp->nblk_end - cp->nblk_begin - 1));
@@ -387,12 +387,12 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    // the instance's last block: FP64 sum of the block partials in block order
-    // (four interleaved accumulators keep the dependent FP64 chain short)
+    // the instance's last block: double-float sum of the block partials in a
+    // fixed order (FP32 pipe; GB300's FP64 pipe made this tail several us)
     const int nb0 = cp->nblk_begin, nb1 = cp->nblk_end;
-    double a4[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int j = nb0 + threadIdx.x, q = 0; j < nb1; j += TH, q = (q + 1) & 3) a4[q] += __ldcg(st.npart + j);
-    double R2 = block_sum((a4[0] + a4[1]) + (a4[2] + a4[3]), shd);
+    DFloat acc{0.f, 0.f};
+    for (int j = nb0 + threadIdx.x; j < nb1; j += TH) acc = df_add(acc, __ldcg(st.npartf + j));
+    const double R2 = df_double(block_sum_df(acc, shf));
     if (threadIdx.x != 0) return;
     // The fields this decision reads are loaded together (one round trip),
     // updated in registers and stored back: every other block has read the

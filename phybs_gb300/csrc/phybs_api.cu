@@ -91,6 +91,7 @@ struct pbs_handle {
     CgState *h_cg = nullptr;
     DevBuf<double2> tpart;
     DevBuf<double> npart;
+    DevBuf<float> npartf;
     DevBuf<InstCtl> ctl;
     DevBuf<int> active;
     // host pinned
@@ -122,7 +123,7 @@ struct pbs_handle {
         s.uh = uh.p; s.ul = ul.p; s.dd = dd.p; s.oh = oh.p; s.ol = ol.p; s.u0h = u0h.p; s.u0l = u0l.p;
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
         s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p;
-        s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.ctl = ctl.p; s.active = active.p;
+        s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.npartf = npartf.p; s.ctl = ctl.p; s.active = active.p;
         s.cpart = cpart.p; s.part = part.p; s.parth = parth.p; s.rslot = rslot.p;
         return s;
     }
@@ -143,7 +144,7 @@ struct pbs_handle {
         for (auto b : ci) b->release();
         DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
         for (auto b : cf) b->release();
-        tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); ctl.release();
+        tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release();
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
         DevBuf<float4> *cv[] = {&cg_b, &cg_x, &cg_r, &cg_z, &cg_p, &cg_q};
@@ -446,7 +447,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
-    CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk));
+    CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk)); CKC(h->npartf.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
     CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T)); CKC(h->rslot.alloc(12 * (size_t)T));
     CKC(prepare_chunk_kernels());

@@ -39,7 +39,8 @@
 //   part, parth float4[L]          per (node, chunk) partial force / Jacobi-diagonal sums
 //   cpart       double2[n_chunks]  per chunk {sum e, sum e^2}
 //   rslot       double[3][4T]      per-step FP64 corner forces at the base, by gather slot
-//   npart       double[n_nblk]     per node-block |g|^2
+//   npart       double[n_nblk]     per node-block |g|^2 (warm-start reference)
+//   npartf      float[n_nblk]      per node-block |g|^2 of a pass (FP32 block sums)
 //   ctl         InstCtl[n_inst]    per-instance descent state
 #pragma once
 #include <cuda_runtime.h>
@@ -155,6 +156,7 @@ struct DevState {
     float *tf, *hd;
     double2 *tpart, *cpart;
     double *npart;
+    float *npartf;
     float4 *part, *parth;
     double *rslot;  // 3 * 4T: FP64 corner forces at the base, by gather slot
     InstCtl *ctl;
