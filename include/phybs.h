@@ -304,11 +304,13 @@ int pbs_mlp_gradient(pbs_mlp *t, const float *X, const float *Y, int n, float *g
 int pbs_mlp_set_data(pbs_mlp *t, const float *X, const float *Y, const float *W, int n);
 int pbs_mlp_train(pbs_mlp *t, int steps, int batch, float lr, unsigned long long seed, float *losses);
 
-/* Install (enabled != 0) or switch off the warm start on a solver handle.
- * theta: pbs_mlp_param_count() values; feat_mean / feat_std: the 24 feature
- * standardisation constants; out_std: the 3 output scales (the network
- * predicts correction / (out_std * s), s the node's motion scale, see
- * pbs_warm_start_features).  Each pbs_step then
+/* Install (enabled = 1 or 2) or switch off (0) the warm start on a solver
+ * handle.  theta: pbs_mlp_param_count() values; feat_mean / feat_std: the 24
+ * feature standardisation constants; out_std: the 3 output scales (the
+ * network predicts correction / (out_std * s), s the node's motion scale, see
+ * pbs_warm_start_features).  The correction is added to the plain guess
+ * (enabled = 1) or to the constant-acceleration extrapolation of the node's
+ * last two displacements, u0 + 2 d1 - d2 (enabled = 2).  Each pbs_step then
  * evaluates the network on the plain guess's features, keeps the predicted
  * guess for an instance only if its energy is not higher than the plain
  * guess's, and measures the residual tolerance against the plain guess's

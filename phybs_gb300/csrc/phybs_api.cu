@@ -69,6 +69,7 @@ struct pbs_handle {
     // learned warm start
     DevBuf<float> ws_theta, ws_stats;  // NPARAM; feat mean 24, feat std 24, out std 3
     bool ws_enabled = false;
+    int ws_base = 0;  // 0: corrections to the plain guess, 1: to the extrapolation u0 + 2 d1 - d2
     bool guess_pending = false;  // parity 1 holds a caller guess for the next step
     int sms = 148;
     DevBuf<float> tf, hd, staging, staging2;
@@ -603,7 +604,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
             CK(launch_ws_choose(s, m, h->dparams, st));
         else
             CK(launch_ws_predict(s, m, h->dparams, st, h->ws_theta.p, h->ws_stats.p, h->ws_stats.p + 24,
-                                 h->ws_stats.p + 48, h->hd.p, h->sms));
+                                 h->ws_stats.p + 48, h->hd.p, h->sms, h->ws_base, h->material));
         h->guess_pending = false;
     }
     // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
@@ -719,6 +720,7 @@ int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean
         h->ws_enabled = false;
         return PBS_OK;
     }
+    if (enabled != 1 && enabled != 2) return PBS_E_INVALID_ARG;
     const int np = pbs_mlp_param_count();
     if (!theta || !feat_mean || !feat_std || !out_std) return PBS_E_INVALID_ARG;
     for (int i = 0; i < np; ++i)
@@ -736,6 +738,7 @@ int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean
     CK(cudaMemcpy(h->ws_theta.p, theta, sizeof(float) * np, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->ws_stats.p, st.data(), sizeof(float) * 51, cudaMemcpyHostToDevice));
     h->ws_enabled = true;
+    h->ws_base = enabled == 2 ? 1 : 0;
     return PBS_OK;
 }
 

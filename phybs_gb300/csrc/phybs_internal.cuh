@@ -116,6 +116,8 @@ struct __align__(16) InstCtl {
     int node_begin, node_end, tet_begin, tet_end;
     int tblk_begin, tblk_end, nblk_begin, nblk_end;
     int cblk_begin, cblk_end, pad4, pad5;  // the instance's chunks
+    double g1;                             // |g| at the learned candidate (extrapolation base)
+    double pad6;
 };
 
 // |g| / |g0| of an instance's last pass (-1 before the first pass).
@@ -217,7 +219,7 @@ cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
 cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *theta,
                               const float *feat_mean, const float *feat_std, const float *out_std, float *tetF,
-                              int sms);
+                              int sms, int base, int material);
 cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
                                const int *pad2user, float *out, float *scale_out);

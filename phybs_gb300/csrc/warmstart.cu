@@ -44,6 +44,54 @@ __global__ void __launch_bounds__(BLOCK) k_ws_force(DevMesh m, DevParams p, DevS
     tf4[sl.w] = make_float4(f[9], f[10], f[11], 0.f);
 }
 
+// |g|^2 at the learned candidate (parity 1), with its elastic forces gathered
+// from the slots k_ws_force filled (incremental mode: the increment from the
+// plain guess, whose force is in b), reduced per instance into ctl.g1.
+__global__ void __launch_bounds__(BLOCK) k_ws_gcand(DevMesh m, DevParams p, DevState st) {
+    __shared__ double sh[BLOCK / 32];
+    __shared__ int is_last;
+    const int b = blockIdx.x;
+    InstCtl *cp = st.ctl + m.nblk_inst[b];
+    if (cp->done) return;
+    const int i = b * BLOCK + threadIdx.x;
+    const float4 info = m.info[i];
+    double r2 = 0.0;
+    if (info.z == 0.f) {
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        const float4 *tf4 = reinterpret_cast<const float4 *>(st.tf);
+        for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+            const float4 f = tf4[j];
+            fx += f.x;
+            fy += f.y;
+            fz += f.z;
+        }
+        const float4 uh = st.uh[m.Np + i], ul = st.ul[m.Np + i], th = st.th[i], tl = st.tl[i], bh = st.bh[i],
+                     bl = st.bl[i];
+        const float mh = info.x * p.h2inv;
+        const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
+        const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
+        const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
+        r2 = (double)gx * gx + (double)gy * gy + (double)gz * gz;
+    }
+    const double s = block_sum(r2, sh);
+    if (threadIdx.x == 0) {
+        st.npart[b] = s;
+        __threadfence();
+        const unsigned int prev = atomicAdd(&cp->counter_n, 1u);
+        is_last = (prev == (unsigned int)(cp->nblk_end - cp->nblk_begin - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double R2 = 0.0;
+    for (int j = cp->nblk_begin + threadIdx.x; j < cp->nblk_end; j += BLOCK) R2 += __ldcg(st.npart + j);
+    R2 = block_sum(R2, sh);
+    if (threadIdx.x == 0) {
+        cp->counter_n = 0;
+        cp->g1 = sqrt(R2);
+    }
+}
+
 // |g|^2 at the plain guess (parity 0), reduced per instance into ctl.g0.
 __global__ void __launch_bounds__(BLOCK) k_ws_gref(DevMesh m, DevParams p, DevState st) {
     __shared__ double sh[BLOCK / 32];
@@ -163,6 +211,7 @@ __global__ void k_ws_features(DevMesh m, DevParams p, DevState st, const float *
 struct WsNet {
     const float *theta;
     const float *feat_mean, *feat_std, *out_std;  // 24, 24, 3
+    int base;  // 0: the correction is added to the plain guess; 1: to u0 + 2 d1 - d2
 };
 
 // Features -> standardised BF16 fragments -> MLP -> candidate guess in
@@ -235,6 +284,16 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
             if (info.z != 2.f) {
                 float hx = st.uh[i].x, hy = st.uh[i].y, hz = st.uh[i].z;
                 float lx = st.ul[i].x, ly = st.ul[i].y, lz = st.ul[i].z;
+                if (info.z == 0.f && net.base == 1) {
+                    // the constant-acceleration extrapolation of the last two
+                    // displacements: u0 + d1 + (d1 - d2)
+                    const float4 h0 = st.u0h[i], l0 = st.u0l[i], d1 = st.hist1[i], d2 = st.hist2[i];
+                    hx = h0.x; hy = h0.y; hz = h0.z;
+                    lx = l0.x; ly = l0.y; lz = l0.z;
+                    add_comp(hx, lx, d1.x + (d1.x - d2.x));
+                    add_comp(hy, ly, d1.y + (d1.y - d2.y));
+                    add_comp(hz, lz, d1.z + (d1.z - d2.z));
+                }
                 if (info.z == 0.f) {
                     const float sc = tscale[w][lane];
                     add_comp(hx, lx, tile[w][lane][0] * os[0] * sc);
@@ -250,7 +309,10 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
 }
 
 // Energies of the plain guess (parity 0) and the candidate (parity 1).
-__global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevState st) {
+// residual: also require the candidate's |g| below the plain guess's (the
+// extrapolation base, whose energy can undercut the plain guess's while its
+// gradient, which the stop test measures, is larger).
+__global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevState st, int residual) {
     __shared__ double sh[BLOCK / 32];
     __shared__ int is_last;
     const int b = blockIdx.x;
@@ -301,7 +363,7 @@ __global__ void __launch_bounds__(BLOCK) k_ws_judge(DevMesh m, DevParams p, DevS
     if (threadIdx.x == 0) {
         cp->counter_t = 0;
         // a finite candidate also wins over a plain guess whose energy is not finite
-        cp->ws_used = (isfinite(E1) && (E1 <= E0 || !isfinite(E0))) ? 1 : 0;
+        cp->ws_used = (isfinite(E1) && (E1 <= E0 || !isfinite(E0)) && (!residual || cp->g1 < cp->g0)) ? 1 : 0;
     }
 }
 
@@ -328,7 +390,7 @@ static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
     k_ws_guess_pins<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
-    k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
+    k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, 0);
     k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -347,13 +409,22 @@ cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p,
 
 cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *theta,
                               const float *feat_mean, const float *feat_std, const float *out_std, float *tetF,
-                              int sms) {
+                              int sms, int base, int material) {
     k_ws_tet_F<<<nblk(m.Tp, 256), 256, 0, s>>>(m, st, tetF);
-    WsNet net{theta, feat_mean, feat_std, out_std};
+    WsNet net{theta, feat_mean, feat_std, out_std, base};
     const int tiles = nblk(m.Np, 16);
     const int blocks = std::min(nblk(tiles, 4), 8 * sms);
     k_ws_infer<<<blocks, 128, 0, s>>>(m, p, st, tetF, net);
-    k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st);
+    if (base == 1) {  // the candidate's gradient for the residual test
+        DevState s1 = st;
+        s1.ul = st.ul + m.Np;
+        if (material == PBS_MATERIAL_STRETCH)
+            k_ws_force<PBS_MATERIAL_STRETCH><<<m.n_tblk, BLOCK, 0, s>>>(m, p, s1, st.uh + m.Np);
+        else
+            k_ws_force<PBS_MATERIAL_NEOHOOKEAN><<<m.n_tblk, BLOCK, 0, s>>>(m, p, s1, st.uh + m.Np);
+        k_ws_gcand<<<m.n_nblk, BLOCK, 0, s>>>(m, p, st);
+    }
+    k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, base == 1);
     k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

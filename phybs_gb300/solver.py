@@ -180,7 +180,8 @@ class DescentSolver:
             L.check(L.lib().pbs_set_warm_start(self._h, None, None, None, None, C.c_int(0)), "pbs_set_warm_start")
             return
         th, fm, fs, os_ = (_f32(model.theta), _f32(model.feat_mean), _f32(model.feat_std), _f32(model.out_std))
-        L.check(L.lib().pbs_set_warm_start(self._h, _ptr(th), _ptr(fm), _ptr(fs), _ptr(os_), C.c_int(1)),
+        mode = 2 if getattr(model, "base", "inertial") == "extrapolation" else 1
+        L.check(L.lib().pbs_set_warm_start(self._h, _ptr(th), _ptr(fm), _ptr(fs), _ptr(os_), C.c_int(mode)),
                 "pbs_set_warm_start")
 
     def velocities(self):

@@ -81,9 +81,12 @@ def ellipsoid_scenario(rng):
 
 
 def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int = 60, verbose: bool = True,
-             mix=(0.5, 0.3, 0.2)):
+             mix=(0.5, 0.3, 0.2), base: str = "inertial"):
     """Solve frames of randomly drawn scenarios; mix = the fractions of runs
-    that are box1m, box and ellipsoid."""
+    that are box1m, box and ellipsoid.  Targets are the converged positions
+    relative to the plain guess (base "inertial") or to the extrapolation
+    x0 + 2 d1 - d2 of the last two displacements ("extrapolation"), over the
+    node's motion scale."""
     rng = np.random.default_rng(seed)
     X, Y, W = [], [], []
     done = 0
@@ -106,16 +109,19 @@ def generate(frames: int, nodes_per_frame: int, seed: int, frames_per_run: int =
         # the 1M-tet pulls run over their ramp only: the benchmark's regime
         n_frames = min(boundary.ramp if kind == "box1m" else frames_per_run, frames - done)
         its = []
+        hist = [s.positions().astype(np.float64)] * 3  # the solver starts with zero displacement history
         for f in range(n_frames):
             if boundary is not None:
                 boundary(s, f)
             feats, xin, scale = s.warm_start_features()
             its.append(s.step(raise_on_error=False))
+            xs = s.positions()
+            x_base = xin if base == "inertial" else hist[-1] + 2.0 * (hist[-1] - hist[-2]) - (hist[-2] - hist[-3])
+            hist = hist[1:] + [xs.astype(np.float64)]
             if s.last_status != 0 or not s.stats()["converged"]:
                 continue
-            xs = s.positions()
             pick = rng.choice(free, size=min(nodes_per_frame, free.size), replace=False)
-            y = (xs[pick] - xin[pick]) / scale[pick, None]
+            y = ((xs[pick] - x_base[pick]) / scale[pick, None]).astype(np.float32)
             X.append(feats[pick])
             Y.append(y)
             # every frame weighs the same in relative terms: 1 / mean |y|^2
@@ -207,6 +213,8 @@ def main():
     ap.add_argument("--data-max", type=int, default=0, help="save at most this many samples (0 = all)")
     ap.add_argument("--from-data", default=None, help="fit to (X, Y, W) saved by --data instead of generating")
     ap.add_argument("--mix", default="0.7,0.2,0.1", help="fractions of box1m, box and ellipsoid runs")
+    ap.add_argument("--base", default="inertial", choices=("inertial", "extrapolation"),
+                    help="what the predicted correction is added to")
     args = ap.parse_args()
     t0 = time.time()
     if args.from_data:
@@ -214,7 +222,7 @@ def main():
             X, Y, W = z["X"], z["Y"], z["W"]
     else:
         X, Y, W = generate(args.frames, args.nodes_per_frame, args.seed,
-                           mix=tuple(float(v) for v in args.mix.split(",")))
+                           mix=tuple(float(v) for v in args.mix.split(",")), base=args.base)
     print(f"data: {X.shape[0]} samples in {time.time() - t0:.0f}s", flush=True)
     if args.data and not args.from_data:
         keep = np.arange(X.shape[0])
@@ -222,6 +230,7 @@ def main():
             keep = np.sort(np.random.default_rng(args.seed).choice(X.shape[0], args.data_max, replace=False))
         np.savez_compressed(args.data, X=X[keep], Y=Y[keep], W=W[keep])
     model = fit(X, Y, W, steps=args.steps, seed=args.seed)
+    model.base = args.base
     from .warmstart import DEFAULT_MODEL
     model.save(args.out or DEFAULT_MODEL)
     print(f"saved {args.out or DEFAULT_MODEL} ({time.time() - t0:.0f}s total)")

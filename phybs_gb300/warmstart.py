@@ -120,15 +120,20 @@ class WarmStartModel:
     feat_mean: np.ndarray
     feat_std: np.ndarray
     out_std: np.ndarray
+    # what the correction is added to: "inertial" (the plain guess) or
+    # "extrapolation" (u0 + 2 d1 - d2, the last two displacements)
+    base: str = "inertial"
 
     def save(self, path):
-        np.savez(path, theta=self.theta, feat_mean=self.feat_mean, feat_std=self.feat_std, out_std=self.out_std)
+        np.savez(path, theta=self.theta, feat_mean=self.feat_mean, feat_std=self.feat_std, out_std=self.out_std,
+                 base=np.array(self.base))
 
     @classmethod
     def load(cls, path):
         with np.load(path) as z:
+            base = str(z["base"]) if "base" in z.files else "inertial"
             return cls(z["theta"].astype(np.float32), z["feat_mean"].astype(np.float32),
-                       z["feat_std"].astype(np.float32), z["out_std"].astype(np.float32))
+                       z["feat_std"].astype(np.float32), z["out_std"].astype(np.float32), base)
 
 
 DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "warmstart_model.npz")

@@ -86,6 +86,44 @@ def test_zero_network_keeps_plain_result():
     b.close()
 
 
+def test_zero_network_on_extrapolation_base_is_the_extrapolation():
+    """With the extrapolation base (warm-start mode 2), a zero network's
+    candidate is u0 + 2 d1 - d2.  After three plain steps, the next step equals
+    the plain solver's started from that guess (pbs_set_guess) when the judge
+    keeps it, and the plain step when the judge (energy not higher and, for
+    this base, a smaller gradient norm) rejects it."""
+    m, x0, boundary = _pull_case()
+    theta = np.zeros(MLPTrainer(seed=0).n_params, np.float32)
+    model = WarmStartModel(theta, np.zeros(24, np.float32), np.ones(24, np.float32), np.ones(3, np.float32),
+                           base="extrapolation")
+    sv = [DescentSolver(m, positions=x0, params=residual_params()) for _ in range(3)]
+    hist = [sv[0].positions().astype(np.float64)] * 3
+    free = m.pin_mask() == 0
+    for f in range(3):
+        for s in sv:
+            boundary(s, f)
+            s.step()
+        hist = hist[1:] + [sv[0].positions().astype(np.float64)]
+    plain, guessed, learned = sv
+    learned.set_warm_start(model)
+    for s in sv:
+        boundary(s, 3)
+    _, xin, _ = guessed.warm_start_features()
+    guess = xin.copy()
+    extrap = hist[-1] + 2.0 * (hist[-1] - hist[-2]) - (hist[-2] - hist[-3])
+    guess[free] = extrap[free]
+    guessed.set_guess(guess.astype(np.float32))
+    ip, ig, il = plain.step(), guessed.step(), learned.step()
+    used = learned.stats()["warm_start_used"]
+    ref, iref = (guessed, ig) if used else (plain, ip)
+    if used:
+        assert guessed.stats()["warm_start_used"] == 1
+    assert abs(il - iref) <= 2, (used, il, iref)  # the two guesses agree to FP32 rounding
+    assert np.abs(learned.positions() - ref.positions()).max() <= 1e-5 * m.bbox_diagonal()
+    for s in sv:
+        s.close()
+
+
 def test_bad_prediction_falls_back():
     """A network that predicts a large wrong correction raises the energy; the
     judge rejects it and the step equals the plain one."""
