@@ -309,14 +309,19 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     __threadfence();
     // the instance's last chunk: fixed-order sums (two interleaved
     // accumulators a value), then accept / reject
-    double ea[2] = {0.0, 0.0}, eb[2] = {0.0, 0.0};
-    for (int j = cp->cblk_begin + threadIdx.x, q = 0; j < cp->cblk_end; j += THREADS, q ^= 1) {
+    double ea0 = 0.0, ea1 = 0.0, eb0 = 0.0, eb1 = 0.0;
+    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += 2 * THREADS) {
         const double2 v = __ldcg(st.cpart + j);
-        ea[q] += v.x;
-        eb[q] += v.y;
+        ea0 += v.x;
+        eb0 += v.y;
+        if (j + THREADS < cp->cblk_end) {
+            const double2 w = __ldcg(st.cpart + j + THREADS);
+            ea1 += w.x;
+            eb1 += w.y;
+        }
     }
-    const double E = block_sum(ea[0] + ea[1], sh);
-    const double E2 = block_sum(eb[0] + eb[1], sh);
+    const double E = block_sum(ea0 + ea1, sh);
+    const double E2 = block_sum(eb0 + eb1, sh);
     if (threadIdx.x != 0) return;
     InstCtl ci = *cp;  // one load, updates in registers, one store (as in the node kernel)
     ci.counter_t = 0;

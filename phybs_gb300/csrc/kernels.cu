@@ -221,8 +221,12 @@ struct PassCtx {
 
 // Jacobi step with Chebyshev extrapolation (or restore / save) of node i;
 // returns its |g|^2 (FP32: three positive squares).
+// NPRE: partials of the node loaded together with its state words (a node of
+// the 1M box touches 2-4 chunks of 256 tets; the rest cost one more round
+// trip).
+template <int NPRE>
 __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &p, const DevState &st, int i,
-                                             const NodeConst &in, const NodeIn &nn, const float4 &f0, const float4 &f1,
+                                             const NodeConst &in, const NodeIn &nn, const float4 (&f)[NPRE],
                                              const PassCtx &c) {
     float r2 = 0.f;
     if (in.info.z == 2.f) return r2;
@@ -245,18 +249,19 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
         }
         if (in.info.z == 0.f) {
             float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
-            // this node's per-chunk partial sums, in chunk order
-            fx += f0.x;
-            fy += f0.y;
-            fz += f0.z;
-            fx += f1.x;
-            fy += f1.y;
-            fz += f1.z;
-            for (int j = nn.pa + 2; j < nn.pe; ++j) {
-                const float4 f = st.part[j];
-                fx += f.x;
-                fy += f.y;
-                fz += f.z;
+            // this node's per-chunk partial sums, in chunk order (the first
+            // NPRE loaded with the state words, the rest here)
+#pragma unroll
+            for (int j = 0; j < NPRE; ++j) {
+                fx += f[j].x;
+                fy += f[j].y;
+                fz += f[j].z;
+            }
+            for (int j = nn.pa + NPRE; j < nn.pe; ++j) {
+                const float4 q = st.part[j];
+                fx += q.x;
+                fy += q.y;
+                fz += q.z;
             }
             if (c.do_h) {
                 for (int j = nn.pa; j < nn.pe; ++j) {
@@ -338,12 +343,13 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     pdl_wait();  // the chunk kernel's partials and decisions are visible from here
     // the state words and the first partials go out together with the
     // instance's control block: the pass's parity is known at launch
-    float4 f0[NPT], f1[NPT];
+    constexpr int NPRE = NPT == 1 ? 4 : 2;  // two nodes a thread: registers are short
+    float4 fp[NPT][NPRE];
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
         const int i = b * BLOCK + threadIdx.x + j * TH;
-        f0[j] = in[j].pa < in[j].pe ? st.part[in[j].pa] : z4;
-        f1[j] = in[j].pa + 1 < in[j].pe ? st.part[in[j].pa + 1] : z4;
+#pragma unroll
+        for (int q = 0; q < NPRE; ++q) fp[j][q] = in[j].pa + q < in[j].pe ? st.part[in[j].pa + q] : z4;
         in[j].uh = st.uh[cur + i];
         in[j].ul = st.ul[cur + i];
         in[j].dd = st.dd[cur + i];
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
         nc.tl = s_c[2][l];
         nc.bh = s_c[3][l];
         nc.bl = s_c[4][l];
-        r2 += node_update(m, p, st, b * BLOCK + l, nc, in[j], f0[j], f1[j], ctx);
+        r2 += node_update<NPRE>(m, p, st, b * BLOCK + l, nc, in[j], fp[j], ctx);
     }
     const float sr = block_sum_f(r2, sh);
     if (threadIdx.x == 0) {

@@ -875,7 +875,8 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
                                     {512, 2048, 832, 0}, {256, 640, 320, 0}, {256, 512, 256, 1},
                                     {256, 384, 208, 1},  {128, 256, 160, 1}, {128, 384, 208, 1},
                                     {256, 256, 160, 2},  {128, 256, 160, 2}, {256, 512, 256, 2},
-                                    {128, 128, 96, 2}};
+                                    {128, 128, 96, 2},   {128, 384, 208, 0}, {256, 384, 208, 0},
+                                    {128, 192, 128, 0},  {256, 256, 160, 0}};
     const int n = (int)(sizeof(shapes) / sizeof(shapes[0]));
     const bool can_stage = h->material == PBS_MATERIAL_NEOHOOKEAN;
     const int t0 = h->chunk_threads, c0 = h->chunk_tets, n0 = h->chunk_nodes, s0 = h->chunk_stage;

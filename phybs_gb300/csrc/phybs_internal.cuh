@@ -174,7 +174,12 @@ __device__ __host__ __forceinline__ void chebyshev_schedule(const DevParams &p, 
 #else
     omega = 4.0f / (4.0f - rho * rho * omega);
 #endif
-    for (int i = 0; i < p.n_profile; ++i) {
+    // a fixed trip count (n_profile <= 4): constant indices keep the kernel
+    // parameter's arrays out of local memory
+    bool hit = false;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (hit || i >= p.n_profile) continue;
         if (k == p.profile_k[i] - 1) { rho = 0.0f; omega = 1.0f; }
         if (k == p.profile_k[i]) {
             rho = p.profile_rho[i];
@@ -183,7 +188,7 @@ __device__ __host__ __forceinline__ void chebyshev_schedule(const DevParams &p, 
 #else
             omega = 2.0f / (2.0f - rho * rho);
 #endif
-            break;
+            hit = true;
         }
     }
 }
