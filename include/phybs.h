@@ -384,6 +384,58 @@ int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face)
  * (m: lumped mass, 1e8 for a pinned node). */
 int pbs_drag_face_ring(pbs_handle *h, int face, const float *drag, float *ext);
 
+/* ---- Strain-based position-based dynamics and projective dynamics ----
+ * The reference's two CPU integrators besides the descent, selected in
+ * fvm.cpp:162-171.  Both share positions and velocities with pbs_step; a step
+ * starts from the FP32 positions pbs_read_positions returns and stores the
+ * new ones exactly (up to the compensated split of the state). */
+
+/* PosBaseDynamic::doStepStrainConstraints (PosBaseDynamic.cpp:12-53) with
+ * solveStrainConstraints (:55-117), strain-based dynamics of Mueller et al.
+ * 2014:
+ *   p = x + dt (v + dt w f),  f = gravity + ext (3*N floats or NULL),
+ *   w = 1 / mass (0 at a pinned node);
+ *   `iterations` Gauss-Seidel sweeps over the tets in their caller order, each
+ *   tet projecting its six Green-strain constraints S_ij = f_i . f_j
+ *   (f_i = P Dm^-1 e_i, P the deformed edge matrix) onto S_ii = 1 (weight
+ *   stretch[i]) and S_ij = 0 (weight shear[i + j - 1]); a constraint whose
+ *   w-weighted gradient norm is below 1e-6 is skipped;
+ *   v = (p - x) 0.99 / dt,  x = p.
+ * The reference uses 5 sweeps, stretch = (1, 1, 1), shear = (0.8, 0.8, 0.8)
+ * (NULL selects these) and the viewer's time step.  The sweeps run on the
+ * device in the caller's tet order exactly: tets are grouped by dependency
+ * level (a tet's level is one more than that of the last earlier tet sharing
+ * a node), so a level's tets share no node and each sees precisely the
+ * updates of the tets before it.  The arithmetic is FP32 without contraction
+ * in the reference's operation order (the stretch multiplier in FP64, as the
+ * reference's double literal makes it), so a step equals the serial CPU
+ * sweep's bit for bit on the same rest data. */
+int pbs_pbd_step(pbs_handle *h, float dt, int iterations, const float *stretch, const float *shear,
+                 const float *ext);
+
+/* ProjDynamic::doProjDynamics (ProjDynamic.cpp:442-480) with its solver
+ * matrix (buildGlobalSolverMatrix, :48-100) and local projections
+ * (projectLocalConstraints2 on 4 threads, :351-434):
+ *   s = (x + dt v + dt^2 w f) m / dt^2   (f = gravity + ext, m the lumped
+ *        mass, 1e8 at a pinned node, w = 1 / m, 0 at a pinned node);
+ *   `iterations` times: R_t = U V^T of the SVD of each tet's F at the current
+ *   iterate p (JacobiSVD with det U, det V fixed by flipping the first,
+ *   largest-singular-value column: an inverted tet's R flips that direction),
+ *   b = s + sum_t k vol_t A_t^T R_t, and p = A^-1 b with
+ *   A = M / dt_m^2 + sum_t k vol_t A_t^T A_t (A_t maps corner positions to F);
+ *   v = (p - x) / dt 0.99,  x = p.
+ * The reference: k = 1e6, 5 iterations, dt = 0.03 for the right-hand side and
+ * the integrator's time step for A (dt_matrix; 0 takes dt), and an MKL
+ * Pardiso LDL^T factorisation of A.  Here A is assembled once per (dt_matrix,
+ * k) as block rows and each global step solves for the correction d of the
+ * current iterate p: r = b - A p (FP64 accumulation), A d = r by block-Jacobi
+ * preconditioned conjugate gradients until (e^T D^-1 e)^1/2 <= tol
+ * (r^T D^-1 r)^1/2 for the CG residual e, or max_cg iterations
+ * (PBS_E_ITER_CAP, the state advanced), then p += d.  cg_iters_out: total CG
+ * iterations of the step (may be NULL). */
+int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int iterations, const float *ext,
+                float tol, int max_cg, int *cg_iters_out);
+
 #ifdef __cplusplus
 }
 #endif

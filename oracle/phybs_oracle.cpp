@@ -750,4 +750,121 @@ int orc_node_eval(int prec, int material, int hessian_closed, int n, const doubl
     return 0;
 }
 
+// Rest data in FP32 exactly as TetMesh::initModel forms it (TetMesh.cpp:186-216)
+// with Eigen 3.2's 3x3 determinant (row-0 cofactor expansion, Determinant.h)
+// and inverse (adjugate of the column-0 cofactors times 1 / det,
+// Inverse.h:117-159): Dm^-1 row-major (9T), inverse masses (N; 0 when
+// pinned) and gravity_y = -gravity * lumped mass (N).
+static inline float eig_cof(const float m[3][3], int i, int j) {
+    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+    return m[i1][j1] * m[i2][j2] - m[i1][j2] * m[i2][j1];
+}
+
+int orc_rest_eigen32(int n, const float *pos, int t, const int *tets, float density, float gravity,
+                     const int *pin_mask, float *dinv9, float *inv_mass, float *grav_y) {
+    std::vector<float> mass(n, 0.0f);
+    for (int i = 0; i < t; ++i) {
+        const int *q = tets + 4 * (size_t)i;
+        float m[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) m[r][c] = pos[3 * (size_t)q[c + 1] + r] - pos[3 * (size_t)q[0] + r];
+        const float det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                          m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                          m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        const float vol = (float)((double)std::fabs(det) / 6.0);
+        const float w = (float)((double)vol / 4.0 * (double)density);
+        for (int c = 0; c < 4; ++c) mass[q[c]] += w;
+        const float c0[3] = {eig_cof(m, 0, 0), eig_cof(m, 1, 0), eig_cof(m, 2, 0)};
+        const float d = c0[0] * m[0][0] + (c0[1] * m[1][0] + c0[2] * m[2][0]);
+        const float inv = 1.0f / d;
+        float *o = dinv9 + 9 * (size_t)i;
+        for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 3; ++k) o[3 * r + k] = (r == 0 ? c0[k] : eig_cof(m, k, r)) * inv;
+    }
+    for (int i = 0; i < n; ++i) {
+        grav_y[i] = -gravity * mass[i];
+        inv_mass[i] = pin_mask[i] ? 0.0f : (float)(1.0 / (double)mass[i]);
+    }
+    return 0;
+}
+
+// Strain-based position-based dynamics, FP32 in the reference's operation
+// order (this file is built with -ffp-contract=off):
+// PosBaseDynamic::doStepStrainConstraints (PosBaseDynamic.cpp:12-53) and
+// solveStrainConstraints (:55-117).  Eigen 3.2 evaluates a 3x3 * 3x1 product
+// as ((a0 b0 + a1 b1) + a2 b2) (CoeffBasedProduct.h) and a 3-vector dot or
+// squaredNorm as x0 + (x1 + x2) (redux_novec_unroller's halving).
+// dinv9: Dm^-1 row-major per tet; pos, vel: 3n in/out.
+static inline float pbd_dot3(const float *a, const float *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+
+static void pbd_tet(const float *p[4], const float w[4], const float *D, const float *stretch, const float *shear,
+                    float eps, float dp[4][3]) {
+    std::memset(dp, 0, sizeof(float) * 12);
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j <= i; ++j) {
+            float P[3][3];  // P(r, c): column c = (p_{c+1} + dp_{c+1}) - (p_0 + dp_0)
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) P[r][c] = (p[c + 1][r] + dp[c + 1][r]) - (p[0][r] + dp[0][r]);
+            float fi[3], fj[3];
+            for (int r = 0; r < 3; ++r) {
+                fi[r] = (P[r][0] * D[3 * 0 + i] + P[r][1] * D[3 * 1 + i]) + P[r][2] * D[3 * 2 + i];
+                fj[r] = (P[r][0] * D[3 * 0 + j] + P[r][1] * D[3 * 1 + j]) + P[r][2] * D[3 * 2 + j];
+            }
+            const float Sij = pbd_dot3(fi, fj);
+            float d[4][3] = {{0.f, 0.f, 0.f}};
+            for (int k = 0; k < 3; ++k) {
+                for (int r = 0; r < 3; ++r) {
+                    d[k + 1][r] = fj[r] * D[3 * k + i] + fi[r] * D[3 * k + j];
+                    d[0][r] -= d[k + 1][r];
+                }
+            }
+            float lambda = w[0] * pbd_dot3(d[0], d[0]) + w[1] * pbd_dot3(d[1], d[1]) + w[2] * pbd_dot3(d[2], d[2]) +
+                           w[3] * pbd_dot3(d[3], d[3]);
+            if (lambda < eps) continue;
+            if (i == j)
+                lambda = (float)(((double)Sij - 1.0) / (double)lambda * (double)stretch[i]);
+            else
+                lambda = Sij / lambda * shear[i + j - 1];
+            for (int c = 0; c < 4; ++c) {
+                const float s = lambda * w[c];
+                for (int r = 0; r < 3; ++r) dp[c][r] -= s * d[c][r];
+            }
+        }
+    }
+}
+
+int orc_pbd_step(int n, int t, const int *tets, const float *dinv9, const float *inv_mass, const float *forces,
+                 float dt, int iters, const float *stretch, const float *shear, float eps, float *pos, float *vel) {
+    std::vector<float> p(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const float s = dt * inv_mass[i];
+        for (int r = 0; r < 3; ++r) {
+            const size_t k = 3 * (size_t)i + r;
+            p[k] = pos[k] + dt * (vel[k] + s * forces[k]);
+        }
+    }
+    for (int it = 0; it < iters; ++it) {
+        for (int j = 0; j < t; ++j) {
+            const int *q = tets + 4 * (size_t)j;
+            float cp[4][3];
+            const float *pp[4];
+            float w[4];
+            for (int c = 0; c < 4; ++c) {
+                for (int r = 0; r < 3; ++r) cp[c][r] = p[3 * (size_t)q[c] + r];
+                pp[c] = cp[c];
+                w[c] = inv_mass[q[c]];
+            }
+            float dp[4][3];
+            pbd_tet(pp, w, dinv9 + 9 * (size_t)j, stretch, shear, eps, dp);
+            for (int c = 0; c < 4; ++c)
+                for (int r = 0; r < 3; ++r) p[3 * (size_t)q[c] + r] += dp[c][r];
+        }
+    }
+    for (size_t k = 0; k < 3 * (size_t)n; ++k) {
+        vel[k] = (p[k] - pos[k]) * 0.99f / dt;
+        pos[k] = p[k];
+    }
+    return 0;
+}
+
 }  // extern "C"

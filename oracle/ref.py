@@ -35,13 +35,18 @@ def lib():
         _lib.ref_create_faces.restype = C.c_void_p
         _lib.ref_total_energy.restype = C.c_float
         _lib.ref_ext_energy.restype = C.c_float
+        _lib.ref_pd_create.restype = C.c_void_p
+        _lib.ref_pd_create.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        _lib.ref_pd_destroy.argtypes = [C.c_void_p]
+        _lib.ref_pd_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float]
+        _lib.ref_pbd_step.argtypes = [C.c_void_p, C.c_float]
         for name in ["ref_destroy", "ref_set_h", "ref_set_profile", "ref_set_lame", "ref_get_lame", "ref_get_rest",
                      "ref_get_nodes", "ref_set_nodes", "ref_get_vel", "ref_set_vel", "ref_get_vel_old",
                      "ref_set_vel_old", "ref_set_ext", "ref_get_mass", "ref_get_gravity", "ref_get_vol",
                      "ref_get_dminv", "ref_get_an", "ref_force_nh", "ref_force_stretch", "ref_elastic_energy",
                      "ref_hessian_diag", "ref_element_stiffness", "ref_total_energy", "ref_csr_sizes", "ref_csr",
                      "ref_step", "ref_get_scalars", "ref_face_ring_size", "ref_face_ring", "ref_pick_face",
-                     "ref_drag_face_ring", "ref_get_ext"]:
+                     "ref_drag_face_ring", "ref_get_ext", "ref_get_inv_mass"]:
             getattr(_lib, name).argtypes = None
     return _lib
 
@@ -72,6 +77,7 @@ class RefSim:
         self.h = C.c_void_p(h)
 
     def close(self):
+        self._pd_close()
         if self.h:
             lib().ref_destroy(self.h)
             self.h = None
@@ -208,3 +214,27 @@ class RefSim:
         out = np.zeros(5, np.float32)
         lib().ref_get_scalars(self.h, _p(out))
         return dict(zip(["alpha", "energy", "energy_old", "rho", "omega"], out.tolist()))
+
+    # -- position-based and projective dynamics (PosBaseDynamic.cpp, ProjDynamic.cpp)
+    def inv_mass(self):
+        return self._get("ref_get_inv_mass", (self.n,))
+
+    def pbd_step(self, dt):
+        """One doStepStrainConstraints step on the mesh's nodes and velocities."""
+        lib().ref_pbd_step(self.h, dt)
+
+    def pd_step(self, dt, dt_matrix=None, iterations=5):
+        """One doProjDynamics step; the integrator (and its factorised solver
+        matrix) is built on first use for (dt_matrix, iterations)."""
+        key = (dt if dt_matrix is None else dt_matrix, iterations)
+        if getattr(self, "_pd_key", None) != key:
+            self._pd_close()
+            self._pd = C.c_void_p(lib().ref_pd_create(self.h, key[0], key[1]))
+            self._pd_key = key
+        lib().ref_pd_step(self._pd, self.h, dt)
+
+    def _pd_close(self):
+        if getattr(self, "_pd", None):
+            lib().ref_pd_destroy(self._pd)
+            self._pd = None
+            self._pd_key = None

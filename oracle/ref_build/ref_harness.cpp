@@ -2,8 +2,9 @@
 //
 // TEST INFRASTRUCTURE ONLY.  This file is compiled together with the
 // unmodified reference sources FVM/TetMesh.cpp, FVM/IsotropicMaterial.cpp,
-// FVM/IsotropicNeohookeanMaterial.cpp and FVM/DescentOptimize.cpp (read in
-// place from the reference tree by oracle/ref_build/Makefile) into
+// FVM/IsotropicNeohookeanMaterial.cpp, FVM/DescentOptimize.cpp,
+// FVM/PosBaseDynamic.cpp and FVM/ProjDynamic.cpp (read in place from the
+// reference tree by oracle/ref_build/Makefile) into
 // oracle/_ref/libphybs_ref.so.  It is the parity anchor for the restated
 // oracle (oracle/phybs_oracle.cpp) and the generator of tests/golden fixtures.
 //
@@ -37,6 +38,8 @@
 #include "TetMesh.h"
 #include "IsotropicNeohookeanMaterial.h"
 #include "DescentOptimize.h"
+#include "PosBaseDynamic.h"
+#include "ProjDynamic.h"
 #undef private
 #undef protected
 
@@ -292,6 +295,42 @@ void ref_get_ext(void *h, float *out) {
 float ref_ext_energy(void *h, const float *pos) {
     RefSim *s = S(h);
     return s->mesh->computeExternalForcesEnergy(as_pos(pos, s->mesh->getNodesNum()));
+}
+
+// Inverse lumped masses (0 at a pinned node; TetMesh.cpp:207-215).
+void ref_get_inv_mass(void *h, float *out) {
+    auto &m = S(h)->mesh->getInvMasses();
+    std::memcpy(out, m.data(), sizeof(float) * m.size());
+}
+
+// One strain-based PBD step as the viewer runs it (fvm.cpp:162-165): forces =
+// TetMesh::computeExternalForces() (gravity + external + pin springs), then
+// PosBaseDynamic::doStepStrainConstraints on the mesh's nodes and velocities.
+void ref_pbd_step(void *h, float dt) {
+    TetMesh *m = S(h)->mesh.get();
+    PosBaseDynamic pbd(m->getNodes(), m->getTetsNum());
+    Eigen::MatrixXf f = m->computeExternalForces();
+    pbd.doStepStrainConstraints(m->getNodes(), m->getVelocities(), f, m->getDmInvs(), m->getTets(),
+                                m->getInvMasses(), dt);
+}
+
+// Projective dynamics (ProjDynamic.cpp): the integrator object, its solver
+// matrix for time step dt_matrix (FVM::SetTypeComputing, fvm.cpp:300-307) and
+// one doProjDynamics step at dt with `iterations` local/global iterations
+// (the reference's 5; fvm.cpp:167-170 passes dt = 0.03).
+void *ref_pd_create(void *h, float dt_matrix, int iterations) {
+    TetMesh *m = S(h)->mesh.get();
+    ProjDynamic *pd = new ProjDynamic(S(h)->mesh);
+    pd->m_iterations = iterations;
+    pd->buildGlobalSolverMatrix(m->getMasses(), m->getTets(), dt_matrix, m->getDmInvs());
+    return pd;
+}
+void ref_pd_destroy(void *pd) { delete static_cast<ProjDynamic *>(pd); }
+void ref_pd_step(void *pd, void *h, float dt) {
+    TetMesh *m = S(h)->mesh.get();
+    static_cast<ProjDynamic *>(pd)->doProjDynamics(m->getNodes(), m->getVelocities(), m->getMasses(),
+                                                   m->getInvMasses(), m->getTets(), dt, m->getDmInvs(),
+                                                   m->computeExternalForces());
 }
 
 }  // extern "C"

@@ -120,6 +120,7 @@ public:
     void start() {}
     int restart() { return 0; }
     long long elapsed() const { return 0; }
+    void invalidate() {}
 };
 
 // Types named only by RenderWidget.h's class declaration (never instantiated).

@@ -1,0 +1,502 @@
+// The reference's two other CPU integrators, on the device:
+//
+// Strain-based position-based dynamics (PosBaseDynamic.cpp:12-117, Mueller et
+// al. 2014): Gauss-Seidel sweeps over the tets in the caller's order.  A
+// serial sweep is reproduced exactly by dependency levels: a tet's level is
+// one more than the highest level of the earlier tets that share one of its
+// nodes, so a level's tets share no node and each reads exactly the updates of
+// the tets before it in the serial order.  One thread-block cluster sweeps an
+// instance level by level, the cluster barrier ordering the levels (its
+// arrive/wait carry release/acquire semantics for the global positions):
+// 2,320 levels of ~430 tets for the 1M-tet box, 920 for the 24K bar.  The
+// arithmetic is FP32 with every product and sum rounded separately (no
+// contraction) in Eigen 3.2's order, so a sweep is the CPU's bit for bit.
+//
+// Projective dynamics (ProjDynamic.cpp:48-100, 351-480): per-tet polar
+// rotations from the modified SVD, a fixed-order gather of the right-hand
+// side, and the constant global matrix A = L (x) I3.  A and b are of the size
+// of the inertial term M p / dt^2 (positions, not displacements), so each
+// global solve is a correction: r = b - A p with FP64 accumulation, A d = r by
+// the block-Jacobi conjugate gradients of the backward-Euler step (relative to
+// r, in FP32), p += d.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "../../include/phybs.h"
+#include "phybs_internal.cuh"
+#include "tet_math.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pbs {
+
+namespace {
+
+constexpr int kPbdCluster = 8;
+constexpr int kPbdThreads = 128;
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+// Eigen 3.2's 3-vector dot / squaredNorm: x0 + (x1 + x2)
+__device__ __forceinline__ float dot3e(const float a[3], const float b[3]) {
+    return fadd(fmul(a[0], b[0]), fadd(fmul(a[1], b[1]), fmul(a[2], b[2])));
+}
+
+// float(((double)S - 1.0) / (double)lam * (double)k): the reference's stretch
+// multiplier, whose double literal makes it FP64 (PosBaseDynamic.cpp:100).
+// GB300's FP64 pipe is narrow, so the value is formed in double-float FP32
+// (error below 2^-45 relative) and rounded; the FP64 expression is evaluated
+// only when that value lies within 2^-40 relative of a float rounding
+// boundary, where the two roundings could differ (or for zero, non-finite or
+// tiny values).
+__device__ __forceinline__ float pbd_stretch_mult(float S, float lam, float k) {
+    float ah, al;
+    two_sum(S, -1.0f, ah, al);  // S - 1 = ah + al exactly
+    if (ah == 0.0f && al == 0.0f) return fmul(0.0f, k);
+    const float q1 = __fdiv_rn(ah, lam);
+    const float r = fadd(__fmaf_rn(-q1, lam, ah), al);  // the remainder (exact) plus al
+    const float q2 = __fdiv_rn(r, lam);
+    const float p1 = fmul(q1, k);
+    const float p2 = __fmaf_rn(q2, k, __fmaf_rn(q1, k, -p1));  // q1 k - p1 is exact
+    const float c = fadd(p1, p2);
+    const float d = fadd(fsub(p1, c), p2);  // (p1 + p2) - c
+    const float ac = fabsf(c);
+    if (ac < 1e-30f || ac > 1e30f || !isfinite(ac))
+        return __double2float_rn(__dmul_rn(__ddiv_rn(__dsub_rn((double)S, 1.0), (double)lam), (double)k));
+    // the float boundary on d's side of c: half the gap to the neighbour
+    const float away = __int_as_float(__float_as_int(ac) + 1), toward = __int_as_float(__float_as_int(ac) - 1);
+    const float half = ((d >= 0.0f) == (c >= 0.0f)) ? 0.5f * (away - ac) : 0.5f * (ac - toward);
+    if (fabsf(d) + ac * 0x1p-40f < half) return c;
+    return __double2float_rn(__dmul_rn(__ddiv_rn(__dsub_rn((double)S, 1.0), (double)lam), (double)k));
+}
+
+struct PbdConst {
+    float stretch[3], shear[3], eps;
+};
+
+// solveStrainConstraints (PosBaseDynamic.cpp:55-117) for one tet: p[c].xyz
+// the corner positions, p[c].w the inverse masses, D = Dm^-1 row-major.
+__device__ __forceinline__ void pbd_project(const float4 p[4], const float D[9], const PbdConst &k, float dp[4][3]) {
+    const float pw[4] = {p[0].w, p[1].w, p[2].w, p[3].w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) dp[c][0] = dp[c][1] = dp[c][2] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+            const float x0[3] = {fadd(p[0].x, dp[0][0]), fadd(p[0].y, dp[0][1]), fadd(p[0].z, dp[0][2])};
+            float P[3][3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float4 &q = p[c + 1];
+                P[0][c] = fsub(fadd(q.x, dp[c + 1][0]), x0[0]);
+                P[1][c] = fsub(fadd(q.y, dp[c + 1][1]), x0[1]);
+                P[2][c] = fsub(fadd(q.z, dp[c + 1][2]), x0[2]);
+            }
+            float fi[3], fj[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                fi[r] = fadd(fadd(fmul(P[r][0], D[i]), fmul(P[r][1], D[3 + i])), fmul(P[r][2], D[6 + i]));
+                fj[r] = fadd(fadd(fmul(P[r][0], D[j]), fmul(P[r][1], D[3 + j])), fmul(P[r][2], D[6 + j]));
+            }
+            const float S = dot3e(fi, fj);
+            float d[4][3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) d[0][r] = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    d[kk + 1][r] = fadd(fmul(fj[r], D[3 * kk + i]), fmul(fi[r], D[3 * kk + j]));
+                    d[0][r] = fsub(d[0][r], d[kk + 1][r]);
+                }
+            float lam = fmul(pw[0], dot3e(d[0], d[0]));
+            lam = fadd(lam, fmul(pw[1], dot3e(d[1], d[1])));
+            lam = fadd(lam, fmul(pw[2], dot3e(d[2], d[2])));
+            lam = fadd(lam, fmul(pw[3], dot3e(d[3], d[3])));
+            if (lam < k.eps) continue;
+            if (i == j) lam = pbd_stretch_mult(S, lam, k.stretch[i]);
+            else lam = fmul(__fdiv_rn(S, lam), k.shear[i + j - 1]);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float s = fmul(lam, pw[c]);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) dp[c][r] = fsub(dp[c][r], fmul(s, d[c][r]));
+            }
+        }
+    }
+}
+
+// One cluster per group of levels (an instance): `iterations` sweeps over its
+// levels; a level's tets are split into kPbdCluster contiguous runs, one per
+// CTA.  Positions are read through L2 (ld.global.cg); the cluster barrier
+// orders one level's writes before the next level's reads.
+__global__ void __cluster_dims__(kPbdCluster, 1, 1) __launch_bounds__(kPbdThreads)
+    k_pbd_sweep(PbdView v, int iterations, PbdConst k) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int g = blockIdx.x / kPbdCluster;
+    const int rank = (int)cl.block_rank();
+    const int l0 = v.grp[g], l1 = v.grp[g + 1];
+    for (int it = 0; it < iterations; ++it) {
+        for (int l = l0; l < l1; ++l) {
+            const int a = v.lvl[l], e = v.lvl[l + 1];
+            const int chunk = (e - a + kPbdCluster - 1) / kPbdCluster;
+            const int b0 = a + rank * chunk, b1 = min(b0 + chunk, e);
+            for (int j = b0 + (int)threadIdx.x; j < b1; j += kPbdThreads) {
+                const int4 q = __ldg(v.tet + j);
+                const float4 r0 = __ldg(v.d0 + j), r1 = __ldg(v.d1 + j), r2 = __ldg(v.d2 + j);
+                const float D[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+                const int id[4] = {q.x, q.y, q.z, q.w};
+                float4 p[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) p[c] = __ldcg(v.px + id[c]);
+                float dp[4][3];
+                pbd_project(p, D, k, dp);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    v.px[id[c]] = make_float4(fadd(p[c].x, dp[c][0]), fadd(p[c].y, dp[c][1]), fadd(p[c].z, dp[c][2]),
+                                              p[c].w);
+            }
+            cl.sync();
+        }
+    }
+}
+
+// slot of column `target` in block row [b, e) (columns ascending), e if absent
+__device__ __forceinline__ int col_slot(const int *col, int b, int e, int target) {
+    int lo = b, hi = e;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (col[mid] < target) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < e && col[lo] == target) ? lo : e;
+}
+
+// 1 / lumped mass as the reference forms it (1.0 / m: an FP64 quotient
+// rounded to FP32, TetMesh.cpp:209), 0 at a pinned node
+__device__ __forceinline__ float inv_mass_of(const float4 &info) {
+    return info.z == 1.f ? 0.f : __double2float_rn(__ddiv_rn(1.0, (double)info.x));
+}
+
+__device__ __forceinline__ float4 state_pos4(const DevMesh &m, const DevState &st, int i) {
+    const float4 X = m.rest[i], h = st.u0h[i], l = st.u0l[i];
+    return make_float4(state_position(X.x, h.x, l.x), state_position(X.y, h.y, l.y), state_position(X.z, h.z, l.z),
+                       0.f);
+}
+
+// f = gravity + ext of a node (the caller's forces; the pin spring that
+// TetMesh::computeExternalForces puts on a pinned node is multiplied by its
+// zero inverse mass in both integrators)
+__device__ __forceinline__ float3 node_force(const float4 &info, const float4 *ext, int i) {
+    float3 f = make_float3(0.f, info.y, 0.f);
+    if (ext) {
+        const float4 e = ext[i];
+        f = make_float3(fadd(f.x, e.x), fadd(f.y, e.y), fadd(f.z, e.z));
+    }
+    return f;
+}
+
+// ---- the PBD step's rest data, formed exactly as TetMesh::initModel does in
+// FP32 (TetMesh.cpp:186-216) with Eigen 3.2's 3x3 determinant (row-0
+// cofactor expansion) and inverse (adjugate of the column-0 cofactors times
+// 1 / det): the sweeps then see the reference's own Dm^-1 and masses.
+__device__ __forceinline__ float eig_cof(const float m[3][3], int i, int j) {
+    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+    return fsub(fmul(m[i1][j1], m[i2][j2]), fmul(m[i1][j2], m[i2][j1]));
+}
+
+// level-ordered tet j (padded tet order[j]): Dm^-1 rows, and its lumped-mass
+// share vol / 4 * density by padded tet
+__global__ void k_pbd_rest(DevMesh m, const int *order, int n, float density, float4 *d0, float4 *d1, float4 *d2,
+                           float *share) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int tp = order[j];
+    const int4 q = m.tets[tp];
+    const float4 X0 = m.rest[q.x], X1 = m.rest[q.y], X2 = m.rest[q.z], X3 = m.rest[q.w];
+    const float m_[3][3] = {{fsub(X1.x, X0.x), fsub(X2.x, X0.x), fsub(X3.x, X0.x)},
+                            {fsub(X1.y, X0.y), fsub(X2.y, X0.y), fsub(X3.y, X0.y)},
+                            {fsub(X1.z, X0.z), fsub(X2.z, X0.z), fsub(X3.z, X0.z)}};
+    const float det = fadd(fsub(fmul(m_[0][0], fsub(fmul(m_[1][1], m_[2][2]), fmul(m_[1][2], m_[2][1]))),
+                                fmul(m_[0][1], fsub(fmul(m_[1][0], m_[2][2]), fmul(m_[1][2], m_[2][0])))),
+                           fmul(m_[0][2], fsub(fmul(m_[1][0], m_[2][1]), fmul(m_[1][1], m_[2][0]))));
+    const float vol = __double2float_rn(__ddiv_rn((double)fabsf(det), 6.0));
+    share[tp] = __double2float_rn(__dmul_rn(__ddiv_rn((double)vol, 4.0), (double)density));
+    const float c0[3] = {eig_cof(m_, 0, 0), eig_cof(m_, 1, 0), eig_cof(m_, 2, 0)};
+    const float d = fadd(fmul(c0[0], m_[0][0]), fadd(fmul(c0[1], m_[1][0]), fmul(c0[2], m_[2][0])));
+    const float inv = __fdiv_rn(1.0f, d);
+    d0[j] = make_float4(fmul(c0[0], inv), fmul(c0[1], inv), fmul(c0[2], inv), 0.f);
+    d1[j] = make_float4(fmul(eig_cof(m_, 0, 1), inv), fmul(eig_cof(m_, 1, 1), inv), fmul(eig_cof(m_, 2, 1), inv), 0.f);
+    d2[j] = make_float4(fmul(eig_cof(m_, 0, 2), inv), fmul(eig_cof(m_, 1, 2), inv), fmul(eig_cof(m_, 2, 2), inv), 0.f);
+}
+
+// per node: lumped mass summed in tet order, {1 / mass (FP64 quotient
+// rounded; 0 when pinned), -gravity * mass}
+__global__ void k_pbd_mass(DevMesh m, const float *share, float gravity, float2 *node) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const float4 info = m.info[i];
+    if (info.z == 2.f) { node[i] = make_float2(0.f, 0.f); return; }
+    float s = 0.f;
+    for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) s = fadd(s, share[m.inc[j] >> 2]);
+    node[i] = make_float2(info.z == 1.f ? 0.f : __double2float_rn(__ddiv_rn(1.0, (double)s)), fmul(-gravity, s));
+}
+
+// p = x + dt (v + (dt w) f), px = (p, w), x0 = x (PosBaseDynamic.cpp:24-30);
+// node = {w, gravity_y} of the PBD rest data
+__global__ void k_pbd_begin(DevMesh m, DevState st, const float2 *node, const float4 *ext, float dt, float4 *px,
+                            float4 *x0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const float4 info = m.info[i];
+    if (info.z == 2.f) { px[i] = x0[i] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
+    const float4 x = state_pos4(m, st, i), v = st.v[i];
+    const float2 nd = node[i];
+    const float w = nd.x, s = fmul(dt, w);
+    float3 f = make_float3(0.f, nd.y, 0.f);
+    if (ext) {
+        const float4 e = ext[i];
+        f = make_float3(fadd(f.x, e.x), fadd(f.y, e.y), fadd(f.z, e.z));
+    }
+    px[i] = make_float4(fadd(x.x, fmul(dt, fadd(v.x, fmul(s, f.x)))), fadd(x.y, fmul(dt, fadd(v.y, fmul(s, f.y)))),
+                        fadd(x.z, fmul(dt, fadd(v.z, fmul(s, f.z)))), w);
+    x0[i] = x;
+}
+
+// x = p and v = ((p - x) 0.99) / dt (PosBaseDynamic.cpp:51-52), or, with
+// divide_first, ((p - x) / dt) 0.99 (ProjDynamic.cpp:477-478); the state keeps
+// p - X exactly as (hi, lo)
+__global__ void k_dyn_end(DevMesh m, DevState st, const float4 *px, const float4 *x0, float dt, int divide_first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np || m.info[i].z == 2.f) return;
+    const float4 p = px[i], x = x0[i], X = m.rest[i];
+    const float c = 0.99f;
+    float3 v;
+    if (divide_first)
+        v = make_float3(fmul(__fdiv_rn(fsub(p.x, x.x), dt), c), fmul(__fdiv_rn(fsub(p.y, x.y), dt), c),
+                        fmul(__fdiv_rn(fsub(p.z, x.z), dt), c));
+    else
+        v = make_float3(__fdiv_rn(fmul(fsub(p.x, x.x), c), dt), __fdiv_rn(fmul(fsub(p.y, x.y), c), dt),
+                        __fdiv_rn(fmul(fsub(p.z, x.z), c), dt));
+    float h[3], l[3];
+    two_sum(p.x, -X.x, h[0], l[0]);
+    two_sum(p.y, -X.y, h[1], l[1]);
+    two_sum(p.z, -X.z, h[2], l[2]);
+    st.u0h[i] = make_float4(h[0], h[1], h[2], 0.f);
+    st.u0l[i] = make_float4(l[0], l[1], l[2], 0.f);
+    st.v[i] = make_float4(v.x, v.y, v.z, 0.f);
+}
+
+// ---------------------------------------------------------------- projective dynamics
+// Row i of A = M / dt_m^2 + sum_t k vol_t (w_a . w_b) I3 as 3x3 blocks (the
+// off-diagonal dofs zero), in the node's incidence order; D^-1 = 1 / a_ii.
+__global__ void __launch_bounds__(128) k_pd_assemble(DevMesh m, BsrView A, float inv_dt2, float stiffness,
+                                                     float *dinv9) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const int rb = A.ptr[i], re = A.ptr[i + 1];
+    float *row = A.val + 9 * (size_t)rb;
+    for (int k = 0; k < 9 * (re - rb); ++k) row[k] = 0.f;
+    const float4 info = m.info[i];
+    if (info.z != 2.f) {
+        for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+            const int ent = m.inc[j], t = ent >> 2, c = ent & 3;
+            const int4 q = m.tets[t];
+            const int qn[4] = {q.x, q.y, q.z, q.w};
+            const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+            const float w[4][3] = {{-(r0.x + r1.x + r2.x), -(r0.y + r1.y + r2.y), -(r0.z + r1.z + r2.z)},
+                                   {r0.x, r0.y, r0.z},
+                                   {r1.x, r1.y, r1.z},
+                                   {r2.x, r2.y, r2.z}};
+            const float kv = stiffness * fabsf(r0.w);
+            for (int cc = 0; cc < 4; ++cc) {
+                const int sl = col_slot(A.col, rb, re, qn[cc]);
+                if (sl == re) continue;  // (the pattern holds every tet's node pairs)
+                const float g = kv * (w[c][0] * w[cc][0] + w[c][1] * w[cc][1] + w[c][2] * w[cc][2]);
+                float *blk = row + 9 * (sl - rb);
+                blk[0] += g;
+                blk[4] += g;
+                blk[8] += g;
+            }
+        }
+    }
+    const int dsl = col_slot(A.col, rb, re, i);
+    float inv = 0.f;
+    if (dsl < re) {
+        float *d = row + 9 * (dsl - rb);
+        const float md = info.z == 2.f ? 1.f : info.x * inv_dt2;
+        d[0] += md;
+        d[4] += md;
+        d[8] += md;
+        inv = 1.f / d[0];
+    }
+    for (int k = 0; k < 9; ++k) dinv9[9 * (size_t)i + k] = (k % 4 == 0) ? inv : 0.f;
+}
+
+// s = (x + dt v + (dt^2 w) f) m / dt^2 (ProjDynamic.cpp:447-463); p = x0 = x
+__global__ void k_pd_begin(DevMesh m, DevState st, const float4 *ext, float dt, float4 *s, float4 *px, float4 *x0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    const float4 info = m.info[i];
+    if (info.z == 2.f) {
+        s[i] = px[i] = x0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 x = state_pos4(m, st, i), v = st.v[i];
+    const float dt2 = fmul(dt, dt), a = fmul(dt2, inv_mass_of(info)), mm = info.x;
+    const float3 f = node_force(info, ext, i);
+    const float sx = fadd(fadd(x.x, fmul(dt, v.x)), fmul(a, f.x));
+    const float sy = fadd(fadd(x.y, fmul(dt, v.y)), fmul(a, f.y));
+    const float sz = fadd(fadd(x.z, fmul(dt, v.z)), fmul(a, f.z));
+    s[i] = make_float4(__fdiv_rn(fmul(sx, mm), dt2), __fdiv_rn(fmul(sy, mm), dt2), __fdiv_rn(fmul(sz, mm), dt2), 0.f);
+    px[i] = x;
+    x0[i] = x;
+}
+
+// Per tet: R = U V^T with JacobiSVD's determinant fix (first, largest
+// columns negated), i.e. U diag(sg, 1, sg) V^T of the modified SVD
+// (sg = sign of the smallest singular value); corner a's projection
+// k vol R w_a into its gather slot.
+__global__ void __launch_bounds__(128) k_pd_local(DevMesh m, const float4 *px, float stiffness, float4 *slot) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.Tp) return;
+    const int4 q = m.tets[t];
+    if (q.x < 0) return;
+    const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
+    const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    const float4 x0 = px[q.x], x1 = px[q.y], x2 = px[q.z], x3 = px[q.w];
+    const float ds[3][3] = {{x1.x - x0.x, x2.x - x0.x, x3.x - x0.x},
+                            {x1.y - x0.y, x2.y - x0.y, x3.y - x0.y},
+                            {x1.z - x0.z, x2.z - x0.z, x3.z - x0.z}};
+    float G[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            G[3 * r + c] = ds[r][0] * dinv[c] + ds[r][1] * dinv[3 + c] + ds[r][2] * dinv[6 + c] - (r == c ? 1.f : 0.f);
+    float U[9], sv[3], V[9], sign3;
+    svd_disp<float, 4>(G, U, sv, V, sign3);
+    const float sg = sign3 < 0.f ? -1.f : 1.f;
+    float R[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) R[3 * r + c] = sg * U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + sg * U[3 * r + 2] * V[3 * c + 2];
+    const float kv = stiffness * fabsf(r0.w);
+    const float w[4][3] = {{-(r0.x + r1.x + r2.x), -(r0.y + r1.y + r2.y), -(r0.z + r1.z + r2.z)},
+                           {r0.x, r0.y, r0.z},
+                           {r1.x, r1.y, r1.z},
+                           {r2.x, r2.y, r2.z}};
+    const int4 sl = m.tslot[t];
+    const int sls[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        slot[sls[a]] = make_float4(kv * (R[0] * w[a][0] + R[1] * w[a][1] + R[2] * w[a][2]),
+                                   kv * (R[3] * w[a][0] + R[4] * w[a][1] + R[5] * w[a][2]),
+                                   kv * (R[6] * w[a][0] + R[7] * w[a][1] + R[8] * w[a][2]), 0.f);
+    }
+}
+
+// b = s + the node's projections in incidence order (ascending tet, as the
+// reference's m_proj_idx lists them)
+__global__ void k_pd_rhs(DevMesh m, const float4 *s, const float4 *slot, float4 *b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np) return;
+    float4 a = s[i];
+    for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
+        const float4 c = slot[j];
+        a.x += c.x;
+        a.y += c.y;
+        a.z += c.z;
+    }
+    b[i] = a;
+}
+
+// r = b - A p with FP64 accumulation (b and A p are both of the size of the
+// inertial term M p / dt^2 and cancel to the size of the step's change), the
+// correction d = 0
+__global__ void k_pd_residual(int Np, BsrView A, float4 *b, const float4 *p, float4 *d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Np) return;
+    const float4 bi = b[i];
+    double rx = bi.x, ry = bi.y, rz = bi.z;
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+        const float *a = A.val + 9 * (size_t)k;
+        const float4 v = p[A.col[k]];
+        rx -= (double)a[0] * v.x + (double)a[1] * v.y + (double)a[2] * v.z;
+        ry -= (double)a[3] * v.x + (double)a[4] * v.y + (double)a[5] * v.z;
+        rz -= (double)a[6] * v.x + (double)a[7] * v.y + (double)a[8] * v.z;
+    }
+    b[i] = make_float4((float)rx, (float)ry, (float)rz, 0.f);
+    d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_pd_apply(int Np, float4 *p, const float4 *d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Np) return;
+    const float4 a = p[i], c = d[i];
+    p[i] = make_float4(a.x + c.x, a.y + c.y, a.z + c.z, a.w);
+}
+
+}  // namespace
+
+cudaError_t launch_pd_residual(cudaStream_t s, int Np, const BsrView &A, float4 *b, const float4 *p, float4 *d) {
+    k_pd_residual<<<(Np + 255) / 256, 256, 0, s>>>(Np, A, b, p, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pd_apply(cudaStream_t s, int Np, float4 *p, const float4 *d) {
+    k_pd_apply<<<(Np + 255) / 256, 256, 0, s>>>(Np, p, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pbd_rest(cudaStream_t s, const DevMesh &m, const int *order, int n, float density, float gravity,
+                            float4 *d0, float4 *d1, float4 *d2, float *share, float2 *node) {
+    if (n > 0) k_pbd_rest<<<(n + 127) / 128, 128, 0, s>>>(m, order, n, density, d0, d1, d2, share);
+    k_pbd_mass<<<(m.Np + 255) / 256, 256, 0, s>>>(m, share, gravity, node);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pbd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float2 *node,
+                             const float4 *ext, float dt, float4 *px, float4 *x0) {
+    k_pbd_begin<<<(m.Np + 255) / 256, 256, 0, s>>>(m, st, node, ext, dt, px, x0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pbd_sweeps(cudaStream_t s, const PbdView &v, int n_groups, int iterations, const float stretch[3],
+                              const float shear[3]) {
+    PbdConst k;
+    for (int i = 0; i < 3; ++i) { k.stretch[i] = stretch[i]; k.shear[i] = shear[i]; }
+    k.eps = 1e-6f;
+    k_pbd_sweep<<<n_groups * kPbdCluster, kPbdThreads, 0, s>>>(v, iterations, k);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dyn_end(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *px, const float4 *x0,
+                           float dt, int divide_first) {
+    k_dyn_end<<<(m.Np + 255) / 256, 256, 0, s>>>(m, st, px, x0, dt, divide_first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pd_assemble(cudaStream_t s, const DevMesh &m, const BsrView &A, float dt_matrix, float stiffness,
+                               float *dinv9) {
+    k_pd_assemble<<<(m.Np + 127) / 128, 128, 0, s>>>(m, A, 1.f / (dt_matrix * dt_matrix), stiffness, dinv9);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *ext, float dt,
+                            float4 *rhs0, float4 *px, float4 *x0) {
+    k_pd_begin<<<(m.Np + 255) / 256, 256, 0, s>>>(m, st, ext, dt, rhs0, px, x0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pd_local(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float4 *slot,
+                            const float4 *rhs0, float4 *b) {
+    k_pd_local<<<(m.Tp + 127) / 128, 128, 0, s>>>(m, px, stiffness, slot);
+    k_pd_rhs<<<(m.Np + 255) / 256, 256, 0, s>>>(m, rhs0, slot, b);
+    return cudaGetLastError();
+}
+
+}  // namespace pbs

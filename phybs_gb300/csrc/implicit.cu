@@ -201,10 +201,11 @@ __device__ __forceinline__ void block_sums(double a0, double a1, double a2, int 
     }
 }
 
-// r = b - A x, z = D^-1 r, p = z; partial r.z, r.r, b.b
+// r = b - A x, z = D^-1 r, p = z; partial r.z, r.r and b.b (pnorm = 0) or
+// b.D^-1 b (pnorm = 1, the preconditioned norm)
 __global__ void __launch_bounds__(kThreads) k_cg_init(int Np, BsrView A, const float *dinv9, const float4 *b,
                                                       const float4 *x, float4 *r, float4 *z, float4 *p,
-                                                      double *part) {
+                                                      double *part, int pnorm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0, bb = 0.0;
     if (i < Np) {
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int Np, BsrView A, const f
         p[i] = zi;
         rz = dot4(ri, zi);
         rr = dot4(ri, ri);
-        bb = dot4(bi, bi);
+        bb = pnorm ? dot4(bi, block_apply(dinv9 + 9 * (size_t)i, bi)) : dot4(bi, bi);
     }
     block_sums(rz, rr, bb, 3, part, gridDim.x);
 }
@@ -267,9 +268,10 @@ __global__ void __launch_bounds__(kThreads) k_cg_direction(int Np, const float4 
 }
 
 // The scalars of one CG stage from the block partials, summed in block order
-// by one CTA.  stage 0: after init; 1: alpha = rz / pq; 2: beta, convergence.
+// by one CTA.  stage 0: after init; 1: alpha = rz / pq; 2: beta, convergence
+// (|r|^2 <= tol2 |b|^2, or r.D^-1 r <= tol2 b.D^-1 b when pnorm).
 __global__ void __launch_bounds__(kThreads) k_cg_scalars(int nblk, const double *part, CgState *cs, int stage,
-                                                         double tol2, int max_iters) {
+                                                         double tol2, int max_iters, int pnorm) {
     __shared__ double sh[3][kThreads / 32];
     const int nv = stage == 1 ? 1 : (stage == 0 ? 3 : 2);
     if (cs->done && stage != 0) return;
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_scalars(int nblk, const double 
         c.iters = 0;
         c.status = PBS_OK;
         c.done = 0;
-        if (!(s[1] <= tol2 * s[2])) {
+        if (!((pnorm ? s[0] : s[1]) <= tol2 * s[2])) {
             if (!isfinite(s[1])) { c.status = PBS_E_NONFINITE; c.done = 1; }
         } else {
             c.done = 1;  // the initial guess already solves it
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_scalars(int nblk, const double 
         c.rz = s[0];
         c.rr = s[1];
         if (!isfinite(s[1])) { c.status = PBS_E_NONFINITE; c.done = 1; }
-        else if (s[1] <= tol2 * c.bb) c.done = 1;
+        else if ((pnorm ? s[0] : s[1]) <= tol2 * c.bb) c.done = 1;
         else if (c.iters >= max_iters) { c.status = PBS_E_ITER_CAP; c.done = 1; }
     }
 }
@@ -345,21 +347,22 @@ cudaError_t launch_be_assemble(cudaStream_t s, const DevMesh &m, const DevState 
 }
 
 cudaError_t launch_cg_init(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, const float4 *b,
-                           const float4 *x, float4 *r, float4 *z, float4 *p, double *part, CgState *cs, double tol2) {
+                           const float4 *x, float4 *r, float4 *z, float4 *p, double *part, CgState *cs, double tol2,
+                           int pnorm) {
     const int g = cg_blocks(Np);
-    k_cg_init<<<g, kThreads, 0, s>>>(Np, A, dinv9, b, x, r, z, p, part);
-    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 0, tol2, 0);
+    k_cg_init<<<g, kThreads, 0, s>>>(Np, A, dinv9, b, x, r, z, p, part, pnorm);
+    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 0, tol2, 0, pnorm);
     return cudaGetLastError();
 }
 
 cudaError_t launch_cg_iteration(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, float4 *x, float4 *r,
                                 float4 *z, float4 *p, float4 *q, double *part, CgState *cs, double tol2,
-                                int max_iters) {
+                                int max_iters, int pnorm) {
     const int g = cg_blocks(Np);
     k_cg_spmv<<<g, kThreads, 0, s>>>(Np, A, p, q, part, cs);
-    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 1, tol2, max_iters);
+    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 1, tol2, max_iters, pnorm);
     k_cg_update<<<g, kThreads, 0, s>>>(Np, dinv9, p, q, x, r, z, part, cs);
-    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 2, tol2, max_iters);
+    k_cg_scalars<<<1, kThreads, 0, s>>>(g, part, cs, 2, tol2, max_iters, pnorm);
     k_cg_direction<<<g, kThreads, 0, s>>>(Np, z, p, cs);
     return cudaGetLastError();
 }

@@ -538,9 +538,9 @@ __global__ void k_pack_positions(DevMesh m, const float4 *uh, const float4 *ul, 
     const int u = pad2user[i];
     if (u < 0) return;
     const float4 X = m.rest[i], h = uh[i], l = ul[i];
-    dst[3 * (size_t)u] = X.x + (h.x + l.x);
-    dst[3 * (size_t)u + 1] = X.y + (h.y + l.y);
-    dst[3 * (size_t)u + 2] = X.z + (h.z + l.z);
+    dst[3 * (size_t)u] = state_position(X.x, h.x, l.x);
+    dst[3 * (size_t)u + 1] = state_position(X.y, h.y, l.y);
+    dst[3 * (size_t)u + 2] = state_position(X.z, h.z, l.z);
 }
 
 // u = x - X exactly as (hi, lo)

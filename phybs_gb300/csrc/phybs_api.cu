@@ -95,6 +95,20 @@ struct pbs_handle {
     DevBuf<float> npartf;
     DevBuf<InstCtl> ctl;
     DevBuf<int> active;
+    // strain-based PBD (levels built on first use) and projective dynamics
+    // (its matrix built per (dt_matrix, stiffness)); dyn_* are their per-step
+    // positions, start positions and right-hand-side base
+    std::vector<int> h_inst_tets;  // per instance: first, end padded tet
+    bool pbd_ready = false;
+    int pbd_groups = 0;
+    DevBuf<int> pbd_grp, pbd_lvl;
+    DevBuf<int4> pbd_tet;
+    DevBuf<float4> pbd_d0, pbd_d1, pbd_d2;
+    DevBuf<float2> pbd_node;  // {1 / mass, gravity_y} of the PBD rest data
+    bool pd_ready = false;
+    float pd_dtm = 0.f, pd_k = 0.f;
+    DevBuf<float> pd_val, pd_dinv;
+    DevBuf<float4> dyn_px, dyn_x0, dyn_s;
     // host pinned
     int *h_active = nullptr;   // 2 slots
     InstCtl *h_ctl = nullptr;
@@ -148,6 +162,10 @@ struct pbs_handle {
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release();
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
+        pbd_grp.release(); pbd_lvl.release(); pbd_tet.release(); pbd_d0.release(); pbd_d1.release(); pbd_d2.release();
+        pbd_node.release();
+        pd_val.release(); pd_dinv.release(); dyn_px.release(); dyn_x0.release(); dyn_s.release();
+        pbd_ready = pd_ready = false;
         DevBuf<float4> *cv[] = {&cg_b, &cg_x, &cg_r, &cg_z, &cg_p, &cg_q};
         for (auto b : cv) b->release();
         if (h_cg) cudaFreeHost(h_cg);
@@ -349,6 +367,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         ctl[b].nblk_end = pn / BLOCK; ctl[b].tblk_end = pt / BLOCK;
         ctl[b].rho = 0.f; ctl[b].omega = 1.f; ctl[b].alpha = h->params.alpha0;
         for (int i = nptr[b]; i < nptr[b + 1]; ++i) h->user2pad[i] = node_off[b] + (i - nptr[b]);
+        h->h_inst_tets.push_back(ctl[b].tet_begin);
+        h->h_inst_tets.push_back(ctl[b].tet_end);
     }
     const int Np = pn, Tp = pt;
     for (int b = 0; b < B; ++b) {  // mean edge length: cbrt(6 * mean |vol|)
@@ -1153,6 +1173,163 @@ int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, co
     CK(cudaStreamSynchronize(s));
     h->guess_pending = false;
     return c.done ? c.status : PBS_E_ITER_CAP;
+}
+
+// ---- strain-based PBD and projective dynamics
+
+// Levels of the caller's tet order per instance (a tet one level above the
+// last earlier tet touching any of its nodes), the level-ordered tets, and
+// the step's rest data formed as the reference forms it (launch_pbd_rest).
+static int ensure_pbd(pbs_handle *h) {
+    if (h->pbd_ready) return PBS_OK;
+    const int B = h->B, Tp = h->Tp;
+    std::vector<int> level(Tp, -1), last(h->Np, -1), grp(B + 1, 0), nlev(B, 0);
+    for (int b = 0; b < B; ++b) {
+        int top = -1;
+        for (int tp = h->h_inst_tets[2 * b]; tp < h->h_inst_tets[2 * b + 1]; ++tp) {
+            const int4 q = h->h_tets_pad[tp];
+            if (q.x < 0) continue;
+            const int l = 1 + std::max(std::max(last[q.x], last[q.y]), std::max(last[q.z], last[q.w]));
+            level[tp] = l;
+            last[q.x] = last[q.y] = last[q.z] = last[q.w] = l;
+            top = std::max(top, l);
+        }
+        nlev[b] = top + 1;
+        grp[b + 1] = grp[b] + nlev[b];
+    }
+    const int L = grp[B];
+    std::vector<int> lvl(L + 1, 0);
+    for (int b = 0; b < B; ++b)
+        for (int tp = h->h_inst_tets[2 * b]; tp < h->h_inst_tets[2 * b + 1]; ++tp)
+            if (level[tp] >= 0) lvl[grp[b] + level[tp] + 1]++;
+    for (int l = 0; l < L; ++l) lvl[l + 1] += lvl[l];
+    const int n = lvl[L];
+    std::vector<int> fill(lvl.begin(), lvl.end() - 1), order(std::max(n, 1));
+    for (int b = 0; b < B; ++b)
+        for (int tp = h->h_inst_tets[2 * b]; tp < h->h_inst_tets[2 * b + 1]; ++tp)
+            if (level[tp] >= 0) order[fill[grp[b] + level[tp]]++] = tp;
+    std::vector<int4> tet(std::max(n, 1));
+    for (int j = 0; j < n; ++j) tet[j] = h->h_tets_pad[order[j]];
+    const size_t nn = (size_t)std::max(n, 1);
+    CK(h->pbd_grp.alloc(B + 1)); CK(h->pbd_lvl.alloc(L + 1)); CK(h->pbd_tet.alloc(nn));
+    CK(h->pbd_d0.alloc(nn)); CK(h->pbd_d1.alloc(nn)); CK(h->pbd_d2.alloc(nn)); CK(h->pbd_node.alloc(h->Np));
+    CK(cudaMemcpy(h->pbd_grp.p, grp.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->pbd_lvl.p, lvl.data(), sizeof(int) * (L + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->pbd_tet.p, tet.data(), sizeof(int4) * n, cudaMemcpyHostToDevice));
+    DevBuf<int> ord;  // level order -> padded tet, needed only here
+    CK(ord.alloc(nn));
+    cudaError_t e = cudaMemcpy(ord.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = launch_pbd_rest(h->stream, h->mesh(), ord.p, n, h->density, h->gravity, h->pbd_d0.p, h->pbd_d1.p,
+                            h->pbd_d2.p, h->staging2.p, h->pbd_node.p);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    ord.release();
+    CK(e);
+    h->pbd_groups = B;
+    h->pbd_ready = true;
+    return PBS_OK;
+}
+
+static int ensure_dyn_buffers(pbs_handle *h) {
+    if (h->dyn_px.p) return PBS_OK;
+    CK(h->dyn_px.alloc(h->Np)); CK(h->dyn_x0.alloc(h->Np)); CK(h->dyn_s.alloc(h->Np));
+    return PBS_OK;
+}
+
+static bool finite_n(const float *v, int n) {
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+int pbs_pbd_step(pbs_handle *h, float dt, int iterations, const float *stretch, const float *shear,
+                 const float *ext) {
+    if (!h || !(dt > 0.f) || !std::isfinite(dt) || iterations < 0 || (stretch && !finite_n(stretch, 3)) ||
+        (shear && !finite_n(shear, 3)))
+        return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_pbd(h);
+    if (rc == PBS_OK) rc = ensure_dyn_buffers(h);
+    if (rc == PBS_OK && ext) rc = upload_user(h, ext, h->ext.p);
+    if (rc != PBS_OK) return rc;
+    const float st_def[3] = {1.f, 1.f, 1.f}, sh_def[3] = {0.8f, 0.8f, 0.8f};
+    cudaStream_t s = h->stream;
+    const DevMesh m = h->mesh();
+    const DevState st = h->state();
+    CK(launch_pbd_begin(s, m, st, h->pbd_node.p, ext ? h->ext.p : nullptr, dt, h->dyn_px.p, h->dyn_x0.p));
+    if (iterations > 0) {
+        PbdView v;
+        v.grp = h->pbd_grp.p; v.lvl = h->pbd_lvl.p; v.tet = h->pbd_tet.p;
+        v.d0 = h->pbd_d0.p; v.d1 = h->pbd_d1.p; v.d2 = h->pbd_d2.p; v.px = h->dyn_px.p;
+        CK(launch_pbd_sweeps(s, v, h->pbd_groups, iterations, stretch ? stretch : st_def, shear ? shear : sh_def));
+    }
+    CK(launch_dyn_end(s, m, st, h->dyn_px.p, h->dyn_x0.p, dt, 0));
+    CK(cudaStreamSynchronize(s));
+    h->guess_pending = false;
+    return PBS_OK;
+}
+
+int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int iterations, const float *ext,
+                float tol, int max_cg, int *cg_iters_out) {
+    if (!h || !(dt > 0.f) || !std::isfinite(dt) || !(dt_matrix >= 0.f) || !std::isfinite(dt_matrix) ||
+        !(stiffness > 0.f) || !std::isfinite(stiffness) || iterations < 0 || !(tol > 0.f) || max_cg <= 0)
+        return PBS_E_INVALID_ARG;
+    CK(cudaSetDevice(h->device));
+    const float dtm = dt_matrix > 0.f ? dt_matrix : dt;
+    int rc = ensure_bsr(h);
+    if (rc == PBS_OK) rc = ensure_dyn_buffers(h);
+    if (rc == PBS_OK && ext) rc = upload_user(h, ext, h->ext.p);
+    if (rc != PBS_OK) return rc;
+    cudaStream_t s = h->stream;
+    const DevMesh m = h->mesh();
+    const DevState st = h->state();
+    BsrView A;
+    A.ptr = h->bsr_ptr.p;
+    A.col = h->bsr_col.p;
+    if (!h->pd_val.p) {
+        int nnzb = 0;
+        CK(cudaMemcpy(&nnzb, h->bsr_ptr.p + h->Np, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(h->pd_val.alloc(9 * (size_t)nnzb));
+        CK(h->pd_dinv.alloc(9 * (size_t)h->Np));
+    }
+    A.val = h->pd_val.p;
+    if (!h->pd_ready || h->pd_dtm != dtm || h->pd_k != stiffness) {
+        CK(launch_pd_assemble(s, m, A, dtm, stiffness, h->pd_dinv.p));
+        h->pd_ready = true;
+        h->pd_dtm = dtm;
+        h->pd_k = stiffness;
+    }
+    CK(launch_pd_begin(s, m, st, ext ? h->ext.p : nullptr, dt, h->dyn_s.p, h->dyn_px.p, h->dyn_x0.p));
+    const double tol2 = (double)tol * (double)tol;
+    int total = 0, status = PBS_OK;
+    for (int it = 0; it < iterations; ++it) {
+        CK(launch_pd_local(s, m, h->dyn_px.p, stiffness, reinterpret_cast<float4 *>(h->tf.p), h->dyn_s.p,
+                           h->cg_b.p));
+        CK(launch_pd_residual(s, h->Np, A, h->cg_b.p, h->dyn_px.p, h->cg_x.p));
+        CK(launch_cg_init(s, h->Np, A, h->pd_dinv.p, h->cg_b.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
+                          h->cg_part.p, h->cg_state.p, tol2, 1));
+        for (int k0 = 0; k0 < max_cg; k0 += 16) {
+            for (int k = 0; k < 16 && k0 + k < max_cg; ++k)
+                CK(launch_cg_iteration(s, h->Np, A, h->pd_dinv.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
+                                       h->cg_q.p, h->cg_part.p, h->cg_state.p, tol2, max_cg, 1));
+            CK(cudaMemcpyAsync(h->h_cg, h->cg_state.p, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (h->h_cg->done) break;
+        }
+        const CgState c = *h->h_cg;
+        total += c.iters;
+        if (c.status == PBS_E_NONFINITE) {
+            if (cg_iters_out) *cg_iters_out = total;
+            return PBS_E_NONFINITE;  // the state is left as it was
+        }
+        if (!c.done || c.status == PBS_E_ITER_CAP) status = PBS_E_ITER_CAP;
+        CK(launch_pd_apply(s, h->Np, h->dyn_px.p, h->cg_x.p));
+    }
+    CK(launch_dyn_end(s, m, st, h->dyn_px.p, h->dyn_x0.p, dt, 1));
+    CK(cudaStreamSynchronize(s));
+    h->guess_pending = false;
+    if (cg_iters_out) *cg_iters_out = total;
+    return status;
 }
 
 int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {

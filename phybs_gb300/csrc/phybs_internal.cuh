@@ -293,12 +293,45 @@ int cg_blocks(int Np);
 cudaError_t launch_be_assemble(cudaStream_t s, const DevMesh &m, const DevState &st, int material, const BsrView &A,
                                float dt, float alpha, float beta, const float4 *ext, float4 *b, float4 *x,
                                float *dinv9);
+// pnorm: stop on the preconditioned norm r.D^-1 r <= tol2 b.D^-1 b instead
+// of |r|^2 <= tol2 |b|^2 (rows of very different scale, e.g. pinned nodes'
+// 1e8 masses)
 cudaError_t launch_cg_init(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, const float4 *b,
-                           const float4 *x, float4 *r, float4 *z, float4 *p, double *part, CgState *cs, double tol2);
+                           const float4 *x, float4 *r, float4 *z, float4 *p, double *part, CgState *cs, double tol2,
+                           int pnorm = 0);
 cudaError_t launch_cg_iteration(cudaStream_t s, int Np, const BsrView &A, const float *dinv9, float4 *x, float4 *r,
                                 float4 *z, float4 *p, float4 *q, double *part, CgState *cs, double tol2,
-                                int max_iters);
+                                int max_iters, int pnorm = 0);
 cudaError_t launch_be_finish(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *x, float dt);
+
+// Strain-based PBD schedule: levels of mutually node-disjoint tets in the
+// caller's order; group g (an instance) sweeps levels grp[g] .. grp[g+1]-1,
+// level l holds tets lvl[l] .. lvl[l+1]-1 of the level-ordered copies.
+struct PbdView {
+    const int *grp, *lvl;
+    const int4 *tet;              // padded node ids
+    const float4 *d0, *d1, *d2;   // rows of Dm^-1
+    float4 *px;                   // positions; .w = inverse mass
+};
+// The PBD rest data as the reference forms it in FP32: Dm^-1 rows of the
+// level-ordered tets (order[j] = padded tet) and per node {1 / mass (0 when
+// pinned), -gravity * mass}; share: scratch of Tp floats.
+cudaError_t launch_pbd_rest(cudaStream_t s, const DevMesh &m, const int *order, int n, float density, float gravity,
+                            float4 *d0, float4 *d1, float4 *d2, float *share, float2 *node);
+cudaError_t launch_pbd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float2 *node,
+                             const float4 *ext, float dt, float4 *px, float4 *x0);
+cudaError_t launch_pbd_sweeps(cudaStream_t s, const PbdView &v, int n_groups, int iterations, const float stretch[3],
+                              const float shear[3]);
+cudaError_t launch_dyn_end(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *px, const float4 *x0,
+                           float dt, int divide_first);
+cudaError_t launch_pd_assemble(cudaStream_t s, const DevMesh &m, const BsrView &A, float dt_matrix, float stiffness,
+                               float *dinv9);
+cudaError_t launch_pd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *ext, float dt,
+                            float4 *rhs0, float4 *px, float4 *x0);
+cudaError_t launch_pd_residual(cudaStream_t s, int Np, const BsrView &A, float4 *b, const float4 *p, float4 *d);
+cudaError_t launch_pd_apply(cudaStream_t s, int Np, float4 *p, const float4 *d);
+cudaError_t launch_pd_local(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float4 *slot,
+                            const float4 *rhs0, float4 *b);
 
 struct HandleView {
     int device;

@@ -18,6 +18,7 @@
 
 #include "../../include/phybs.h"
 #include "phybs_internal.cuh"
+#include "tet_math.cuh"
 
 namespace pbs {
 
@@ -25,11 +26,11 @@ namespace {
 
 constexpr int kPickThreads = 256;
 
-// The caller-visible position of padded node i: rest + (u hi + u lo), the
-// value pbs_read_positions returns.
+// The caller-visible position of padded node i (the value
+// pbs_read_positions returns).
 __device__ __forceinline__ float3 node_pos(const DevMesh &m, const float4 *uh, const float4 *ul, int i) {
     const float4 X = m.rest[i], h = uh[i], l = ul[i];
-    return make_float3(X.x + (h.x + l.x), X.y + (h.y + l.y), X.z + (h.z + l.z));
+    return make_float3(state_position(X.x, h.x, l.x), state_position(X.y, h.y, l.y), state_position(X.z, h.z, l.z));
 }
 
 __device__ __forceinline__ float3 sub3(float3 a, float3 b) {

@@ -398,6 +398,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     const float bb = __fsub_rn(s, a);
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
+// The FP32 position of a node whose state is rest X plus displacement
+// hi + lo, rounded once (the three terms summed in FP64 first): exactly the
+// position a caller uploaded, whose displacement was split exactly.
+__device__ __forceinline__ float state_position(float X, float hi, float lo) {
+    return __double2float_rn(__dadd_rn(__dadd_rn((double)X, (double)hi), (double)lo));
+}
 // (hi, lo) + b, renormalised so that |lo| <= ulp(hi) / 2.
 __device__ __forceinline__ void add_comp(float &hi, float &lo, float b) {
     float s, e;

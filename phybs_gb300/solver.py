@@ -211,6 +211,31 @@ class DescentSolver:
         self.last_status = rc
         return it.value, res.value
 
+    # -- strain-based PBD and projective dynamics (PosBaseDynamic.cpp, ProjDynamic.cpp) --
+    def pbd_step(self, dt: float = 0.03, iterations: int = 5, stretch=None, shear=None, ext=None):
+        """One PosBaseDynamic::doStepStrainConstraints step (defaults: the
+        reference's 5 sweeps, stretch 1, shear 0.8), bit-identical to the
+        serial CPU sweep on the same rest data."""
+        st = _f32(stretch, (3,)) if stretch is not None else None
+        sh = _f32(shear, (3,)) if shear is not None else None
+        e = _f32(ext, (-1, 3)) if ext is not None else None
+        L.check(L.lib().pbs_pbd_step(self._h, C.c_float(dt), C.c_int(iterations), _ptr(st), _ptr(sh), _ptr(e)),
+                "pbs_pbd_step")
+
+    def pd_step(self, dt: float = 0.03, dt_matrix: float = 0.0, stiffness: float = 1e6, iterations: int = 5,
+                ext=None, tol: float = 1e-6, max_cg: int = 20000, raise_on_cap: bool = True) -> int:
+        """One ProjDynamic::doProjDynamics step (defaults: the reference's
+        stiffness 1e6, 5 local/global iterations, A formed with dt); returns
+        the step's total CG iterations."""
+        it = C.c_int()
+        e = _f32(ext, (-1, 3)) if ext is not None else None
+        rc = L.lib().pbs_pd_step(self._h, C.c_float(dt), C.c_float(dt_matrix), C.c_float(stiffness),
+                                 C.c_int(iterations), _ptr(e), C.c_float(tol), C.c_int(max_cg), C.byref(it))
+        if rc != L.PBS_OK and (raise_on_cap or rc != L.PBS_E_ITER_CAP):
+            L.check(rc, "pbs_pd_step")
+        self.last_status = rc
+        return it.value
+
     # -- surface picking and drag forces (TetMesh.cpp:229-277, 378-418, 446-470) --
     def set_surface(self, faces):
         """Boundary triangles (F, 3) in caller node ids, e.g. load_tetgen_faces()."""

@@ -11,7 +11,9 @@ deformed probe state (IsotropicNeohookeanMaterial.cpp:135-173,
 IsotropicMaterial.cpp:360-409, 503-682), the stiffness CSR pattern
 (IsotropicMaterial.cpp:554-644) for small meshes, and the node positions and
 velocities after successive DescentOptimize::doDescentOpt steps
-(DescentOptimize.cpp:146-243).  Meshes are the procedural workloads of the
+(DescentOptimize.cpp:146-243); and, in separate fixtures, the surface
+picking / drag, element stiffness and PBD / projective-dynamics outputs.
+Meshes are the procedural workloads of the
 benchmark configurations, at fixture-friendly sizes, plus two of the
 reference's own tetgen meshes.
 """
@@ -177,8 +179,65 @@ def make_stiffness(name, cfg, rng, n_sample=64):
     print(name, len(sample), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def inverted_positions(rest, tets, pins, rng, n_nodes=3):
+    """Rest positions with a few interior free nodes moved 2 edge lengths in
+    random directions: the incident tets on that side invert (det F < 0)."""
+    x = rest.astype(np.float64).copy()
+    edge = float(np.median(np.linalg.norm(rest[tets[:, 1]] - rest[tets[:, 0]], axis=1)))
+    pinned = set(int(p) for p in pins)
+    counts = np.bincount(tets.reshape(-1), minlength=len(rest))
+    cand = [i for i in np.argsort(-counts) if int(i) not in pinned][: 4 * n_nodes]
+    for i in rng.choice(cand, size=n_nodes, replace=False):
+        d = rng.normal(size=3)
+        x[i] += 2.0 * edge * d / np.linalg.norm(d)
+    return x.astype(np.float32)
+
+
+def make_dynamics(name, cfg, rng, pbd_steps=3, pd_steps=2, dt=0.03):
+    """The reference's strain-based PBD (PosBaseDynamic.cpp:12-117) and
+    projective dynamics (ProjDynamic.cpp:48-100, 351-480, with Eigen's
+    SimplicialLDLT standing in for MKL Pardiso) trajectories from a twisted
+    state, the first step with external forces on a few nodes, plus one
+    projective step from a state with inverted tets; with the reference's rest
+    data (Dm^-1 row-major, inverse masses, volumes)."""
+    m = cfg["mesh"]
+    sim = REF.RefSim(m.rest, m.tets, m.pins, float(m.young[0]), float(m.poisson[0]), density=m.density)
+    rest = sim.rest()
+    edge = float(np.median(np.linalg.norm(rest[m.tets[:, 1]] - rest[m.tets[:, 0]], axis=1)))
+    x0 = M.twist_positions(rest, cfg["probe_twist"] / 2, axis=twist_axis(rest))
+    x0 = (x0 + rng.normal(0.0, 0.02 * edge, x0.shape)).astype(np.float32)
+    x0[m.pins] = rest[m.pins]
+    free = np.setdiff1d(np.arange(len(rest)), m.pins)
+    ext = np.zeros_like(rest)
+    pull = rng.choice(free, size=min(6, len(free)), replace=False)
+    ext[pull] = rng.normal(0.0, 0.05, (len(pull), 3)).astype(np.float32)
+    out = dict(rest=rest, tets=m.tets, pins=m.pins, dminv=sim.dminv(), inv_mass=sim.inv_mass(), mass=sim.mass(),
+               vol=sim.vol(), gravity=sim.gravity(), x0=x0, ext=ext, dt=np.float32(dt))
+    zero = np.zeros_like(rest)
+    for kind, steps in (("pbd", pbd_steps), ("pd", pd_steps)):
+        sim.set_nodes(x0)
+        sim.set_vel(zero)
+        for k in range(steps):
+            sim.set_ext(ext if k == 0 else zero)
+            if kind == "pbd":
+                sim.pbd_step(dt)
+            else:
+                sim.pd_step(dt)
+            out[f"x_{kind}{k}"], out[f"v_{kind}{k}"] = sim.nodes(), sim.vel()
+    xi = inverted_positions(rest, m.tets, m.pins, rng)
+    assert (M.signed_volumes(xi, m.tets) < 0).any()
+    sim.set_nodes(xi)
+    sim.set_vel(zero)
+    sim.set_ext(zero)
+    sim.pd_step(dt)
+    out.update(x_inv=xi, x_pd_inv=sim.nodes(), v_pd_inv=sim.vel())
+    sim.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, len(rest), len(m.tets), os.path.getsize(os.path.join(HERE, name + ".npz")))
+
+
 if __name__ == "__main__":
-    # `make_golden.py surface` / `make_golden.py stiffness` write only those fixtures
+    # `make_golden.py surface|stiffness|dynamics` write only those fixtures
     only = sys.argv[1] if len(sys.argv) > 1 else None
     rng = np.random.default_rng(20261203)
     if only is None:
@@ -193,3 +252,8 @@ if __name__ == "__main__":
         all_cases = cases()
         for n in ("bar_small", "model_bar", "ellipsoid_small"):
             make_stiffness("stiffness_" + n, all_cases[n], krng)
+    if only in (None, "dynamics"):
+        drng = np.random.default_rng(20261206)
+        all_cases = cases()
+        for n in ("bar_small", "model_bar", "ellipsoid_small"):
+            make_dynamics("dynamics_" + n, all_cases[n], drng)
