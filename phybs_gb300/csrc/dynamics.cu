@@ -128,38 +128,75 @@ __device__ __forceinline__ void pbd_project(const float4 p[4], const float D[9],
     }
 }
 
+// A level-ordered tet's static record (ids, Dm^-1 rows).
+struct PbdTet {
+    int4 q;
+    float4 r0, r1, r2;
+};
+
+__device__ __forceinline__ PbdTet pbd_load(const PbdView &v, int j) {
+    PbdTet t;
+    t.q = __ldg(v.tet + j);
+    t.r0 = __ldg(v.d0 + j);
+    t.r1 = __ldg(v.d1 + j);
+    t.r2 = __ldg(v.d2 + j);
+    return t;
+}
+
+__device__ __forceinline__ void pbd_apply(const PbdView &v, const PbdTet &t, const PbdConst &k) {
+    const float D[9] = {t.r0.x, t.r0.y, t.r0.z, t.r1.x, t.r1.y, t.r1.z, t.r2.x, t.r2.y, t.r2.z};
+    const int id[4] = {t.q.x, t.q.y, t.q.z, t.q.w};
+    float4 p[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) p[c] = __ldcg(v.px + id[c]);
+    float dp[4][3];
+    pbd_project(p, D, k, dp);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        v.px[id[c]] = make_float4(fadd(p[c].x, dp[c][0]), fadd(p[c].y, dp[c][1]), fadd(p[c].z, dp[c][2]), p[c].w);
+}
+
 // One cluster per group of levels (an instance): `iterations` sweeps over its
 // levels; a level's tets are split into kPbdCluster contiguous runs, one per
 // CTA.  Positions are read through L2 (ld.global.cg); the cluster barrier
-// orders one level's writes before the next level's reads.
+// orders one level's writes before the next level's reads.  A thread's first
+// static record of the next level is loaded before the barrier, so a level's
+// dependent chain starts at the position loads.
 __global__ void __cluster_dims__(kPbdCluster, 1, 1) __launch_bounds__(kPbdThreads)
     k_pbd_sweep(PbdView v, int iterations, PbdConst k) {
     cg::cluster_group cl = cg::this_cluster();
     const int g = blockIdx.x / kPbdCluster;
     const int rank = (int)cl.block_rank();
     const int l0 = v.grp[g], l1 = v.grp[g + 1];
-    for (int it = 0; it < iterations; ++it) {
-        for (int l = l0; l < l1; ++l) {
-            const int a = v.lvl[l], e = v.lvl[l + 1];
-            const int chunk = (e - a + kPbdCluster - 1) / kPbdCluster;
-            const int b0 = a + rank * chunk, b1 = min(b0 + chunk, e);
-            for (int j = b0 + (int)threadIdx.x; j < b1; j += kPbdThreads) {
-                const int4 q = __ldg(v.tet + j);
-                const float4 r0 = __ldg(v.d0 + j), r1 = __ldg(v.d1 + j), r2 = __ldg(v.d2 + j);
-                const float D[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-                const int id[4] = {q.x, q.y, q.z, q.w};
-                float4 p[4];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) p[c] = __ldcg(v.px + id[c]);
-                float dp[4][3];
-                pbd_project(p, D, k, dp);
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    v.px[id[c]] = make_float4(fadd(p[c].x, dp[c][0]), fadd(p[c].y, dp[c][1]), fadd(p[c].z, dp[c][2]),
-                                              p[c].w);
-            }
-            cl.sync();
+    if (l0 == l1 || iterations <= 0) return;  // uniform over the cluster
+    // this thread's run [j, b1) of level l
+    auto run_of = [&](int l, int &j, int &b1) {
+        const int a = v.lvl[l], e = v.lvl[l + 1];
+        const int chunk = (e - a + kPbdCluster - 1) / kPbdCluster;
+        const int b0 = a + rank * chunk;
+        b1 = min(b0 + chunk, e);
+        j = b0 + (int)threadIdx.x;
+    };
+    int j, b1;
+    run_of(l0, j, b1);
+    PbdTet cur = pbd_load(v, j < b1 ? j : v.lvl[l0]);
+    const int total = iterations * (l1 - l0);
+    for (int s = 0; s < total; ++s) {
+        const int l = l0 + s % (l1 - l0);
+        // next level's first record (for the last level of the last sweep: none)
+        int jn = 0, bn = 0;
+        PbdTet nxt = cur;
+        if (s + 1 < total) {
+            const int ln = l + 1 < l1 ? l + 1 : l0;
+            run_of(ln, jn, bn);
+            if (jn < bn) nxt = pbd_load(v, jn);
         }
+        if (j < b1) pbd_apply(v, cur, k);
+        for (int jj = j + kPbdThreads; jj < b1; jj += kPbdThreads) pbd_apply(v, pbd_load(v, jj), k);
+        cl.sync();
+        cur = nxt;
+        j = jn;
+        b1 = bn;
     }
 }
 
@@ -290,15 +327,15 @@ __global__ void k_dyn_end(DevMesh m, DevState st, const float4 *px, const float4
 }
 
 // ---------------------------------------------------------------- projective dynamics
-// Row i of A = M / dt_m^2 + sum_t k vol_t (w_a . w_b) I3 as 3x3 blocks (the
-// off-diagonal dofs zero), in the node's incidence order; D^-1 = 1 / a_ii.
+// Row i of A = M / dt_m^2 + sum_t k vol_t (w_a . w_b) I3, one value a block
+// (A.scalar), in the node's incidence order; D^-1 = 1 / a_ii.
 __global__ void __launch_bounds__(128) k_pd_assemble(DevMesh m, BsrView A, float inv_dt2, float stiffness,
                                                      float *dinv9) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
     const int rb = A.ptr[i], re = A.ptr[i + 1];
-    float *row = A.val + 9 * (size_t)rb;
-    for (int k = 0; k < 9 * (re - rb); ++k) row[k] = 0.f;
+    float *row = A.val + rb;
+    for (int k = 0; k < re - rb; ++k) row[k] = 0.f;
     const float4 info = m.info[i];
     if (info.z != 2.f) {
         for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
@@ -314,23 +351,15 @@ __global__ void __launch_bounds__(128) k_pd_assemble(DevMesh m, BsrView A, float
             for (int cc = 0; cc < 4; ++cc) {
                 const int sl = col_slot(A.col, rb, re, qn[cc]);
                 if (sl == re) continue;  // (the pattern holds every tet's node pairs)
-                const float g = kv * (w[c][0] * w[cc][0] + w[c][1] * w[cc][1] + w[c][2] * w[cc][2]);
-                float *blk = row + 9 * (sl - rb);
-                blk[0] += g;
-                blk[4] += g;
-                blk[8] += g;
+                row[sl - rb] += kv * (w[c][0] * w[cc][0] + w[c][1] * w[cc][1] + w[c][2] * w[cc][2]);
             }
         }
     }
     const int dsl = col_slot(A.col, rb, re, i);
     float inv = 0.f;
     if (dsl < re) {
-        float *d = row + 9 * (dsl - rb);
-        const float md = info.z == 2.f ? 1.f : info.x * inv_dt2;
-        d[0] += md;
-        d[4] += md;
-        d[8] += md;
-        inv = 1.f / d[0];
+        row[dsl - rb] += info.z == 2.f ? 1.f : info.x * inv_dt2;
+        inv = 1.f / row[dsl - rb];
     }
     for (int k = 0; k < 9; ++k) dinv9[9 * (size_t)i + k] = (k % 4 == 0) ? inv : 0.f;
 }
@@ -422,12 +451,12 @@ __global__ void k_pd_residual(int Np, BsrView A, float4 *b, const float4 *p, flo
     if (i >= Np) return;
     const float4 bi = b[i];
     double rx = bi.x, ry = bi.y, rz = bi.z;
-    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-        const float *a = A.val + 9 * (size_t)k;
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {  // A.scalar: blocks a I3
+        const double a = A.val[k];
         const float4 v = p[A.col[k]];
-        rx -= (double)a[0] * v.x + (double)a[1] * v.y + (double)a[2] * v.z;
-        ry -= (double)a[3] * v.x + (double)a[4] * v.y + (double)a[5] * v.z;
-        rz -= (double)a[6] * v.x + (double)a[7] * v.y + (double)a[8] * v.z;
+        rx -= a * v.x;
+        ry -= a * v.y;
+        rz -= a * v.z;
     }
     b[i] = make_float4((float)rx, (float)ry, (float)rz, 0.f);
     d[i] = make_float4(0.f, 0.f, 0.f, 0.f);

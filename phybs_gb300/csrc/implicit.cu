@@ -164,6 +164,16 @@ __global__ void __launch_bounds__(128) k_be_assemble(DevMesh m, DevState st, Bsr
 
 __device__ __forceinline__ float4 bsr_row_mul(const BsrView &A, int i, const float4 *p) {
     float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (A.scalar) {  // blocks a I3: one value a block
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            const float a = A.val[k];
+            const float4 v = p[A.col[k]];
+            sx += a * v.x;
+            sy += a * v.y;
+            sz += a * v.z;
+        }
+        return f4(sx, sy, sz);
+    }
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
         const float *a = A.val + 9 * (size_t)k;
         const float4 v = p[A.col[k]];

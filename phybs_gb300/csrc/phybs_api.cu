@@ -90,6 +90,12 @@ struct pbs_handle {
     DevBuf<double> cg_part;
     DevBuf<CgState> cg_state;
     CgState *h_cg = nullptr;
+    // 16 CG iterations captured as one graph, for the system and stop rule of
+    // the key (rebuilt when they change)
+    cudaGraphExec_t cg_exec = nullptr;
+    const void *cg_key[3] = {nullptr, nullptr, nullptr};
+    double cg_key_tol2 = -1.0;
+    int cg_key_int[3] = {-1, -1, -1};
     DevBuf<double2> tpart;
     DevBuf<double> npart;
     DevBuf<float> npartf;
@@ -170,6 +176,8 @@ struct pbs_handle {
         for (auto b : cv) b->release();
         if (h_cg) cudaFreeHost(h_cg);
         h_cg = nullptr;
+        if (cg_exec) cudaGraphExecDestroy(cg_exec);
+        cg_exec = nullptr;
         bsr_ready = false;
         if (h_active) cudaFreeHost(h_active);
         if (h_ctl) cudaFreeHost(h_ctl);
@@ -1132,6 +1140,36 @@ static int ensure_bsr(pbs_handle *h) {
     return PBS_OK;
 }
 
+// Launches 16 CG iterations on A x = b (state in cg_state) as one graph; the
+// kernels of a finished solve return at once, so a group may overrun the cap.
+static int cg_group(pbs_handle *h, const BsrView &A, const float *dinv9, float4 *x, double tol2, int max_iters,
+                    int pnorm) {
+    const void *key[3] = {A.val, dinv9, x};
+    const int ki[3] = {max_iters, pnorm, A.scalar};
+    bool same = h->cg_exec && h->cg_key_tol2 == tol2;
+    for (int k = 0; k < 3; ++k) same = same && key[k] == h->cg_key[k] && ki[k] == h->cg_key_int[k];
+    if (!same) {
+        if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
+        h->cg_exec = nullptr;
+        cudaStream_t s = h->stream;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 16 && e == cudaSuccess; ++k)
+            e = launch_cg_iteration(s, h->Np, A, dinv9, x, h->cg_r.p, h->cg_z.p, h->cg_p.p, h->cg_q.p, h->cg_part.p,
+                                    h->cg_state.p, tol2, max_iters, pnorm);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&h->cg_exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        CK(e);
+        for (int k = 0; k < 3; ++k) { h->cg_key[k] = key[k]; h->cg_key_int[k] = ki[k]; }
+        h->cg_key_tol2 = tol2;
+    }
+    CK(cudaGraphLaunch(h->cg_exec, h->stream));
+    return PBS_OK;
+}
+
 int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, const float *ext, float tol,
                             int max_iters, int *iters_out, double *residual_out) {
     if (!h || !(dt > 0.f) || !(alpha >= 0.f) || !(beta >= 0.f) || !(tol > 0.f) || max_iters <= 0)
@@ -1158,9 +1196,8 @@ int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, co
     // iterations in groups of 16; every kernel of a finished solve returns at
     // once, and the host reads the state once per group
     for (int it = 0; it < max_iters; it += 16) {
-        for (int k = 0; k < 16 && it + k < max_iters; ++k)
-            CK(launch_cg_iteration(s, h->Np, A, h->cg_dinv.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
-                                   h->cg_q.p, h->cg_part.p, h->cg_state.p, tol2, max_iters));
+        rc = cg_group(h, A, h->cg_dinv.p, h->cg_x.p, tol2, max_iters, 0);
+        if (rc != PBS_OK) return rc;
         CK(cudaMemcpyAsync(h->h_cg, h->cg_state.p, sizeof(CgState), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         if (h->h_cg->done) break;
@@ -1286,10 +1323,11 @@ int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int i
     BsrView A;
     A.ptr = h->bsr_ptr.p;
     A.col = h->bsr_col.p;
+    A.scalar = 1;
     if (!h->pd_val.p) {
         int nnzb = 0;
         CK(cudaMemcpy(&nnzb, h->bsr_ptr.p + h->Np, sizeof(int), cudaMemcpyDeviceToHost));
-        CK(h->pd_val.alloc(9 * (size_t)nnzb));
+        CK(h->pd_val.alloc((size_t)nnzb));
         CK(h->pd_dinv.alloc(9 * (size_t)h->Np));
     }
     A.val = h->pd_val.p;
@@ -1309,9 +1347,8 @@ int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int i
         CK(launch_cg_init(s, h->Np, A, h->pd_dinv.p, h->cg_b.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
                           h->cg_part.p, h->cg_state.p, tol2, 1));
         for (int k0 = 0; k0 < max_cg; k0 += 16) {
-            for (int k = 0; k < 16 && k0 + k < max_cg; ++k)
-                CK(launch_cg_iteration(s, h->Np, A, h->pd_dinv.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
-                                       h->cg_q.p, h->cg_part.p, h->cg_state.p, tol2, max_cg, 1));
+            rc = cg_group(h, A, h->pd_dinv.p, h->cg_x.p, tol2, max_cg, 1);
+            if (rc != PBS_OK) return rc;
             CK(cudaMemcpyAsync(h->h_cg, h->cg_state.p, sizeof(CgState), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             if (h->h_cg->done) break;

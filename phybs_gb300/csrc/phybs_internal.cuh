@@ -283,7 +283,8 @@ cudaError_t launch_drag_ring(cudaStream_t s, const DevMesh &m, const DevState &s
 // nodes (columns ascending per block row) and the conjugate-gradient state.
 struct BsrView {
     const int *ptr, *col;
-    float *val;  // 9 per block, row-major
+    float *val;      // 9 per block, row-major; or 1 per block (a I3) when scalar
+    int scalar = 0;
 };
 struct CgState {
     double rz, rr, bb, alpha, beta;
