@@ -478,6 +478,72 @@ def run_batch(args, rank, world):
     print(json.dumps(line))
 
 
+def run_dynamics(args, rank, world, kind):
+    """The reference's other two integrators on the 1M-tet box (50 x 50 x 80
+    cubes, 5-tet split, top face pinned), twisted 0.3 rad about its long axis
+    and released under gravity: `pbd` = strain-based PBD with the reference's
+    5 sweeps, stretch 1, shear 0.8 (PosBaseDynamic.cpp), dt = 1/30; `pd` =
+    projective dynamics with stiffness 1e6 and 5 local/global iterations
+    (ProjDynamic.cpp), dt = 0.03, CG to 1e-6.  A step is one call through the
+    C ABI (synchronous; positions stay on the device)."""
+    import torch
+
+    from phybs_gb300 import meshes as M
+    from phybs_gb300.solver import DescentSolver
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    m, _, _, _ = box_workload(args.seed, args.scale)
+    x = M.twist_positions(m.rest, 0.3, axis=2).astype(np.float32)
+    x[m.pins] = m.rest[m.pins]
+    s = DescentSolver(m, positions=x)
+    step = (lambda: s.pbd_step(1 / 30)) if kind == "pbd" else (lambda: s.pd_step(0.03, tol=1e-6))
+    for _ in range(args.warmup):
+        step()
+    stream = torch.cuda.ExternalStream(s.stream())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cg = []
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = step()
+            if kind == "pd":
+                cg.append(r)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    s.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": ("strain-based PBD steps/s (5 sweeps)" if kind == "pbd" else
+                   "projective-dynamics steps/s (5 local/global iterations)") + ", 1M-tet box, 1 GB300",
+        "value": world * args.steps / t, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"box 50x50x80 cubes, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes, top pinned, "
+                               f"twisted 0.3 rad, gravity", "seed": args.seed},
+        "clocks": clk.summary(),
+    }
+    if kind == "pd":
+        line["cg_iterations_per_step"] = cg
+    else:
+        L = M.pbd_levels(m.tets, m.n_nodes)
+        line["roofline"] = {"bound": "latency", "levels": L, "level_sweeps_per_step": 5 * L,
+                            "us_per_level": t / args.steps / (5 * L) * 1e6}
+        if not args.no_cpu_baseline:
+            from oracle import projective as P
+            dinv, w, grav = P.rest_eigen32(m.rest, m.tets, m.pin_mask(), density=float(m.density))
+            t0 = time.perf_counter()
+            P.pbd_step(x, np.zeros_like(x), w, m.tets, dinv, grav, 1 / 30)
+            cs = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": 1.0 / cs, "unit": "steps/s", "cores": 1, "kind": "port",
+                                    "sample": "one step on the full mesh: the serial FP32 restatement of "
+                                              "PosBaseDynamic (orc_pbd_step), bit-identical to the reference"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -493,8 +559,9 @@ def main():
                     help="pass stress evaluation (default: incremental)")
     ap.add_argument("--shape", default=None,
                     help="launch shapes 'threads,tets,nodes,staged,node_npt' instead of autotuning (profiling runs)")
-    ap.add_argument("--workload", choices=["box1m", "batch"], default="box1m",
-                    help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances")
+    ap.add_argument("--workload", choices=["box1m", "batch", "pbd", "pd"], default="box1m",
+                    help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances; pbd / pd: the "
+                         "strain-based PBD / projective-dynamics steps on the 1M-tet box")
     args = ap.parse_args()
     if args.stress is not None:
         global INCREMENTAL_STRESS
@@ -510,6 +577,8 @@ def main():
         torch.distributed.init_process_group("gloo")
     if args.workload == "batch":
         run_batch(args, rank, world)
+    elif args.workload in ("pbd", "pd"):
+        run_dynamics(args, rank, world, args.workload)
     else:
         run_ours(args, rank, world)
     if world > 1:

@@ -428,7 +428,9 @@ int pbs_pbd_step(pbs_handle *h, float dt, int iterations, const float *stretch, 
  * the integrator's time step for A (dt_matrix; 0 takes dt), and an MKL
  * Pardiso LDL^T factorisation of A.  Here A is assembled once per (dt_matrix,
  * k) as block rows and each global step solves for the correction d of the
- * current iterate p: r = b - A p (FP64 accumulation), A d = r by block-Jacobi
+ * current iterate p: r = b - A p formed per tet from edge differences
+ * (M / dt^2 (x - p + dt v + dt^2 w f) + sum_t k vol_t A_t^T vec(R_t - F_t):
+ * no absolute coordinate enters), A d = r by block-Jacobi
  * preconditioned conjugate gradients until (e^T D^-1 e)^1/2 <= tol
  * (r^T D^-1 r)^1/2 for the CG residual e, or max_cg iterations
  * (PBS_E_ITER_CAP, the state advanced), then p += d.  cg_iters_out: total CG

@@ -13,12 +13,14 @@
 // contraction) in Eigen 3.2's order, so a sweep is the CPU's bit for bit.
 //
 // Projective dynamics (ProjDynamic.cpp:48-100, 351-480): per-tet polar
-// rotations from the modified SVD, a fixed-order gather of the right-hand
-// side, and the constant global matrix A = L (x) I3.  A and b are of the size
-// of the inertial term M p / dt^2 (positions, not displacements), so each
-// global solve is a correction: r = b - A p with FP64 accumulation, A d = r by
-// the block-Jacobi conjugate gradients of the backward-Euler step (relative to
-// r, in FP32), p += d.
+// rotations from the modified SVD and the constant global matrix A = L (x) I3.
+// A p and b are of the size of the positions times the stiffness, and an
+// FP32 A's rows do not sum to zero exactly, so applied to absolute positions
+// it would add forces proportional to the distance from the origin.  Each
+// global solve is therefore a correction from a residual formed without
+// absolute coordinates: r = b - A p = M / dt^2 ((x - p) + q) +
+// sum_t k vol (R - F) w_a (edge differences only), A d = r by the
+// block-Jacobi conjugate gradients of the backward-Euler step, p += d.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -364,30 +366,32 @@ __global__ void __launch_bounds__(128) k_pd_assemble(DevMesh m, BsrView A, float
     for (int k = 0; k < 9; ++k) dinv9[9 * (size_t)i + k] = (k % 4 == 0) ? inv : 0.f;
 }
 
-// s = (x + dt v + (dt^2 w) f) m / dt^2 (ProjDynamic.cpp:447-463); p = x0 = x
-__global__ void k_pd_begin(DevMesh m, DevState st, const float4 *ext, float dt, float4 *s, float4 *px, float4 *x0) {
+// q = dt v + (dt^2 w) f, the inertial target's offset from x (the reference's
+// s = (x + dt v + dt^2 w f) m / dt^2, ProjDynamic.cpp:447-463, is
+// m / dt^2 (x + q)); p = x0 = x
+__global__ void k_pd_begin(DevMesh m, DevState st, const float4 *ext, float dt, float4 *q, float4 *px, float4 *x0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
     const float4 info = m.info[i];
     if (info.z == 2.f) {
-        s[i] = px[i] = x0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        q[i] = px[i] = x0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     const float4 x = state_pos4(m, st, i), v = st.v[i];
-    const float dt2 = fmul(dt, dt), a = fmul(dt2, inv_mass_of(info)), mm = info.x;
+    const float dt2 = fmul(dt, dt), a = fmul(dt2, inv_mass_of(info));
     const float3 f = node_force(info, ext, i);
-    const float sx = fadd(fadd(x.x, fmul(dt, v.x)), fmul(a, f.x));
-    const float sy = fadd(fadd(x.y, fmul(dt, v.y)), fmul(a, f.y));
-    const float sz = fadd(fadd(x.z, fmul(dt, v.z)), fmul(a, f.z));
-    s[i] = make_float4(__fdiv_rn(fmul(sx, mm), dt2), __fdiv_rn(fmul(sy, mm), dt2), __fdiv_rn(fmul(sz, mm), dt2), 0.f);
+    q[i] = make_float4(fadd(fmul(dt, v.x), fmul(a, f.x)), fadd(fmul(dt, v.y), fmul(a, f.y)),
+                       fadd(fmul(dt, v.z), fmul(a, f.z)), 0.f);
     px[i] = x;
     x0[i] = x;
 }
 
 // Per tet: R = U V^T with JacobiSVD's determinant fix (first, largest
 // columns negated), i.e. U diag(sg, 1, sg) V^T of the modified SVD
-// (sg = sign of the smallest singular value); corner a's projection
-// k vol R w_a into its gather slot.
+// (sg = sign of the smallest singular value).  Corner a's share of the
+// global step's residual, k vol (R - F) w_a (its projection k vol R w_a
+// less its share of A p, both from edge differences: no absolute coordinate
+// enters), goes into its gather slot.
 __global__ void __launch_bounds__(128) k_pd_local(DevMesh m, const float4 *px, float stiffness, float4 *slot) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.Tp) return;
@@ -408,11 +412,13 @@ __global__ void __launch_bounds__(128) k_pd_local(DevMesh m, const float4 *px, f
     float U[9], sv[3], V[9], sign3;
     svd_disp<float, 4>(G, U, sv, V, sign3);
     const float sg = sign3 < 0.f ? -1.f : 1.f;
-    float R[9];
+    float E[9];  // R - F = R - I - G
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) R[3 * r + c] = sg * U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + sg * U[3 * r + 2] * V[3 * c + 2];
+        for (int c = 0; c < 3; ++c)
+            E[3 * r + c] = (sg * U[3 * r] * V[3 * c] + U[3 * r + 1] * V[3 * c + 1] + sg * U[3 * r + 2] * V[3 * c + 2] -
+                            (r == c ? 1.f : 0.f)) - G[3 * r + c];
     const float kv = stiffness * fabsf(r0.w);
     const float w[4][3] = {{-(r0.x + r1.x + r2.x), -(r0.y + r1.y + r2.y), -(r0.z + r1.z + r2.z)},
                            {r0.x, r0.y, r0.z},
@@ -422,44 +428,38 @@ __global__ void __launch_bounds__(128) k_pd_local(DevMesh m, const float4 *px, f
     const int sls[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        slot[sls[a]] = make_float4(kv * (R[0] * w[a][0] + R[1] * w[a][1] + R[2] * w[a][2]),
-                                   kv * (R[3] * w[a][0] + R[4] * w[a][1] + R[5] * w[a][2]),
-                                   kv * (R[6] * w[a][0] + R[7] * w[a][1] + R[8] * w[a][2]), 0.f);
+        slot[sls[a]] = make_float4(kv * (E[0] * w[a][0] + E[1] * w[a][1] + E[2] * w[a][2]),
+                                   kv * (E[3] * w[a][0] + E[4] * w[a][1] + E[5] * w[a][2]),
+                                   kv * (E[6] * w[a][0] + E[7] * w[a][1] + E[8] * w[a][2]), 0.f);
     }
 }
 
-// b = s + the node's projections in incidence order (ascending tet, as the
-// reference's m_proj_idx lists them)
-__global__ void k_pd_rhs(DevMesh m, const float4 *s, const float4 *slot, float4 *b) {
+// The global step's residual r = b - A p = m / dt_m^2 (x - p) + m / dt^2 q
+// + (m / dt^2 - m / dt_m^2) x (zero unless A was formed with another time
+// step) + the node's (R - F) slots in incidence order (ascending tet, as the
+// reference's m_proj_idx lists them); the correction d = 0
+__global__ void k_pd_rhs(DevMesh m, const float4 *q, const float4 *x0, const float4 *px, const float4 *slot,
+                         float inv_dt2, float inv_dtm2, float4 *r, float4 *d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
-    float4 a = s[i];
+    d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 info = m.info[i];
+    if (info.z == 2.f) { r[i] = d[i]; return; }
+    const float4 qq = q[i], x = x0[i], p = px[i];
+    const float mb = info.x * inv_dt2, mm = info.x * inv_dtm2, mx = mb - mm;
+    float4 a = make_float4(mm * (x.x - p.x) + mb * qq.x, mm * (x.y - p.y) + mb * qq.y, mm * (x.z - p.z) + mb * qq.z, 0.f);
+    if (mx != 0.f) {
+        a.x += mx * x.x;
+        a.y += mx * x.y;
+        a.z += mx * x.z;
+    }
     for (int j = m.inc_ptr[i]; j < m.inc_ptr[i + 1]; ++j) {
         const float4 c = slot[j];
         a.x += c.x;
         a.y += c.y;
         a.z += c.z;
     }
-    b[i] = a;
-}
-
-// r = b - A p with FP64 accumulation (b and A p are both of the size of the
-// inertial term M p / dt^2 and cancel to the size of the step's change), the
-// correction d = 0
-__global__ void k_pd_residual(int Np, BsrView A, float4 *b, const float4 *p, float4 *d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Np) return;
-    const float4 bi = b[i];
-    double rx = bi.x, ry = bi.y, rz = bi.z;
-    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {  // A.scalar: blocks a I3
-        const double a = A.val[k];
-        const float4 v = p[A.col[k]];
-        rx -= a * v.x;
-        ry -= a * v.y;
-        rz -= a * v.z;
-    }
-    b[i] = make_float4((float)rx, (float)ry, (float)rz, 0.f);
-    d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    r[i] = a;
 }
 
 __global__ void k_pd_apply(int Np, float4 *p, const float4 *d) {
@@ -470,11 +470,6 @@ __global__ void k_pd_apply(int Np, float4 *p, const float4 *d) {
 }
 
 }  // namespace
-
-cudaError_t launch_pd_residual(cudaStream_t s, int Np, const BsrView &A, float4 *b, const float4 *p, float4 *d) {
-    k_pd_residual<<<(Np + 255) / 256, 256, 0, s>>>(Np, A, b, p, d);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_pd_apply(cudaStream_t s, int Np, float4 *p, const float4 *d) {
     k_pd_apply<<<(Np + 255) / 256, 256, 0, s>>>(Np, p, d);
@@ -516,15 +511,16 @@ cudaError_t launch_pd_assemble(cudaStream_t s, const DevMesh &m, const BsrView &
 }
 
 cudaError_t launch_pd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *ext, float dt,
-                            float4 *rhs0, float4 *px, float4 *x0) {
-    k_pd_begin<<<(m.Np + 255) / 256, 256, 0, s>>>(m, st, ext, dt, rhs0, px, x0);
+                            float4 *q, float4 *px, float4 *x0) {
+    k_pd_begin<<<(m.Np + 255) / 256, 256, 0, s>>>(m, st, ext, dt, q, px, x0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pd_local(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float4 *slot,
-                            const float4 *rhs0, float4 *b) {
+cudaError_t launch_pd_residual(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float dt,
+                               float dt_matrix, float4 *slot, const float4 *q, const float4 *x0, float4 *r, float4 *d) {
     k_pd_local<<<(m.Tp + 127) / 128, 128, 0, s>>>(m, px, stiffness, slot);
-    k_pd_rhs<<<(m.Np + 255) / 256, 256, 0, s>>>(m, rhs0, slot, b);
+    k_pd_rhs<<<(m.Np + 255) / 256, 256, 0, s>>>(m, q, x0, px, slot, 1.f / (dt * dt),
+                                                1.f / (dt_matrix * dt_matrix), r, d);
     return cudaGetLastError();
 }
 

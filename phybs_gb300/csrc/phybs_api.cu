@@ -1341,9 +1341,8 @@ int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int i
     const double tol2 = (double)tol * (double)tol;
     int total = 0, status = PBS_OK;
     for (int it = 0; it < iterations; ++it) {
-        CK(launch_pd_local(s, m, h->dyn_px.p, stiffness, reinterpret_cast<float4 *>(h->tf.p), h->dyn_s.p,
-                           h->cg_b.p));
-        CK(launch_pd_residual(s, h->Np, A, h->cg_b.p, h->dyn_px.p, h->cg_x.p));
+        CK(launch_pd_residual(s, m, h->dyn_px.p, stiffness, dt, dtm, reinterpret_cast<float4 *>(h->tf.p),
+                              h->dyn_s.p, h->dyn_x0.p, h->cg_b.p, h->cg_x.p));
         CK(launch_cg_init(s, h->Np, A, h->pd_dinv.p, h->cg_b.p, h->cg_x.p, h->cg_r.p, h->cg_z.p, h->cg_p.p,
                           h->cg_part.p, h->cg_state.p, tol2, 1));
         for (int k0 = 0; k0 < max_cg; k0 += 16) {

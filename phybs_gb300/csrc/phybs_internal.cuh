@@ -328,11 +328,12 @@ cudaError_t launch_dyn_end(cudaStream_t s, const DevMesh &m, const DevState &st,
 cudaError_t launch_pd_assemble(cudaStream_t s, const DevMesh &m, const BsrView &A, float dt_matrix, float stiffness,
                                float *dinv9);
 cudaError_t launch_pd_begin(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *ext, float dt,
-                            float4 *rhs0, float4 *px, float4 *x0);
-cudaError_t launch_pd_residual(cudaStream_t s, int Np, const BsrView &A, float4 *b, const float4 *p, float4 *d);
+                            float4 *q, float4 *px, float4 *x0);
+// r = b - A p of the global step at iterate px (and d = 0), from the per-tet
+// rotations; slot: scratch of one float4 a gather slot
+cudaError_t launch_pd_residual(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float dt,
+                               float dt_matrix, float4 *slot, const float4 *q, const float4 *x0, float4 *r, float4 *d);
 cudaError_t launch_pd_apply(cudaStream_t s, int Np, float4 *p, const float4 *d);
-cudaError_t launch_pd_local(cudaStream_t s, const DevMesh &m, const float4 *px, float stiffness, float4 *slot,
-                            const float4 *rhs0, float4 *b);
 
 struct HandleView {
     int device;

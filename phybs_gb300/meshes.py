@@ -391,3 +391,17 @@ def write_tetgen_nodes(path: str, pos: np.ndarray) -> None:
         f.write(f"{p.shape[0]} 3 0 0\n")
         for i, (x, y, z) in enumerate(p):
             f.write(f"{i} {x:.9g} {y:.9g} {z:.9g}\n")
+
+
+def pbd_levels(tets: np.ndarray, n_nodes: int) -> int:
+    """Number of dependency levels of a Gauss-Seidel sweep over the tets in
+    their order (a tet's level is one more than the highest level of the
+    earlier tets sharing a node with it): the length of the chain the
+    strain-based PBD step runs level by level."""
+    last = np.full(n_nodes, -1, np.int64)
+    top = -1
+    for q in np.asarray(tets, np.int64).reshape(-1, 4):
+        lv = max(last[q[0]], last[q[1]], last[q[2]], last[q[3]]) + 1
+        last[q] = lv
+        top = max(top, lv)
+    return int(top + 1)

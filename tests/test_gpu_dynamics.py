@@ -142,6 +142,28 @@ def test_pd_close_to_reference(g):
     s.close()
 
 
+def test_pd_packed_batch():
+    """Three uneven boxes in one handle (one block-diagonal system, one CG):
+    each instance within 2e-5 of its bounding-box diagonal of the FP64
+    restatement of that instance alone."""
+    m = M.batch_of_boxes(3, seed=9, nxy=(3, 6), nz=(5, 12))
+    x = M.twist_positions(m.rest, 0.05, axis=2).astype(np.float32)
+    x[m.pins] = m.rest[m.pins]
+    s = DescentSolver(m, positions=x)
+    dinv, w, grav = device_rest(s, m)
+    _, svol, mass, _ = s.rest_data()
+    s.pd_step(0.03, tol=1e-7)
+    got = s.positions()
+    for b in range(m.n_instances):
+        n0, n1 = m.instance_node_ptr[b], m.instance_node_ptr[b + 1]
+        t0, t1 = m.instance_tet_ptr[b], m.instance_tet_ptr[b + 1]
+        xo, _ = P.pd_step(x[n0:n1], np.zeros((n1 - n0, 3)), mass[n0:n1], w[n0:n1], m.tets[t0:t1] - n0,
+                          dinv[t0:t1].reshape(-1, 3, 3), np.abs(svol[t0:t1]), grav[n0:n1], dt=0.03)
+        err = np.abs(got[n0:n1] - xo).max() / bbox_diag(m.rest[n0:n1])
+        assert err < 2e-5, (b, err)
+    s.close()
+
+
 def test_pd_cap_and_arguments():
     m = M.bar_mesh(8, 3, 3, edge=0.025)
     s = DescentSolver(m)
