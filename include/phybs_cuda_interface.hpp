@@ -18,8 +18,13 @@
 //     0.03, CUDAInterface.cu:644);
 //   - errors are reported: every call throws phybs::Error on a PBS_E_* code
 //     (the reference ignores CUDA errors);
-//   - there is no backward-Euler path (doBackEuler / computeInnerforces /
-//     computeGlobalStiffnessMatrix are not part of the descent step).
+//   - the backward-Euler path (fvm.cpp:179-183) keeps its three calls:
+//     computeInnerforces and computeGlobalStiffnessMatrix are no-ops and
+//     doBackEuler runs the whole step (pbs_backward_euler_step assembles the
+//     forces and the matrix itself);
+//   - pbdStep and projectiveDynamicsStep run the viewer's other two
+//     integrators (PosBaseDynamic / ProjDynamic, fvm.cpp:162-171) on the same
+//     state.
 #pragma once
 
 #include <stdexcept>
@@ -90,6 +95,32 @@ public:
     void updateNodePositions(const float *hostNode) { check(pbs_update_positions(h_, hostNode), "pbs_update_positions"); }
     // CUDAInterface::reset (CUDAInterface.cu:776)
     void reset() { check(pbs_reset(h_), "pbs_reset"); }
+
+    // CUDAInterface::computeInnerforces / computeGlobalStiffnessMatrix /
+    // doBackEuler (CUDAInterface.cu:784-884): h = 0.03, alpha = beta = 0.02.
+    void computeInnerforces() {}
+    void computeGlobalStiffnessMatrix() {}
+    void doBackEuler(float *hostNode, float h = 0.03f, float tol = 1e-6f, int max_iters = 4000) {
+        int rc = pbs_backward_euler_step(h_, h, 0.02f, 0.02f, nullptr, tol, max_iters, nullptr, nullptr);
+        if (rc != PBS_OK && rc != PBS_E_ITER_CAP) throw Error(rc, "pbs_backward_euler_step");
+        check(pbs_read_positions(h_, hostNode), "pbs_read_positions");
+    }
+
+    // PosBaseDynamic::doStepStrainConstraints (fvm.cpp:162-165): 5 sweeps,
+    // stretch 1, shear 0.8; hostExternForces 3N floats or nullptr.
+    void pbdStep(float t, const float *hostExternForces, float *hostNode, int sweeps = 5) {
+        check(pbs_pbd_step(h_, t, sweeps, nullptr, nullptr, hostExternForces), "pbs_pbd_step");
+        check(pbs_read_positions(h_, hostNode), "pbs_read_positions");
+    }
+
+    // ProjDynamic::doProjDynamics (fvm.cpp:167-170, matrix at fvm.cpp:305):
+    // t = 0.03 for the step, tMatrix the integrator's time step for A.
+    void projectiveDynamicsStep(float t, float tMatrix, const float *hostExternForces, float *hostNode,
+                                float tol = 1e-6f, int max_cg = 20000) {
+        int rc = pbs_pd_step(h_, t, tMatrix, 1e6f, 5, hostExternForces, tol, max_cg, nullptr);
+        if (rc != PBS_OK && rc != PBS_E_ITER_CAP) throw Error(rc, "pbs_pd_step");
+        check(pbs_read_positions(h_, hostNode), "pbs_read_positions");
+    }
 
     pbs_handle *handle() const { return h_; }
     pbs_step_params &params() { return params_; }

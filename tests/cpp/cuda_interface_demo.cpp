@@ -1,7 +1,9 @@
 // Drives the CUDAInterface-shaped wrapper the way FVM/fvm.cpp does
-// (construct from a mesh, doDescentOpt, updateNodePositions, reset) on a
-// 2x1x1-cube bar.  Prints "pattern <nnz>" (host-only), then either
-// "step <max |x - rest|>" or "error <code>" when no GB300 is present.
+// (construct from a mesh, doDescentOpt, updateNodePositions, reset, and the
+// backward-Euler, PBD and projective-dynamics steps) on a 2x1x1-cube bar.
+// Prints "pattern <nnz>" (host-only), then either "step <max |x - rest|>"
+// followed by "backeuler", "pbd" and "pd" lines of the same form, or
+// "error <code>" when no GB300 is present.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -52,6 +54,22 @@ int main() {
         ci.updateNodePositions(out.data());
         ci.reset();
         std::printf("step %g\n", dmax);
+        // the viewer's other integrators on the same handle (fvm.cpp:162-183)
+        auto moved = [&]() {
+            float d = 0.f;
+            for (int i = 0; i < 3 * n; ++i) d = std::fmax(d, std::fabs(out[i] - rest[i]));
+            return d;
+        };
+        ci.computeInnerforces();
+        ci.computeGlobalStiffnessMatrix();
+        ci.doBackEuler(out.data());
+        std::printf("backeuler %g\n", moved());
+        ci.reset();
+        ci.pbdStep(1.0f / 30, ext.data(), out.data());
+        std::printf("pbd %g\n", moved());
+        ci.reset();
+        ci.projectiveDynamicsStep(0.03f, 0.03f, ext.data(), out.data());
+        std::printf("pd %g\n", moved());
     } catch (const phybs::Error &e) {
         std::printf("error %d\n", e.code());
     }
