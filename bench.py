@@ -250,6 +250,26 @@ def tune_shape(args, m):
         s.close()
 
 
+def sync_ranks(world: int) -> None:
+    """Barrier over the ranks, then wait for this rank's device: both sides
+    of every timed region."""
+    import torch
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+
+def max_over_ranks(t: float, world: int) -> float:
+    """The slowest rank's time, on every rank: the job's time for `value`
+    (replicas: each rank steps its own copy of the workload)."""
+    if world > 1:
+        import torch
+        tt = torch.tensor([t], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    return t
+
+
 def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
     """One arm over frames 0 .. W+K-1 on a fresh handle.  Returns the timed
     K frames' results: device time (CUDA events on the library's stream) or,
@@ -274,13 +294,8 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
         s.set_node_positions(bottom, pin_xyz[f])
         s.step(raise_on_error=False)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
     res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0}
-    barrier()
+    sync_ranks(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         t0 = time.perf_counter()
@@ -297,13 +312,9 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
             res["status"].append(st["status"])
             res["ws_used"] += st["warm_start_used"]
         e1.record(stream)
-        barrier()
+        sync_ranks(world)
         t_host = time.perf_counter() - t0
-    t = t_host if e2e else e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(t_host if e2e else e0.elapsed_time(e1) / 1e3, world)
     res["seconds"] = t
     res["frames_per_s"] = world * args.steps / t
     res["clocks"] = clk.summary()
@@ -430,7 +441,7 @@ def run_batch(args, rank, world):
     stream = torch.cuda.ExternalStream(s.stream())
     for _ in range(args.warmup):
         s.step(raise_on_error=False)
-    torch.cuda.synchronize()
+    sync_ranks(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     iters, passes, launches, statuses = [], 0, 0, []
     with ClockSampler(dev) as clk:
@@ -443,8 +454,8 @@ def run_batch(args, rank, world):
             launches += launches_per_frame(st["graph_launches"], False) - 1  # no boundary upload
             statuses.append(st["status"])
         e1.record(stream)
-        torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
+        sync_ranks(world)
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
     prof, prof_err = None, None
     try:
         prof = s.profile_kernels(20)
@@ -501,7 +512,7 @@ def run_dynamics(args, rank, world, kind):
     for _ in range(args.warmup):
         step()
     stream = torch.cuda.ExternalStream(s.stream())
-    torch.cuda.synchronize()
+    sync_ranks(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     cg = []
     with ClockSampler(dev) as clk:
@@ -511,8 +522,8 @@ def run_dynamics(args, rank, world, kind):
             if kind == "pd":
                 cg.append(r)
         e1.record(stream)
-        torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
+        sync_ranks(world)
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
     s.close()
     if rank != 0:
         return
