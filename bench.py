@@ -529,12 +529,13 @@ def run_dynamics(args, rank, world, kind):
         return
     line = {
         "metric": ("strain-based PBD steps/s (5 sweeps)" if kind == "pbd" else
-                   "projective-dynamics steps/s (5 local/global iterations)") + ", 1M-tet box, 1 GB300",
+                   "projective-dynamics steps/s (5 local/global iterations)") +
+                  (", 1M-tet box, 1 GB300" if args.scale == 1.0 else f", {m.n_tets}-tet box, 1 GB300"),
         "value": world * args.steps / t, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"box 50x50x80 cubes, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes, top pinned, "
-                               f"twisted 0.3 rad, gravity", "seed": args.seed},
+        "config": {"workload": f"box, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes, top pinned, "
+                               f"twisted 0.3 rad, gravity", "seed": args.seed, "scale": args.scale},
         "clocks": clk.summary(),
     }
     if kind == "pd":

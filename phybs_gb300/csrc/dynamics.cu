@@ -6,8 +6,9 @@
 // one more than the highest level of the earlier tets that share one of its
 // nodes, so a level's tets share no node and each reads exactly the updates of
 // the tets before it in the serial order.  One thread-block cluster sweeps an
-// instance level by level, the cluster barrier ordering the levels (its
-// arrive/wait carry release/acquire semantics for the global positions):
+// instance level by level (16 CTAs when the handle holds few instances, else
+// 8), the cluster barrier ordering the levels (its arrive/wait carry
+// release/acquire semantics for the global positions):
 // 2,320 levels of ~430 tets for the 1M-tet box, 920 for the 24K bar.  The
 // arithmetic is FP32 with every product and sum rounded separately (no
 // contraction) in Eigen 3.2's order, so a sweep is the CPU's bit for bit.
@@ -34,7 +35,9 @@ namespace pbs {
 
 namespace {
 
-constexpr int kPbdCluster = 8;
+// CTAs a PBD cluster sweeps an instance with: 16 (the non-portable maximum,
+// opted into at launch) when a handle holds few instances, else 8
+constexpr int kPbdClusterMax = 16;
 constexpr int kPbdThreads = 128;
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
@@ -48,7 +51,7 @@ __device__ __forceinline__ float dot3e(const float a[3], const float b[3]) {
 // float(((double)S - 1.0) / (double)lam * (double)k): the reference's stretch
 // multiplier, whose double literal makes it FP64 (PosBaseDynamic.cpp:100).
 // GB300's FP64 pipe is narrow, so the value is formed in double-float FP32
-// (error below 2^-45 relative) and rounded; the FP64 expression is evaluated
+// (error below 2^-44 relative) and rounded; the FP64 expression is evaluated
 // only when that value lies within 2^-40 relative of a float rounding
 // boundary, where the two roundings could differ (or for zero, non-finite or
 // tiny values).
@@ -56,9 +59,15 @@ __device__ __forceinline__ float pbd_stretch_mult(float S, float lam, float k) {
     float ah, al;
     two_sum(S, -1.0f, ah, al);  // S - 1 = ah + al exactly
     if (ah == 0.0f && al == 0.0f) return fmul(0.0f, k);
-    const float q1 = __fdiv_rn(ah, lam);
-    const float r = fadd(__fmaf_rn(-q1, lam, ah), al);  // the remainder (exact) plus al
-    const float q2 = __fdiv_rn(r, lam);
+    // (ah + al) / lam as q1 + q2 from one approximate reciprocal: q1 is within
+    // a few ulp, the remainder ah - q1 lam is formed by one fma (exact, or
+    // rounded at 2^-24 of itself) and corrected by q2; |error| < 2^-45 of the
+    // quotient, well inside the boundary test's 2^-40 margin below
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(lam));
+    const float q1 = fmul(ah, inv);
+    const float r = fadd(__fmaf_rn(-q1, lam, ah), al);
+    const float q2 = fmul(r, inv);
     const float p1 = fmul(q1, k);
     const float p2 = __fmaf_rn(q2, k, __fmaf_rn(q1, k, -p1));  // q1 k - p1 is exact
     const float c = fadd(p1, p2);
@@ -159,22 +168,22 @@ __device__ __forceinline__ void pbd_apply(const PbdView &v, const PbdTet &t, con
 }
 
 // One cluster per group of levels (an instance): `iterations` sweeps over its
-// levels; a level's tets are split into kPbdCluster contiguous runs, one per
-// CTA.  Positions are read through L2 (ld.global.cg); the cluster barrier
+// levels; a level's tets are split into one contiguous run per CTA of the
+// cluster.  Positions are read through L2 (ld.global.cg); the cluster barrier
 // orders one level's writes before the next level's reads.  A thread's first
 // static record of the next level is loaded before the barrier, so a level's
 // dependent chain starts at the position loads.
-__global__ void __cluster_dims__(kPbdCluster, 1, 1) __launch_bounds__(kPbdThreads)
-    k_pbd_sweep(PbdView v, int iterations, PbdConst k) {
+__global__ void __launch_bounds__(kPbdThreads) k_pbd_sweep(PbdView v, int iterations, PbdConst k) {
     cg::cluster_group cl = cg::this_cluster();
-    const int g = blockIdx.x / kPbdCluster;
+    const int csize = (int)cl.num_blocks();
+    const int g = blockIdx.x / csize;
     const int rank = (int)cl.block_rank();
     const int l0 = v.grp[g], l1 = v.grp[g + 1];
     if (l0 == l1 || iterations <= 0) return;  // uniform over the cluster
     // this thread's run [j, b1) of level l
     auto run_of = [&](int l, int &j, int &b1) {
         const int a = v.lvl[l], e = v.lvl[l + 1];
-        const int chunk = (e - a + kPbdCluster - 1) / kPbdCluster;
+        const int chunk = (e - a + csize - 1) / csize;
         const int b0 = a + rank * chunk;
         b1 = min(b0 + chunk, e);
         j = b0 + (int)threadIdx.x;
@@ -199,6 +208,82 @@ __global__ void __cluster_dims__(kPbdCluster, 1, 1) __launch_bounds__(kPbdThread
         cur = nxt;
         j = jn;
         b1 = bn;
+    }
+}
+
+// The same sweep with the instance's positions held in the cluster's
+// distributed shared memory: CTA r of the 16 keeps nodes [r S, (r + 1) S) of
+// the instance, and a tet corner is addressed by its code (owner CTA << 16 |
+// offset), so every level's position loads and stores go SM to SM instead of
+// through L2, and the cluster barrier releases shared-memory writes only.
+// Used when an instance's nodes fit (S * 16 B of dynamic shared memory a CTA).
+__device__ __forceinline__ float4 *dsm_node(cg::cluster_group &cl, float4 *s_px, int code) {
+    return cl.map_shared_rank(s_px, (unsigned)code >> 16) + (code & 0xffff);
+}
+
+__global__ void __launch_bounds__(kPbdThreads)
+    k_pbd_sweep_dsmem(PbdView v, const int4 *codes, const int4 *gnode, int iterations, PbdConst k) {
+    extern __shared__ float4 s_px[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int csize = (int)cl.num_blocks();
+    const int g = blockIdx.x / csize;
+    const int rank = (int)cl.block_rank();
+    const int4 gn = gnode[g];  // {first padded node, slice S, node count}
+    const int nb = gn.x, S = gn.y, cnt = gn.z;
+    for (int j = threadIdx.x; j < S; j += kPbdThreads) {
+        const int n = rank * S + j;
+        if (n < cnt) s_px[j] = v.px[nb + n];
+    }
+    cl.sync();
+    const int l0 = v.grp[g], l1 = v.grp[g + 1];
+    const int total = iterations > 0 ? iterations * (l1 - l0) : 0;
+    auto run_of = [&](int l, int &j, int &b1) {
+        const int a = v.lvl[l], e = v.lvl[l + 1];
+        const int chunk = (e - a + csize - 1) / csize;
+        const int b0 = a + rank * chunk;
+        b1 = min(b0 + chunk, e);
+        j = b0 + (int)threadIdx.x;
+    };
+    auto apply = [&](const PbdTet &t) {
+        const float D[9] = {t.r0.x, t.r0.y, t.r0.z, t.r1.x, t.r1.y, t.r1.z, t.r2.x, t.r2.y, t.r2.z};
+        float4 *ptr[4] = {dsm_node(cl, s_px, t.q.x), dsm_node(cl, s_px, t.q.y), dsm_node(cl, s_px, t.q.z),
+                          dsm_node(cl, s_px, t.q.w)};
+        float4 p[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) p[c] = *ptr[c];
+        float dp[4][3];
+        pbd_project(p, D, k, dp);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            *ptr[c] = make_float4(fadd(p[c].x, dp[c][0]), fadd(p[c].y, dp[c][1]), fadd(p[c].z, dp[c][2]), p[c].w);
+    };
+    PbdView vc = v;  // the static records with corner codes in place of node ids
+    vc.tet = codes;
+    int j = 0, b1 = 0;
+    PbdTet cur;
+    if (total > 0) {
+        run_of(l0, j, b1);
+        cur = pbd_load(vc, j < b1 ? j : v.lvl[l0]);
+    }
+    for (int st = 0; st < total; ++st) {
+        const int l = l0 + st % (l1 - l0);
+        // the next level's first record before this level's chain
+        int jn = 0, bn = 0;
+        PbdTet nxt = cur;
+        if (st + 1 < total) {
+            run_of(l + 1 < l1 ? l + 1 : l0, jn, bn);
+            if (jn < bn) nxt = pbd_load(vc, jn);
+        }
+        if (j < b1) apply(cur);
+        for (int jj = j + kPbdThreads; jj < b1; jj += kPbdThreads) apply(pbd_load(vc, jj));
+        cl.sync();
+        cur = nxt;
+        j = jn;
+        b1 = bn;
+    }
+    for (int j = threadIdx.x; j < S; j += kPbdThreads) {
+        const int n = rank * S + j;
+        if (n < cnt) v.px[nb + n] = s_px[j];
     }
 }
 
@@ -494,8 +579,84 @@ cudaError_t launch_pbd_sweeps(cudaStream_t s, const PbdView &v, int n_groups, in
     PbdConst k;
     for (int i = 0; i < 3; ++i) { k.stretch[i] = stretch[i]; k.shear[i] = shear[i]; }
     k.eps = 1e-6f;
-    k_pbd_sweep<<<n_groups * kPbdCluster, kPbdThreads, 0, s>>>(v, iterations, k);
-    return cudaGetLastError();
+    static int big_ok = -1;  // whether 16-CTA clusters of this kernel can be resident
+    if (big_ok < 0) {
+        big_ok = 0;
+        if (cudaFuncSetAttribute(k_pbd_sweep, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t q = {};
+            q.gridDim = dim3(kPbdClusterMax);
+            q.blockDim = dim3(kPbdThreads);
+            cudaLaunchAttribute qa;
+            qa.id = cudaLaunchAttributeClusterDimension;
+            qa.val.clusterDim.x = kPbdClusterMax;
+            qa.val.clusterDim.y = 1;
+            qa.val.clusterDim.z = 1;
+            q.attrs = &qa;
+            q.numAttrs = 1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveClusters(&n, k_pbd_sweep, &q) == cudaSuccess && n > 0) big_ok = 1;
+        }
+        cudaGetLastError();  // a refused query leaves no error behind
+    }
+    const int csize = (big_ok && n_groups <= 4) ? kPbdClusterMax : 8;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(n_groups * csize);
+    cfg.blockDim = dim3(kPbdThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = csize;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_pbd_sweep, v, iterations, k);
+}
+
+bool pbd_dsmem_fits(int smem_bytes) {
+    if (smem_bytes > 227 * 1024) return false;
+    if (cudaFuncSetAttribute(k_pbd_sweep_dsmem, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(k_pbd_sweep_dsmem, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t q = {};
+    q.gridDim = dim3(kPbdClusterMax);
+    q.blockDim = dim3(kPbdThreads);
+    q.dynamicSmemBytes = smem_bytes;
+    cudaLaunchAttribute qa;
+    qa.id = cudaLaunchAttributeClusterDimension;
+    qa.val.clusterDim.x = kPbdClusterMax;
+    qa.val.clusterDim.y = 1;
+    qa.val.clusterDim.z = 1;
+    q.attrs = &qa;
+    q.numAttrs = 1;
+    int n = 0;
+    const bool ok = cudaOccupancyMaxActiveClusters(&n, k_pbd_sweep_dsmem, &q) == cudaSuccess && n > 0;
+    cudaGetLastError();
+    return ok;
+}
+
+cudaError_t launch_pbd_sweeps_dsmem(cudaStream_t s, const PbdView &v, const int4 *codes, const int4 *gnode,
+                                    int n_groups, int smem_bytes, int iterations, const float stretch[3],
+                                    const float shear[3]) {
+    PbdConst k;
+    for (int i = 0; i < 3; ++i) { k.stretch[i] = stretch[i]; k.shear[i] = shear[i]; }
+    k.eps = 1e-6f;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(n_groups * kPbdClusterMax);
+    cfg.blockDim = dim3(kPbdThreads);
+    cfg.dynamicSmemBytes = smem_bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = kPbdClusterMax;
+    at.val.clusterDim.y = 1;
+    at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_pbd_sweep_dsmem, v, codes, gnode, iterations, k);
 }
 
 cudaError_t launch_dyn_end(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *px, const float4 *x0,

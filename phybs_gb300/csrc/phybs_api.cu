@@ -105,12 +105,16 @@ struct pbs_handle {
     // (its matrix built per (dt_matrix, stiffness)); dyn_* are their per-step
     // positions, start positions and right-hand-side base
     std::vector<int> h_inst_tets;  // per instance: first, end padded tet
+    std::vector<int> h_inst_nodes;  // per instance: first, end padded node
     bool pbd_ready = false;
     int pbd_groups = 0;
     DevBuf<int> pbd_grp, pbd_lvl;
     DevBuf<int4> pbd_tet;
     DevBuf<float4> pbd_d0, pbd_d1, pbd_d2;
     DevBuf<float2> pbd_node;  // {1 / mass, gravity_y} of the PBD rest data
+    // distributed-shared-memory variant: per-corner codes and per-group ranges
+    int pbd_smem = 0;  // 0: positions stay in global memory
+    DevBuf<int4> pbd_codes, pbd_gnode;
     bool pd_ready = false;
     float pd_dtm = 0.f, pd_k = 0.f;
     DevBuf<float> pd_val, pd_dinv;
@@ -169,7 +173,7 @@ struct pbs_handle {
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
         pbd_grp.release(); pbd_lvl.release(); pbd_tet.release(); pbd_d0.release(); pbd_d1.release(); pbd_d2.release();
-        pbd_node.release();
+        pbd_node.release(); pbd_codes.release(); pbd_gnode.release();
         pd_val.release(); pd_dinv.release(); dyn_px.release(); dyn_x0.release(); dyn_s.release();
         pbd_ready = pd_ready = false;
         DevBuf<float4> *cv[] = {&cg_b, &cg_x, &cg_r, &cg_z, &cg_p, &cg_q};
@@ -377,6 +381,8 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
         for (int i = nptr[b]; i < nptr[b + 1]; ++i) h->user2pad[i] = node_off[b] + (i - nptr[b]);
         h->h_inst_tets.push_back(ctl[b].tet_begin);
         h->h_inst_tets.push_back(ctl[b].tet_end);
+        h->h_inst_nodes.push_back(ctl[b].node_begin);
+        h->h_inst_nodes.push_back(ctl[b].node_end);
     }
     const int Np = pn, Tp = pt;
     for (int b = 0; b < B; ++b) {  // mean edge length: cbrt(6 * mean |vol|)
@@ -1263,6 +1269,37 @@ static int ensure_pbd(pbs_handle *h) {
     ord.release();
     CK(e);
     h->pbd_groups = B;
+    // positions in the cluster's distributed shared memory when every
+    // instance's nodes fit 16 slices (a few instances; batches of many small
+    // instances keep the global-memory sweep)
+    h->pbd_smem = 0;
+    if (B <= 4) {
+        int slice = 0;
+        for (int b = 0; b < B; ++b)
+            slice = std::max(slice, (h->h_inst_nodes[2 * b + 1] - h->h_inst_nodes[2 * b] + 15) / 16);
+        const int smem = std::max(slice, 1) * (int)sizeof(float4);
+        if (slice <= 0xffff && pbd_dsmem_fits(smem)) {
+            std::vector<int4> gn(B), codes(std::max(n, 1));
+            for (int b = 0; b < B; ++b) {
+                const int nb = h->h_inst_nodes[2 * b], cnt = h->h_inst_nodes[2 * b + 1] - nb;
+                gn[b] = make_int4(nb, std::max((cnt + 15) / 16, 1), cnt, 0);
+            }
+            for (int b = 0; b < B; ++b)
+                for (int j = lvl[grp[b]]; j < lvl[grp[b + 1]]; ++j) {
+                    const int *q = &tet[j].x;
+                    int c[4];
+                    for (int k = 0; k < 4; ++k) {
+                        const int loc = q[k] - gn[b].x;
+                        c[k] = ((loc / gn[b].y) << 16) | (loc % gn[b].y);
+                    }
+                    codes[j] = make_int4(c[0], c[1], c[2], c[3]);
+                }
+            CK(h->pbd_codes.alloc(codes.size())); CK(h->pbd_gnode.alloc(B));
+            CK(cudaMemcpy(h->pbd_codes.p, codes.data(), sizeof(int4) * codes.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->pbd_gnode.p, gn.data(), sizeof(int4) * B, cudaMemcpyHostToDevice));
+            h->pbd_smem = smem;
+        }
+    }
     h->pbd_ready = true;
     return PBS_OK;
 }
@@ -1298,7 +1335,11 @@ int pbs_pbd_step(pbs_handle *h, float dt, int iterations, const float *stretch, 
         PbdView v;
         v.grp = h->pbd_grp.p; v.lvl = h->pbd_lvl.p; v.tet = h->pbd_tet.p;
         v.d0 = h->pbd_d0.p; v.d1 = h->pbd_d1.p; v.d2 = h->pbd_d2.p; v.px = h->dyn_px.p;
-        CK(launch_pbd_sweeps(s, v, h->pbd_groups, iterations, stretch ? stretch : st_def, shear ? shear : sh_def));
+        if (h->pbd_smem > 0)
+            CK(launch_pbd_sweeps_dsmem(s, v, h->pbd_codes.p, h->pbd_gnode.p, h->pbd_groups, h->pbd_smem, iterations,
+                                       stretch ? stretch : st_def, shear ? shear : sh_def));
+        else
+            CK(launch_pbd_sweeps(s, v, h->pbd_groups, iterations, stretch ? stretch : st_def, shear ? shear : sh_def));
     }
     CK(launch_dyn_end(s, m, st, h->dyn_px.p, h->dyn_x0.p, dt, 0));
     CK(cudaStreamSynchronize(s));

@@ -323,6 +323,15 @@ cudaError_t launch_pbd_begin(cudaStream_t s, const DevMesh &m, const DevState &s
                              const float4 *ext, float dt, float4 *px, float4 *x0);
 cudaError_t launch_pbd_sweeps(cudaStream_t s, const PbdView &v, int n_groups, int iterations, const float stretch[3],
                               const float shear[3]);
+// The sweeps with an instance's positions in its 16-CTA cluster's
+// distributed shared memory: codes = per tet corner (owner CTA << 16 |
+// offset), gnode = per group {first padded node, slice, node count};
+// pbd_dsmem_fits: whether 16-CTA clusters with smem_bytes a CTA can be
+// resident (sets the kernel's attributes).
+bool pbd_dsmem_fits(int smem_bytes);
+cudaError_t launch_pbd_sweeps_dsmem(cudaStream_t s, const PbdView &v, const int4 *codes, const int4 *gnode,
+                                    int n_groups, int smem_bytes, int iterations, const float stretch[3],
+                                    const float shear[3]);
 cudaError_t launch_dyn_end(cudaStream_t s, const DevMesh &m, const DevState &st, const float4 *px, const float4 *x0,
                            float dt, int divide_first);
 cudaError_t launch_pd_assemble(cudaStream_t s, const DevMesh &m, const BsrView &A, float dt_matrix, float stiffness,

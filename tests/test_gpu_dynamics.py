@@ -91,10 +91,12 @@ def test_pbd_box_and_options_bitwise(iterations, stretch, shear):
     s.close()
 
 
-def test_pbd_packed_batch_bitwise():
-    """Three uneven boxes packed in one handle: each instance's sweep (one
-    cluster each) equals the restatement of that instance alone."""
-    m = M.batch_of_boxes(3, seed=7, nxy=(3, 6), nz=(5, 12))
+@pytest.mark.parametrize("n_inst", [3, 6])
+def test_pbd_packed_batch_bitwise(n_inst):
+    """Uneven boxes packed in one handle: each instance's sweep (one cluster
+    each: 16 CTAs for up to four instances, 8 beyond) equals the restatement
+    of that instance alone."""
+    m = M.batch_of_boxes(n_inst, seed=7, nxy=(3, 6), nz=(5, 12))
     x = M.twist_positions(m.rest, 0.05, axis=2).astype(np.float32)
     x[m.pins] = m.rest[m.pins]
     s = DescentSolver(m, positions=x)
