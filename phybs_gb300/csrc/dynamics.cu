@@ -644,6 +644,10 @@ cudaError_t launch_pbd_sweeps_dsmem(cudaStream_t s, const PbdView &v, const int4
     PbdConst k;
     for (int i = 0; i < 3; ++i) { k.stretch[i] = stretch[i]; k.shear[i] = shear[i]; }
     k.eps = 1e-6f;
+    // the kernel's shared-memory limit is per function, not per handle: set
+    // it for this launch (another handle may have set a smaller one)
+    cudaError_t e = cudaFuncSetAttribute(k_pbd_sweep_dsmem, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(n_groups * kPbdClusterMax);
     cfg.blockDim = dim3(kPbdThreads);
