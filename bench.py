@@ -490,13 +490,16 @@ def run_batch(args, rank, world):
 
 
 def run_dynamics(args, rank, world, kind):
-    """The reference's other two integrators on the 1M-tet box (50 x 50 x 80
-    cubes, 5-tet split, top face pinned), twisted 0.3 rad about its long axis
-    and released under gravity: `pbd` = strain-based PBD with the reference's
+    """The reference's other integrators on the 1M-tet box (50 x 50 x 80
+    cubes, 5-tet split, both end faces pinned at rest), twisted about its
+    long axis by 0.3 rad sin(pi s) (s the height fraction) and stepped under
+    gravity: `pbd` = strain-based PBD with the reference's
     5 sweeps, stretch 1, shear 0.8 (PosBaseDynamic.cpp), dt = 1/30; `pd` =
     projective dynamics with stiffness 1e6 and 5 local/global iterations
-    (ProjDynamic.cpp), dt = 0.03, CG to 1e-6.  A step is one call through the
-    C ABI (synchronous; positions stay on the device)."""
+    (ProjDynamic.cpp), dt = 0.03, CG to 1e-6; `be` = the linearly implicit
+    backward-Euler step (CUDAInterface::doBackEuler), dt = 0.03,
+    alpha = beta = 0.02, CG to 1e-6.  A step is one call through the C ABI
+    (synchronous; positions stay on the device)."""
     import torch
 
     from phybs_gb300 import meshes as M
@@ -505,10 +508,16 @@ def run_dynamics(args, rank, world, kind):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     m, _, _, _ = box_workload(args.seed, args.scale)
-    x = M.twist_positions(m.rest, 0.3, axis=2).astype(np.float32)
-    x[m.pins] = m.rest[m.pins]
+    # twisted 0.3 rad at mid-height, 0 at both pinned end faces (which stay at
+    # rest: the backward-Euler step's pins are springs to the rest positions)
+    x = M.twist_positions(m.rest, 0.3, axis=2, profile="sine").astype(np.float32)
     s = DescentSolver(m, positions=x)
-    step = (lambda: s.pbd_step(1 / 30)) if kind == "pbd" else (lambda: s.pd_step(0.03, tol=1e-6))
+    if kind == "pbd":
+        step = lambda: s.pbd_step(1 / 30)
+    elif kind == "pd":
+        step = lambda: s.pd_step(0.03, tol=1e-6)
+    else:
+        step = lambda: s.backward_euler_step(dt=0.03, tol=1e-6, max_iters=20000)[0]
     for _ in range(args.warmup):
         step()
     stream = torch.cuda.ExternalStream(s.stream())
@@ -519,7 +528,7 @@ def run_dynamics(args, rank, world, kind):
         e0.record(stream)
         for _ in range(args.steps):
             r = step()
-            if kind == "pd":
+            if kind in ("pd", "be"):
                 cg.append(r)
         e1.record(stream)
         sync_ranks(world)
@@ -528,17 +537,19 @@ def run_dynamics(args, rank, world, kind):
     if rank != 0:
         return
     line = {
-        "metric": ("strain-based PBD steps/s (5 sweeps)" if kind == "pbd" else
-                   "projective-dynamics steps/s (5 local/global iterations)") +
+        "metric": {"pbd": "strain-based PBD steps/s (5 sweeps)",
+                   "pd": "projective-dynamics steps/s (5 local/global iterations)",
+                   "be": "backward-Euler steps/s (CG to 1e-6)"}[kind] +
                   (", 1M-tet box, 1 GB300" if args.scale == 1.0 else f", {m.n_tets}-tet box, 1 GB300"),
         "value": world * args.steps / t, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"box, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes, top pinned, "
-                               f"twisted 0.3 rad, gravity", "seed": args.seed, "scale": args.scale},
+        "config": {"workload": f"box, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes, both ends pinned, "
+                               f"twisted 0.3 rad sin(pi s) along its height, gravity", "seed": args.seed,
+                   "scale": args.scale},
         "clocks": clk.summary(),
     }
-    if kind == "pd":
+    if kind in ("pd", "be"):
         line["cg_iterations_per_step"] = cg
     else:
         L = M.pbd_levels(m.tets, m.n_nodes)
@@ -571,9 +582,9 @@ def main():
                     help="pass stress evaluation (default: incremental)")
     ap.add_argument("--shape", default=None,
                     help="launch shapes 'threads,tets,nodes,staged,node_npt' instead of autotuning (profiling runs)")
-    ap.add_argument("--workload", choices=["box1m", "batch", "pbd", "pd"], default="box1m",
-                    help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances; pbd / pd: the "
-                         "strain-based PBD / projective-dynamics steps on the 1M-tet box")
+    ap.add_argument("--workload", choices=["box1m", "batch", "pbd", "pd", "be"], default="box1m",
+                    help="box1m: the 1M-tet pull (the headline); batch: 256 uneven instances; pbd / pd / be: the "
+                         "strain-based PBD / projective-dynamics / backward-Euler steps on the 1M-tet box")
     args = ap.parse_args()
     if args.stress is not None:
         global INCREMENTAL_STRESS
@@ -589,7 +600,7 @@ def main():
         torch.distributed.init_process_group("gloo")
     if args.workload == "batch":
         run_batch(args, rank, world)
-    elif args.workload in ("pbd", "pd"):
+    elif args.workload in ("pbd", "pd", "be"):
         run_dynamics(args, rank, world, args.workload)
     else:
         run_ours(args, rank, world)
