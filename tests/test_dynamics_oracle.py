@@ -92,3 +92,38 @@ def test_pd_inverted_tets_match_reference(g):
     xs, _ = P.pd_step(g["x_inv"], np.zeros_like(g["x_inv"]), g["mass"], g["inv_mass"], g["tets"], g["dminv"],
                       g["vol"], g["gravity"], dt=float(g["dt"]), flip=2)
     assert np.abs(xs - g["x_pd_inv"]).max() / diag > 1e-3
+
+
+def test_pd_split_time_step_matches_reference():
+    """The reference forms its matrix with the integrator's time step
+    (fvm.cpp:300-307) and steps with dt = 0.03 (fvm.cpp:169): with the two
+    different, the restatement still follows the reference's own build."""
+    from oracle import ref as R
+    if not R.available():
+        pytest.skip("reference build not available")
+    g = load_golden("dynamics_bar_small")
+    sim = R.RefSim(g["rest"], g["tets"], g["pins"], 5e5, 0.45)
+    sim.set_nodes(g["x0"])
+    sim.set_vel(np.zeros_like(g["x0"]))
+    sim.set_ext(np.zeros_like(g["x0"]))
+    sim.pd_step(0.03, dt_matrix=0.02)
+    x, _ = P.pd_step(g["x0"], np.zeros_like(g["x0"]), g["mass"], g["inv_mass"], g["tets"], g["dminv"], g["vol"],
+                     g["gravity"], dt=0.03, dt_matrix=0.02)
+    diag = bbox_diag(g["rest"])
+    assert np.abs(x - sim.nodes()).max() / diag < 5e-5
+    same_dt, _ = P.pd_step(g["x0"], np.zeros_like(g["x0"]), g["mass"], g["inv_mass"], g["tets"], g["dminv"],
+                           g["vol"], g["gravity"], dt=0.03)
+    assert np.abs(x - same_dt).max() / diag > 1e-4  # the split changes the step
+    sim.close()
+
+
+def test_pbd_levels_count():
+    """The dependency-level count of a Gauss-Seidel sweep: a chain of tets
+    sharing a node has one level per tet; tets sharing no node, one level."""
+    from phybs_gb300 import meshes as M
+    chain = np.array([[0, 1, 2, 3], [3, 4, 5, 6], [6, 7, 8, 9]])
+    assert M.pbd_levels(chain, 10) == 3
+    apart = np.array([[0, 1, 2, 3], [4, 5, 6, 7], [8, 9, 10, 11]])
+    assert M.pbd_levels(apart, 12) == 1
+    m = M.box_mesh(10, 10, 40, edge=0.005, seed=0)
+    assert M.pbd_levels(m.tets, m.n_nodes) == 920
