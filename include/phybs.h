@@ -19,7 +19,10 @@
  *   - every function returns PBS_OK (0) or a negative PBS_E_* code; the
  *     library never exits the process and never prints.
  *   - one handle = one CUDA stream on the current device; a handle is not
- *     thread-safe.  Calls are synchronous unless stated otherwise.
+ *     thread-safe.  Calls are synchronous unless stated otherwise.  The
+ *     handle's stream is non-blocking (it does not wait for the legacy
+ *     default stream); every call makes the handle's device current and
+ *     restores the caller's current device before it returns.
  *   - there is no CPU path: without a usable GB300 (sm_103) every call that
  *     needs the device fails with PBS_E_CUDA / PBS_E_NO_DEVICE.
  */
@@ -44,19 +47,19 @@ extern "C" {
 
 /* Materials.  Both are the neo-Hookean energy
  *   Psi = mu/2 (I1 - 3) - mu ln J + lambda/2 (ln J)^2,
- * evaluated through the invariants (IsotropicNeohookeanMaterial.cpp:146)
+ * evaluated through the invariants (IsotropicNeohookeanMaterial.cpp:104)
  * or through the principal stretches of the modified SVD
  * (IsotropicMaterial.cpp:360-409, Xu et al. 2015). */
 #define PBS_MATERIAL_NEOHOOKEAN 0
 #define PBS_MATERIAL_STRETCH 1
 
 /* Line-search rejection behaviour. */
-#define PBS_CONTROL_REFERENCE 0 /* alpha *= shrink; iterations -= k - 8; redo k (DescentOptimize.cpp:166-177) */
+#define PBS_CONTROL_REFERENCE 0 /* alpha *= shrink; iterations -= k - 8; redo k (DescentOptimize.cpp:111-122) */
 #define PBS_CONTROL_RESTART 1   /* alpha *= shrink; restore x, restart the Chebyshev history and rho schedule;
                                    the iteration budget is unchanged                                          */
 
 /* Energy clamp per tet. */
-#define PBS_CLAMP_CPU 0 /* e > 1e-6 ? e : 0   (IsotropicNeohookeanMaterial.cpp:171) */
+#define PBS_CLAMP_CPU 0 /* e > 1e-6 ? e : 0   (IsotropicNeohookeanMaterial.cpp:129) */
 #define PBS_CLAMP_GPU 1 /* max(e, 0)          (CUDAInterface.cu:549)               */
 
 typedef struct pbs_handle pbs_handle;
@@ -77,7 +80,7 @@ typedef struct pbs_mesh_desc {
 } pbs_mesh_desc;
 
 /* Step parameters.  pbs_default_params() returns the reference preset: the
- * constants of DescentOptimize.cpp:59-77,146-240 and CUDAInterface.cu:911-1006
+ * constants of DescentOptimize.cpp:4-22,91-185 and CUDAInterface.cu:911-1006
  * (h = 0.03, 96 iterations, alpha 0.1 / 0.7 / 0.01, line search every 8,
  * Hessian diagonal every 32, rho profile {1:0.96, 7:0.991, 10:0.999},
  * damping 0.99, warm start 0.2, CPU energy clamp, gravity and external
@@ -96,7 +99,7 @@ typedef struct pbs_step_params {
     float damping;            /* v = damping * (x - x0) / h                      */
     float warm_start;         /* x_init = x~ + warm_start * h * (v - v_old)      */
     float body_force_scale;  /* times gravity + external forces enter the gradient:
-                                 2 = DescentOptimize.cpp:107 with IsotropicNeohookeanMaterial.cpp:140,
+                                 2 = DescentOptimize.cpp:52 with IsotropicNeohookeanMaterial.cpp:98,
                                  1 = CUDAInterface.cu:600-602 (physical)          */
     int energy_clamp;         /* PBS_CLAMP_*                                     */
     int pass_cap;             /* hard cap on device passes per step; 0 = max_iters + 16 */
@@ -142,7 +145,7 @@ int pbs_create(const pbs_mesh_desc *desc, pbs_handle **out);
 void pbs_destroy(pbs_handle *h);
 
 /* Lame parameters as the reference forms them from (E, nu)
- * (IsotropicNeohookeanMaterial.cpp:57-58, CUDAInterface.cu:704-705):
+ * (IsotropicNeohookeanMaterial.cpp:15-16, CUDAInterface.cu:704-705):
  * mu = E / (2 (1 + nu)), lambda = 2 mu / (1 - 2 nu) when reference_formula
  * is nonzero, else the textbook lambda = 2 mu nu / (1 - 2 nu). */
 void pbs_lame(float young, float poisson, int reference_formula, float *mu, float *lambda);
@@ -173,7 +176,7 @@ int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old);
  * xyz: 3*count floats) before the next step.  This is how a caller prescribes
  * the motion of pinned nodes: the reference has no such call, its harness
  * writes TetMesh::getNodes() directly (pinned nodes stay where they are put
- * within a step, DescentOptimize.cpp:109-113 / CUDAInterface.cu:578-585). */
+ * within a step, DescentOptimize.cpp:54-58 / CUDAInterface.cu:578-585). */
 int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float *xyz);
 /* Initial guess for the next pbs_step only (3*N positions, caller order;
  * pinned nodes keep their prescribed positions).  The step treats it as it
@@ -218,7 +221,14 @@ int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *
  * memory in its own pool.  No counterpart in the reference.
  *   - positions and forces are DEVICE pointers on the handle's device; the
  *     two kernels are enqueued on the handle's stream (pbs_get_stream) and
- *     the call returns without waiting for them.
+ *     the call returns without waiting for them.  That stream is created
+ *     non-blocking: it does not wait for the legacy default stream or any
+ *     other stream of the caller.  Order the work that writes `positions`
+ *     before the call, and the work that reads `forces` after it, against
+ *     pbs_get_stream's stream (enqueue it there, or use events).
+ *   - positions are not checked for finiteness (they stay on the device):
+ *     a non-finite position gives non-finite forces, where pbs_eval_nodes
+ *     would return PBS_E_INVALID_ARG.
  *   - allocates nothing: the per-tet corner-force scratch is one fixed
  *     24 MiB array in the library's device image, which bounds the mesh to
  *     PBS_EVAL_STATIC_MAX_TETS tets after padding (each instance's tet count
@@ -226,10 +236,12 @@ int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *
  *     pointers with PBS_E_INVALID_ARG.
  *   - the first call on a device looks up that array's address (with the
  *     device current) and keeps it; make this first call before any stream
- *     capture.
+ *     capture.  After a cudaDeviceReset the next call looks it up again
+ *     (make that one before any capture too).
  *   - every call on a device shares the array: calls whose kernels overlap
  *     on the GPU (different streams with no ordering between them) race and
- *     corrupt each other's forces.  Nothing in it needs to start at zero. */
+ *     corrupt each other's forces.  Nothing in it needs to start at zero.
+ *   - the caller's current device is left as it was. */
 #define PBS_EVAL_STATIC_MAX_TETS 524288
 int pbs_eval_nodes_static(pbs_handle *h, const float *positions, float *forces);
 
@@ -376,7 +388,7 @@ int pbs_get_face_ring(pbs_handle *h, int face, int *ring, int capacity, int *siz
  * whose centre lies nearest the ray (orig, dir), within the length of face 0's
  * first edge; *face = -1 when none does.  orig and dir: 3 floats each. */
 int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face);
-/* TetMesh::dragFaceRing (TetMesh.cpp:446-470): the external forces of a drag
+/* TetMesh::dragFaceRing (TetMesh.cpp:443-470): the external forces of a drag
  * of `face` along drag (3 floats) at the current positions, written to ext
  * (3 * N floats, caller order; zero off the ring) for the next pbs_step:
  * factor = min(|drag| / r * 100, 800) with r face 0's first edge, factor * m

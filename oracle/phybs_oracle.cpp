@@ -6,16 +6,16 @@
 // reference every result is measured against), the reference CPU solver:
 //
 //   rest state          TetMesh.cpp:186-216, computeANs TetMesh.cpp:279-294
-//   Lame parameters     IsotropicNeohookeanMaterial.cpp:57-58 (lambda = 2mu/(1-2nu))
-//   NH forces           IsotropicNeohookeanMaterial.cpp:135-156
+//   Lame parameters     IsotropicNeohookeanMaterial.cpp:15-16 (lambda = 2mu/(1-2nu))
+//   NH forces           IsotropicNeohookeanMaterial.cpp:93-114
 //   stretch forces      IsotropicMaterial.cpp:360-409 with the modified SVD
 //                       IsotropicMaterial.cpp:16-60 and the principal-stretch
-//                       gradient IsotropicNeohookeanMaterial.cpp:92-102
-//   energy              IsotropicNeohookeanMaterial.cpp:158-173
+//                       gradient IsotropicNeohookeanMaterial.cpp:50-60
+//   energy              IsotropicNeohookeanMaterial.cpp:116-131
 //   Hessian diagonal    IsotropicMaterial.cpp:503-552 + 872-1019 (Xu et al. 2015
 //                       dP/dF through SVD derivatives, eps-perturbed spectrum),
-//                       stretch Hessian IsotropicNeohookeanMaterial.cpp:105-133
-//   descent step        DescentOptimize.cpp:90-243
+//                       stretch Hessian IsotropicNeohookeanMaterial.cpp:63-91
+//   descent step        DescentOptimize.cpp:35-188
 //
 // The SVD is a cyclic Jacobi eigen-solve of F^T F (converged to the working
 // precision) with sigma_i = |F v_i|, followed by the reference's sign fix-ups;
@@ -199,7 +199,7 @@ template <typename R> M3<R> deformation_gradient(const R *x, const int *t, const
     return mul(Ds, Dinv);
 }
 
-// IsotropicNeohookeanMaterial.cpp:146: P = mu (F - F^-T) + lambda ln(det F) F^-T
+// IsotropicNeohookeanMaterial.cpp:104: P = mu (F - F^-T) + lambda ln(det F) F^-T
 template <typename R> M3<R> pk1_nh(const M3<R> &F, R mu, R lambda) {
     M3<R> FiT = transpose(inv3(F));
     R lj = std::log(det3(F));
@@ -209,12 +209,12 @@ template <typename R> M3<R> pk1_nh(const M3<R> &F, R mu, R lambda) {
     return P;
 }
 
-// IsotropicNeohookeanMaterial.cpp:92-102
+// IsotropicNeohookeanMaterial.cpp:50-60
 template <typename R> void stretch_gradient(const R s[3], R mu, R lambda, R g[3]) {
     R tmp = lambda * (std::log(s[0]) + std::log(s[1]) + std::log(s[2])) - mu;
     for (int i = 0; i < 3; ++i) g[i] = mu * s[i] + tmp / s[i];
 }
-// IsotropicNeohookeanMaterial.cpp:105-133 (row-major 3x3)
+// IsotropicNeohookeanMaterial.cpp:63-91 (row-major 3x3)
 template <typename R> void stretch_hessian(const R s[3], R mu, R lambda, R h[9]) {
     R tmp = lambda * (std::log(s[0]) + std::log(s[1]) + std::log(s[2]));
     R tmp1 = mu + lambda - tmp, tmp2 = tmp - mu;
@@ -240,7 +240,7 @@ template <typename R> M3<R> pk1_stretch(const M3<R> &F, R mu, R lambda) {
 }
 
 // Corner forces: H = P * AN; corners 1..3 take H's columns, corner 0 takes
-// minus their sum (IsotropicNeohookeanMaterial.cpp:147-152).
+// minus their sum (IsotropicNeohookeanMaterial.cpp:105-110).
 template <typename R> void corner_forces(const M3<R> &P, const M3<R> &AN, R out[12]) {
     M3<R> H = mul(P, AN);
     for (int d = 0; d < 3; ++d) {
@@ -251,7 +251,7 @@ template <typename R> void corner_forces(const M3<R> &P, const M3<R> &AN, R out[
     }
 }
 
-// IsotropicNeohookeanMaterial.cpp:164-171; clamp 0: e > 1e-6 ? e : 0 (CPU),
+// IsotropicNeohookeanMaterial.cpp:122-130; clamp 0: e > 1e-6 ? e : 0 (CPU),
 // clamp 1: max(e, 0) (CUDAInterface.cu:549).
 // keep_nan: an inverted tet's NaN energy stays NaN (RESTART control) instead of
 // the reference clamps' 0.
@@ -486,7 +486,7 @@ typedef struct orc_params {
     float profile_rho[4];
     float damping, warm_start;
     float body_force_scale;  // times gravity + external forces enter the gradient (2: DescentOptimize.cpp:52 with
-                             // IsotropicNeohookeanMaterial.cpp:140; 1: CUDAInterface.cu:600-602)
+                             // IsotropicNeohookeanMaterial.cpp:98; 1: CUDAInterface.cu:600-602)
     int energy_clamp;
     int material;           // 0 NH invariants, 1 stretch-based
     int hessian_closed;     // 1: closed-form diagonal, 0: SVD (Xu et al.) path
@@ -593,7 +593,7 @@ int orc_svd(int prec, int count, const double *F9, double *U9, double *S3, doubl
     return 0;
 }
 
-// One descent time step of one instance (DescentOptimize.cpp:146-243), in
+// One descent time step of one instance (DescentOptimize.cpp:91-188), in
 // precision `prec`.  State in/out: x0 (node positions at step start ->
 // end), v, v_old (the reference's m_vel_old).  ext: external forces (3N).
 // The Chebyshev scalars rho/omega persist across steps in *cheb (2 values)
@@ -611,7 +611,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
         for (size_t i = 0; i < N3; ++i) ex[i] = ext ? (R)ext[i] : R(0);
         const R h = (R)p->h;
         const R h2inv = R(1) / (h * h);
-        // DescentOptimize::initialization (DescentOptimize.cpp:90-96)
+        // DescentOptimize::initialization (DescentOptimize.cpp:35-41)
         std::vector<R> xt(N3), x(N3), xlast(N3), xold(N3), xnext(N3), g(N3), hq(N3, R(0)), fel;
         for (size_t i = 0; i < N3; ++i) {
             xt[i] = x0[i] + h * v[i];
@@ -644,7 +644,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             ++passes;
             if (k % p->line_search_every == 0 || force_check) {
                 force_check = false;
-                // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:118-144): the
+                // DescentOptimize::computeTotalEnergy (DescentOptimize.cpp:63-89): the
                 // gravity term 0.5 m 2 g y is -gravity_y . y; plus the external work
                 // -f_ext . x over free nodes.
                 const R Ee = elastic_energy(m, x, p->energy_clamp, restart ? 1 : 0);
@@ -675,7 +675,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                 for (int i = 0; i < n; ++i)
                     for (int d = 0; d < 3; ++d) hq[3 * i + d] += (R)m.mass[i] * h2inv;
             }
-            // DescentOptimize::computeGradient (DescentOptimize.cpp:98-116).
+            // DescentOptimize::computeGradient (DescentOptimize.cpp:43-61).
             elastic_forces(m, x, p->material, fel);
             double r2 = 0;
             for (int i = 0; i < n; ++i)
@@ -696,7 +696,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             ratio = g0 > 0 ? r / g0 : 0.0;
             if (p->tol > 0 && k > 0 && r <= (double)p->tol * g0) { converged = 1; break; }
             for (size_t id = 0; id < N3; ++id) xnext[id] = x[id] + alpha * (g[id] / -hq[id]);
-            // Chebyshev schedule (DescentOptimize.cpp:211-233)
+            // Chebyshev schedule (DescentOptimize.cpp:156-178)
             const int ks = k - k_restart;
             if (ks == 0) { rho = 0; omega = 1; }
             omega = R(4) / (R(4) - rho * rho * omega);
@@ -709,7 +709,7 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             xlast = x;
             x = xnext;
         }
-        // DescentOptimize.cpp:238-240
+        // DescentOptimize.cpp:183-185
         for (size_t i = 0; i < N3; ++i) {
             vold[i] = v[i];
             v[i] = (R)p->damping * (x[i] - x0[i]) / h;

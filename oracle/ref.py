@@ -46,13 +46,30 @@ def lib():
                      "ref_get_dminv", "ref_get_an", "ref_force_nh", "ref_force_stretch", "ref_elastic_energy",
                      "ref_hessian_diag", "ref_element_stiffness", "ref_total_energy", "ref_csr_sizes", "ref_csr",
                      "ref_step", "ref_get_scalars", "ref_face_ring_size", "ref_face_ring", "ref_pick_face",
-                     "ref_drag_face_ring", "ref_get_ext", "ref_get_inv_mass"]:
+                     "ref_drag_face_ring", "ref_get_ext", "ref_get_inv_mass", "ref_load_model"]:
             getattr(_lib, name).argtypes = None
     return _lib
 
 
 def _f(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def load_model(stem: str):
+    """TetMesh's own loader (TetMesh.cpp:14-151) on ``<stem>.node/.ele/.face``:
+    (rest (N, 3) float32 after its x0.1 scaling, tets (T, 4) int32 in file
+    order, pins selected by its hard-coded rule (TetMesh.cpp:38-39))."""
+    for ext in (".node", ".ele", ".face"):
+        if not os.path.exists(stem + ext):  # the loader would exit the process
+            raise FileNotFoundError(stem + ext)
+    L = lib()
+    n, t, p = C.c_int(), C.c_int(), C.c_int()
+    L.ref_load_model(stem.encode(), C.byref(n), C.byref(t), C.byref(p), None, None, None)
+    rest = np.zeros((n.value, 3), np.float32)
+    tets = np.zeros((t.value, 4), np.int32)
+    pins = np.zeros(p.value, np.int32)
+    L.ref_load_model(stem.encode(), C.byref(n), C.byref(t), C.byref(p), _p(rest), _p(tets), _p(pins))
+    return rest, tets, pins
 
 
 def _p(a):

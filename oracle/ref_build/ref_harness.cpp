@@ -210,7 +210,7 @@ void ref_force_stretch(void *h, const float *pos, int nthreads, float *out) {
     std::memcpy(out, f.data(), sizeof(float) * f.size());
 }
 
-// Per-tet clamped elastic energy (IsotropicNeohookeanMaterial.cpp:158-173).
+// Per-tet clamped elastic energy (IsotropicNeohookeanMaterial.cpp:116-131).
 void ref_elastic_energy(void *h, const float *pos, float *out) {
     RefSim *s = S(h);
     s->mat->computeElasticEnergyFromPos(as_pos(pos, s->mesh->getNodesNum()));
@@ -218,7 +218,7 @@ void ref_elastic_energy(void *h, const float *pos, float *out) {
     std::memcpy(out, e.data(), sizeof(float) * e.size());
 }
 
-// diag(K(pos)) as DescentOptimize.cpp:188 forms it (before adding M/h^2).
+// diag(K(pos)) as DescentOptimize.cpp:133 forms it (before adding M/h^2).
 void ref_hessian_diag(void *h, const float *pos, float *out) {
     RefSim *s = S(h);
     Eigen::SparseMatrix<float, Eigen::RowMajor> K =
@@ -325,6 +325,24 @@ void *ref_pd_create(void *h, float dt_matrix, int iterations) {
     pd->buildGlobalSolverMatrix(m->getMasses(), m->getTets(), dt_matrix, m->getDmInvs());
     return pd;
 }
+// TetMesh's own loader (TetMesh.cpp:14-151, run by its constructor) on the
+// tetgen files <stem>.node/.ele/.face: rest positions after its x0.1 scaling
+// (3 x n_nodes, column-major), tets in file order (4 x n_tets) and the nodes its
+// hard-coded rule pins (TetMesh.cpp:38-39).  Pass NULL outputs to read the
+// sizes only.  The caller checks that the three files exist: the loader exits
+// the process when one is missing.
+void ref_load_model(const char *stem, int *n_nodes, int *n_tets, int *n_pins, float *rest, int *tets, int *pins) {
+    phybs_shim_set_mesh_stem(stem);
+    TetMesh m;
+    phybs_shim_set_mesh_stem("");
+    *n_nodes = m.getNodesNum();
+    *n_tets = m.getTetsNum();
+    *n_pins = (int)m.m_constraintIDs.size();
+    if (rest) std::memcpy(rest, m.getRestPosition().data(), sizeof(float) * 3 * (size_t)*n_nodes);
+    if (tets) std::memcpy(tets, m.getTets().data(), sizeof(int) * 4 * (size_t)*n_tets);
+    if (pins) std::memcpy(pins, m.m_constraintIDs.data(), sizeof(int) * (size_t)*n_pins);
+}
+
 void ref_pd_destroy(void *pd) { delete static_cast<ProjDynamic *>(pd); }
 void ref_pd_step(void *pd, void *h, float dt) {
     TetMesh *m = S(h)->mesh.get();

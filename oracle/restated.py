@@ -100,7 +100,7 @@ def rest(pos, tets, pin_mask, density=1000.0, prec=64) -> Rest:
 
 def lame(young, poisson, reference_lambda=True):
     """mu = E / (2 (1 + nu)); lambda = 2 mu / (1 - 2 nu) as the reference computes it
-    (IsotropicNeohookeanMaterial.cpp:57-58), or the textbook 2 mu nu / (1 - 2 nu)."""
+    (IsotropicNeohookeanMaterial.cpp:15-16), or the textbook 2 mu nu / (1 - 2 nu)."""
     e = np.asarray(young, np.float32)
     nu = np.asarray(poisson, np.float32)
     mu = (np.float32(0.5) * e / (np.float32(1) + nu)).astype(np.float32)

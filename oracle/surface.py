@@ -14,7 +14,7 @@ of a MatrixXf on both sides).
 * face_rings         TetMesh::computeBoundfaceRingIndices  TetMesh.cpp:229-277
 * normals_centers    TetMesh::computeBoundfaceNormals      TetMesh.cpp:378-393
 * pick_face          TetMesh::pickFacebyRay                TetMesh.cpp:395-418
-* drag_face_ring     TetMesh::dragFaceRing                 TetMesh.cpp:446-470
+* drag_face_ring     TetMesh::dragFaceRing                 TetMesh.cpp:443-470
 * ext_energy         TetMesh::computeExternalForcesEnergy  TetMesh.cpp:595-614
 """
 from __future__ import annotations

@@ -23,7 +23,7 @@
 // On line-search passes the CTA also adds the clamped tet energies and its
 // share of the instance's node energy terms (FP64, fixed order); the
 // instance's last chunk to finish decides accept / reject
-// (DescentOptimize.cpp:162-183) before any node moves.
+// (DescentOptimize.cpp:107-128) before any node moves.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -274,7 +274,7 @@ __device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const f
 // Line-search pass: adds the chunk's share of the instance's node energy terms
 // to the thread's tet energies e, stores the chunk's {sum e, sum e^2}, and in
 // the instance's last chunk to finish sums the chunks in order and decides
-// accept / reject (DescentOptimize.cpp:162-183).  The sums run in
+// accept / reject (DescentOptimize.cpp:107-128).  The sums run in
 // double-float (e) and FP32 (e^2, a noise scale), the chunk totals and their
 // sum in FP64.  Called by every thread of the CTA; *is_last is a shared word.
 template <int THREADS>

@@ -54,7 +54,15 @@ __device__ __forceinline__ float dot3e(const float a[3], const float b[3]) {
 // (error below 2^-44 relative) and rounded; the FP64 expression is evaluated
 // only when that value lies within 2^-40 relative of a float rounding
 // boundary, where the two roundings could differ (or for zero, non-finite or
-// tiny values).
+// tiny values).  Published methods used: the quotient is Markstein's
+// correction of an approximate reciprocal by its exact FMA remainder
+// r = a - q b (P. Markstein, "IA-64 and Elementary Functions", 2000, ch. 8);
+// S - 1 and the product by k use the error-free transformations TwoSum
+// (Knuth, TAOCP vol. 2, 4.2.2) and the FMA form of TwoProduct (Ogita, Rump
+// and Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005),
+// and the final renormalisation is Dekker's FastTwoSum (Dekker, Numer. Math.
+// 18, 1971).  The boundary test then decides whether the double-float value
+// determines the FP32 rounding of the exact FP64 quotient.
 __device__ __forceinline__ float pbd_stretch_mult(float S, float lam, float k) {
     float ah, al;
     two_sum(S, -1.0f, ah, al);  // S - 1 = ah + al exactly

@@ -8,7 +8,7 @@
 //           terms, reduced in FP64.  Corner terms are summed per node in
 //           shared memory into one partial per (node, chunk).  The instance's
 //           last chunk to finish decides accept / reject
-//           (DescentOptimize.cpp:162-183) before any node moves.  Replaces
+//           (DescentOptimize.cpp:107-128) before any node moves.  Replaces
 //           computeForceKd (CUDAInterface.cu:495-568) and its 13-25 atomics
 //           per tet.
 //   k_node  one thread per node: adds its partials in chunk order -- no
@@ -119,7 +119,7 @@ __device__ __forceinline__ const InstCtl &node_ctl(const DevMesh &m, const DevSt
     return st.ctl[m.nblk_inst[i / BLOCK]];
 }
 
-// DescentOptimize::initialization (DescentOptimize.cpp:90-96) /
+// DescentOptimize::initialization (DescentOptimize.cpp:35-41) /
 // initDescentOpt (CUDAInterface.cu:482-493) in displacement form:
 // u~ = u0 + h v, u_init = u~ + warm_start h (v - v_old); plus the external-
 // force upload.  Writes parity 0 (k_init_ctl resets it).
@@ -177,7 +177,7 @@ __global__ void k_guess_fallback(DevMesh m, DevState st) {
     st.ub[i] = h0;
 }
 
-// v_old <- v; v = damping (u - u0) / h; u0 <- u  (DescentOptimize.cpp:238-240)
+// v_old <- v; v = damping (u - u0) / h; u0 <- u  (DescentOptimize.cpp:183-185)
 __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2user) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
@@ -234,7 +234,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
     const float4 uh = nn.uh, ul = nn.ul, dd = nn.dd;
     float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
     if (c.action == ACT_RESTORE) {
-        // x <- x_old (DescentOptimize.cpp:171); the Chebyshev history keeps
+        // x <- x_old (DescentOptimize.cpp:116); the Chebyshev history keeps
         // x_last = x_{k-1} = u - d (the reference does not restore it), or
         // restarts it under PBS_CONTROL_RESTART
         nh = st.oh[i];
@@ -243,7 +243,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
             nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
                              ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
     } else {
-        if (c.action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:181)
+        if (c.action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:126)
             st.oh[i] = uh;
             st.ol[i] = ul;
         }
@@ -286,7 +286,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
             const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
             const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
             r2 = fmaf(gx, gx, fmaf(gy, gy, gz * gz));
-            // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:197-205), then the
+            // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:142-150), then the
             // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
             // d' = (omega - 1) d + omega delta
             const float alpha = c.alpha, omega = c.omega;

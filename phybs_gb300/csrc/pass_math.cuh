@@ -55,7 +55,7 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 }
 
 // Energy terms of one free node: 1/2 m |u - u~|^2 / h^2 - g_y u_y - f_ext . u
-// (DescentOptimize.cpp:128-142 / CUDAInterface.cu:589-597), measured from the
+// (DescentOptimize.cpp:73-87 / CUDAInterface.cu:589-597), measured from the
 // rest shape so that no large constant rides along in the sum.
 __device__ __forceinline__ double node_energy(const DevState &st, const float4 &info, const float4 &uh,
                                               const float4 &ul, int i, float h2inv) {

@@ -551,7 +551,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
 
 void pbs_destroy(pbs_handle *h) {
     if (!h) return;
-    cudaSetDevice(h->device);
+    DeviceScope scope(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->release();
     delete h;
@@ -562,7 +562,7 @@ int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lam
     if (model != PBS_MATERIAL_NEOHOOKEAN && model != PBS_MATERIAL_STRETCH) return PBS_E_INVALID_ARG;
     for (int i = 0; i < count; ++i)
         if (!std::isfinite(mu[i]) || !std::isfinite(lambda[i])) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     // stage mu and lambda through the (3N-float) staging buffer's neighbour
     DevBuf<float> buf;
     CK(buf.alloc(2 * (size_t)count));
@@ -619,7 +619,7 @@ static int ensure_graph(pbs_handle *h) {
 
 int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = ensure_graph(h);
     if (rc != PBS_OK) return rc;
     cudaStream_t s = h->stream;
@@ -690,7 +690,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
 
 int pbs_read_positions(pbs_handle *h, float *out) {
     if (!h || !out) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     CK(launch_pack_positions(h->stream, h->mesh(), h->u0h.p, h->u0l.p, h->pad2user.p, h->staging.p));
     CK(cudaMemcpyAsync(out, h->staging.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -724,14 +724,14 @@ static int upload_positions(pbs_handle *h, const float *positions, float4 *hi, f
 
 int pbs_update_positions(pbs_handle *h, const float *positions) {
     if (!h || !positions) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     return upload_positions(h, positions, h->u0h.p, h->u0l.p);
 }
 
 int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float *xyz) {
     if (!h || count < 0 || count > h->N || (count > 0 && (!ids || !xyz))) return PBS_E_INVALID_ARG;
     if (count == 0) return PBS_OK;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     std::vector<int> pad(count);
     for (int i = 0; i < count; ++i) {
         if (ids[i] < 0 || ids[i] >= h->N) return PBS_E_INVALID_ARG;
@@ -749,7 +749,7 @@ int pbs_set_node_positions(pbs_handle *h, int count, const int *ids, const float
 int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean, const float *feat_std,
                        const float *out_std, int enabled) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     if (!enabled) {
         h->ws_enabled = false;
         return PBS_OK;
@@ -778,7 +778,7 @@ int pbs_set_warm_start(pbs_handle *h, const float *theta, const float *feat_mean
 
 int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, float *x_init, float *scale) {
     if (!h || !features) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     cudaStream_t s = h->stream;
     DevMesh m = h->mesh();
     DevState st = h->state();
@@ -803,7 +803,7 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
 
 int pbs_set_guess(pbs_handle *h, const float *positions) {
     if (!h || !positions) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = upload_positions(h, positions, h->uh.p + h->Np, h->ul.p + h->Np);
     if (rc != PBS_OK) return rc;
     h->guess_pending = true;
@@ -882,7 +882,7 @@ extern "C" {
 
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
     if (!h || passes <= 0 || !tet_ms || !node_ms) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     return time_passes(h, passes, tet_ms, node_ms);
 }
 
@@ -893,14 +893,14 @@ int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_no
         (staged && threads == 512) ||
         chunk_smem(chunk_tets, chunk_nodes, true, staged) > (size_t)CHUNK_MAX_SMEM)
         return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     h->node_npt = node_npt;
     return set_pass_layout(h, threads, chunk_tets, chunk_nodes, staged, nullptr);
 }
 
 int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
     if (!h || passes <= 0) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     // chunk shapes: CTA threads, tets per chunk, nodes a chunk may touch,
     // staging (neo-Hookean only: 1 = rows staged in shared memory, 2 = the
     // persistent double-buffered kernel)
@@ -969,7 +969,7 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out) {
 
 int pbs_read_velocities(pbs_handle *h, float *v, float *v_old) {
     if (!h || (!v && !v_old)) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = PBS_OK;
     if (v) rc = download_user(h, h->v.p, v);
     if (rc == PBS_OK && v_old) rc = download_user(h, h->vold.p, v_old);
@@ -978,7 +978,7 @@ int pbs_read_velocities(pbs_handle *h, float *v, float *v_old) {
 
 int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old) {
     if (!h || (!v && !v_old)) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = PBS_OK;
     if (v) rc = upload_user(h, v, h->v.p);
     if (rc == PBS_OK && v_old) rc = upload_user(h, v_old, h->vold.p);
@@ -987,7 +987,7 @@ int pbs_write_velocities(pbs_handle *h, const float *v, const float *v_old) {
 
 int pbs_reset(pbs_handle *h) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     CK(cudaMemsetAsync(h->u0h.p, 0, sizeof(float4) * h->Np, h->stream));
     CK(cudaMemsetAsync(h->u0l.p, 0, sizeof(float4) * h->Np, h->stream));
     CK(cudaMemsetAsync(h->v.p, 0, sizeof(float4) * h->Np, h->stream));
@@ -1030,7 +1030,7 @@ int pbs_set_surface(pbs_handle *h, const int *faces, int n_faces) {
     if (!h || n_faces < 0 || (n_faces > 0 && !faces)) return PBS_E_INVALID_ARG;
     for (size_t i = 0; i < 3 * (size_t)n_faces; ++i)
         if (faces[i] < 0 || faces[i] >= h->N) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     h->faces_pad.release(); h->ring_pad.release(); h->pick_id.release(); h->pick_d2.release();
     h->n_faces = 0;
     h->h_ring_ptr.assign(1, 0);
@@ -1090,7 +1090,7 @@ static bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinit
 
 int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face) {
     if (!h || !orig || !dir || !face || h->n_faces == 0 || !finite3(orig) || !finite3(dir)) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     const int nb = pick_blocks(h->n_faces, h->sms);
     CK(launch_pick_face(h->stream, h->mesh(), h->state(), h->n_faces, h->faces_pad.p,
                         make_float3(orig[0], orig[1], orig[2]), make_float3(dir[0], dir[1], dir[2]), nb, h->pick_d2.p,
@@ -1104,7 +1104,7 @@ int pbs_pick_face(pbs_handle *h, const float *orig, const float *dir, int *face)
 
 int pbs_drag_face_ring(pbs_handle *h, int face, const float *drag, float *ext) {
     if (!h || !drag || !ext || face < 0 || face >= h->n_faces || !finite3(drag)) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     const int b = h->h_ring_ptr[face], len = h->h_ring_ptr[face + 1] - b;
     CK(launch_drag_ring(h->stream, h->mesh(), h->state(), h->faces_pad.p, h->ring_pad.p, b, len,
                         make_float3(drag[0], drag[1], drag[2]), h->drag_ext.p));
@@ -1180,7 +1180,7 @@ int pbs_backward_euler_step(pbs_handle *h, float dt, float alpha, float beta, co
                             int max_iters, int *iters_out, double *residual_out) {
     if (!h || !(dt > 0.f) || !(alpha >= 0.f) || !(beta >= 0.f) || !(tol > 0.f) || max_iters <= 0)
         return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = ensure_bsr(h);
     if (rc != PBS_OK) return rc;
     if (ext) {
@@ -1321,7 +1321,7 @@ int pbs_pbd_step(pbs_handle *h, float dt, int iterations, const float *stretch, 
     if (!h || !(dt > 0.f) || !std::isfinite(dt) || iterations < 0 || (stretch && !finite_n(stretch, 3)) ||
         (shear && !finite_n(shear, 3)))
         return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     int rc = ensure_pbd(h);
     if (rc == PBS_OK) rc = ensure_dyn_buffers(h);
     if (rc == PBS_OK && ext) rc = upload_user(h, ext, h->ext.p);
@@ -1352,7 +1352,7 @@ int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int i
     if (!h || !(dt > 0.f) || !std::isfinite(dt) || !(dt_matrix >= 0.f) || !std::isfinite(dt_matrix) ||
         !(stiffness > 0.f) || !std::isfinite(stiffness) || iterations < 0 || !(tol > 0.f) || max_cg <= 0)
         return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     const float dtm = dt_matrix > 0.f ? dt_matrix : dt;
     int rc = ensure_bsr(h);
     if (rc == PBS_OK) rc = ensure_dyn_buffers(h);
@@ -1411,7 +1411,7 @@ int pbs_pd_step(pbs_handle *h, float dt, float dt_matrix, float stiffness, int i
 
 int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {
     if (!h || !row_ptr || !entries) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     std::vector<int> iptr(h->Np + 1), ient(4 * (size_t)h->T);
     CK(cudaMemcpy(iptr.data(), h->inc_ptr.p, sizeof(int) * (h->Np + 1), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(ient.data(), h->inc.p, sizeof(int) * 4 * (size_t)h->T, cudaMemcpyDeviceToHost));
@@ -1431,7 +1431,7 @@ int pbs_get_incidence(pbs_handle *h, int *row_ptr, int *entries) {
 
 int pbs_get_rest_data(pbs_handle *h, float *dm_inv9, float *signed_vol, float *mass, float *grav_y) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     std::vector<float4> r0(h->Tp), r1(h->Tp), r2(h->Tp), inf(h->Np);
     CK(cudaMemcpy(r0.data(), h->row0.p, sizeof(float4) * h->Tp, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(r1.data(), h->row1.p, sizeof(float4) * h->Tp, cudaMemcpyDeviceToHost));
@@ -1471,7 +1471,7 @@ static int eval_common(pbs_handle *h, const float *positions, const float4 **xsr
 
 int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, float *energy, float *hess_diag) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     const float4 *x;
     int rc = eval_common(h, positions, &x);
     if (rc != PBS_OK) return rc;
@@ -1495,7 +1495,7 @@ int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, f
 
 int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag) {
     if (!h) return PBS_E_INVALID_ARG;
-    CK(cudaSetDevice(h->device));
+    PBS_DEVICE_SCOPE(h->device);
     const float4 *x;
     int rc = eval_common(h, positions, &x);
     if (rc != PBS_OK) return rc;

@@ -166,7 +166,7 @@ struct DevState {
 };
 
 // Chebyshev omega for iteration k from the persistent (rho, omega), as
-// DescentOptimize.cpp:211-230 / CUDAInterface.cu:967-986 compute it in FP32.
+// DescentOptimize.cpp:156-175 / CUDAInterface.cu:967-986 compute it in FP32.
 __device__ __host__ __forceinline__ void chebyshev_schedule(const DevParams &p, int k, float &rho, float &omega) {
     if (k == 0) { rho = 0.0f; omega = 1.0f; }
 #ifdef __CUDA_ARCH__
@@ -264,7 +264,42 @@ cudaError_t launch_eval_tets(cudaStream_t s, const DevMesh &m, const float4 *uh,
 cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, const float *hd, const int *pad2user,
                           float *force_user, float *hd_user);
 
+// Makes a handle's device current for the rest of an entry point's scope and
+// puts the caller's current device back on every return path: a call on a
+// handle never changes which device the caller's own CUDA work goes to.
+class DeviceScope {
+  public:
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) {
+            cudaGetLastError();
+            prev_ = -1;
+        }
+        if (prev_ == device) {
+            prev_ = -1;  // already current: nothing to restore
+            ok_ = true;
+        } else {
+            ok_ = cudaSetDevice(device) == cudaSuccess;
+        }
+    }
+    ~DeviceScope() {
+        if (prev_ >= 0) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+    bool ok() const { return ok_; }
+
+  private:
+    int prev_ = -1;
+    bool ok_ = false;
+};
+
 }  // namespace pbs
+
+// Enters a handle's device for the enclosing entry point (see DeviceScope);
+// returns PBS_E_CUDA when the device cannot be made current.
+#define PBS_DEVICE_SCOPE(dev)                  \
+    ::pbs::DeviceScope pbs_device_scope__(dev); \
+    if (!pbs_device_scope__.ok()) return PBS_E_CUDA
 
 struct pbs_handle;
 

@@ -16,9 +16,13 @@
 // rejected with PBS_E_CAPACITY.
 //
 // Set-up: the first call on a device looks up the array's device address
-// with that device current (cudaGetSymbolAddress) and keeps it for the later
-// calls on that device.  That first call should come before any stream
-// capture.
+// with that device current (cudaGetSymbolAddress) and keeps it, together with
+// the identity of the device's CUDA context, for the later calls on that
+// device.  That first call should come before any stream capture.  A later
+// call that finds another context current (the caller reset the device with
+// cudaDeviceReset, which unloads the library's device image) looks the
+// address up again, so no call writes through an address of a context that
+// no longer exists; that call too should come before any capture.
 //
 // Every call on a device shares the one array.  Two calls whose kernels
 // overlap on the GPU (on different streams: two handles, or two threads with
@@ -26,9 +30,9 @@
 // them on one stream or with events.  Nothing in the array has to start at
 // zero: the second kernel of a call reads only the slots the first kernel of
 // the same call has written.
+#include <cuda.h>  // CUcontext / CUresult of the two driver calls looked up below
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <cstdint>
 #include <mutex>
 
@@ -46,24 +50,61 @@ constexpr int kMaxDevices = 64;
 // 12 floats per padded tet: corner c's force at [12 t + 3 c, 12 t + 3 c + 2].
 static __device__ __align__(256) float g_corner_scratch[12 * (size_t)PBS_EVAL_STATIC_MAX_TETS];
 
-std::atomic<float *> g_scratch_ptr[kMaxDevices];
+// Per device: the scratch address and the id of the context it belongs to.
+struct ScratchSlot {
+    float *ptr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+ScratchSlot g_slot[kMaxDevices];
 std::mutex g_setup_mutex;
 
-// Device address of g_corner_scratch on `device` (which is current).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Unique id (for the process's lifetime) of the current CUDA context, or 0
+// when the driver cannot tell.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of g_corner_scratch on `device` (which is current): looked
+// up once per device and context.  Without a context id (an old driver) it is
+// looked up on every call.
 int scratch_for_device(int device, float **out) {
     if (device < 0 || device >= kMaxDevices) return PBS_E_CAPACITY;
-    float *p = g_scratch_ptr[device].load(std::memory_order_acquire);
-    if (!p) {
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        p = g_scratch_ptr[device].load(std::memory_order_relaxed);
-        if (!p) {
-            void *addr = nullptr;
-            if (cudaGetSymbolAddress(&addr, g_corner_scratch) != cudaSuccess || !addr) return PBS_E_CUDA;
-            p = static_cast<float *>(addr);
-            g_scratch_ptr[device].store(p, std::memory_order_release);
+    const unsigned long long id = current_context_id();
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    ScratchSlot &s = g_slot[device];
+    if (!s.ptr || id == 0 || s.ctx_id != id) {
+        void *addr = nullptr;
+        if (cudaGetSymbolAddress(&addr, g_corner_scratch) != cudaSuccess || !addr) {
+            cudaGetLastError();
+            s = ScratchSlot();
+            return PBS_E_CUDA;
         }
+        s.ptr = static_cast<float *>(addr);
+        s.ctx_id = id;
     }
-    *out = p;
+    *out = s.ptr;
     return PBS_OK;
 }
 
@@ -141,7 +182,7 @@ int pbs_eval_nodes_static(pbs_handle *h, const float *positions, float *forces) 
     HandleView v;
     handle_view(h, &v);
     if (v.mesh.Tp > PBS_EVAL_STATIC_MAX_TETS) return PBS_E_CAPACITY;
-    if (cudaSetDevice(v.device) != cudaSuccess) return PBS_E_CUDA;
+    PBS_DEVICE_SCOPE(v.device);
     float *scratch = nullptr;
     int rc = scratch_for_device(v.device, &scratch);
     if (rc != PBS_OK) return rc;

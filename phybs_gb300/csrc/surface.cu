@@ -4,7 +4,7 @@
 //
 //   k_pick_faces + k_pick_final   TetMesh::computeBoundfaceNormals +
 //                                 TetMesh::pickFacebyRay (TetMesh.cpp:378-418)
-//   k_drag_ring                   TetMesh::dragFaceRing (TetMesh.cpp:446-470)
+//   k_drag_ring                   TetMesh::dragFaceRing (TetMesh.cpp:443-470)
 //
 // Every float operation is written with explicit round-to-nearest intrinsics
 // in the reference's order (no contraction into FMA), so face ids and forces

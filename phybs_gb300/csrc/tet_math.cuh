@@ -18,16 +18,16 @@
 //
 // Reference semantics reproduced:
 //   F = Ds * Dm^-1                                      TetMesh.cpp:307-316
-//   neo-Hookean P = mu (F - F^-T) + lambda ln J F^-T     IsotropicNeohookeanMaterial.cpp:146
+//   neo-Hookean P = mu (F - F^-T) + lambda ln J F^-T     IsotropicNeohookeanMaterial.cpp:104
 //   stretch-based P = U diag(P^) V^T,
-//       P^_i = mu s_i + (lambda sum_j ln s_j - mu) / s_i  IsotropicNeohookeanMaterial.cpp:92-102
+//       P^_i = mu s_i + (lambda sum_j ln s_j - mu) / s_i  IsotropicNeohookeanMaterial.cpp:50-60
 //       with the modified SVD of IsotropicMaterial.cpp:16-60 (U, V rotations,
 //       an inversion's sign on the smallest singular value)
 //   corner forces H = P * AN, AN = -(det Dm / 6) Dm^-T   TetMesh.cpp:279-294
 //       (computeANs' cross-product normals equal -(det Dm/6) Dm^-T exactly),
 //       corners 1..3 = H's columns, corner 0 = minus their sum
 //   energy vol * (mu/2 (I1-3) - mu ln J + lambda/2 ln^2 J), clamped
-//                                                        IsotropicNeohookeanMaterial.cpp:164-171
+//                                                        IsotropicNeohookeanMaterial.cpp:122-130
 //   Jacobi diagonal: diagonal of K = -df/dx (IsotropicMaterial.cpp:503-552,
 //       which builds the full 12x12 element matrix from Xu et al.'s
 //       SVD-derivative dP/dF).  For this energy, restricted to one row d of F,
@@ -208,7 +208,7 @@ template <typename T> __device__ __forceinline__ T energy_density(const Kin<T> &
 }
 
 __device__ __forceinline__ float clamp_energy(float e, int clamp_cpu) {
-    if (clamp_cpu) return e > 1e-6f ? e : 0.0f;  // IsotropicNeohookeanMaterial.cpp:171
+    if (clamp_cpu) return e > 1e-6f ? e : 0.0f;  // IsotropicNeohookeanMaterial.cpp:129
     return fmaxf(e, 0.0f);                       // CUDAInterface.cu:549
 }
 

@@ -331,23 +331,31 @@ def _read_table(path: str):
 
 
 def load_tetgen(stem: str, scale: float = 1.0, young: float = 5e5, poisson: float = 0.45,
-                pins=None) -> TetMeshData:
+                pins=None, orient: bool = True) -> TetMeshData:
     """Load ``<stem>.node`` and ``<stem>.ele`` (tetgen text).
 
-    Index base follows the files (the reference meshes are 0-based).  Unlike
-    the reference loader, no coordinate scaling or pin rule is hard-coded:
-    ``scale`` and ``pins`` are arguments.
+    Coordinates are formed as TetMesh::initNodesFromFile forms them
+    (TetMesh.cpp:36-37): each decimal read into an FP32 float, then the column
+    multiplied by the scale rounded to FP32, in FP32; with ``scale`` = 0.1 the
+    positions equal the reference loader's bit for bit.  Index base follows
+    the files (the reference meshes are 0-based).  Unlike the reference
+    loader, no scaling or pin rule is hard-coded: ``scale`` and ``pins`` are
+    arguments.  ``orient``: swap corners 2 and 3 of every negatively oriented
+    tet (the device path wants positive orientation); False keeps the file's
+    corner order, as the reference loader does (TetMesh.cpp:93-114).
     """
     head, rows = _read_table(stem + ".node")
     n = int(head[0])
     ids = np.array([int(r[0]) for r in rows[:n]], np.int64)
-    pos = np.array([[float(r[1]), float(r[2]), float(r[3])] for r in rows[:n]], np.float64) * scale
+    pos = np.array([[float(r[1]), float(r[2]), float(r[3])] for r in rows[:n]], np.float64).astype(np.float32)
+    if scale != 1.0:
+        pos = (pos * np.float32(scale)).astype(np.float32)
     base = int(ids.min()) if n else 0
     head, rows = _read_table(stem + ".ele")
     t = int(head[0])
     tets = np.array([[int(r[1]), int(r[2]), int(r[3]), int(r[4])] for r in rows[:t]], np.int64) - base
-    tets = orient_positive(pos, tets)
-    return TetMeshData(pos.astype(np.float32), tets, np.zeros(0, np.int32) if pins is None else pins,
+    tets = orient_positive(pos, tets) if orient else tets.astype(np.int32)
+    return TetMeshData(pos, tets, np.zeros(0, np.int32) if pins is None else pins,
                        young, poisson, name=os.path.basename(stem))
 
 

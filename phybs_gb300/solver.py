@@ -22,7 +22,7 @@ from . import _lib as L
 from .meshes import TetMeshData
 
 PRESETS = {
-    # DescentOptimize (CPU) reference semantics: DescentOptimize.cpp:59-77,146-243
+    # DescentOptimize (CPU) reference semantics: DescentOptimize.cpp:4-22,91-188
     "cpu_reference": dict(body_force_scale=2.0, energy_clamp=L.PBS_CLAMP_CPU),
     # CUDAInterface (GPU) reference semantics: CUDAInterface.cu:572-609, 911-1007
     "gpu_reference": dict(body_force_scale=1.0, energy_clamp=L.PBS_CLAMP_GPU),

@@ -7,11 +7,11 @@ oracle/_ref by oracle/ref_build/Makefile):
 
 Each fixture freezes, for one mesh, the reference's outputs: the rest state it
 loaded (TetMesh.cpp:186-216), forces / energies / Hessian diagonal at a
-deformed probe state (IsotropicNeohookeanMaterial.cpp:135-173,
+deformed probe state (IsotropicNeohookeanMaterial.cpp:93-131,
 IsotropicMaterial.cpp:360-409, 503-682), the stiffness CSR pattern
 (IsotropicMaterial.cpp:554-644) for small meshes, and the node positions and
 velocities after successive DescentOptimize::doDescentOpt steps
-(DescentOptimize.cpp:146-243); and, in separate fixtures, the surface
+(DescentOptimize.cpp:91-188); and, in separate fixtures, the surface
 picking / drag, element stiffness and PBD / projective-dynamics outputs.
 Meshes are the procedural workloads of the
 benchmark configurations, at fixture-friendly sizes, plus two of the
@@ -28,8 +28,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle import REFERENCE_TREE  # noqa: E402
+if not os.environ.get("PHYBS_REFERENCE") and os.path.isdir("/root/reference/FVM"):
+    os.environ["PHYBS_REFERENCE"] = "/root/reference"
+import oracle  # noqa: E402
 from oracle import ref as REF  # noqa: E402
+
+REFERENCE_TREE = oracle.reference_tree()
+if REFERENCE_TREE is None:
+    raise SystemExit("make_golden.py reads the reference checkout: set PHYBS_REFERENCE")
 from phybs_gb300 import meshes as M  # noqa: E402
 
 
@@ -236,9 +242,60 @@ def make_dynamics(name, cfg, rng, pbd_steps=3, pd_steps=2, dt=0.03):
     print(name, len(rest), len(m.tets), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def make_reference_lines():
+    """reference_lines.json: the line count of every C/C++/CUDA source under
+    the reference's FVM/ and 3rd/CUDA_helper/, by file name, so that the
+    file:line citations of this repository can be checked without the
+    reference checkout (tests/test_citations.py)."""
+    import json
+    out = {}
+    for sub in ("FVM", os.path.join("3rd", "CUDA_helper")):
+        d = os.path.join(REFERENCE_TREE, sub)
+        for f in sorted(os.listdir(d)):
+            if f.endswith((".cpp", ".cu", ".h", ".hpp", ".cuh")):
+                with open(os.path.join(d, f), "rb") as fh:
+                    out[f] = len(fh.read().splitlines())
+    with open(os.path.join(HERE, "reference_lines.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+        fh.write("\n")
+    print("reference_lines.json", len(out), "files")
+
+
+def make_loader_digests():
+    """loader_models.json: for every tetgen mesh the reference ships
+    (model/*/*.node with .ele and .face), what TetMesh's own loader
+    (TetMesh.cpp:14-151) makes of it -- node and tet counts, the nodes its
+    hard-coded rule pins, and SHA-256 digests of its FP32 rest positions
+    (after the x0.1 scaling) and int32 tets in file order -- so that
+    meshes.load_tetgen can be checked against it bit for bit
+    (tests/test_loader_parity.py)."""
+    import glob
+    import hashlib
+    import json
+    out = {}
+    for node in sorted(glob.glob(os.path.join(REFERENCE_TREE, "model", "*", "*.node"))):
+        stem = node[:-len(".node")]
+        if not all(os.path.exists(stem + e) for e in (".ele", ".face")):
+            continue
+        rest, tets, pins = REF.load_model(stem)
+        rel = os.path.relpath(stem, os.path.join(REFERENCE_TREE, "model"))
+        out[rel] = dict(n_nodes=int(rest.shape[0]), n_tets=int(tets.shape[0]), pins=pins.tolist(),
+                        rest_sha256=hashlib.sha256(np.ascontiguousarray(rest, np.float32).tobytes()).hexdigest(),
+                        tets_sha256=hashlib.sha256(np.ascontiguousarray(tets, np.int32).tobytes()).hexdigest())
+    with open(os.path.join(HERE, "loader_models.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+        fh.write("\n")
+    print("loader_models.json", len(out), "meshes")
+
+
 if __name__ == "__main__":
-    # `make_golden.py surface|stiffness|dynamics` write only those fixtures
+    # `make_golden.py surface|stiffness|dynamics|lines|loader|inverted` write
+    # only those fixtures
     only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only in (None, "lines"):
+        make_reference_lines()
+    if only in (None, "loader"):
+        make_loader_digests()
     rng = np.random.default_rng(20261203)
     if only is None:
         for n, c in cases().items():

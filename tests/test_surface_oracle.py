@@ -44,7 +44,7 @@ def test_normals_centres_and_picks(sg, k):
 
 @pytest.mark.parametrize("k", [0, 1])
 def test_drag_forces_and_energy(sg, k):
-    """dragFaceRing and computeExternalForcesEnergy (TetMesh.cpp:446-470, 595-614)."""
+    """dragFaceRing and computeExternalForcesEnergy (TetMesh.cpp:443-470, 595-614)."""
     x = sg[f"x{k}"]
     rings = S.face_rings(sg["faces"], x.shape[0])
     for j, (f, d) in enumerate(zip(sg[f"drag_face{k}"], sg[f"drag{k}"])):

@@ -37,12 +37,16 @@ def _deformed(mesh, seed):
 
 
 def _static_forces(s, x):
-    xd = torch.from_numpy(np.ascontiguousarray(x.reshape(-1))).to("cuda")
-    fd = torch.full_like(xd, float("nan"))
-    rc = L.lib().pbs_eval_nodes_static(s._h, C.c_void_p(xd.data_ptr()), C.c_void_p(fd.data_ptr()))
-    L.check(rc, "pbs_eval_nodes_static")
+    # the handle's stream does not wait for torch's: the inputs are written,
+    # and the forces read, on that stream itself
+    with torch.cuda.stream(torch.cuda.ExternalStream(s.stream())):
+        xd = torch.from_numpy(np.ascontiguousarray(x.reshape(-1))).to("cuda")
+        fd = torch.full_like(xd, float("nan"))
+        rc = L.lib().pbs_eval_nodes_static(s._h, C.c_void_p(xd.data_ptr()), C.c_void_p(fd.data_ptr()))
+        L.check(rc, "pbs_eval_nodes_static")
+        out = fd.cpu().numpy().reshape(-1, 3)
     torch.cuda.synchronize()
-    return fd.cpu().numpy().reshape(-1, 3)
+    return out
 
 
 @pytest.mark.parametrize("material", [L.PBS_MATERIAL_NEOHOOKEAN, L.PBS_MATERIAL_STRETCH])
@@ -57,6 +61,35 @@ def test_static_scratch_forces_match_eval_nodes(material):
         scale = np.abs(ref).max()
         assert scale > 0
         assert np.abs(got - ref).max() <= RTOL * scale, (call, np.abs(got - ref).max() / scale)
+    s.close()
+
+
+def test_static_scratch_allocates_nothing():
+    """After one call (which loads the library's device image, scratch
+    included), further calls leave the device's free memory unchanged and the
+    caller's current device as it was."""
+    mesh = M.box_mesh(10, 8, 12, edge=0.01, seed=4, young=2e5, poisson=0.4)
+    s = DescentSolver(mesh)
+    x = _deformed(mesh, 1)
+    with torch.cuda.stream(torch.cuda.ExternalStream(s.stream())):
+        xd = torch.from_numpy(np.ascontiguousarray(x.reshape(-1))).to("cuda")
+        fd = torch.empty_like(xd)
+    torch.cuda.synchronize()
+    lib = L.lib()
+    args = (s._h, C.c_void_p(xd.data_ptr()), C.c_void_p(fd.data_ptr()))
+    L.check(lib.pbs_eval_nodes_static(*args), "pbs_eval_nodes_static")
+    torch.cuda.synchronize()
+    dev = torch.cuda.current_device()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(8):
+        L.check(lib.pbs_eval_nodes_static(*args), "pbs_eval_nodes_static")
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.cuda.current_device() == dev
+    ref, _ = s.eval_nodes(x)
+    got = fd.cpu().numpy().reshape(-1, 3)
+    assert np.abs(got - ref).max() <= RTOL * np.abs(ref).max()
     s.close()
 
 
