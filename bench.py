@@ -50,12 +50,6 @@ UNIT = "frames/s"
 # x_next 12 B written, amortised over tets): 56 + 64 N / T.
 STATIC_BYTES_PER_TET = 56.0
 BYTES_PER_NODE = 64.0
-# Iterations a frame of the box workload takes with the plain descent (mean
-# over the timed frames 3..29 of the GPU solve, seed 0, incremental stress,
-# alpha_grow 1.2: 772); used only by the CPU reference arm, which times a
-# bounded sample of iterations and cannot afford whole frames at 1M tets.
-REFERENCE_ITERS_PER_FRAME = 772.0
-CPU_SAMPLE_ITERS = 32
 BATCH_ITERS = 96  # doDescentOpt(h, iterations) as fvm.cpp:187 calls it
 
 
@@ -177,50 +171,85 @@ def ncu_traffic():
     return None
 
 
-def cpu_baseline_sample(m, bottom, length, frame, iters=CPU_SAMPLE_ITERS, threads=0):
-    """CPU restatement of the reference step: seconds per iteration on the
-    full mesh (one Jacobi-diagonal refresh and four energy checks per 32
-    iterations, as the reference's schedule has).  The per-tet loops run on
-    `threads` host threads (0 = all cores; the reference's DescentOptimize is
-    serial, its material classes use OpenMP); returns (s/iteration, passes,
-    threads)."""
+class CpuFrames:
+    """The CPU restatement of the reference's descent step (oracle/phybs_oracle.cpp,
+    DescentOptimize.cpp:91-188 with the benchmark's control: RESTART, alpha0,
+    alpha growth, one Chebyshev stage, iterate to |g| <= 1e-4 |g0|) on the
+    box workload, whole frames.  Its per-tet loops (forces, energies, Hessian
+    diagonal) run on `threads` host threads (0 = all cores; the reference's
+    DescentOptimize itself is serial, its material classes use OpenMP); the
+    results do not depend on the thread count."""
+
+    def __init__(self, m, bottom, length, threads=0, prec=32, x=None, v=None, v_old=None):
+        from oracle import restated as O
+        from phybs_gb300.solver import lame_arrays
+        self.O = O
+        self.m, self.bottom, self.length, self.prec = m, bottom, length, prec
+        self.threads = O.set_threads(threads)
+        self.mu, self.lam = lame_arrays(m.young, m.poisson)
+        self.pm = m.pin_mask()
+        self.r = O.rest(m.rest, m.tets, self.pm, prec=prec)
+        self.st = O.StepState(m.rest if x is None else x, v, v_old)
+        self.p = O.make_params(h=1 / 30, max_iters=20000, tol=1e-4, control=1, body_force_scale=1.0,
+                               energy_clamp=1, alpha0=ALPHA0, profile=((10, RHO),), alpha_grow=ALPHA_GROW,
+                               hessian_closed=1)
+
+    def frame(self, f):
+        """Frame f whole: (seconds, iterations, converged)."""
+        self.st.x0[self.bottom] = bottom_positions(self.m, self.bottom, self.length, f)
+        t0 = time.perf_counter()
+        o = self.O.step(self.st, self.p, self.m.tets, self.r, self.mu, self.lam, self.pm, prec=self.prec)
+        return time.perf_counter() - t0, int(o.passes), int(o.converged)
+
+
+def cpu_force_comparator(m, x, calls=3, threads=0):
+    """The reference's OpenMP force evaluation computeInnerForcesfromFhats2
+    (IsotropicMaterial.cpp:411-453, ported: FP32, the modified SVD of every
+    tet, one global lock around the node scatter) at positions x on all host
+    cores: seconds per call (best of `calls`) and the thread count."""
     from oracle import restated as O
     from phybs_gb300.solver import lame_arrays
-    threads = O.set_threads(threads)
     mu, lam = lame_arrays(m.young, m.poisson)
-    pm = m.pin_mask()
-    r = O.rest(m.rest, m.tets, pm, prec=32)
-    st = O.StepState(m.rest)
-    st.x0[bottom] = bottom_positions(m, bottom, length, frame)
-    p = O.make_params(h=1 / 30, max_iters=iters, tol=0.0, control=1, body_force_scale=1.0, energy_clamp=1,
-                      alpha0=ALPHA0, profile=((10, RHO),))
-    t0 = time.perf_counter()
-    stats = O.step(st, p, m.tets, r, mu, lam, pm, prec=32)
-    dt = time.perf_counter() - t0
-    return dt / max(stats.passes, 1), stats.passes, threads
+    r = O.rest(m.rest, m.tets, m.pin_mask(), prec=32)
+    best, n = float("inf"), 0
+    for _ in range(calls):
+        t0 = time.perf_counter()
+        O.forces_fhats2_omp(x, m.tets, r.dinv, r.an, mu, lam, threads=threads)
+        best = min(best, time.perf_counter() - t0)
+    if threads <= 0:
+        threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    return best, threads
 
 
 def run_reference(args):
+    """The CPU reference arm: frames 0 .. W-1 run whole and untimed, frames
+    W .. W+K-1 run whole and timed (host wall clock, all host threads)."""
     m, bottom, length, young = box_workload(args.seed, args.scale)
-    ipf = REFERENCE_ITERS_PER_FRAME
-    times = []
-    threads = 1
-    for s in range(args.warmup + args.steps):
-        spi, _, threads = cpu_baseline_sample(m, bottom, length, s)
-        if s >= args.warmup:
-            times.append(spi * ipf)
-    sec_per_frame = float(np.mean(times))
-    value = 1.0 / sec_per_frame
+    cpu = CpuFrames(m, bottom, length, threads=0, prec=args.cpu_prec)
+    times, iters, conv = [], [], []
+    for f in range(args.warmup + args.steps):
+        dt, it, c = cpu.frame(f)
+        if f >= args.warmup:
+            times.append(dt)
+            iters.append(it)
+            conv.append(c)
+    total = float(np.sum(times))
+    value = args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"box {m.n_tets} tets / {m.n_nodes} nodes, plain descent to |g|<=1e-4|g0|",
-                   "seed": args.seed, "young": young},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{CPU_SAMPLE_ITERS} iterations of each frame on the full mesh (FP32 "
-                                   f"restatement of DescentOptimize, per-tet loops on {threads} threads), "
-                                   f"x {ipf:.0f} iterations/frame of the plain GPU descent"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": f"f{args.cpu_prec}",
+        "data": "synthetic",
+        "config": {"workload": f"box 50x50x80 cubes, 5-tet split: {m.n_tets} tets / {m.n_nodes} nodes; bottom face "
+                               f"pulled to 1.5x over 30 frames; plain descent; every frame to |g|<=1e-4|g0|; frames "
+                               f"{args.warmup}..{args.warmup + args.steps - 1} timed",
+                   "seed": args.seed, "young": young, "h": 1 / 30, "tol": 1e-4, "alpha0": ALPHA0, "rho": RHO},
+        "iterations": iters, "iterations_per_frame": float(np.mean(iters)), "converged": conv,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.threads, "kind": "port",
+                         "sample": f"frames {args.warmup}..{args.warmup + args.steps - 1} whole (after frames "
+                                   f"0..{args.warmup - 1} untimed), FP{args.cpu_prec} restatement of "
+                                   f"DescentOptimize with the benchmark's control, per-tet loops on "
+                                   f"{cpu.threads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -295,6 +324,8 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
         s.step(raise_on_error=False)
 
     res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0}
+    # the state the first timed frame starts from (the CPU baseline's start)
+    res["state"] = (s.positions(), *s.velocities())
     sync_ranks(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -334,6 +365,26 @@ def profile_pass(args, m, tune=None):
         return s.profile_kernels(20), None
     except Exception as exc:  # an instance stopped early: no valid per-kernel time
         return None, f"{exc}; {s.stats()}"
+    finally:
+        s.close()
+
+
+def stretch_pass_ms(args, m, x, tune=None):
+    """The GPU's counterpart of the CPU force evaluation: mean time of the
+    per-tet pass kernel (stretch-based forces of every tet, summed per node and
+    chunk) at positions x, CUDA events on the library's stream; None when it
+    cannot be timed."""
+    from phybs_gb300 import _lib as L
+    from phybs_gb300.solver import DescentSolver
+    s = DescentSolver(m, positions=x, material=L.PBS_MATERIAL_STRETCH,
+                      params=solver_params(max_iters=args.max_iters, incremental=0))
+    try:
+        if tune is not None:
+            s.set_chunk_shape(tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], 0, tune["node_npt"])
+        tet_ms, _ = s.profile_kernels(20)
+        return tet_ms
+    except Exception:
+        return None
     finally:
         s.close()
 
@@ -407,13 +458,26 @@ def run_ours(args, rank, world):
         line["speedup_vs_plain"] = warm["frames_per_s"] / plain["frames_per_s"]
         line["clocks_plain"] = plain["clocks"]
     if not args.no_cpu_baseline:
-        spi, n, threads = cpu_baseline_sample(m, bottom, length, args.warmup)
-        ipf = float(np.mean(plain["iters"]))
-        cpu_value = 1.0 / (spi * ipf)
-        line["cpu_baseline"] = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{n} iterations of frame {args.warmup} on the full mesh (FP32 "
-                                          f"restatement of DescentOptimize, per-tet loops on {threads} threads), "
-                                          f"x {ipf:.0f} iterations/frame of the plain descent on the GPU"}
+        # whole frames W .. W+n-1 on the host, from the plain GPU arm's state at
+        # the start of frame W
+        x0, v0, vo0 = plain["state"]
+        cpu = CpuFrames(m, bottom, length, threads=0, prec=args.cpu_prec, x=x0, v=v0, v_old=vo0)
+        n = max(1, min(args.cpu_frames, args.steps))
+        fr = [cpu.frame(args.warmup + j) for j in range(n)]
+        secs = float(sum(t for t, _, _ in fr))
+        line["cpu_baseline"] = {"value": n / secs, "unit": UNIT, "cores": cpu.threads, "kind": "port",
+                                "sample": f"frames {args.warmup}..{args.warmup + n - 1} whole on the full mesh, from "
+                                          f"the plain GPU arm's state at frame {args.warmup} (FP{args.cpu_prec} "
+                                          f"restatement of DescentOptimize with the benchmark's control, per-tet "
+                                          f"loops on {cpu.threads} threads)",
+                                "iterations": [it for _, it, _ in fr], "converged": [c for _, _, c in fr],
+                                "seconds": [round(t, 3) for t, _, _ in fr]}
+        fsec, fthreads = cpu_force_comparator(m, x0, calls=3)
+        line["cpu_force_eval"] = {
+            "what": "the reference's OpenMP computeInnerForcesfromFhats2(nthreads) (IsotropicMaterial.cpp:411-453), "
+                    "ported: stretch-based forces of all tets, FP32, one global lock around the node scatter",
+            "ms_per_call": fsec * 1e3, "cores": fthreads, "tets": T,
+            "gpu_stretch_pass_ms": stretch_pass_ms(args, m, x0, tune)}
     print(json.dumps(line))
 
 
@@ -577,6 +641,13 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="mesh resolution scale (1.0 = the 1M-tet box)")
     ap.add_argument("--max-iters", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-frames", type=int, default=3, help="whole frames the GPU arm's CPU baseline times")
+    # FP64 by default: the FP32 restatement, like the reference, sums the
+    # line search's energies in FP32, and on the 1M-tet box that noise rejects
+    # good steps until alpha falls below 0.01 short of the 1e-4 bar (frame 0:
+    # |g|/|g0| = 2.4e-4 after 1,719 iterations)
+    ap.add_argument("--cpu-prec", type=int, choices=[32, 64], default=64,
+                    help="arithmetic of the CPU restatement (the reference computes in FP32)")
     ap.add_argument("--plain-only", action="store_true", help="time the plain descent only")
     ap.add_argument("--stress", choices=["full", "incremental"], default=None,
                     help="pass stress evaluation (default: incremental)")

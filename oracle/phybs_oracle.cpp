@@ -867,4 +867,72 @@ int orc_pbd_step(int n, int t, const int *tets, const float *dinv9, const float 
     return 0;
 }
 
+// The reference's OpenMP force evaluation,
+// IsotropicMaterial::computeInnerForcesfromFhats2(num_Threads)
+// (IsotropicMaterial.cpp:411-453), in FP32 on `nthreads` threads with its
+// structure: computeFhats (the modified SVD of every tet's F, in parallel,
+// into per-tet Fhat / U / V arrays), then a parallel loop that forms
+// P^ (IsotropicNeohookeanMaterial.cpp:50-60), P = U diag(P^) V^T and
+// H = P AN, and adds the four corner forces to the node array under one
+// global lock.  Forces start at zero (the reference starts from gravity +
+// external forces).  The scatter's order follows the threads' timing, so the
+// sums are not reproducible to the last bit; this is the CPU comparator of
+// the force evaluation, not a parity reference.
+int orc_forces_fhats2_omp(int nthreads, int n, const float *x, int t, const int *tets, const float *dinv9,
+                          const float *an9, const float *mu, const float *lambda, float *forces3) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    std::vector<float> fhat(3 * (size_t)t), Us(9 * (size_t)t), Vs(9 * (size_t)t);
+    // computeFhats(num_Threads)
+#pragma omp parallel for
+    for (int i = 0; i < t; ++i) {
+        M3<float> Dinv, U, V;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) Dinv(r, c) = dinv9[9 * (size_t)i + 3 * r + c];
+        const M3<float> F = deformation_gradient(x, tets + 4 * (size_t)i, Dinv);
+        float S[3];
+        svd_modified(F, U, S, V);
+        for (int k = 0; k < 3; ++k) fhat[3 * (size_t)i + k] = S[k];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                Us[9 * (size_t)i + 3 * r + c] = U(r, c);
+                Vs[9 * (size_t)i + 3 * r + c] = V(r, c);
+            }
+    }
+    for (size_t k = 0; k < 3 * (size_t)n; ++k) forces3[k] = 0.0f;
+#ifdef _OPENMP
+    omp_lock_t lck;
+    omp_init_lock(&lck);
+#endif
+#pragma omp parallel for
+    for (int i = 0; i < t; ++i) {
+        float ph[3];
+        stretch_gradient(&fhat[3 * (size_t)i], mu[i], lambda[i], ph);
+        M3<float> P, AN;
+        const float *U = &Us[9 * (size_t)i], *V = &Vs[9 * (size_t)i];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                P(r, c) = U[3 * r] * ph[0] * V[3 * c] + U[3 * r + 1] * ph[1] * V[3 * c + 1] +
+                          U[3 * r + 2] * ph[2] * V[3 * c + 2];
+                AN(r, c) = an9[9 * (size_t)i + 3 * r + c];
+            }
+        float f[12];
+        corner_forces(P, AN, f);
+        const int *q = tets + 4 * (size_t)i;
+#ifdef _OPENMP
+        omp_set_lock(&lck);
+#endif
+        for (int c = 0; c < 4; ++c)
+            for (int d = 0; d < 3; ++d) forces3[3 * (size_t)q[c] + d] += f[3 * c + d];
+#ifdef _OPENMP
+        omp_unset_lock(&lck);
+#endif
+    }
+#ifdef _OPENMP
+    omp_destroy_lock(&lck);
+#endif
+    return 0;
+}
+
 }  // extern "C"

@@ -133,6 +133,24 @@ def node_eval(x, tets, dinv, an, vol, mu, lam, material=0, hessian_closed=0, pre
     return f, hd
 
 
+def forces_fhats2_omp(x, tets, dinv, an, mu, lam, threads=0):
+    """The reference's OpenMP force evaluation computeInnerForcesfromFhats2
+    (IsotropicMaterial.cpp:411-453) in FP32 on `threads` threads (0 = all host
+    cores): node forces (N, 3) float32, started from zero.  The locked
+    scatter adds in thread-timing order, so the sums vary in the last bits."""
+    if threads <= 0:
+        threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    x, tets = f32(x).reshape(-1, 3), _i(tets).reshape(-1, 4)
+    n, t = x.shape[0], tets.shape[0]
+    out = np.zeros((n, 3), np.float32)
+    mu = f32(np.broadcast_to(mu, (t,)))
+    lam = f32(np.broadcast_to(lam, (t,)))
+    lib().orc_forces_fhats2_omp(C.c_int(threads), C.c_int(n), _p(x), C.c_int(t), _p(tets),
+                                _p(f32(dinv).reshape(-1)), _p(f32(an).reshape(-1)), _p(mu), _p(lam), _p(out))
+    return out
+
+
 def svd(F, prec=64):
     F = _d(F).reshape(-1, 3, 3)
     U, V, S = np.zeros_like(F), np.zeros_like(F), np.zeros((F.shape[0], 3))

@@ -599,7 +599,8 @@ __global__ void k_unpack(int Np, const float *src, const int *pad2user, float4 *
 }
 
 template <int MATERIAL>
-__global__ void k_eval_tets(DevMesh m, const float4 *U, int clamp_cpu, float *tf, float *energy, float *hd) {
+__global__ void k_eval_tets(DevMesh m, const float4 *U, const float4 *UL, int clamp_cpu, float *tf, float *energy,
+                            float *hd, unsigned int *n_fp64_svd) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.Tp) return;
     const int4 q = m.tets[t];
@@ -611,8 +612,21 @@ __global__ void k_eval_tets(DevMesh m, const float4 *U, int clamp_cpu, float *tf
         disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
         kinematics(kin);
         float P[9];
-        if (MATERIAL == PBS_MATERIAL_STRETCH) pk1_stretch(kin, r1.w, r2.w, P);
-        else pk1_neohookean<float>(kin, r1.w, r2.w, P);
+        if (MATERIAL == PBS_MATERIAL_STRETCH) {
+            if (UL)  // near inversion: the FP64 gradient from the exact displacement pairs
+                pk1_stretch_x(kin, r1.w, r2.w, P, n_fp64_svd, [&](double G64[9]) {
+                    disp_gradient_exact(U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w], dinv,
+                                        G64);
+                });
+            else
+                pk1_stretch(kin, r1.w, r2.w, P, n_fp64_svd);
+        } else if (UL) {
+            pk1_neohookean_x(kin, r1.w, r2.w, P, n_fp64_svd, [&](double G64[9]) {
+                disp_gradient_exact(U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w], dinv, G64);
+            });
+        } else {
+            pk1_neohookean<float>(kin, r1.w, r2.w, P);
+        }
         corner_forces(P, dinv, r0.w, f);
         e = clamp_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), clamp_cpu);
         hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
@@ -733,11 +747,13 @@ cudaError_t launch_scatter_positions(cudaStream_t s, const DevMesh &m, int count
     return cudaGetLastError();
 }
 cudaError_t launch_eval_tets(cudaStream_t s, const DevMesh &m, const float4 *uh, int material, int clamp_cpu,
-                             float *tf, float *energy, float *hd) {
+                             float *tf, float *energy, float *hd, unsigned int *n_fp64_svd, const float4 *ul) {
     if (material == PBS_MATERIAL_STRETCH)
-        k_eval_tets<PBS_MATERIAL_STRETCH><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, clamp_cpu, tf, energy, hd);
+        k_eval_tets<PBS_MATERIAL_STRETCH><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, ul, clamp_cpu, tf, energy, hd,
+                                                                          n_fp64_svd);
     else
-        k_eval_tets<PBS_MATERIAL_NEOHOOKEAN><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, clamp_cpu, tf, energy, hd);
+        k_eval_tets<PBS_MATERIAL_NEOHOOKEAN><<<nblk(m.Tp, 128), 128, 0, s>>>(m, uh, ul, clamp_cpu, tf, energy, hd,
+                                                                             n_fp64_svd);
     return cudaGetLastError();
 }
 cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, const float *hd, const int *pad2user,

@@ -174,8 +174,17 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
         disp_gradient<float>(z, f4add(f4sub(x1, x0), f4sub(l1, l0)), f4add(f4sub(x2, x0), f4sub(l2, l0)),
                              f4add(f4sub(x3, x0), f4sub(l3, l0)), dinv, kin.G);
         kinematics(kin);
-        if (MATERIAL == PBS_MATERIAL_STRETCH) pk1_stretch(kin, mu, lambda, P);
-        else pk1_neohookean<float>(kin, mu, lambda, P);
+        // near inversion (det F < 1e-3, or a stretch-material tet whose FP32
+        // spectrum has sigma_3 < 0.1): the FP64 stress from the exact pairs
+        bool exact = 1.0f + kin.d < 1e-3f;
+        if (!exact) {
+            if (MATERIAL == PBS_MATERIAL_STRETCH) exact = !stretch_pk1<float>(kin.G, mu, lambda, P);
+            else pk1_neohookean<float>(kin, mu, lambda, P);
+        }
+        if (exact)
+            pk1_exact_fp64(MATERIAL, x0, x1, x2, x3, l0, l1, l2, l3,
+                           make_float4(dinv[0], dinv[1], dinv[2], 0.f), make_float4(dinv[3], dinv[4], dinv[5], 0.f),
+                           make_float4(dinv[6], dinv[7], dinv[8], 0.f), mu, lambda, P);
     }
     corner_forces(P, dinv, svol, f);
 }

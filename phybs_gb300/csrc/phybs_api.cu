@@ -73,6 +73,7 @@ struct pbs_handle {
     bool guess_pending = false;  // parity 1 holds a caller guess for the next step
     int sms = 148;
     DevBuf<float> tf, hd, staging, staging2;
+    int last_fp64_svd = 0;  // tets of the last pbs_eval_tets whose stretch stress took the FP64 SVD
     // boundary surface for picking and drag forces: faces and rings in padded
     // node ids on the device, rings in caller ids on the host
     int n_faces = 0;
@@ -1458,13 +1459,17 @@ int pbs_get_rest_data(pbs_handle *h, float *dm_inv9, float *signed_vol, float *m
 
 // The saved-state buffers are rewritten at iteration 0 of every step, so
 // between steps they serve as scratch for evaluating given positions.
-static int eval_common(pbs_handle *h, const float *positions, const float4 **xsrc) {
+// The displacement pair (hi, lo) the probes evaluate: the uploaded positions,
+// or the current state.
+static int eval_common(pbs_handle *h, const float *positions, const float4 **xsrc, const float4 **xlo = nullptr) {
     if (positions) {
         int rc = upload_positions(h, positions, h->oh.p, h->ol.p);
         if (rc != PBS_OK) return rc;
         *xsrc = h->oh.p;
+        if (xlo) *xlo = h->ol.p;
     } else {
         *xsrc = h->u0h.p;
+        if (xlo) *xlo = h->u0l.p;
     }
     return PBS_OK;
 }
@@ -1472,17 +1477,28 @@ static int eval_common(pbs_handle *h, const float *positions, const float4 **xsr
 int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, float *energy, float *hess_diag) {
     if (!h) return PBS_E_INVALID_ARG;
     PBS_DEVICE_SCOPE(h->device);
-    const float4 *x;
-    int rc = eval_common(h, positions, &x);
+    const float4 *x, *xl;
+    int rc = eval_common(h, positions, &x, &xl);
     if (rc != PBS_OK) return rc;
     // per-tet outputs land in tf / hd / staging2 (padded order), then are
     // compacted into the caller's tet order on the host
-    CK(launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, h->staging2.p, h->hd.p));
+    struct Counter {  // freed on every return path
+        DevBuf<unsigned int> b;
+        ~Counter() { b.release(); }
+    } n64_buf;
+    DevBuf<unsigned int> &n64 = n64_buf.b;
+    CK(n64.alloc(1));
+    CK(cudaMemsetAsync(n64.p, 0, sizeof(unsigned int), h->stream));
+    CK(launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, h->staging2.p, h->hd.p,
+                        n64.p, xl));
     std::vector<float> tf(12 * (size_t)h->Tp), hd(12 * (size_t)h->Tp), en(h->Tp);
+    unsigned int n64_host = 0;
     CK(cudaMemcpyAsync(tf.data(), h->tf.p, sizeof(float) * tf.size(), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(hd.data(), h->hd.p, sizeof(float) * hd.size(), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(en.data(), h->staging2.p, sizeof(float) * en.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&n64_host, n64.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    h->last_fp64_svd = (int)n64_host;
     for (int tp = 0; tp < h->Tp; ++tp) {
         int t = h->h_tet_user[tp];
         if (t < 0) continue;
@@ -1493,15 +1509,22 @@ int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, f
     return PBS_OK;
 }
 
+int pbs_eval_fp64_svd_count(pbs_handle *h, int *count) {
+    if (!h || !count) return PBS_E_INVALID_ARG;
+    *count = h->last_fp64_svd;
+    return PBS_OK;
+}
+
 int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag) {
     if (!h) return PBS_E_INVALID_ARG;
     PBS_DEVICE_SCOPE(h->device);
-    const float4 *x;
-    int rc = eval_common(h, positions, &x);
+    const float4 *x, *xl;
+    int rc = eval_common(h, positions, &x, &xl);
     if (rc != PBS_OK) return rc;
     DevBuf<float> out;
     CK(out.alloc(6 * (size_t)h->N));
-    cudaError_t e = launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, nullptr, h->hd.p);
+    cudaError_t e = launch_eval_tets(h->stream, h->mesh(), x, h->material, h->dparams.clamp_cpu, h->tf.p, nullptr,
+                                     h->hd.p, nullptr, xl);
     if (e == cudaSuccess) e = launch_gather(h->stream, h->mesh(), h->tf.p, h->hd.p, h->pad2user.p, out.p, out.p + 3 * (size_t)h->N);
     if (e == cudaSuccess && forces) e = cudaMemcpyAsync(forces, out.p, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess && hess_diag) e = cudaMemcpyAsync(hess_diag, out.p + 3 * (size_t)h->N, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream);

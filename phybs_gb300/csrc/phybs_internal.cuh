@@ -259,8 +259,12 @@ cudaError_t launch_pack(cudaStream_t s, int Np, const float4 *src, const int *pa
 cudaError_t launch_unpack(cudaStream_t s, int Np, const float *src_user, const int *pad2user, float4 *dst);
 cudaError_t launch_scatter_positions(cudaStream_t s, const DevMesh &m, int count, const int *ids_pad,
                                      const float *xyz, float4 *uh, float4 *ul);
+// n_fp64_svd: when not null, counts the tets whose stretch-based stress took
+// the FP64 SVD (det F < 1e-3); ul: the displacements' low words (when not
+// null, a near-inverted tet forms its FP64 gradient from the exact pairs)
 cudaError_t launch_eval_tets(cudaStream_t s, const DevMesh &m, const float4 *uh, int material, int clamp_cpu,
-                             float *tf, float *energy, float *hd);
+                             float *tf, float *energy, float *hd, unsigned int *n_fp64_svd = nullptr,
+                             const float4 *ul = nullptr);
 cudaError_t launch_gather(cudaStream_t s, const DevMesh &m, const float *tf, const float *hd, const int *pad2user,
                           float *force_user, float *hd_user);
 

@@ -317,9 +317,18 @@ __device__ __forceinline__ void svd_disp(const T G[9], T U[9], T s[3], T V[9], T
     sign3 = B[8] < T(0) ? T(-1) : T(1);
 }
 
-template <typename T> __device__ __forceinline__ void stretch_pk1(const T G[9], T mu, T lambda, float P[9]) {
+// Smallest singular value below which the FP32 eigen-analysis of
+// F^T F - I is redone in FP64: sigma_3^2 = 1 + s_3 carries the FP32 rounding
+// of s_3 (about 2^-24 absolute), a relative 2^-24 / sigma_3^2 on sigma_3^2,
+// which stays below 1e-5 of the stress only for sigma_3 above ~0.08.
+constexpr float STRETCH_FP32_MIN_SIGMA2 = 0.01f;
+
+// The stretch-based P from G; returns false (P untouched) when the FP32
+// spectrum is too ill-conditioned to use (T = float and sigma_3 < 0.1).
+template <typename T> __device__ __forceinline__ bool stretch_pk1(const T G[9], T mu, T lambda, float P[9]) {
     T U[9], s[3], V[9], sign3;
     svd_disp<T, sizeof(T) == 4 ? 4 : 8>(G, U, s, V, sign3);
+    if (sizeof(T) == 4 && T(1) + s[2] < T(STRETCH_FP32_MIN_SIGMA2)) return false;
     T sig[3], ph[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) sig[i] = sqrt_t<T>(T(1) + s[i]);
@@ -336,18 +345,93 @@ template <typename T> __device__ __forceinline__ void stretch_pk1(const T G[9], 
         for (int j = 0; j < 3; ++j)
             P[3 * i + j] = (float)(U[3 * i] * ph[0] * V[3 * j] + U[3 * i + 1] * ph[1] * V[3 * j + 1] +
                                    U[3 * i + 2] * ph[2] * V[3 * j + 2]);
+    return true;
 }
 
-// Stretch-based P (IsotropicMaterial.cpp:370-384); FP64 when det F < 1e-3.
-__device__ __forceinline__ void pk1_stretch(const Kin<float> &k, float mu, float lambda, float P[9]) {
-    if (1.0f + k.d < 1e-3f) {
-        double Gd[9];
+// Displacement gradient in FP64 from the corners' displacements held as
+// exact FP32 (hi, lo) pairs: near inversion det F = 1 + d loses |d| / J
+// relative digits when G carries FP32 rounding (an absolute 2^-24 on d is a
+// relative 2^-24 / J on J), so a near-inverted tet forms G from the full pairs.
+__device__ __forceinline__ void disp_gradient_exact(const float4 &h0, const float4 &h1, const float4 &h2,
+                                                    const float4 &h3, const float4 &l0, const float4 &l1,
+                                                    const float4 &l2, const float4 &l3, const float dinv[9],
+                                                    double G[9]) {
+    const double u0[3] = {(double)h0.x + l0.x, (double)h0.y + l0.y, (double)h0.z + l0.z};
+    const double u1[3] = {(double)h1.x + l1.x, (double)h1.y + l1.y, (double)h1.z + l1.z};
+    const double u2[3] = {(double)h2.x + l2.x, (double)h2.y + l2.y, (double)h2.z + l2.z};
+    const double u3[3] = {(double)h3.x + l3.x, (double)h3.y + l3.y, (double)h3.z + l3.z};
 #pragma unroll
-        for (int i = 0; i < 9; ++i) Gd[i] = k.G[i];
-        stretch_pk1<double>(Gd, (double)mu, (double)lambda, P);
-    } else {
-        stretch_pk1<float>(k.G, mu, lambda, P);
+    for (int r = 0; r < 3; ++r) {
+        const double d1 = u1[r] - u0[r], d2 = u2[r] - u0[r], d3 = u3[r] - u0[r];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) G[3 * r + c] = d1 * (double)dinv[c] + d2 * (double)dinv[3 + c] + d3 * (double)dinv[6 + c];
     }
+}
+
+// Stretch-based P (IsotropicMaterial.cpp:370-384).  The SVD runs in FP64 for
+// near-inverted tets: det F < 1e-3, and also any tet whose FP32 spectrum
+// gives sigma_3 < 0.1 (see STRETCH_FP32_MIN_SIGMA2).  exact(double G[9])
+// fills the FP64 gradient for that case (from the corners' exact displacement
+// pairs where the caller has them).  n_fp64: when not null, counts the tets
+// that took the FP64 SVD (a parity probe's evidence that the branch ran).
+template <class Exact>
+__device__ __forceinline__ void pk1_stretch_x(const Kin<float> &k, float mu, float lambda, float P[9],
+                                              unsigned int *n_fp64, Exact exact) {
+    if (1.0f + k.d < 1e-3f || !stretch_pk1<float>(k.G, mu, lambda, P)) {
+        if (n_fp64) atomicAdd(n_fp64, 1u);
+        double Gd[9];
+        exact(Gd);
+        stretch_pk1<double>(Gd, (double)mu, (double)lambda, P);
+    }
+}
+
+// Neo-Hookean P with the same near-inversion rule: below det F = 1e-3 the
+// FP32 gradient's rounding (2^-24 absolute on J) is a relative 2^-24 / J on
+// F^-T, so the stress is formed in FP64 from exact(G) and rounded.
+template <class Exact>
+__device__ __forceinline__ void pk1_neohookean_x(const Kin<float> &k, float mu, float lambda, float P[9],
+                                                 unsigned int *n_fp64, Exact exact) {
+    if (1.0f + k.d < 1e-3f) {
+        if (n_fp64) atomicAdd(n_fp64, 1u);
+        Kin<double> kd;
+        exact(kd.G);
+        kinematics(kd);
+        double Pd[9];
+        pk1_neohookean<double>(kd, (double)mu, (double)lambda, Pd);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) P[i] = (float)Pd[i];
+    } else {
+        pk1_neohookean<float>(k, mu, lambda, P);
+    }
+}
+
+// The FP64 stress of a near-inverted tet (either material) from its corners'
+// exact displacement pairs h + l and the rows of Dm^-1; out of line, so the
+// pass kernels' common path keeps its registers.  Returns P rounded to FP32.
+static __device__ __noinline__ void pk1_exact_fp64(int material, float4 h0, float4 h1, float4 h2, float4 h3, float4 l0,
+                                            float4 l1, float4 l2, float4 l3, float4 r0, float4 r1, float4 r2,
+                                            float mu, float lambda, float *P) {
+    const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    Kin<double> kd;
+    disp_gradient_exact(h0, h1, h2, h3, l0, l1, l2, l3, dinv, kd.G);
+    if (material == 1) {  // PBS_MATERIAL_STRETCH
+        stretch_pk1<double>(kd.G, (double)mu, (double)lambda, P);
+        return;
+    }
+    kinematics(kd);
+    double Pd[9];
+    pk1_neohookean<double>(kd, (double)mu, (double)lambda, Pd);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) P[i] = (float)Pd[i];
+}
+
+// The same with the FP64 gradient taken from the FP32 one.
+__device__ __forceinline__ void pk1_stretch(const Kin<float> &k, float mu, float lambda, float P[9],
+                                            unsigned int *n_fp64 = nullptr) {
+    pk1_stretch_x(k, mu, lambda, P, n_fp64, [&](double Gd[9]) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Gd[i] = (double)k.G[i];
+    });
 }
 
 // Corner forces f[3c + d]: H = -svol * P * Dinv^T; corner 0 = -(sum of 1..3).

@@ -284,6 +284,13 @@ class DescentSolver:
         L.check(L.lib().pbs_eval_tets(self._h, _ptr(xx), _ptr(cf), _ptr(en), _ptr(hd)), "pbs_eval_tets")
         return cf, en, hd
 
+    def eval_fp64_svd_count(self) -> int:
+        """Tets of the last eval_tets call whose stretch-based stress took the
+        FP64 SVD (det F < 1e-3)."""
+        n = C.c_int()
+        L.check(L.lib().pbs_eval_fp64_svd_count(self._h, C.byref(n)), "pbs_eval_fp64_svd_count")
+        return int(n.value)
+
     def eval_nodes(self, x=None):
         f = np.empty((self.n, 3), np.float32)
         hd = np.empty((self.n, 3), np.float32)

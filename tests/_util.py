@@ -13,7 +13,7 @@ def golden_names(prefix=""):
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
     if prefix:
         return [n for n in names if n.startswith(prefix)]
-    return [n for n in names if not n.startswith(("surface_", "stiffness_", "dynamics_"))]
+    return [n for n in names if not n.startswith(("surface_", "stiffness_", "dynamics_", "probe_"))]
 
 
 def load_golden(name):

@@ -242,6 +242,47 @@ def make_dynamics(name, cfg, rng, pbd_steps=3, pd_steps=2, dt=0.03):
     print(name, len(rest), len(m.tets), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def compressed_probe(rest, edge, rng):
+    """A state with near-inverted tets: the bar's y extent is scaled by
+    c(s) = 10^(-5 (s - 1/4) / (3/4)) beyond a quarter of its length s (1 down
+    to 1e-5), x and z jittered by 1% of the edge, then the bar turned 30
+    degrees about y (so F is not diagonal).  det F spans 1 .. ~1e-5, no tet
+    inverts."""
+    x = np.asarray(rest, np.float64).copy()
+    s = (x[:, 0] - x[:, 0].min()) / (x[:, 0].max() - x[:, 0].min())
+    c = 10.0 ** np.where(s < 0.25, 0.0, -5.0 * (s - 0.25) / 0.75)
+    x[:, 1] = x[:, 1] * c
+    x[:, 0] += rng.normal(0.0, 0.01 * edge, x.shape[0])
+    x[:, 2] += rng.normal(0.0, 0.01 * edge, x.shape[0])
+    th = np.deg2rad(30.0)
+    x0, z0 = x[:, 0].copy(), x[:, 2].copy()
+    x[:, 0] = np.cos(th) * x0 - np.sin(th) * z0
+    x[:, 2] = np.sin(th) * x0 + np.cos(th) * z0
+    return x.astype(np.float32)
+
+
+def make_inverted(name="probe_inverted_bar"):
+    """probe_inverted_bar.npz: the reference's node forces (both materials;
+    the stretch-based one through its modified SVD, IsotropicMaterial.cpp:16-60)
+    at a state whose tets have det F from 1 down to ~1e-5
+    (compressed_probe), for the near-inversion parity test
+    (tests/test_gpu_inverted.py)."""
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    sim = REF.RefSim(m.rest, m.tets, m.pins, float(m.young[0]), float(m.poisson[0]), density=m.density)
+    rest = sim.rest()
+    mu, lam = sim.lame()
+    x = compressed_probe(rest, 0.025, np.random.default_rng(20261207))
+    J = M.signed_volumes(x, m.tets) / M.signed_volumes(rest, m.tets)
+    assert (J > 0).all() and ((J > 1e-5) & (J < 1e-3)).sum() >= 100
+    out = dict(rest=rest, tets=m.tets, pins=m.pins, mu=mu, lam=lam, young=np.float32(m.young[0]),
+               poisson=np.float32(m.poisson[0]), dminv=sim.dminv(), an=sim.an(), vol=sim.vol(), mass=sim.mass(),
+               gravity=sim.gravity(), probe_x=x, probe_force_nh=sim.force_nh(x),
+               probe_force_stretch=sim.force_stretch(x))
+    sim.close()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, m.n_nodes, m.n_tets, int((J < 1e-3).sum()), "tets below det F 1e-3")
+
+
 def make_reference_lines():
     """reference_lines.json: the line count of every C/C++/CUDA source under
     the reference's FVM/ and 3rd/CUDA_helper/, by file name, so that the
@@ -296,6 +337,8 @@ if __name__ == "__main__":
         make_reference_lines()
     if only in (None, "loader"):
         make_loader_digests()
+    if only in (None, "inverted"):
+        make_inverted()
     rng = np.random.default_rng(20261203)
     if only is None:
         for n, c in cases().items():

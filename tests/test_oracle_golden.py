@@ -72,6 +72,18 @@ def test_stretch_forces(g, prec):
     assert rel_max(f, elastic_from_ref(g, "probe_force_stretch")) < 2e-5
 
 
+def test_openmp_force_evaluation_port(g):
+    """The port of the reference's OpenMP computeInnerForcesfromFhats2(nthreads)
+    (the CPU comparator bench.py times) gives the reference's forces at any
+    thread count: its locked scatter only reorders the FP32 sums."""
+    ref = elastic_from_ref(g, "probe_force_stretch")
+    for threads in (1, 3):
+        f = O.forces_fhats2_omp(g["probe_x"], g["tets"], g["dminv"], g["an"], g["mu"], g["lam"], threads=threads)
+        f = f.astype(np.float64)
+        f[g["pins"]] = 0.0
+        assert rel_max(f, ref) < 2e-5
+
+
 def test_energy(g):
     _, e, _ = O.tet_eval(g["probe_x"], g["tets"], g["dminv"], g["an"], g["vol"], g["mu"], g["lam"], clamp=0,
                          forces=False, hdiag=False)
