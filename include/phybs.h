@@ -213,7 +213,7 @@ int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, f
 /* Parity probe: how many tets of the last pbs_eval_tets call had their stress
  * evaluated in FP64 from the exact displacements: near-inverted tets, det F <
  * 1e-3 (for the stretch-based material also any tet whose smallest singular
- * value is below 0.1: the FP64 SVD of the near-inverted tets the reference's
+ * value is below 0.3: the FP64 SVD of the near-inverted tets the reference's
  * modified SVD, IsotropicMaterial.cpp:16-60, resolves). */
 int pbs_eval_fp64_svd_count(pbs_handle *h, int *count);
 /* Elastic forces (3*N) and Hessian diagonal (3*N) assembled by the

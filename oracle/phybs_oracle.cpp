@@ -371,6 +371,9 @@ template <typename R> struct Mesh {
     std::vector<R> mass, grav_y;   // mass: pinned = 1e8; grav_y = -9.8 * lumped mass (pre-pin)
     std::vector<int> pinned;
     std::vector<int> iptr, ient;   // node -> 4 * tet + corner, ascending tet
+    // per-tet scratch reused by every pass (a fresh 12T buffer per pass cost
+    // more in page faults than the arithmetic on a 1M-tet mesh)
+    mutable std::vector<R> all, e;
 };
 
 template <typename R> Mesh<R> load_mesh(int n, int t, const int *tets, const double *dinv9, const double *an9,
@@ -419,7 +422,8 @@ template <typename R> void gather_nodes(const Mesh<R> &m, const std::vector<R> &
 // Per-node elastic force in tet order (the reference's scatter order).
 template <typename R> void elastic_forces(const Mesh<R> &m, const std::vector<R> &x, int material, std::vector<R> &f) {
     f.assign(3 * (size_t)m.n, R(0));
-    std::vector<R> all(12 * (size_t)m.t);
+    std::vector<R> &all = m.all;
+    all.resize(12 * (size_t)m.t);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         const int *t = m.tets + 4 * i;
@@ -432,7 +436,8 @@ template <typename R> void elastic_forces(const Mesh<R> &m, const std::vector<R>
 
 template <typename R> void hessian_diag_nodes(const Mesh<R> &m, const std::vector<R> &x, int closed, std::vector<R> &hd) {
     hd.assign(3 * (size_t)m.n, R(0));
-    std::vector<R> all(12 * (size_t)m.t);
+    std::vector<R> &all = m.all;
+    all.resize(12 * (size_t)m.t);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         const int *t = m.tets + 4 * i;
@@ -445,7 +450,8 @@ template <typename R> void hessian_diag_nodes(const Mesh<R> &m, const std::vecto
 
 // Sum of the clamped tet energies, added in tet order.
 template <typename R> R elastic_energy(const Mesh<R> &m, const std::vector<R> &x, int clamp, int keep_nan) {
-    std::vector<R> e(m.t);
+    std::vector<R> &e = m.e;
+    e.resize(m.t);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < m.t; ++i) {
         M3<R> F = deformation_gradient(x.data(), m.tets + 4 * i, m.tin[i].Dinv);
@@ -677,7 +683,8 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             }
             // DescentOptimize::computeGradient (DescentOptimize.cpp:43-61).
             elastic_forces(m, x, p->material, fel);
-            double r2 = 0;
+            // the gradient in parallel (elementwise), |g|^2 summed in node order
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < n; ++i)
                 for (int d = 0; d < 3; ++d) {
                     size_t id = 3 * (size_t)i + d;
@@ -685,8 +692,9 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                     R gv = (x[id] - xt[id]) * m.mass[i] * h2inv - fel[id] - (R)p->body_force_scale * body;
                     if (m.pinned[i]) gv = 0;
                     g[id] = gv;
-                    r2 += (double)gv * (double)gv;
                 }
+            double r2 = 0;
+            for (size_t id = 0; id < N3; ++id) r2 += (double)g[id] * (double)g[id];
             if (!std::isfinite(r2)) {
                 if (!restart) break;  // the device stops with PBS_E_NONFINITE
                 force_check = true;   // the next iteration measures the energy and restores
@@ -695,7 +703,8 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
             if (k == 0) g0 = r;
             ratio = g0 > 0 ? r / g0 : 0.0;
             if (p->tol > 0 && k > 0 && r <= (double)p->tol * g0) { converged = 1; break; }
-            for (size_t id = 0; id < N3; ++id) xnext[id] = x[id] + alpha * (g[id] / -hq[id]);
+#pragma omp parallel for schedule(static)
+            for (long long id = 0; id < (long long)N3; ++id) xnext[id] = x[id] + alpha * (g[id] / -hq[id]);
             // Chebyshev schedule (DescentOptimize.cpp:156-178)
             const int ks = k - k_restart;
             if (ks == 0) { rho = 0; omega = 1; }
@@ -704,10 +713,13 @@ int orc_step(int prec, const orc_params *p, int n, int t, const int *tets, const
                 if (ks == p->profile_k[i] - 1) { rho = 0; omega = 1; }
                 if (ks == p->profile_k[i]) { rho = (R)p->profile_rho[i]; omega = R(2) / (R(2) - rho * rho); break; }
             }
-            if (omega != R(1))
-                for (size_t id = 0; id < N3; ++id) xnext[id] = omega * (xnext[id] - xlast[id]) + xlast[id];
-            xlast = x;
-            x = xnext;
+            if (omega != R(1)) {
+#pragma omp parallel for schedule(static)
+                for (long long id = 0; id < (long long)N3; ++id) xnext[id] = omega * (xnext[id] - xlast[id]) + xlast[id];
+            }
+            // xlast <- x, x <- xnext (xnext is rewritten before it is read again)
+            std::swap(xlast, x);
+            std::swap(x, xnext);
         }
         // DescentOptimize.cpp:183-185
         for (size_t i = 0; i < N3; ++i) {

@@ -196,6 +196,8 @@ struct ChunkView {
     const float4 *uh, *ul, *ub;
     const float4 *r0, *r1, *r2;
     const uint4 *cor;
+    const int4 *meta;    // local-node records (their global ids locate the rest positions)
+    const float4 *rest;  // rest positions, for the FP64 stress of a near-inverted tet
 };
 
 // Corner forces of the chunk's tets into the slots; on line-search passes
@@ -215,7 +217,8 @@ __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkVi
         pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
                                      INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
                                      INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
-                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
+                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f,
+                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}}, check);
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
             sx[sl[cc]] = f[3 * cc];
@@ -243,7 +246,8 @@ __device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float *s
         pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
                                      INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
                                      INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
-                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f);
+                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f,
+                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
         hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
@@ -307,21 +311,29 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     __syncthreads();
     if (!*is_last) return;
     __threadfence();
-    // the instance's last chunk: fixed-order sums (two interleaved
-    // accumulators a value), then accept / reject
-    double ea0 = 0.0, ea1 = 0.0, eb0 = 0.0, eb1 = 0.0;
-    for (int j = cp->cblk_begin + threadIdx.x; j < cp->cblk_end; j += 2 * THREADS) {
-        const double2 v = __ldcg(st.cpart + j);
-        ea0 += v.x;
-        eb0 += v.y;
-        if (j + THREADS < cp->cblk_end) {
-            const double2 w = __ldcg(st.cpart + j + THREADS);
-            ea1 += w.x;
-            eb1 += w.y;
+    // the instance's last chunk: fixed-order sums (each thread adds its chunks
+    // in ascending order, then the block tree), then accept / reject.  The
+    // partials are loaded eight at a time ahead of their additions: this tail
+    // runs on one CTA while the rest of the GPU waits, and one load round trip
+    // per partial made it several microseconds
+    constexpr int U = 8;
+    double ea = 0.0, eb = 0.0;
+    const int cb = cp->cblk_begin, ce = cp->cblk_end;
+    for (int j0 = cb + threadIdx.x; j0 < ce; j0 += U * THREADS) {
+        double2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = j0 + u * THREADS;
+            v[u] = j < ce ? __ldcg(st.cpart + j) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            ea += v[u].x;
+            eb += v[u].y;
         }
     }
-    const double E = block_sum(ea0 + ea1, sh);
-    const double E2 = block_sum(eb0 + eb1, sh);
+    const double E = block_sum(ea, sh);
+    const double E2 = block_sum(eb, sh);
     if (threadIdx.x != 0) return;
     InstCtl ci = *cp;  // one load, updates in registers, one store (as in the node kernel)
     ci.counter_t = 0;
@@ -471,6 +483,8 @@ __global__ void __launch_bounds__(THREADS, INC ? PBS_INC_THREADS_PER_SM / THREAD
     v.r1 = STAGE ? s_r1 : m.qrow1 + tq0;
     v.r2 = STAGE ? s_r2 : m.qrow2 + tq0;
     v.cor = STAGE ? s_cor : m.qcor + tq0;
+    v.meta = meta;
+    v.rest = m.rest;
     chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cp, k, check, do_h, cur, v, meta, nt, nl, s_x, s_y, s_z, sh,
                                        &is_last);
 }
@@ -682,6 +696,8 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             v.r1 = sb.r1;
             v.r2 = sb.r2;
             v.cor = sb.cor;
+            v.meta = sb.meta;
+            v.rest = m.rest;
             chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cur.cp, cur.k, cur.check, cur.do_h, cur.cur, v, sb.meta,
                                                cur.nt, cur.nl, s_x, s_y, s_z, sh, &is_last);
         }

@@ -356,13 +356,27 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
         in[j].diag = st.diag[i];
     }
     InstCtl *cp = st.ctl + inst;
+    // the control fields the instance's last block reads for its decision,
+    // fetched now with the state words instead of after the block reduction
+    __shared__ int s_ci[6];  // passes, par, status, iters, g0_fixed, k_restart
+    __shared__ double s_g0;
+    if (threadIdx.x == 0) {
+        s_ci[0] = cp->passes;
+        s_ci[1] = cp->par;
+        s_ci[2] = cp->status;
+        s_ci[3] = cp->iters;
+        s_ci[4] = cp->g0_fixed;
+        s_ci[5] = cp->k_restart;
+        s_g0 = cp->g0;
+    }
     cp_async_wait_all();  // this thread's own constants
     if (cp->done) return;
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const int action = check ? cp->action : ACT_STEP;
     const bool do_h = (k % p.hd_every) == 0;
-    float rho = cp->rho, omega = cp->omega;
+    const float rho_in = cp->rho, omega_in = cp->omega;
+    float rho = rho_in, omega = omega_in;
     chebyshev_schedule(p, k - cp->k_restart, rho, omega);
     PassCtx ctx;
     ctx.action = action;
@@ -397,7 +411,17 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     // fixed order (FP32 pipe; GB300's FP64 pipe made this tail several us)
     const int nb0 = cp->nblk_begin, nb1 = cp->nblk_end;
     DFloat acc{0.f, 0.f};
-    for (int j = nb0 + threadIdx.x; j < nb1; j += TH) acc = df_add(acc, __ldcg(st.npartf + j));
+    // eight partials in flight a thread ahead of their additions (ascending
+    // order per thread, as one at a time would add them)
+    constexpr int U = 8;
+    for (int j0 = nb0 + threadIdx.x; j0 < nb1; j0 += U * TH) {
+        float v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = j0 + u * TH < nb1 ? __ldcg(st.npartf + j0 + u * TH) : 0.f;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j0 + u * TH < nb1) acc = df_add(acc, v[u]);
+    }
     const double R2 = df_double(block_sum_df(acc, shf));
     if (threadIdx.x != 0) return;
     // The fields this decision reads are loaded together (one round trip),
@@ -405,12 +429,12 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     // control block, and the next kernel reads it only after its
     // grid-dependency wait.  No FP64 square root or division per pass: the stop
     // test compares |g|^2 with (tol g0)^2; the ratio is formed on the host.
-    int passes = cp->passes + 1, par_c = cp->par, kk = k, done = 0, converged = 0, status = cp->status;
-    int force_check = 0, k_restart = cp->k_restart;
-    const int iters = cp->iters, g0_fixed = cp->g0_fixed;
-    const float alpha = cp->alpha;
-    double g0 = cp->g0;
-    float rho_n = cp->rho, omega_n = cp->omega;
+    int passes = s_ci[0] + 1, par_c = s_ci[1], kk = k, done = 0, converged = 0, status = s_ci[2];
+    int force_check = 0, k_restart = s_ci[5];
+    const int iters = s_ci[3], g0_fixed = s_ci[4];
+    const float alpha = ctx.alpha;
+    double g0 = s_g0;
+    float rho_n = rho_in, omega_n = omega_in;
     if (action == ACT_RESTORE) {
         par_c = 1 - par_c;  // the restored state; k is redone
         if (p.control == PBS_CONTROL_RESTART) k_restart = k;  // rerun the rho schedule from here
@@ -612,18 +636,19 @@ __global__ void k_eval_tets(DevMesh m, const float4 *U, const float4 *UL, int cl
         disp_gradient<float>(U[q.x], U[q.y], U[q.z], U[q.w], dinv, kin.G);
         kinematics(kin);
         float P[9];
+        // near inversion: the FP64 gradient from the absolute positions
+        const CornerRest cr{m.rest, nullptr, {q.x, q.y, q.z, q.w}};
+        auto exact = [&](double G64[9]) {
+            position_gradient_exact(cr, U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w], dinv,
+                                    G64);
+        };
         if (MATERIAL == PBS_MATERIAL_STRETCH) {
-            if (UL)  // near inversion: the FP64 gradient from the exact displacement pairs
-                pk1_stretch_x(kin, r1.w, r2.w, P, n_fp64_svd, [&](double G64[9]) {
-                    disp_gradient_exact(U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w], dinv,
-                                        G64);
-                });
+            if (UL)
+                pk1_stretch_x(kin, r1.w, r2.w, P, n_fp64_svd, exact);
             else
                 pk1_stretch(kin, r1.w, r2.w, P, n_fp64_svd);
         } else if (UL) {
-            pk1_neohookean_x(kin, r1.w, r2.w, P, n_fp64_svd, [&](double G64[9]) {
-                disp_gradient_exact(U[q.x], U[q.y], U[q.z], U[q.w], UL[q.x], UL[q.y], UL[q.z], UL[q.w], dinv, G64);
-            });
+            pk1_neohookean_x(kin, r1.w, r2.w, P, n_fp64_svd, exact);
         } else {
             pk1_neohookean<float>(kin, r1.w, r2.w, P);
         }

@@ -153,13 +153,16 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 // Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
 // INC (compile time): the incremental neo-Hookean form, where l carries the
 // corner's increment w = (u hi - base) + u lo (formed once per node) and x is
-// unused; without INC, a is unused.
+// unused; without INC, a is unused.  cr locates the corners' rest positions
+// for the FP64 stress of a near-inverted tet (full stress only).  full_kin:
+// kin must hold the full current kinematics (energy, Jacobi diagonal); a plain
+// incremental pass needs only det F and ln J.
 template <int MATERIAL, bool INC>
 __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
                                               const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
                                               const float4 &a0, const float4 &a1, const float4 &a2, const float4 &a3,
                                               const float dinv[9], float svol, float mu, float lambda, Kin<float> &kin,
-                                              float f[12]) {
+                                              float f[12], const CornerRest &cr, bool full_kin = true) {
     float P[9];
     if (MATERIAL != PBS_MATERIAL_STRETCH && INC) {
         Kin<float> k0;
@@ -167,7 +170,7 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
         kinematics(k0);
         float dG[9];
         disp_gradient<float>(l0, l1, l2, l3, dinv, dG);
-        pk1_neohookean_inc(k0, dG, mu, lambda, kin, P);
+        pk1_neohookean_inc(k0, dG, mu, lambda, full_kin, kin, P);
     } else {
         // Du = (u_j,hi - u_0,hi) + (u_j,lo - u_0,lo)
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -175,14 +178,14 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
                              f4add(f4sub(x3, x0), f4sub(l3, l0)), dinv, kin.G);
         kinematics(kin);
         // near inversion (det F < 1e-3, or a stretch-material tet whose FP32
-        // spectrum has sigma_3 < 0.1): the FP64 stress from the exact pairs
+        // spectrum has sigma_3 < 0.3): the FP64 stress from the absolute positions
         bool exact = 1.0f + kin.d < 1e-3f;
         if (!exact) {
             if (MATERIAL == PBS_MATERIAL_STRETCH) exact = !stretch_pk1<float>(kin.G, mu, lambda, P);
             else pk1_neohookean<float>(kin, mu, lambda, P);
         }
         if (exact)
-            pk1_exact_fp64(MATERIAL, x0, x1, x2, x3, l0, l1, l2, l3,
+            pk1_exact_fp64(MATERIAL, cr, x0, x1, x2, x3, l0, l1, l2, l3,
                            make_float4(dinv[0], dinv[1], dinv[2], 0.f), make_float4(dinv[3], dinv[4], dinv[5], 0.f),
                            make_float4(dinv[6], dinv[7], dinv[8], 0.f), mu, lambda, P);
     }
@@ -199,17 +202,21 @@ __device__ __forceinline__ void pass_forces_v(const DevParams &p, const float4 &
                                               const float4 &x3, const float4 &l0, const float4 &l1, const float4 &l2,
                                               const float4 &l3, const float4 &a0, const float4 &a1, const float4 &a2,
                                               const float4 &a3, const float dinv[9], float svol, float mu,
-                                              float lambda, Kin<float> &kin, float f[12]) {
+                                              float lambda, Kin<float> &kin, float f[12], const CornerRest &cr) {
     if (MATERIAL != PBS_MATERIAL_STRETCH && p.incremental)
-        pass_forces_c<MATERIAL, true>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
+        pass_forces_c<MATERIAL, true>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f,
+                                      cr);
     else
-        pass_forces_c<MATERIAL, false>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
+        pass_forces_c<MATERIAL, false>(x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f,
+                                       cr);
 }
 
+// rest: the rest positions by padded node id (q's ids)
 template <int MATERIAL>
 __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U, const float4 *UL, const float4 *U0,
                                             const int4 &q, const float dinv[9], float svol, float mu, float lambda,
-                                            Kin<float> &kin, float f[12]) {
+                                            Kin<float> &kin, float f[12], const float4 *rest) {
+    const CornerRest cr{rest, nullptr, {q.x, q.y, q.z, q.w}};
     const bool inc = MATERIAL != PBS_MATERIAL_STRETCH && p.incremental;
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 x0 = U[q.x], x1 = U[q.y], x2 = U[q.z], x3 = U[q.w];
@@ -218,9 +225,10 @@ __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U,
     if (inc)
         pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment(x0, l0, a0), node_increment(x1, l1, a1),
                                 node_increment(x2, l2, a2), node_increment(x3, l3, a3), a0, a1, a2, a3, dinv, svol,
-                                mu, lambda, kin, f);
+                                mu, lambda, kin, f, cr);
     else
-        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f);
+        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f,
+                                cr);
 }
 
 }  // namespace pbs

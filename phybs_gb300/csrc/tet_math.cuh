@@ -41,7 +41,10 @@
 // exact rotations, sorting (det V kept +1), Givens QR for U -- applied to
 // S = F^T F - I = G + G^T + G^T G, whose eigenvalues s_i give sigma_i - 1
 // without cancellation (sigma_i^2 = 1 + s_i, ln sigma_i = log1p(s_i) / 2).
-// Near-inverted tets (det F < 1e-3) redo the SVD in FP64.
+// Near-inverted tets (det F < 1e-3, or smallest singular value below 0.3 from
+// the FP32 spectrum) redo the SVD in FP64 with F formed from the absolute
+// positions (position_gradient_exact); neo-Hookean tets with det F < 1e-3 take
+// their stress in FP64 the same way.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -127,61 +130,83 @@ template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T
         }
 }
 
+// log1p(y) for the small argument of an increment: its Taylor series to y^6
+// where that is exact to FP32 (|y| < 1/32: the first dropped term is below
+// 2^-32 of y), log1pf beyond.
+__device__ __forceinline__ float log1p_small(float y) {
+    if (fabsf(y) < 0.03125f) {
+        float s = 1.0f / 6.0f;
+        s = fmaf(y, -s, 0.2f);
+        s = fmaf(y, -s, 0.25f);
+        s = fmaf(y, -s, 1.0f / 3.0f);
+        s = fmaf(y, -s, 0.5f);
+        s = fmaf(y, -s, 1.0f);
+        return y * s;
+    }
+    return log1pf(y);
+}
+
 // dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, from the base kinematics
-// k0 (the step's start, with ln J0) and the increment dG.  With P = mu F +
-// (lambda ln J - mu) F^-T:
-//   dP = mu dG - (lambda ln J - mu) F0^-T dG^T F^-T + lambda (ln J - ln J0) F0^-T
-// (F^-T - F0^-T = -F0^-T dF^T F^-T), ln J - ln J0 = log1p(dJ / J0) and
-//   dJ = cof(F0) : dG + F0 : cof(dG) + det dG
-// -- no term subtracts the two states' O(1) quantities, so dP is accurate to
-// FP32 relative to itself rather than to P.  The scale factors 1/J0 and 1/J
-// multiply only O(|dG|) terms and use the fast reciprocal (a few ulp).
-// Also returns the current kinematics k: G = G0 + dG, det F - 1 = d0 + dJ and
-// ln J = ln J0 + log1p(dJ / J0).
+// k0 (the step's start, with cof G0, tr G0, det F0 - 1 and ln J0) and the
+// increment dG.  With P = mu F + c F^-T, c = lambda ln J - mu, F^-T = cof F / J,
+// and the exact expansion of the cofactor,
+//   cof(F0 + dG) = cof F0 + dC,  dC = B(F0, dG) + cof dG,
+//   B(A, D)_ij = A_i'j' D_i"j" + D_i'j' A_i"j" - A_i'j" D_i"j' - D_i'j" A_i"j'
+//   (i' = i+1, i" = i+2 mod 3: the bilinear part of the 3x3 cofactor),
+// the increment is
+//   dP = mu dG + (c / J) dC + [lambda dl - c dJ / J] / J0 * cof F0
+//   dJ = cof F0 : dG + F0 : cof dG + det dG,   dl = ln J - ln J0 = log1p(dJ / J0),
+// where every term is O(|dG|): no term subtracts the two states' O(1)
+// quantities, so dP is accurate to FP32 relative to itself rather than to P.
+// The scale factors 1/J0 and 1/J multiply only O(|dG|) terms and use the fast
+// reciprocal (a few ulp).  Fills k.d = d0 + dJ and k.lnJ = ln J0 + dl; with
+// full_kin also k.G = G0 + dG and its cofactor, trace and invariants (the
+// energy and the Jacobi diagonal need them; a plain pass does not); FiT, when
+// not null, receives F^-T = (cof F0 + dC) / J.
 __device__ __forceinline__ void pk1_neohookean_inc(const Kin<float> &k0, const float dG[9], float mu, float lambda,
-                                                   Kin<float> &k, float dP[9]) {
-    float F0iT[9], FiT[9], cofdG[9];
-    const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
+                                                   bool full_kin, Kin<float> &k, float dP[9],
+                                                   float *FiT = nullptr) {
+    // F0 = I + G0 and cof F0 = (1 + tr G0) I - G0^T + cof G0 are formed where
+    // they are used (a few additions) rather than held: registers are short
+    auto F0 = [&](int i, int j) { return ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j]; };
+    auto cof0 = [&](int i, int j) {
+        return ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
+    };
+    float cofdG[9];
     cofactor3<float>(dG, cofdG);
     float dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float cof0 = ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
-            const float F0 = ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j];
-            dJ += cof0 * dG[3 * i + j] + F0 * cofdG[3 * i + j];
-            F0iT[3 * i + j] = cof0 * rJ0;
-        }
-    const float dl = log1pf(dJ * rJ0);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
-    cofactor3<float>(k.G, k.cofG);
-    k.tr = k.G[0] + k.G[4] + k.G[8];
-    k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
-    k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+        for (int j = 0; j < 3; ++j) dJ += cof0(i, j) * dG[3 * i + j] + F0(i, j) * cofdG[3 * i + j];
+    const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
+    const float dl = log1p_small(dJ * rJ0);
     k.d = k0.d + dJ;
     k.lnJ = k0.lnJ + dl;
     const float rJ = __fdividef(1.0f, 1.0f + k.d);
+    const float c = lambda * k.lnJ - mu;
+    const float s1 = c * rJ, s2 = (lambda * dl - c * dJ * rJ) * rJ0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            FiT[3 * i + j] = ((i == j ? 1.0f + k.tr : 0.0f) - k.G[3 * j + i] + k.cofG[3 * i + j]) * rJ;
-    // M = F0^-T dG^T F^-T
-    float A[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) A[3 * i + j] = F0iT[3 * i] * dG[3 * j] + F0iT[3 * i + 1] * dG[3 * j + 1] + F0iT[3 * i + 2] * dG[3 * j + 2];
-    const float c1 = lambda * k.lnJ - mu, c2 = lambda * dl;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
-            dP[3 * i + j] = mu * dG[3 * i + j] - c1 * M + c2 * F0iT[3 * i + j];
+            const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+            const float dC = F0(i1, j1) * dG[3 * i2 + j2] + dG[3 * i1 + j1] * F0(i2, j2) -
+                             F0(i1, j2) * dG[3 * i2 + j1] - dG[3 * i1 + j2] * F0(i2, j1) + cofdG[3 * i + j];
+            const float c0 = cof0(i, j);
+            dP[3 * i + j] = mu * dG[3 * i + j] + s1 * dC + s2 * c0;
+            if (FiT) FiT[3 * i + j] = (c0 + dC) * rJ;
         }
+    }
+    if (full_kin) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
+        cofactor3<float>(k.G, k.cofG);
+        k.tr = k.G[0] + k.G[4] + k.G[8];
+        k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
+        k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+    }
 }
 
 // phi(d) = d - log1p(d) >= 0, by its Taylor series where that is exact to FP32.
@@ -318,13 +343,15 @@ __device__ __forceinline__ void svd_disp(const T G[9], T U[9], T s[3], T V[9], T
 }
 
 // Smallest singular value below which the FP32 eigen-analysis of
-// F^T F - I is redone in FP64: sigma_3^2 = 1 + s_3 carries the FP32 rounding
-// of s_3 (about 2^-24 absolute), a relative 2^-24 / sigma_3^2 on sigma_3^2,
-// which stays below 1e-5 of the stress only for sigma_3 above ~0.08.
-constexpr float STRETCH_FP32_MIN_SIGMA2 = 0.01f;
+// F^T F - I is redone in FP64 (the SVD of a near-inverted tet): sigma_3^2 =
+// 1 + s_3 carries the FP32 rounding of s_3 (about 2^-24 absolute), a relative
+// 2^-25 / sigma_3^2 on sigma_3, and the stress's (lambda ln J - mu) / sigma_3
+// term scales that by up to 1 / sigma_3 in the corner forces: about 1e-6 at
+// sigma_3 = 0.3, 3e-5 at 0.1.
+constexpr float STRETCH_FP32_MIN_SIGMA2 = 0.09f;
 
 // The stretch-based P from G; returns false (P untouched) when the FP32
-// spectrum is too ill-conditioned to use (T = float and sigma_3 < 0.1).
+// spectrum is too ill-conditioned to use (T = float and sigma_3 < 0.3).
 template <typename T> __device__ __forceinline__ bool stretch_pk1(const T G[9], T mu, T lambda, float P[9]) {
     T U[9], s[3], V[9], sign3;
     svd_disp<T, sizeof(T) == 4 ? 4 : 8>(G, U, s, V, sign3);
@@ -348,29 +375,44 @@ template <typename T> __device__ __forceinline__ bool stretch_pk1(const T G[9], 
     return true;
 }
 
-// Displacement gradient in FP64 from the corners' displacements held as
-// exact FP32 (hi, lo) pairs: near inversion det F = 1 + d loses |d| / J
-// relative digits when G carries FP32 rounding (an absolute 2^-24 on d is a
-// relative 2^-24 / J on J), so a near-inverted tet forms G from the full pairs.
-__device__ __forceinline__ void disp_gradient_exact(const float4 &h0, const float4 &h1, const float4 &h2,
-                                                    const float4 &h3, const float4 &l0, const float4 &l1,
-                                                    const float4 &l2, const float4 &l3, const float dinv[9],
-                                                    double G[9]) {
-    const double u0[3] = {(double)h0.x + l0.x, (double)h0.y + l0.y, (double)h0.z + l0.z};
-    const double u1[3] = {(double)h1.x + l1.x, (double)h1.y + l1.y, (double)h1.z + l1.z};
-    const double u2[3] = {(double)h2.x + l2.x, (double)h2.y + l2.y, (double)h2.z + l2.z};
-    const double u3[3] = {(double)h3.x + l3.x, (double)h3.y + l3.y, (double)h3.z + l3.z};
+// Where a tet's four rest positions are: rest[meta[id[c]].x] (chunk-local
+// ids) or rest[id[c]] (padded node ids, meta null).
+struct CornerRest {
+    const float4 *rest;
+    const int4 *meta;
+    int id[4];
+    __device__ __forceinline__ float4 get(int c) const { return rest[meta ? meta[id[c]].x : id[c]]; }
+};
+
+// F - I in FP64 with F = Ds Dm^-1 formed from the corners' absolute
+// positions x = X + (u hi + u lo), as the reference defines F
+// (TetMesh.cpp:307-316).  Near inversion the FP32 displacement form loses
+// 2^-24 / sigma_min of the stress: det F = 1 + d carries the rounding of d, and
+// F = I + Du Dm^-1 also differs from Ds Dm^-1 by Dm (Dm^-1)_fp32 - I, an
+// O(2^-24) perturbation that is a relative 2^-24 / sigma_min change of the
+// smallest singular value.  A near-inverted tet therefore takes this form.
+__device__ __forceinline__ void position_gradient_exact(const CornerRest &cr, const float4 &h0, const float4 &h1,
+                                                        const float4 &h2, const float4 &h3, const float4 &l0,
+                                                        const float4 &l1, const float4 &l2, const float4 &l3,
+                                                        const float dinv[9], double G[9]) {
+    const float4 X0 = cr.get(0), X1 = cr.get(1), X2 = cr.get(2), X3 = cr.get(3);
+    const double x0[3] = {(double)X0.x + h0.x + l0.x, (double)X0.y + h0.y + l0.y, (double)X0.z + h0.z + l0.z};
+    const double x1[3] = {(double)X1.x + h1.x + l1.x, (double)X1.y + h1.y + l1.y, (double)X1.z + h1.z + l1.z};
+    const double x2[3] = {(double)X2.x + h2.x + l2.x, (double)X2.y + h2.y + l2.y, (double)X2.z + h2.z + l2.z};
+    const double x3[3] = {(double)X3.x + h3.x + l3.x, (double)X3.y + h3.y + l3.y, (double)X3.z + h3.z + l3.z};
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-        const double d1 = u1[r] - u0[r], d2 = u2[r] - u0[r], d3 = u3[r] - u0[r];
+        const double d1 = x1[r] - x0[r], d2 = x2[r] - x0[r], d3 = x3[r] - x0[r];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) G[3 * r + c] = d1 * (double)dinv[c] + d2 * (double)dinv[3 + c] + d3 * (double)dinv[6 + c];
+        for (int c = 0; c < 3; ++c)
+            G[3 * r + c] = d1 * (double)dinv[c] + d2 * (double)dinv[3 + c] + d3 * (double)dinv[6 + c] -
+                           (r == c ? 1.0 : 0.0);
     }
 }
 
 // Stretch-based P (IsotropicMaterial.cpp:370-384).  The SVD runs in FP64 for
 // near-inverted tets: det F < 1e-3, and also any tet whose FP32 spectrum
-// gives sigma_3 < 0.1 (see STRETCH_FP32_MIN_SIGMA2).  exact(double G[9])
+// gives sigma_3 < 0.3 (see STRETCH_FP32_MIN_SIGMA2).  exact(double G[9])
 // fills the FP64 gradient for that case (from the corners' exact displacement
 // pairs where the caller has them).  n_fp64: when not null, counts the tets
 // that took the FP64 SVD (a parity probe's evidence that the branch ran).
@@ -406,14 +448,15 @@ __device__ __forceinline__ void pk1_neohookean_x(const Kin<float> &k, float mu, 
 }
 
 // The FP64 stress of a near-inverted tet (either material) from its corners'
-// exact displacement pairs h + l and the rows of Dm^-1; out of line, so the
-// pass kernels' common path keeps its registers.  Returns P rounded to FP32.
-static __device__ __noinline__ void pk1_exact_fp64(int material, float4 h0, float4 h1, float4 h2, float4 h3, float4 l0,
-                                            float4 l1, float4 l2, float4 l3, float4 r0, float4 r1, float4 r2,
-                                            float mu, float lambda, float *P) {
+// absolute positions (rest + exact displacement pair h + l) and the rows of
+// Dm^-1; out of line, so the pass kernels' common path keeps its registers.
+// Returns P rounded to FP32.
+static __device__ __noinline__ void pk1_exact_fp64(int material, CornerRest cr, float4 h0, float4 h1, float4 h2,
+                                                   float4 h3, float4 l0, float4 l1, float4 l2, float4 l3, float4 r0,
+                                                   float4 r1, float4 r2, float mu, float lambda, float *P) {
     const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
     Kin<double> kd;
-    disp_gradient_exact(h0, h1, h2, h3, l0, l1, l2, l3, dinv, kd.G);
+    position_gradient_exact(cr, h0, h1, h2, h3, l0, l1, l2, l3, dinv, kd.G);
     if (material == 1) {  // PBS_MATERIAL_STRETCH
         stretch_pk1<double>(kd.G, (double)mu, (double)lambda, P);
         return;

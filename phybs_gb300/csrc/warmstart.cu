@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(BLOCK) k_ws_force(DevMesh m, DevParams p, DevS
     const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
     Kin<float> kin;
     float f[12];
-    pass_forces<MATERIAL>(p, U, st.ul, st.ub, q, dinv, r0.w, r1.w, r2.w, kin, f);
+    pass_forces<MATERIAL>(p, U, st.ul, st.ub, q, dinv, r0.w, r1.w, r2.w, kin, f, m.rest);
     const int4 sl = m.tslot[t];
     float4 *tf4 = reinterpret_cast<float4 *>(st.tf);
     tf4[sl.x] = make_float4(f[0], f[1], f[2], 0.f);
