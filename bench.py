@@ -323,7 +323,7 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
         s.set_node_positions(bottom, pin_xyz[f])
         s.step(raise_on_error=False)
 
-    res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0}
+    res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0, "rejections": []}
     # the state the first timed frame starts from (the CPU baseline's start)
     res["state"] = (s.positions(), *s.velocities())
     sync_ranks(world)
@@ -342,6 +342,7 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
             res["launches"] += launches_per_frame(st["graph_launches"], model is not None)
             res["status"].append(st["status"])
             res["ws_used"] += st["warm_start_used"]
+            res["rejections"].append(st["rejections"])
         e1.record(stream)
         sync_ranks(world)
         t_host = time.perf_counter() - t0
@@ -429,7 +430,8 @@ def run_ours(args, rank, world):
     def summary(r):
         return {"frames_per_s": r["frames_per_s"], "ms_per_frame": r["seconds"] / args.steps * 1e3,
                 "iterations_per_frame": float(np.mean(r["iters"])), "iterations": r["iters"],
-                "iterations_per_s": r["passes"] / r["seconds"], "status": r["status"]}
+                "iterations_per_s": r["passes"] / r["seconds"], "status": r["status"],
+                "line_search_rejections": r["rejections"]}
 
     mode = "warm-started (learned per-node MLP, plain descent as fallback and judge)" if warm else \
         "plain descent (no trained warm-start model present)"

@@ -202,11 +202,25 @@ struct ChunkView {
 
 // Corner forces of the chunk's tets into the slots; on line-search passes
 // returns the thread's sum of clamped tet energies.
-template <int MATERIAL, int THREADS, bool INC>
-__device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check, float *sx,
-                                               float *sy, float *sz) {
-    DFloat e{0.f, 0.f};
+// The node words of a tet's four corners from the chunk's shared-memory
+// staging (one 128-bit access each): x = u hi (full stress) or nothing (the
+// incremental form), l = u lo or the increment, a = the base (incremental).
+template <bool INC>
+__device__ __forceinline__ void corner_words(const ChunkView &v, const int lc[4], float4 x[4], float4 l[4],
+                                             float4 a[4]) {
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        x[c] = INC ? z4 : lds128(v.uh + lc[c]);
+        l[c] = lds128(v.ul + lc[c]);
+        a[c] = INC ? lds128(v.ub + lc[c]) : z4;
+    }
+}
+
+template <int MATERIAL, int THREADS, bool INC>
+__device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check,
+                                               float4 *sf) {
+    DFloat e{0.f, 0.f};
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
         int lc[4], sl[4];
@@ -214,17 +228,13 @@ __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkVi
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         Kin<float> kin;
         float f[12];
-        pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
-                                     INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
-                                     INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
-                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f,
-                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}}, check);
+        float4 x[4], l[4], a[4];
+        corner_words<INC>(v, lc, x, l, a);
+        pass_forces_c<MATERIAL, INC>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3], dinv,
+                                     r0.w, r1.w, r2.w, kin, f,
+                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            sx[sl[cc]] = f[3 * cc];
-            sy[sl[cc]] = f[3 * cc + 1];
-            sz[sl[cc]] = f[3 * cc + 2];
-        }
+        for (int cc = 0; cc < 4; ++cc) sts128(sf + sl[cc], f[3 * cc], f[3 * cc + 1], f[3 * cc + 2]);
         if (check)
             e = df_add(e, search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
                                         p.control == PBS_CONTROL_RESTART));
@@ -234,8 +244,7 @@ __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkVi
 
 // Jacobi-diagonal refresh: the same slots carry the 12 diagonal terms.
 template <int MATERIAL, int THREADS, bool INC>
-__device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float *sx, float *sy, float *sz) {
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+__device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float4 *sf) {
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
         int lc[4], sl[4];
@@ -243,33 +252,29 @@ __device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float *s
         const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
         Kin<float> kin;
         float f[12], kd[12];
-        pass_forces_c<MATERIAL, INC>(INC ? z4 : v.uh[lc[0]], INC ? z4 : v.uh[lc[1]], INC ? z4 : v.uh[lc[2]],
-                                     INC ? z4 : v.uh[lc[3]], v.ul[lc[0]], v.ul[lc[1]], v.ul[lc[2]], v.ul[lc[3]],
-                                     INC ? v.ub[lc[0]] : z4, INC ? v.ub[lc[1]] : z4, INC ? v.ub[lc[2]] : z4,
-                                     INC ? v.ub[lc[3]] : z4, dinv, r0.w, r1.w, r2.w, kin, f,
+        float4 x[4], l[4], a[4];
+        corner_words<INC>(v, lc, x, l, a);
+        pass_forces_c<MATERIAL, INC>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3], dinv,
+                                     r0.w, r1.w, r2.w, kin, f,
                                      CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
         hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) {
-            sx[sl[cc]] = kd[3 * cc];
-            sy[sl[cc]] = kd[3 * cc + 1];
-            sz[sl[cc]] = kd[3 * cc + 2];
-        }
+        for (int cc = 0; cc < 4; ++cc) sts128(sf + sl[cc], kd[3 * cc], kd[3 * cc + 1], kd[3 * cc + 2]);
     }
 }
 
 // Sums every local node's slots (in slot order) into its partial for this
 // chunk.  meta: the chunk's local-node records (shared or global memory).
 template <int THREADS>
-__device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const float *sx, const float *sy,
-                                               const float *sz, float4 *out) {
+__device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const float4 *sf, float4 *out) {
     for (int j = threadIdx.x; j < nl; j += THREADS) {
         const int4 md = meta[j];
         float fx = 0.f, fy = 0.f, fz = 0.f;
         for (int s = md.y; s < md.z; ++s) {
-            fx += sx[s];
-            fy += sy[s];
-            fz += sz[s];
+            const float4 q = lds128(sf + s);
+            fx += q.x;
+            fy += q.y;
+            fz += q.z;
         }
         out[md.w] = make_float4(fx, fy, fz, 0.f);
     }
@@ -374,16 +379,15 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
 template <int MATERIAL, int THREADS, bool INC>
 __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p, const DevState &st, int c,
                                            InstCtl *cp, int k, bool check, bool do_h, size_t cur, const ChunkView &v,
-                                           const int4 *meta, int nt, int nl, float *sx, float *sy, float *sz,
-                                           double *sh, int *is_last) {
-    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sx, sy, sz);
+                                           const int4 *meta, int nt, int nl, float4 *sf, double *sh, int *is_last) {
+    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sf);
     __syncthreads();
-    chunk_partials<THREADS>(meta, nl, sx, sy, sz, st.part);
+    chunk_partials<THREADS>(meta, nl, sf, st.part);
     if (do_h) {
         __syncthreads();
-        chunk_hdiag<MATERIAL, THREADS, INC>(v, nt, sx, sy, sz);
+        chunk_hdiag<MATERIAL, THREADS, INC>(v, nt, sf);
         __syncthreads();
-        chunk_partials<THREADS>(meta, nl, sx, sy, sz, st.parth);
+        chunk_partials<THREADS>(meta, nl, sf, st.parth);
     }
     if (check) chunk_line_search<THREADS>(m, p, st, c, cp, k, cur, e, sh, is_last);
 }
@@ -407,9 +411,8 @@ __global__ void __launch_bounds__(THREADS, INC ? PBS_INC_THREADS_PER_SM / THREAD
     // node words: u hi, u lo (without INC) or the increment (with INC), base
     // (INC only); corner slots; with STAGE the rows and records
     float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;
-    float *s_x = reinterpret_cast<float *>(smem4 + (INC ? 3 : 2) * CN);
-    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
-    float4 *s_r0 = reinterpret_cast<float4 *>(s_z + 4 * CT), *s_r1 = s_r0 + CT, *s_r2 = s_r1 + CT;  // STAGE only
+    float4 *s_f = smem4 + (INC ? 3 : 2) * CN;  // corner slots, 4 a tet
+    float4 *s_r0 = s_f + 4 * CT, *s_r1 = s_r0 + CT, *s_r2 = s_r1 + CT;  // STAGE only
     uint4 *s_cor = reinterpret_cast<uint4 *>(s_r2 + CT);
     int4 *s_meta = reinterpret_cast<int4 *>(s_cor + CT);
     __shared__ double sh[THREADS / 32];
@@ -485,7 +488,7 @@ __global__ void __launch_bounds__(THREADS, INC ? PBS_INC_THREADS_PER_SM / THREAD
     v.cor = STAGE ? s_cor : m.qcor + tq0;
     v.meta = meta;
     v.rest = m.rest;
-    chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cp, k, check, do_h, cur, v, meta, nt, nl, s_x, s_y, s_z, sh,
+    chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cp, k, check, do_h, cur, v, meta, nt, nl, s_f, sh,
                                        &is_last);
 }
 
@@ -630,8 +633,7 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
     extern __shared__ float4 smem4[];
     const int CN = m.chunk_nodes, CT = m.chunk_tets;
     const int stride = 4 * CT + (INC ? 4 : 3) * CN;  // float4 words of one staging buffer
-    float *s_x = reinterpret_cast<float *>(smem4 + 2 * stride);
-    float *s_y = s_x + 4 * CT, *s_z = s_y + 4 * CT;
+    float4 *s_f = smem4 + 2 * stride;  // corner slots, 4 a tet
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ double sh[THREADS / 32];
     __shared__ int is_last;
@@ -699,7 +701,7 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             v.meta = sb.meta;
             v.rest = m.rest;
             chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cur.cp, cur.k, cur.check, cur.do_h, cur.cur, v, sb.meta,
-                                               cur.nt, cur.nl, s_x, s_y, s_z, sh, &is_last);
+                                               cur.nt, cur.nl, s_f, sh, &is_last);
         }
         __syncthreads();  // buffer b and the slots are free again
         if (threadIdx.x == 0 && j + 2 < nj) stage_chunk_bulk(m, c + 2 * G, sb, &bar[b]);

@@ -28,6 +28,21 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
                  "l"(gmem)
                  : "memory");
 }
+// One 128-bit shared-memory access for a float4 whose .w may be unused: a
+// node word or a corner-force slot is then one LSU request, not two or three.
+__device__ __forceinline__ float4 lds128(const float4 *p) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "r"((unsigned)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ void sts128(float4 *p, float x, float y, float z) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(x),
+                 "f"(y), "f"(z), "f"(0.f)
+                 : "memory");
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
@@ -154,15 +169,13 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 // INC (compile time): the incremental neo-Hookean form, where l carries the
 // corner's increment w = (u hi - base) + u lo (formed once per node) and x is
 // unused; without INC, a is unused.  cr locates the corners' rest positions
-// for the FP64 stress of a near-inverted tet (full stress only).  full_kin:
-// kin must hold the full current kinematics (energy, Jacobi diagonal); a plain
-// incremental pass needs only det F and ln J.
+// for the FP64 stress of a near-inverted tet (full stress only).
 template <int MATERIAL, bool INC>
 __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
                                               const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
                                               const float4 &a0, const float4 &a1, const float4 &a2, const float4 &a3,
                                               const float dinv[9], float svol, float mu, float lambda, Kin<float> &kin,
-                                              float f[12], const CornerRest &cr, bool full_kin = true) {
+                                              float f[12], const CornerRest &cr) {
     float P[9];
     if (MATERIAL != PBS_MATERIAL_STRETCH && INC) {
         Kin<float> k0;
@@ -170,7 +183,7 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
         kinematics(k0);
         float dG[9];
         disp_gradient<float>(l0, l1, l2, l3, dinv, dG);
-        pk1_neohookean_inc(k0, dG, mu, lambda, full_kin, kin, P);
+        pk1_neohookean_inc(k0, dG, mu, lambda, kin, P);
     } else {
         // Du = (u_j,hi - u_0,hi) + (u_j,lo - u_0,lo)
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);

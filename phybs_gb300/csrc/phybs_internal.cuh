@@ -64,14 +64,15 @@ constexpr int CHUNK_THREADS = 256;
 constexpr int CHUNK_MAX_SMEM = 200 * 1024;
 // Dynamic shared memory of the per-tet pass kernel for a chunk shape and a
 // staging mode: 0 = node words (u hi, u lo, and the force base with
-// incremental stress, 16 B each) and 3 floats per corner slot; 1 = also the
-// chunk's per-tet rows and corner records (64 B per tet) and local-node
-// records (16 B per node); 2 = the persistent kernel, two buffers of rows,
-// records and node words plus one set of slots.
+// incremental stress, 16 B each) and one float4 per corner slot (written and
+// read with one 128-bit access each); 1 = also the chunk's per-tet rows and
+// corner records (64 B per tet) and local-node records (16 B per node); 2 =
+// the persistent kernel, two buffers of rows, records and node words plus one
+// set of slots.
 __host__ __device__ constexpr size_t chunk_smem(int tets, int nodes, bool inc, int stage = 0) {
     return stage == 2 ? 2 * ((inc ? 4 : 3) * sizeof(float4) * (size_t)nodes + 64 * (size_t)tets) +
-                            3 * sizeof(float) * 4 * (size_t)tets
-                      : (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + 3 * sizeof(float) * 4 * (size_t)tets +
+                            sizeof(float4) * 4 * (size_t)tets
+                      : (inc ? 3 : 2) * sizeof(float4) * (size_t)nodes + sizeof(float4) * 4 * (size_t)tets +
                             (stage ? 64 * (size_t)tets + sizeof(int4) * (size_t)nodes : 0);
 }
 

@@ -130,83 +130,61 @@ template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T
         }
 }
 
-// log1p(y) for the small argument of an increment: its Taylor series to y^6
-// where that is exact to FP32 (|y| < 1/32: the first dropped term is below
-// 2^-32 of y), log1pf beyond.
-__device__ __forceinline__ float log1p_small(float y) {
-    if (fabsf(y) < 0.03125f) {
-        float s = 1.0f / 6.0f;
-        s = fmaf(y, -s, 0.2f);
-        s = fmaf(y, -s, 0.25f);
-        s = fmaf(y, -s, 1.0f / 3.0f);
-        s = fmaf(y, -s, 0.5f);
-        s = fmaf(y, -s, 1.0f);
-        return y * s;
-    }
-    return log1pf(y);
-}
-
 // dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, from the base kinematics
-// k0 (the step's start, with cof G0, tr G0, det F0 - 1 and ln J0) and the
-// increment dG.  With P = mu F + c F^-T, c = lambda ln J - mu, F^-T = cof F / J,
-// and the exact expansion of the cofactor,
-//   cof(F0 + dG) = cof F0 + dC,  dC = B(F0, dG) + cof dG,
-//   B(A, D)_ij = A_i'j' D_i"j" + D_i'j' A_i"j" - A_i'j" D_i"j' - D_i'j" A_i"j'
-//   (i' = i+1, i" = i+2 mod 3: the bilinear part of the 3x3 cofactor),
-// the increment is
-//   dP = mu dG + (c / J) dC + [lambda dl - c dJ / J] / J0 * cof F0
-//   dJ = cof F0 : dG + F0 : cof dG + det dG,   dl = ln J - ln J0 = log1p(dJ / J0),
-// where every term is O(|dG|): no term subtracts the two states' O(1)
-// quantities, so dP is accurate to FP32 relative to itself rather than to P.
-// The scale factors 1/J0 and 1/J multiply only O(|dG|) terms and use the fast
-// reciprocal (a few ulp).  Fills k.d = d0 + dJ and k.lnJ = ln J0 + dl; with
-// full_kin also k.G = G0 + dG and its cofactor, trace and invariants (the
-// energy and the Jacobi diagonal need them; a plain pass does not); FiT, when
-// not null, receives F^-T = (cof F0 + dC) / J.
+// k0 (the step's start, with ln J0) and the increment dG.  With P = mu F +
+// (lambda ln J - mu) F^-T:
+//   dP = mu dG - (lambda ln J - mu) F0^-T dG^T F^-T + lambda (ln J - ln J0) F0^-T
+// (F^-T - F0^-T = -F0^-T dF^T F^-T), ln J - ln J0 = log1p(dJ / J0) and
+//   dJ = cof(F0) : dG + F0 : cof(dG) + det dG
+// -- no term subtracts the two states' O(1) quantities, so dP is accurate to
+// FP32 relative to itself rather than to P.  The scale factors 1/J0 and 1/J
+// multiply only O(|dG|) terms and use the fast reciprocal (a few ulp).
+// Also returns the current kinematics k: G = G0 + dG, det F - 1 = d0 + dJ and
+// ln J = ln J0 + log1p(dJ / J0).
 __device__ __forceinline__ void pk1_neohookean_inc(const Kin<float> &k0, const float dG[9], float mu, float lambda,
-                                                   bool full_kin, Kin<float> &k, float dP[9],
-                                                   float *FiT = nullptr) {
-    // F0 = I + G0 and cof F0 = (1 + tr G0) I - G0^T + cof G0 are formed where
-    // they are used (a few additions) rather than held: registers are short
-    auto F0 = [&](int i, int j) { return ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j]; };
-    auto cof0 = [&](int i, int j) {
-        return ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
-    };
-    float cofdG[9];
+                                                   Kin<float> &k, float dP[9]) {
+    float F0iT[9], FiT[9], cofdG[9];
+    const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
     cofactor3<float>(dG, cofdG);
     float dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) dJ += cof0(i, j) * dG[3 * i + j] + F0(i, j) * cofdG[3 * i + j];
-    const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
-    const float dl = log1p_small(dJ * rJ0);
+        for (int j = 0; j < 3; ++j) {
+            const float cof0 = ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
+            const float F0 = ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j];
+            dJ += cof0 * dG[3 * i + j] + F0 * cofdG[3 * i + j];
+            F0iT[3 * i + j] = cof0 * rJ0;
+        }
+    const float dl = log1pf(dJ * rJ0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
+    cofactor3<float>(k.G, k.cofG);
+    k.tr = k.G[0] + k.G[4] + k.G[8];
+    k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
+    k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
     k.d = k0.d + dJ;
     k.lnJ = k0.lnJ + dl;
     const float rJ = __fdividef(1.0f, 1.0f + k.d);
-    const float c = lambda * k.lnJ - mu;
-    const float s1 = c * rJ, s2 = (lambda * dl - c * dJ * rJ) * rJ0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            FiT[3 * i + j] = ((i == j ? 1.0f + k.tr : 0.0f) - k.G[3 * j + i] + k.cofG[3 * i + j]) * rJ;
+    // M = F0^-T dG^T F^-T
+    float A[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A[3 * i + j] = F0iT[3 * i] * dG[3 * j] + F0iT[3 * i + 1] * dG[3 * j + 1] + F0iT[3 * i + 2] * dG[3 * j + 2];
+    const float c1 = lambda * k.lnJ - mu, c2 = lambda * dl;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-            const float dC = F0(i1, j1) * dG[3 * i2 + j2] + dG[3 * i1 + j1] * F0(i2, j2) -
-                             F0(i1, j2) * dG[3 * i2 + j1] - dG[3 * i1 + j2] * F0(i2, j1) + cofdG[3 * i + j];
-            const float c0 = cof0(i, j);
-            dP[3 * i + j] = mu * dG[3 * i + j] + s1 * dC + s2 * c0;
-            if (FiT) FiT[3 * i + j] = (c0 + dC) * rJ;
+            const float M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
+            dP[3 * i + j] = mu * dG[3 * i + j] - c1 * M + c2 * F0iT[3 * i + j];
         }
-    }
-    if (full_kin) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
-        cofactor3<float>(k.G, k.cofG);
-        k.tr = k.G[0] + k.G[4] + k.G[8];
-        k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
-        k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
-    }
 }
 
 // phi(d) = d - log1p(d) >= 0, by its Taylor series where that is exact to FP32.

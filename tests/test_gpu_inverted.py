@@ -11,10 +11,12 @@ reference defines it; the reference does the stretch-based material through
 its modified SVD (IsotropicMaterial.cpp:16-60) in FP32 throughout.
 
 Bars: the FP64-branch tets' corner forces within 1e-5 of the all-FP64
-restatement, tet by tet (max-norm relative per tet), on the device's own rest
-data; every other tet within max(1e-5, 2^-19 / sigma_min) of it per tet -- the
-conditioning of an FP32 evaluation, whose F carries an absolute rounding of a
-few 2^-24, through a stress that varies as 1 / sigma_min; assembled node
+restatement, tet by tet (max-norm per tet, relative to the larger of the
+tet's largest force and its force at unit strain, mu vol |Dm^-1|), on the
+device's own rest data; every other tet within max(1e-5, 2^-19 / sigma_min)
+of it per tet -- the conditioning of an FP32 evaluation, whose F carries an
+absolute rounding of a few 2^-24, through a stress that varies as
+1 / sigma_min; assembled node
 forces within 1e-5 of the FP64 restatement, and no further from it than the
 reference's FP32 forces are from the FP64 restatement on the reference's rest
 data (both errors are printed); and the probe's count of FP64-branch tets
@@ -61,10 +63,18 @@ def _device_rest(s):
     return dinv, an, np.abs(svol)
 
 
-def _per_tet_rel(a, b):
+def _per_tet_rel(a, b, scale):
+    """max |a - b| per tet over the larger of the tet's largest force and its
+    stress scale: a nearly stress-free tet (a rigid turn) has forces near zero
+    that no FP32 evaluation resolves relative to themselves."""
     a = np.asarray(a, np.float64).reshape(-1, 12)
     b = np.asarray(b, np.float64).reshape(-1, 12)
-    return np.abs(a - b).max(1) / np.maximum(np.abs(b).max(1), 1e-300)
+    return np.abs(a - b).max(1) / np.maximum(np.abs(b).max(1), scale)
+
+
+def _stress_scale(g, dinv, vol):
+    """Corner-force size of a tet at unit strain: mu vol |Dm^-1|_F."""
+    return np.asarray(g["mu"], np.float64) * vol * np.linalg.norm(dinv.reshape(-1, 9), axis=1)
 
 
 def _deformation(g, dinv):
@@ -86,7 +96,7 @@ def test_near_inverted_tets_take_the_fp64_branch(g, material):
     stretch = int(material == L.PBS_MATERIAL_STRETCH)
     f64, _, _ = O.tet_eval(g["probe_x"], g["tets"], dinv, an, vol, g["mu"], g["lam"], material=stretch, prec=64,
                            energy=False, hdiag=False)
-    err = _per_tet_rel(cf, f64)
+    err = _per_tet_rel(cf, f64, _stress_scale(g, dinv, vol))
     sig_min = np.linalg.svd(F, compute_uv=False)[:, 2]
     near = J < 1e-3
     fp64 = (near | (sig_min < 0.3)) if stretch else near
@@ -95,7 +105,10 @@ def test_near_inverted_tets_take_the_fp64_branch(g, material):
           f"others {err[~fp64].max():.2e} (worst error / bound {(err[~fp64] / bound[~fp64]).max():.2f}); "
           f"FP64-branch tets {n64} of {len(J)}")
     assert err[fp64].max() < TOL, err[fp64].max()
-    assert (err[~fp64] <= bound[~fp64]).all(), (err[~fp64] / bound[~fp64]).max()
+    r = np.where(fp64, 0.0, err / bound)
+    w = int(np.argmax(r))
+    assert r[w] <= 1.0, dict(tet=w, err=err[w], bound=bound[w], detF=J[w], sigma_min=sig_min[w],
+                             max_force=np.abs(f64[w]).max())
     if stretch:
         # the device classifies from its FP32 spectrum: a tet at the 0.3 edge
         # may fall on either side
