@@ -42,8 +42,13 @@ extern "C" {
 #define PBS_E_NO_DEVICE (-6)   /* no CUDA device, or not compute capability 10.3 */
 #define PBS_E_OUT_OF_MEMORY (-7)
 #define PBS_E_CAPACITY (-8)    /* a size beyond a documented fixed maximum      */
-#define PBS_E_DEVICE_TIMEOUT (-9) /* a kernel's bounded wait on its own copies
+#define PBS_E_DEVICE_TIMEOUT (-9) /* a kernel's bounded wait on its own copies,
+                                     or of the frame engine on a grid barrier,
                                      ran out (the step's results are invalid)   */
+
+/* Pass engines of pbs_step (pbs_set_pass_engine). */
+#define PBS_ENGINE_GRAPH 0
+#define PBS_ENGINE_FRAME 1
 
 /* Materials.  Both are the neo-Hookean energy
  *   Psi = mu/2 (I1 - 3) - mu ln J + lambda/2 (ln J)^2,
@@ -296,6 +301,28 @@ int pbs_autotune(pbs_handle *h, int passes, pbs_tune_result *out);
  * 200 KB; node_npt 1 or 2 nodes per thread of the node kernel.  Call between
  * steps. */
 int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_nodes, int staged, int node_npt);
+/* Pass engine of pbs_step.  PBS_ENGINE_GRAPH (the default): each pass is a
+ * per-tet and a per-node kernel, 16 passes to a captured CUDA graph, and the
+ * host reads the count of running instances between graphs.
+ * PBS_ENGINE_FRAME: one cooperative launch runs all the passes of a step; its
+ * CTAs stay resident for the whole step, grid barriers separate the tet and
+ * node phases of a pass, and every CTA takes the line-search and stop
+ * decisions from the same sums.  For one-instance handles whose chunk shape
+ * is unstaged (staged 0) with 128 or 256 threads; PBS_E_INVALID_ARG
+ * otherwise, and from pbs_step when a later shape or parameter change leaves
+ * the handle outside that set.  The instance's energy and residual sums are
+ * grouped per CTA instead of per chunk, so results agree with the graph
+ * engine's to rounding; they are bit-reproducible run to run.  A barrier wait
+ * that runs out (0.5 s) ends the step with PBS_E_DEVICE_TIMEOUT.
+ * pbs_stats.graph_launches is 0 for a frame-engine step.  No counterpart in
+ * the reference, which launches each kernel from the host. */
+int pbs_set_pass_engine(pbs_handle *h, int engine);
+int pbs_get_pass_engine(pbs_handle *h, int *engine);
+/* pbs_profile_kernels for the frame engine: one frame launch of `passes`
+ * passes from the current state (left as it was), timed with CUDA events;
+ * returns the mean milliseconds per pass.  Fails as pbs_profile_kernels does,
+ * and with PBS_E_INVALID_ARG where the frame engine does not apply. */
+int pbs_profile_frame(pbs_handle *h, int passes, double *pass_ms);
 
 /* ------------------------------------------------------------------------
  * Learned warm start.  A per-node MLP 24 -> 64 -> 64 -> 64 -> 3 (GELU; BF16

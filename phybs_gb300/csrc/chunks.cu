@@ -32,6 +32,8 @@
 #include <vector>
 
 #include "../../include/phybs.h"
+#include "node_update.cuh"
+#include "pass_ctl.cuh"
 #include "pass_math.cuh"
 #include "phybs_internal.cuh"
 #include "tet_math.cuh"
@@ -217,10 +219,13 @@ __device__ __forceinline__ void corner_words(const ChunkView &v, const int lc[4]
     }
 }
 
+// A near-inverted tet (full stress) gets its FP32 forces here and a mark in
+// its corner-0 slot's .w; *any_exact tells whether the thread marked one.
 template <int MATERIAL, int THREADS, bool INC>
 __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check,
-                                               float4 *sf) {
+                                               float4 *sf, bool *any_exact) {
     DFloat e{0.f, 0.f};
+    bool any = false;
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
         const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
         int lc[4], sl[4];
@@ -230,14 +235,55 @@ __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkVi
         float f[12];
         float4 x[4], l[4], a[4];
         corner_words<INC>(v, lc, x, l, a);
-        pass_forces_c<MATERIAL, INC>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3], dinv,
-                                     r0.w, r1.w, r2.w, kin, f,
-                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
+        const bool ex = pass_forces_c<MATERIAL, INC, true>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0],
+                                                           a[1], a[2], a[3], dinv, r0.w, r1.w, r2.w, kin, f,
+                                                           CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
+        any |= ex;
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) sts128(sf + sl[cc], f[3 * cc], f[3 * cc + 1], f[3 * cc + 2]);
+        for (int cc = 0; cc < 4; ++cc)
+            sts128(sf + sl[cc], f[3 * cc], f[3 * cc + 1], f[3 * cc + 2], cc == 0 && ex ? 1.f : 0.f);
         if (check)
             e = df_add(e, search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
                                         p.control == PBS_CONTROL_RESTART));
+    }
+    *any_exact = any;
+    return e;
+}
+
+// The FP64 stress of the chunk's marked (near-inverted) tets, into their
+// slots.  After the tet loop rather than inside it: the loop then carries no
+// call, and keeps its registers.
+template <int MATERIAL, int THREADS>
+__device__ __forceinline__ void chunk_exact(const ChunkView &v, int nt, float4 *sf) {
+    for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
+        int lc[4], sl[4];
+        unpack_cor(v.cor[lt], lc, sl);
+        if (lds128(sf + sl[0]).w == 0.f) continue;
+        const float4 r0 = v.r0[lt], r1 = v.r1[lt], r2 = v.r2[lt];
+        const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+        float4 x[4], l[4], a[4];
+        corner_words<false>(v, lc, x, l, a);
+        float P[9], f[12];
+        pk1_exact_fp64(MATERIAL, CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}}, x[0], x[1], x[2], x[3],
+                       l[0], l[1], l[2], l[3], r0, r1, r2, r1.w, r2.w, P);
+        corner_forces(P, dinv, r0.w, f);
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) sts128(sf + sl[cc], f[3 * cc], f[3 * cc + 1], f[3 * cc + 2]);
+    }
+}
+
+// chunk_forces, then the FP64 stress of a chunk that has a near-inverted tet;
+// every thread sees the finished slots on return.
+template <int MATERIAL, int THREADS, bool INC>
+__device__ __forceinline__ DFloat chunk_forces_all(const DevParams &p, const ChunkView &v, int nt, bool check,
+                                                   float4 *sf) {
+    bool ex;
+    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sf, &ex);
+    if (INC) {
+        __syncthreads();
+    } else if (__syncthreads_or(ex)) {
+        chunk_exact<MATERIAL, THREADS>(v, nt, sf);
+        __syncthreads();
     }
     return e;
 }
@@ -254,9 +300,10 @@ __device__ __forceinline__ void chunk_hdiag(const ChunkView &v, int nt, float4 *
         float f[12], kd[12];
         float4 x[4], l[4], a[4];
         corner_words<INC>(v, lc, x, l, a);
-        pass_forces_c<MATERIAL, INC>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3], dinv,
-                                     r0.w, r1.w, r2.w, kin, f,
-                                     CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
+        // only the kinematics are used here (no FP64 stress needed)
+        pass_forces_c<MATERIAL, INC, true>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3],
+                                           dinv, r0.w, r1.w, r2.w, kin, f,
+                                           CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
         hessian_diag(kin, r1.w, r2.w, dinv, r0.w, kd);
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) sts128(sf + sl[cc], kd[3 * cc], kd[3 * cc + 1], kd[3 * cc + 2]);
@@ -342,33 +389,7 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     if (threadIdx.x != 0) return;
     InstCtl ci = *cp;  // one load, updates in registers, one store (as in the node kernel)
     ci.counter_t = 0;
-    ci.energy = E;
-    // rounding-noise allowance: the FP64 sum of FP32 terms e_i carries a random
-    // error of order 2^-24 sqrt(sum e_i^2); slack 0 is the reference's strict test
-    const double tau = (double)p.energy_slack * 5.9604644775390625e-8 * sqrt(E2);
-    // RESTART control also treats a non-finite energy (a step that inverted
-    // tets) as a rejection; the reference control accepts it (NaN > E_old is
-    // false), and the step then ends with PBS_E_NONFINITE below
-    const bool bad = !isfinite(E) && p.control == PBS_CONTROL_RESTART;
-    if ((k != 0 && E > ci.energy_old + tau) || (bad && k != 0)) {
-        ci.action = ACT_RESTORE;
-        ci.alpha = (float)((double)ci.alpha * (double)p.alpha_shrink);
-        ci.rejections += 1;
-        if (p.control == PBS_CONTROL_REFERENCE) ci.iters -= k - p.ls_every;
-    } else {
-        ci.action = ACT_SAVE_STEP;
-        ci.energy_old = E;
-        // grow only after real steps since the last restore (not on the re-check
-        // of a restored iterate, whose energy is the accepted one)
-        if (p.control == PBS_CONTROL_RESTART && k != 0 && k > ci.k_restart)
-            ci.alpha = fminf(ci.alpha * p.alpha_grow, p.alpha0);
-    }
-    // force_check stays set: the node kernel of this pass reads it to apply the
-    // decision, and clears it
-    if (!isfinite(E) && !(bad && k != 0)) {
-        ci.status = PBS_E_NONFINITE;
-        ci.done = 1;
-    }
+    decide_line_search(ci, p, k, E, E2);
     *cp = ci;
     if (ci.done) atomicSub(st.active, 1);
 }
@@ -380,8 +401,7 @@ template <int MATERIAL, int THREADS, bool INC>
 __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p, const DevState &st, int c,
                                            InstCtl *cp, int k, bool check, bool do_h, size_t cur, const ChunkView &v,
                                            const int4 *meta, int nt, int nl, float4 *sf, double *sh, int *is_last) {
-    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sf);
-    __syncthreads();
+    const DFloat e = chunk_forces_all<MATERIAL, THREADS, INC>(p, v, nt, check, sf);
     chunk_partials<THREADS>(meta, nl, sf, st.part);
     if (do_h) {
         __syncthreads();
@@ -400,11 +420,15 @@ __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p,
 #ifndef PBS_INC_THREADS_PER_SM
 #define PBS_INC_THREADS_PER_SM 1024
 #endif
-// Register budget of the incremental variants: 64 a thread (1024 threads a
-// SM; a few registers spill, and the extra resident warps pay for them: 44.9
-// against 49.7 us a pass on the 1M-tet box at 85 registers).
+// Register budget of the neo-Hookean variants: 64 a thread (1024 threads a
+// SM; with the incremental stress a few registers spill, and the extra
+// resident warps pay for them: 44.9 against 49.7 us a pass on the 1M-tet box
+// at 85 registers).  The full stress needs 64 on its tet loop; the bound
+// keeps the out-of-line FP64 call of a near-inverted tet, after the loop,
+// from raising it.
 template <int MATERIAL, int THREADS, bool INC, bool STAGE>
-__global__ void __launch_bounds__(THREADS, INC ? PBS_INC_THREADS_PER_SM / THREADS : 0)
+__global__ void __launch_bounds__(THREADS,
+                                  MATERIAL == PBS_MATERIAL_NEOHOOKEAN ? PBS_INC_THREADS_PER_SM / THREADS : 0)
     k_tchunk(DevMesh m, DevParams p, DevState st, int par) {
     extern __shared__ float4 smem4[];
     const int CN = m.chunk_nodes, CT = m.chunk_tets;
@@ -839,6 +863,303 @@ int stream_grid(const DevMesh &m, int material, bool inc, int sms) {
         return inc ? stream_fit<PBS_MATERIAL_NEOHOOKEAN, 256, true>(m, sms)
                    : stream_fit<PBS_MATERIAL_NEOHOOKEAN, 256, false>(m, sms);
     return 0;
+}
+
+// ------------------------------------------------------------ persistent frame kernel
+// One cooperative launch runs a whole step's passes for a one-instance handle.
+// Every CTA stays resident (the launch fails otherwise) and walks the chunks
+// b, b + G, ... of each pass's tet phase, then the nodes b * THREADS + t,
+// + G * THREADS, ... of its node phase; grid barriers separate the phases.
+// After each barrier every CTA takes the line-search and pass decisions
+// itself, from the same per-CTA sums in the same order, on its own
+// shared-memory copy of the control block: the copies stay equal, and no
+// "last CTA" tail, kernel launch or host poll sits between passes.  The
+// arithmetic of a tet, a chunk's slot sums and a node's update is the pass
+// kernels' (chunk_forces_all, chunk_partials, node_update); the instance's
+// sums are grouped by CTA instead of by chunk and node block, so results
+// agree with the pass kernels' to rounding, and are bit-reproducible run to
+// run.
+
+// Release / acquire accesses of the barrier words (device scope).
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// A barrier wait that has not ended in half a second means a CTA is gone (a
+// fault elsewhere) or the launch was not co-resident: the kernel records
+// PBS_E_DEVICE_TIMEOUT and every CTA returns instead of spinning on.
+constexpr unsigned long long FRAME_WAIT_NS = 500000000ull;
+
+// Grid-wide barrier: every CTA's writes before it are visible to every CTA
+// after it.  Thread 0 arrives on the counter; the last to arrive resets it and
+// advances the generation (release); the others wait for the generation
+// (acquire), at most FRAME_WAIT_NS, and stop waiting as soon as any CTA has
+// recorded a failure.  gen: the generation this CTA last passed (thread 0).
+__device__ bool frame_barrier(FrameSync *fs, unsigned G, unsigned &gen) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned target = gen + 1;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&fs->count, 1u) + 1u;
+        if (arrived == G) {
+            fs->count = 0u;
+            __threadfence();
+            st_release_u32(&fs->gen, target);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            while (ld_acquire_u32(&fs->gen) != target) {
+                if (*(volatile int *)&fs->err) {
+                    ok = 0;
+                    break;
+                }
+                if (globaltimer_ns() - t0 > FRAME_WAIT_NS) {
+                    atomicExch(&fs->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        gen = target;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Fixed-order FP64 sum of n per-CTA values (ascending per thread, then the
+// block tree): every CTA gets the same bits.
+template <int THREADS>
+__device__ __forceinline__ double2 frame_sum2(const double2 *v, int n, double *sh) {
+    double a = 0.0, b = 0.0;
+    for (int j = threadIdx.x; j < n; j += THREADS) {
+        const double2 x = __ldcg(v + j);
+        a += x.x;
+        b += x.y;
+    }
+    const double A = block_sum(a, sh);
+    const double B = block_sum(b, sh);
+    return make_double2(A, B);
+}
+
+// Register budget of the neo-Hookean frame kernels: the pass loop keeps its
+// control values live across both phases, so they get 896 threads a SM
+// (73 registers) where the pass kernel gets 1024.
+#ifndef PBS_FRAME_THREADS_PER_SM
+#define PBS_FRAME_THREADS_PER_SM 896
+#endif
+template <int MATERIAL, int THREADS, bool INC>
+__global__ void __launch_bounds__(THREADS,
+                                  MATERIAL == PBS_MATERIAL_NEOHOOKEAN ? PBS_FRAME_THREADS_PER_SM / THREADS : 0)
+    k_frame(DevMesh m, DevParams p, DevState st, FrameAux fx) {
+    extern __shared__ float4 smem4[];
+    const int CN = m.chunk_nodes;
+    float4 *s_uh = smem4, *s_ul = smem4 + CN, *s_ub = smem4 + 2 * CN;
+    float4 *s_f = smem4 + (INC ? 3 : 2) * CN;  // corner slots, 4 a tet
+    __shared__ InstCtl sc;                      // this CTA's copy of the control block
+    __shared__ double sh[THREADS / 32];
+    __shared__ float2 shf[THREADS / 32];
+    __shared__ float shs[THREADS / 32];
+    const unsigned G = gridDim.x;
+    const int b = blockIdx.x;
+    unsigned gen = 0;
+    if (threadIdx.x == 0) {
+        sc = st.ctl[0];
+        gen = ld_acquire_u32(&fx.sync->gen);
+    }
+    __syncthreads();
+    bool ok = true;
+    for (int pass = 0; pass < fx.max_passes; ++pass) {
+        if (sc.done) break;
+        const int k = sc.k;
+        const bool check = (k % p.ls_every) == 0 || sc.force_check;
+        const bool do_h = (k % p.hd_every) == 0;
+        const size_t cur = (size_t)sc.par * m.Np;
+        // ---- tet phase: the chunks b, b + G, ...
+        DFloat e{0.f, 0.f};
+        float e2 = 0.f;
+        for (int c = b; c < m.n_chunks; c += (int)G) {
+            const int4 cd = m.chunk[c];
+            const int nt = cd.y, nl = cd.w;
+            const int4 *meta = m.lmeta + cd.z;
+            for (int j = threadIdx.x; j < nl; j += THREADS) {
+                const int g = meta[j].x;
+                const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
+                if (INC) {
+                    const float4 ub = st.ub[g];
+                    s_ul[j] = node_increment(uh, ul, ub);
+                    s_ub[j] = ub;
+                } else {
+                    s_uh[j] = uh;
+                    s_ul[j] = ul;
+                }
+            }
+            __syncthreads();
+            ChunkView v;
+            v.uh = s_uh;
+            v.ul = s_ul;
+            v.ub = s_ub;
+            v.r0 = m.qrow0 + cd.x;
+            v.r1 = m.qrow1 + cd.x;
+            v.r2 = m.qrow2 + cd.x;
+            v.cor = m.qcor + cd.x;
+            v.meta = meta;
+            v.rest = m.rest;
+            const DFloat ec = chunk_forces_all<MATERIAL, THREADS, INC>(p, v, nt, check, s_f);
+            chunk_partials<THREADS>(meta, nl, s_f, st.part);
+            if (do_h) {
+                __syncthreads();
+                chunk_hdiag<MATERIAL, THREADS, INC>(v, nt, s_f);
+                __syncthreads();
+                chunk_partials<THREADS>(meta, nl, s_f, st.parth);
+            }
+            if (check) {
+                e = df_add(e, ec);
+                e2 = fmaf(ec.hi, ec.hi, e2);
+            }
+            __syncthreads();  // the slots and node words are free for the next chunk
+        }
+        if (check) {
+            // this CTA's share of the node energy terms
+            const float4 *U = st.uh + cur;
+            for (int i = b * THREADS + threadIdx.x; i < m.Np; i += (int)G * THREADS) {
+                const float4 info = m.info[i];
+                if (info.z != 0.f) continue;
+                const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+                e = df_add(e, en);
+                e2 = fmaf(en.hi, en.hi, e2);
+            }
+            const DFloat se = block_sum_df(e, shf);
+            const float se2 = block_sum_f(e2, shs);
+            if (threadIdx.x == 0) fx.ce[b] = make_double2(df_double(se), (double)se2);
+        }
+        ok = frame_barrier(fx.sync, G, gen);
+        if (!ok) break;
+        // ---- the line-search decision (every CTA, the same sums)
+        if (check) {
+            const double2 E = frame_sum2<THREADS>(fx.ce, (int)G, sh);
+            if (threadIdx.x == 0) decide_line_search(sc, p, k, E.x, E.y);
+            __syncthreads();
+            if (sc.done) break;
+        }
+        // ---- node phase: the nodes b * THREADS + t, + G * THREADS, ...
+        const int action = check ? sc.action : ACT_STEP;
+        float rho = sc.rho, omega = sc.omega;
+        chebyshev_schedule(p, k - sc.k_restart, rho, omega);
+        PassCtx ctx;
+        ctx.action = action;
+        ctx.do_h = do_h;
+        ctx.alpha = sc.alpha;
+        ctx.omega = omega;
+        ctx.cur = cur;
+        ctx.nxt = (size_t)(1 - sc.par) * m.Np;
+        float r2 = 0.f;
+        for (int i = b * THREADS + threadIdx.x; i < m.Np; i += (int)G * THREADS) {
+            NodeConst nc;
+            nc.info = m.info[i];
+            nc.th = st.th[i];
+            nc.tl = st.tl[i];
+            nc.bh = st.bh[i];
+            nc.bl = st.bl[i];
+            NodeIn nn;
+            nn.pa = m.pptr[i];
+            nn.pe = m.pptr[i + 1];
+            float4 fp[2];  // a node touches 1.7 chunks on average: two prefetched partials
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                fp[q] = nn.pa + q < nn.pe ? st.part[nn.pa + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            nn.uh = st.uh[cur + i];
+            nn.ul = st.ul[cur + i];
+            nn.dd = st.dd[cur + i];
+            nn.diag = st.diag[i];
+            r2 += node_update<2>(m, p, st, i, nc, nn, fp, ctx);
+        }
+        const float sr = block_sum_f(r2, shs);
+        if (threadIdx.x == 0) fx.cr[b] = make_double2((double)sr, 0.0);
+        ok = frame_barrier(fx.sync, G, gen);
+        if (!ok) break;
+        // ---- the pass decision (every CTA, the same sums)
+        const double2 R = frame_sum2<THREADS>(fx.cr, (int)G, sh);
+        if (threadIdx.x == 0) decide_pass(sc, p, k, action, rho, omega, R.x);
+        __syncthreads();
+    }
+    if (b == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            sc.status = PBS_E_DEVICE_TIMEOUT;
+            sc.done = 1;
+        }
+        st.ctl[0] = sc;
+        if (sc.done) atomicSub(st.active, 1);
+    }
+}
+
+template <int MATERIAL, int THREADS, bool INC> static cudaError_t allow_smem_frame() {
+    return cudaFuncSetAttribute(k_frame<MATERIAL, THREADS, INC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                CHUNK_MAX_SMEM);
+}
+
+template <int MATERIAL, int THREADS, bool INC> static int frame_fit(const DevMesh &m, int sms) {
+    if (allow_smem_frame<MATERIAL, THREADS, INC>() != cudaSuccess) return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_frame<MATERIAL, THREADS, INC>, THREADS,
+                                                      chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 0)) != cudaSuccess)
+        return 0;
+    return std::min(m.n_chunks, per_sm * sms);
+}
+
+int frame_grid(const DevMesh &m, int material, bool inc, int sms) {
+    if (m.n_inst != 1 || m.chunk_stage != 0 || m.n_chunks <= 0) return 0;
+    const bool nh_inc = material == PBS_MATERIAL_NEOHOOKEAN && inc;
+    if (material == PBS_MATERIAL_STRETCH) {
+        if (m.chunk_threads == 128) return frame_fit<PBS_MATERIAL_STRETCH, 128, false>(m, sms);
+        if (m.chunk_threads == 256) return frame_fit<PBS_MATERIAL_STRETCH, 256, false>(m, sms);
+        return 0;
+    }
+    if (m.chunk_threads == 128)
+        return nh_inc ? frame_fit<PBS_MATERIAL_NEOHOOKEAN, 128, true>(m, sms)
+                      : frame_fit<PBS_MATERIAL_NEOHOOKEAN, 128, false>(m, sms);
+    if (m.chunk_threads == 256)
+        return nh_inc ? frame_fit<PBS_MATERIAL_NEOHOOKEAN, 256, true>(m, sms)
+                      : frame_fit<PBS_MATERIAL_NEOHOOKEAN, 256, false>(m, sms);
+    return 0;
+}
+
+template <int MATERIAL, int THREADS, bool INC>
+static cudaError_t launch_frame_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st,
+                                  const FrameAux &fx, int grid) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 0);
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_frame<MATERIAL, THREADS, INC>, m, p, st, fx);
+}
+
+cudaError_t launch_frame(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material,
+                         const FrameAux &fx, int grid) {
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    const bool inc = material == PBS_MATERIAL_NEOHOOKEAN && p.incremental;
+    if (material == PBS_MATERIAL_STRETCH) {
+        if (m.chunk_threads == 128) return launch_frame_t<PBS_MATERIAL_STRETCH, 128, false>(s, m, p, st, fx, grid);
+        return launch_frame_t<PBS_MATERIAL_STRETCH, 256, false>(s, m, p, st, fx, grid);
+    }
+    if (m.chunk_threads == 128)
+        return inc ? launch_frame_t<PBS_MATERIAL_NEOHOOKEAN, 128, true>(s, m, p, st, fx, grid)
+                   : launch_frame_t<PBS_MATERIAL_NEOHOOKEAN, 128, false>(s, m, p, st, fx, grid);
+    return inc ? launch_frame_t<PBS_MATERIAL_NEOHOOKEAN, 256, true>(s, m, p, st, fx, grid)
+               : launch_frame_t<PBS_MATERIAL_NEOHOOKEAN, 256, false>(s, m, p, st, fx, grid);
 }
 
 }  // namespace pbs

@@ -21,6 +21,8 @@
 //           step needs no host round trip (the reference syncs every 8
 //           iterations, CUDAInterface.cu:886-890).
 #include "../../include/phybs.h"
+#include "node_update.cuh"
+#include "pass_ctl.cuh"
 #include "pass_math.cuh"
 #include "phybs_internal.cuh"
 #include "tet_math.cuh"
@@ -198,115 +200,8 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 }
 
 // ------------------------------------------------------------ one pass
-// The inputs of one node: the state-independent ones loaded before the
-// grid-dependency wait, the state words right after it.
-struct NodeIn {
-    int pa, pe;
-    float4 uh, ul, dd, diag;
-};
-
-// Per-step node constants staged in shared memory before the grid-dependency
-// wait: mass / gravity / state, x~ (hi, lo), b (hi, lo).
-struct NodeConst {
-    float4 info, th, tl, bh, bl;
-};
-
-// The instance's pass state as the node update needs it.
-struct PassCtx {
-    int action;
-    bool do_h;
-    float alpha, omega;
-    size_t cur, nxt;
-};
-
-// Jacobi step with Chebyshev extrapolation (or restore / save) of node i;
-// returns its |g|^2 (FP32: three positive squares).
-// NPRE: partials of the node loaded together with its state words (a node of
-// the 1M box touches 2-4 chunks of 256 tets; the rest cost one more round
-// trip).
-template <int NPRE>
-__device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &p, const DevState &st, int i,
-                                             const NodeConst &in, const NodeIn &nn, const float4 (&f)[NPRE],
-                                             const PassCtx &c) {
-    float r2 = 0.f;
-    if (in.info.z == 2.f) return r2;
-    const size_t nxt = c.nxt;
-    const float4 uh = nn.uh, ul = nn.ul, dd = nn.dd;
-    float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (c.action == ACT_RESTORE) {
-        // x <- x_old (DescentOptimize.cpp:116); the Chebyshev history keeps
-        // x_last = x_{k-1} = u - d (the reference does not restore it), or
-        // restarts it under PBS_CONTROL_RESTART
-        nh = st.oh[i];
-        nl = st.ol[i];
-        if (in.info.z == 0.f && p.control == PBS_CONTROL_REFERENCE)
-            nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
-                             ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
-    } else {
-        if (c.action == ACT_SAVE_STEP) {  // x_old <- x (DescentOptimize.cpp:126)
-            st.oh[i] = uh;
-            st.ol[i] = ul;
-        }
-        if (in.info.z == 0.f) {
-            float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
-            // this node's per-chunk partial sums, in chunk order (the first
-            // NPRE loaded with the state words, the rest here)
-#pragma unroll
-            for (int j = 0; j < NPRE; ++j) {
-                fx += f[j].x;
-                fy += f[j].y;
-                fz += f[j].z;
-            }
-            for (int j = nn.pa + NPRE; j < nn.pe; ++j) {
-                const float4 q = st.part[j];
-                fx += q.x;
-                fy += q.y;
-                fz += q.z;
-            }
-            if (c.do_h) {
-                for (int j = nn.pa; j < nn.pe; ++j) {
-                    const float4 q = st.parth[j];
-                    hx += q.x;
-                    hy += q.y;
-                    hz += q.z;
-                }
-            }
-            const float mh = in.info.x * p.h2inv;
-            float4 D;
-            if (c.do_h) {
-                D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
-                st.diag[i] = D;
-            } else {
-                D = nn.diag;
-            }
-            // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
-            // force (incremental mode) + body_force_scale (external + gravity)
-            const float4 th = in.th, tl = in.tl, bh = in.bh, bl = in.bl;
-            const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
-            const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
-            const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
-            r2 = fmaf(gx, gx, fmaf(gy, gy, gz * gz));
-            // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:142-150), then the
-            // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as
-            // d' = (omega - 1) d + omega delta
-            const float alpha = c.alpha, omega = c.omega;
-            const float dx = alpha * (gx / -D.x), dy = alpha * (gy / -D.y), dz = alpha * (gz / -D.z);
-            if (omega != 1.0f)
-                nd = make_float4((omega - 1.f) * dd.x + omega * dx, (omega - 1.f) * dd.y + omega * dy,
-                                 (omega - 1.f) * dd.z + omega * dz, 0.f);
-            else
-                nd = make_float4(dx, dy, dz, 0.f);
-            add_comp(nh.x, nl.x, nd.x);
-            add_comp(nh.y, nl.y, nd.y);
-            add_comp(nh.z, nl.z, nd.z);
-        }
-    }
-    st.uh[nxt + i] = nh;
-    st.ul[nxt + i] = nl;
-    st.dd[nxt + i] = nd;
-    return r2;
-}
-
+// (the per-node update itself is node_update.cuh's, shared with the frame
+// kernel)
 
 // One CTA per 256-node block (one instance); NPT nodes per thread.  The
 // per-step constants go to shared memory by cp.async before the
@@ -356,19 +251,11 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
         in[j].diag = st.diag[i];
     }
     InstCtl *cp = st.ctl + inst;
-    // the control fields the instance's last block reads for its decision,
-    // fetched now with the state words instead of after the block reduction
-    __shared__ int s_ci[6];  // passes, par, status, iters, g0_fixed, k_restart
-    __shared__ double s_g0;
-    if (threadIdx.x == 0) {
-        s_ci[0] = cp->passes;
-        s_ci[1] = cp->par;
-        s_ci[2] = cp->status;
-        s_ci[3] = cp->iters;
-        s_ci[4] = cp->g0_fixed;
-        s_ci[5] = cp->k_restart;
-        s_g0 = cp->g0;
-    }
+    // the control block the instance's last block decides on, fetched now with
+    // the state words instead of after the block reduction (no other block
+    // writes it during this kernel but for counter_n, which the decision resets)
+    __shared__ InstCtl s_ci;
+    if (threadIdx.x == 0) s_ci = *cp;
     cp_async_wait_all();  // this thread's own constants
     if (cp->done) return;
     const int k = cp->k;
@@ -424,61 +311,13 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     }
     const double R2 = df_double(block_sum_df(acc, shf));
     if (threadIdx.x != 0) return;
-    // The fields this decision reads are loaded together (one round trip),
-    // updated in registers and stored back: every other block has read the
-    // control block, and the next kernel reads it only after its
-    // grid-dependency wait.  No FP64 square root or division per pass: the stop
-    // test compares |g|^2 with (tol g0)^2; the ratio is formed on the host.
-    int passes = s_ci[0] + 1, par_c = s_ci[1], kk = k, done = 0, converged = 0, status = s_ci[2];
-    int force_check = 0, k_restart = s_ci[5];
-    const int iters = s_ci[3], g0_fixed = s_ci[4];
-    const float alpha = ctx.alpha;
-    double g0 = s_g0;
-    float rho_n = rho_in, omega_n = omega_in;
-    if (action == ACT_RESTORE) {
-        par_c = 1 - par_c;  // the restored state; k is redone
-        if (p.control == PBS_CONTROL_RESTART) k_restart = k;  // rerun the rho schedule from here
-    } else {
-        if (k == 0 && !g0_fixed) g0 = sqrt(R2);
-        cp->r2 = R2;
-        const double lim = (double)p.tol * g0;
-        if (p.tol > 0.f && k > 0 && R2 <= lim * lim) {
-            converged = 1;  // keep x_k (the current parity)
-            done = 1;
-        } else {
-            rho_n = rho;
-            omega_n = omega;
-            par_c = 1 - par_c;
-            kk = k + 1;
-        }
-        if (!isfinite(R2)) {
-            if (p.control == PBS_CONTROL_RESTART && kk > 0) {
-                force_check = 1;  // the next pass measures the energy and restores
-                converged = 0;
-                done = 0;
-            } else {
-                status = PBS_E_NONFINITE;
-                done = 1;
-            }
-        }
-    }
-    if (!done) {
-        if (kk >= iters || alpha < p.alpha_min) done = 1;
-        else if (passes >= p.pass_cap) { done = 1; status = PBS_E_ITER_CAP; }
-    }
-    cp->counter_n = 0;
-    cp->passes = passes;
-    cp->force_check = force_check;  // a forced line-search check was applied in this pass
-    cp->par = par_c;
-    cp->k_restart = k_restart;
-    cp->g0 = g0;
-    cp->rho = rho_n;
-    cp->omega = omega_n;
-    cp->k = kk;
-    cp->converged = converged;
-    cp->status = status;
-    cp->done = done;
-    if (done) atomicSub(st.active, 1);
+    // the decision on the prefetched copy, stored back whole: every other block
+    // has read the control block, and the next kernel reads it only after its
+    // grid-dependency wait
+    InstCtl ci = s_ci;
+    decide_pass(ci, p, k, action, rho, omega, R2);
+    *cp = ci;
+    if (ci.done) atomicSub(st.active, 1);
 }
 
 // Per-step node constant b = f_el(u_base) (incremental mode, FP64) +

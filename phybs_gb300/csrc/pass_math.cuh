@@ -37,9 +37,9 @@ __device__ __forceinline__ float4 lds128(const float4 *p) {
         : "r"((unsigned)__cvta_generic_to_shared(p)));
     return v;
 }
-__device__ __forceinline__ void sts128(float4 *p, float x, float y, float z) {
+__device__ __forceinline__ void sts128(float4 *p, float x, float y, float z, float w = 0.f) {
     asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(x),
-                 "f"(y), "f"(z), "f"(0.f)
+                 "f"(y), "f"(z), "f"(w)
                  : "memory");
 }
 
@@ -169,14 +169,17 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 // INC (compile time): the incremental neo-Hookean form, where l carries the
 // corner's increment w = (u hi - base) + u lo (formed once per node) and x is
 // unused; without INC, a is unused.  cr locates the corners' rest positions
-// for the FP64 stress of a near-inverted tet (full stress only).
-template <int MATERIAL, bool INC>
-__device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
+// for the FP64 stress of a near-inverted tet (full stress only).  DEFER:
+// leave that stress out (f is then not the tet's) and return whether the tet
+// needs it, for a caller that forms it after its loop.
+template <int MATERIAL, bool INC, bool DEFER = false>
+__device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
                                               const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
                                               const float4 &a0, const float4 &a1, const float4 &a2, const float4 &a3,
                                               const float dinv[9], float svol, float mu, float lambda, Kin<float> &kin,
                                               float f[12], const CornerRest &cr) {
     float P[9];
+    bool exact = false;
     if (MATERIAL != PBS_MATERIAL_STRETCH && INC) {
         Kin<float> k0;
         disp_gradient<float>(a0, a1, a2, a3, dinv, k0.G);
@@ -192,17 +195,18 @@ __device__ __forceinline__ void pass_forces_c(const float4 &x0, const float4 &x1
         kinematics(kin);
         // near inversion (det F < 1e-3, or a stretch-material tet whose FP32
         // spectrum has sigma_3 < 0.3): the FP64 stress from the absolute positions
-        bool exact = 1.0f + kin.d < 1e-3f;
+        exact = 1.0f + kin.d < 1e-3f;
         if (!exact) {
             if (MATERIAL == PBS_MATERIAL_STRETCH) exact = !stretch_pk1<float>(kin.G, mu, lambda, P);
             else pk1_neohookean<float>(kin, mu, lambda, P);
         }
-        if (exact)
+        if (exact && !DEFER)
             pk1_exact_fp64(MATERIAL, cr, x0, x1, x2, x3, l0, l1, l2, l3,
                            make_float4(dinv[0], dinv[1], dinv[2], 0.f), make_float4(dinv[3], dinv[4], dinv[5], 0.f),
                            make_float4(dinv[6], dinv[7], dinv[8], 0.f), mu, lambda, P);
     }
     corner_forces(P, dinv, svol, f);
+    return exact;
 }
 
 // The increment of a node for the incremental form: (u hi - base) + u lo.

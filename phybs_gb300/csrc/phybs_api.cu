@@ -126,6 +126,10 @@ struct pbs_handle {
     cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_chunk[2] = {nullptr, nullptr};
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    // persistent frame kernel: its barrier words and per-CTA sums
+    int engine = PBS_ENGINE_GRAPH;
+    DevBuf<FrameSync> fsync;
+    DevBuf<double2> fce, fcr;
     double last_ms = 0.0;
     pbs_stats stats{};
 
@@ -171,6 +175,7 @@ struct pbs_handle {
         DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
         for (auto b : cf) b->release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release();
+        fsync.release(); fce.release(); fcr.release();
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
         pbd_grp.release(); pbd_lvl.release(); pbd_tet.release(); pbd_d0.release(); pbd_d1.release(); pbd_d2.release();
@@ -305,7 +310,7 @@ const char *pbs_error_string(int code) {
         case PBS_E_NO_DEVICE: return "no compute capability 10.3 CUDA device";
         case PBS_E_OUT_OF_MEMORY: return "out of device memory";
         case PBS_E_CAPACITY: return "size beyond the fixed maximum";
-        case PBS_E_DEVICE_TIMEOUT: return "a kernel's bounded wait on its own copies ran out";
+        case PBS_E_DEVICE_TIMEOUT: return "a kernel's bounded wait (its own copies, a grid barrier) ran out";
         default: return "unknown error";
     }
 }
@@ -618,10 +623,43 @@ static int ensure_graph(pbs_handle *h) {
     return PBS_OK;
 }
 
+// CTAs of the frame kernel for the handle's current layout; 0 when the frame
+// engine does not apply to it.
+static int frame_ctas(const pbs_handle *h) {
+    return frame_grid(h->mesh(), h->material, h->material == PBS_MATERIAL_NEOHOOKEAN && h->dparams.incremental,
+                      h->sms);
+}
+
+// Enqueues one frame-kernel launch of at most max_passes passes with params p
+// (the barrier words zeroed first).  PBS_E_INVALID_ARG when the frame engine
+// does not apply to the handle's layout.
+static int launch_frame_step(pbs_handle *h, const DevParams &p, int max_passes) {
+    const int G = frame_ctas(h);
+    if (G <= 0) return PBS_E_INVALID_ARG;
+    cudaStream_t s = h->stream;
+    if (!h->fsync.p) CK(h->fsync.alloc(1));
+    if (h->fce.n < (size_t)G) {
+        h->fce.release();
+        h->fcr.release();
+        CK(h->fce.alloc(G));
+        CK(h->fcr.alloc(G));
+    }
+    CK(cudaMemsetAsync(h->fsync.p, 0, sizeof(FrameSync), s));
+    FrameAux fx;
+    fx.sync = h->fsync.p;
+    fx.ce = h->fce.p;
+    fx.cr = h->fcr.p;
+    fx.max_passes = max_passes;
+    CK(launch_frame(s, h->mesh(), p, h->state(), h->material, fx, G));
+    return PBS_OK;
+}
+
 int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     if (!h) return PBS_E_INVALID_ARG;
     PBS_DEVICE_SCOPE(h->device);
-    int rc = ensure_graph(h);
+    const bool frame = h->engine == PBS_ENGINE_FRAME;
+    if (frame && frame_ctas(h) <= 0) return PBS_E_INVALID_ARG;
+    int rc = frame ? PBS_OK : ensure_graph(h);
     if (rc != PBS_OK) return rc;
     cudaStream_t s = h->stream;
     DevMesh m = h->mesh();
@@ -644,8 +682,14 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     }
     // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
     // of chunk j-1 while chunk j runs, so the device never idles on the poll.
-    const int max_chunks = (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES;
+    // The frame engine: one launch runs every pass of the step (its pass cap
+    // ends it at the latest).
+    const int max_chunks = frame ? 0 : (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES;
     int launched = 0;
+    if (frame) {
+        rc = launch_frame_step(h, h->dparams, h->dparams.pass_cap);
+        if (rc != PBS_OK) return rc;
+    }
     for (int j = 0; j < max_chunks; ++j) {
         ++launched;
         CK(cudaGraphLaunch(h->graph, s));
@@ -879,7 +923,68 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     return PBS_OK;
 }
 
+// The frame engine's counterpart of time_passes: one launch of exactly
+// `passes` passes from the step's start state, timed with CUDA events.
+static int time_frame(pbs_handle *h, int passes, double *pass_ms) {
+    cudaStream_t s = h->stream;
+    DevParams p = h->dparams;
+    p.max_iters = 4 * passes + 64;
+    p.tol = 0.f;
+    p.pass_cap = 4 * passes + 64;
+    DevMesh m = h->mesh();
+    DevState st = h->state();
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
+    if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
+    if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
+    if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+    int rc = PBS_OK;
+    if (e == cudaSuccess) rc = launch_frame_step(h, p, passes);
+    if (e == cudaSuccess && rc == PBS_OK) e = cudaEventRecord(ev[1], s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    float ms = 0.f;
+    if (e == cudaSuccess && rc == PBS_OK) cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    for (auto &x : ev) cudaEventDestroy(x);
+    CK(e);
+    if (rc != PBS_OK) return rc;
+    InstCtl c;
+    CK(cudaMemcpy(&c, h->ctl.p, sizeof(InstCtl), cudaMemcpyDeviceToHost));
+    if (c.status != PBS_OK || c.passes < passes) {
+        pbs_stats S{};
+        S.passes = c.passes; S.iterations = c.k; S.rejections = c.rejections; S.converged = c.converged;
+        S.status = c.status; S.alpha = c.alpha; S.rho = c.rho; S.omega = c.omega; S.energy = c.energy;
+        S.residual_ratio = residual_ratio(c);
+        h->stats = S;
+        return c.status != PBS_OK ? c.status : PBS_E_ITER_CAP;
+    }
+    *pass_ms = ms / passes;
+    return PBS_OK;
+}
+
 extern "C" {
+
+int pbs_set_pass_engine(pbs_handle *h, int engine) {
+    if (!h || (engine != PBS_ENGINE_GRAPH && engine != PBS_ENGINE_FRAME)) return PBS_E_INVALID_ARG;
+    PBS_DEVICE_SCOPE(h->device);
+    if (engine == PBS_ENGINE_FRAME && frame_ctas(h) <= 0) return PBS_E_INVALID_ARG;
+    h->engine = engine;
+    return PBS_OK;
+}
+
+int pbs_get_pass_engine(pbs_handle *h, int *engine) {
+    if (!h || !engine) return PBS_E_INVALID_ARG;
+    *engine = h->engine;
+    return PBS_OK;
+}
+
+int pbs_profile_frame(pbs_handle *h, int passes, double *pass_ms) {
+    if (!h || passes <= 0 || !pass_ms) return PBS_E_INVALID_ARG;
+    PBS_DEVICE_SCOPE(h->device);
+    return time_frame(h, passes, pass_ms);
+}
 
 int pbs_profile_kernels(pbs_handle *h, int passes, double *tet_ms, double *node_ms) {
     if (!h || passes <= 0 || !tet_ms || !node_ms) return PBS_E_INVALID_ARG;

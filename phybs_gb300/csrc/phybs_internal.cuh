@@ -220,6 +220,27 @@ cudaError_t prepare_chunk_kernels();
 // and stress mode on a device with `sms` SMs; 0 when it does not apply.
 int stream_grid(const DevMesh &m, int material, bool inc, int sms);
 
+// The persistent frame kernel (chunks.cu): one cooperative launch runs a
+// step's passes of a one-instance handle, with grid barriers between its tet
+// and node phases.  FrameSync: the barrier's words (zeroed before a launch);
+// ce / cr: per-CTA {sum e, sum e^2} of a check pass and {|g|^2, 0} of a pass.
+struct FrameSync {
+    unsigned int count, gen;
+    int err;  // a barrier wait ran out: the step ends with PBS_E_DEVICE_TIMEOUT
+    int pad;
+};
+struct FrameAux {
+    FrameSync *sync;
+    double2 *ce, *cr;
+    int max_passes;
+};
+// Co-resident CTAs of the frame kernel for this mesh and shape (at most one
+// per chunk); 0 when the kernel does not apply (several instances, a staged
+// chunk shape, a thread count without an instantiation).
+int frame_grid(const DevMesh &m, int material, bool inc, int sms);
+cudaError_t launch_frame(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material,
+                         const FrameAux &fx, int grid);
+
 // Launchers (kernels.cu, warmstart.cu)
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);

@@ -149,6 +149,23 @@ class DescentSolver:
         L.check(L.lib().pbs_profile_kernels(self._h, C.c_int(passes), C.byref(a), C.byref(b)), "pbs_profile_kernels")
         return a.value, b.value
 
+    def profile_frame(self, passes: int = 20) -> float:
+        """Mean milliseconds per pass of one frame-engine launch of `passes` passes."""
+        a = C.c_double()
+        L.check(L.lib().pbs_profile_frame(self._h, C.c_int(passes), C.byref(a)), "pbs_profile_frame")
+        return a.value
+
+    def set_pass_engine(self, engine: str):
+        """'graph' (per-pass kernels in captured graphs) or 'frame' (one
+        persistent cooperative launch a step; one instance, unstaged shape)."""
+        code = {"graph": L.PBS_ENGINE_GRAPH, "frame": L.PBS_ENGINE_FRAME}[engine]
+        L.check(L.lib().pbs_set_pass_engine(self._h, C.c_int(code)), "pbs_set_pass_engine")
+
+    def pass_engine(self) -> str:
+        e = C.c_int()
+        L.check(L.lib().pbs_get_pass_engine(self._h, C.byref(e)), "pbs_get_pass_engine")
+        return "frame" if e.value == L.PBS_ENGINE_FRAME else "graph"
+
     def autotune(self, passes: int = 32) -> dict:
         """Pick the pass kernels' chunk shape by timing candidates on this mesh."""
         r = L.TuneResult()

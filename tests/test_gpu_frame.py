@@ -1,0 +1,196 @@
+"""The frame engine (one persistent cooperative launch a step) against the
+graph engine (per-pass kernels in captured graphs).
+
+Both run the same per-tet and per-node arithmetic; the frame engine groups the
+instance's energy and residual sums per CTA instead of per chunk and node
+block.  With the residual stop off, the residual never steers a step, and the
+energy steers it only through the line-search test, which the regrouping does
+not flip on these meshes: the trajectories are then bit-identical.  With the
+residual stop on (the benchmark's settings), the frame engine's frames must
+match the graph engine's iteration counts within a few passes and positions
+within 1e-4 of the bounding-box diagonal (the bar test_gpu_benchconfig.py
+holds the graph engine to against the all-FP64 restatement).
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from phybs_gb300 import _lib as L
+from phybs_gb300 import meshes as M
+from phybs_gb300.solver import DescentSolver, make_params
+from tests._util import bbox_diag
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+# 128 threads, 128 tets a chunk: tens of chunks on these meshes, so the frame
+# kernel runs tens of CTAs and its grid barriers see real arrivals
+SHAPE = (128, 128, 96, 0, 1)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from phybs_gb300.build import build
+    build()
+
+
+def _pair(mesh, p, material=L.PBS_MATERIAL_NEOHOOKEAN, shape=SHAPE):
+    a = DescentSolver(mesh, params=p, material=material)
+    b = DescentSolver(mesh, params=p, material=material)
+    a.set_chunk_shape(*shape)
+    b.set_chunk_shape(*shape)
+    b.set_pass_engine("frame")
+    assert (a.pass_engine(), b.pass_engine()) == ("graph", "frame")
+    return a, b
+
+
+_CASES = [
+    ("neo-Hookean incremental", L.PBS_MATERIAL_NEOHOOKEAN, 1),
+    ("neo-Hookean full stress", L.PBS_MATERIAL_NEOHOOKEAN, 0),
+    ("stretch", L.PBS_MATERIAL_STRETCH, 0),
+]
+
+
+@pytest.mark.parametrize("name,material,incremental", _CASES, ids=[c[0] for c in _CASES])
+def test_frame_engine_bit_identical_without_residual_stop(name, material, incremental):
+    m = M.bar_mesh(16, 6, 6, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("cpu_reference", h=1 / 30, max_iters=96, incremental_stress=incremental)
+    a, b = _pair(m, p, material=material)
+    for f in range(4):
+        a.step()
+        b.step()
+        sa, sb = a.stats(), b.stats()
+        for key in ("passes", "iterations", "rejections", "converged", "status", "alpha", "rho", "omega"):
+            assert sa[key] == sb[key], (f, key, sa[key], sb[key])
+        assert sb["graph_launches"] == 0 and sa["graph_launches"] > 0
+        assert sb["energy"] == pytest.approx(sa["energy"], rel=1e-12)
+        assert np.array_equal(a.positions(), b.positions()), f
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("control", [L.PBS_CONTROL_REFERENCE, L.PBS_CONTROL_RESTART])
+def test_frame_engine_residual_stop(control):
+    """Every frame iterated to |g| <= 1e-3 |g_0| under both controls: the frame
+    engine stops where the graph engine does (its residual sum is regrouped,
+    so allow a pass or two), takes the same line-search decisions and lands on
+    the same positions to well within the stop tolerance's scale."""
+    m = M.bar_mesh(16, 6, 6, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=4000, tol=1e-3, control=control, alpha0=0.5,
+                    energy_slack=16.0, profile=((10, 0.995),))
+    a, b = _pair(m, p)
+    diag = bbox_diag(m.rest)
+    for f in range(4):
+        a.step()
+        b.step()
+        sa, sb = a.stats(), b.stats()
+        assert sa["status"] == sb["status"] == 0 and sa["converged"] == sb["converged"] == 1, (sa, sb)
+        assert abs(sa["iterations"] - sb["iterations"]) <= 2, (f, sa["iterations"], sb["iterations"])
+        assert sa["rejections"] == sb["rejections"], f
+        assert sb["residual_ratio"] <= 1e-3
+        assert np.abs(a.positions() - b.positions()).max() < 1e-4 * diag, f
+    a.close()
+    b.close()
+
+
+def test_frame_engine_line_search_rejections():
+    """A step size that overshoots (alpha0 1.0 under RESTART control with
+    growth): the line search rejects and restores, and the frame engine takes
+    the same decisions as the graph engine, pass for pass."""
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=20000, tol=1e-4, control=L.PBS_CONTROL_RESTART,
+                    alpha0=1.0, energy_slack=16.0, profile=((10, 0.995),), alpha_grow=1.2)
+    a, b = _pair(m, p, shape=(128, 64, 64, 0, 1))
+    diag = bbox_diag(m.rest)
+    rej = []
+    for f in range(3):
+        a.step()
+        b.step()
+        sa, sb = a.stats(), b.stats()
+        assert sb["status"] == 0 and sb["converged"] == 1, (f, sb)
+        assert sa["rejections"] == sb["rejections"], (f, sa["rejections"], sb["rejections"])
+        assert abs(sa["iterations"] - sb["iterations"]) <= 2, (f, sa["iterations"], sb["iterations"])
+        rej.append(sb["rejections"])
+        assert np.abs(a.positions() - b.positions()).max() < 1e-4 * diag, f
+    print(f"line-search rejections per frame: {rej}")
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("arm", ["plain", "warm"])
+def test_frame_engine_benchmark_settings(arm):
+    """The benchmark's solver settings on its box at 1/5 resolution (8,000
+    tets), first frames of the pull, both arms: frame and graph engines agree
+    on iteration counts within 1% and on positions within 1e-4 of the box's
+    diagonal, every frame converged to 1e-4."""
+    m, bottom, length, young = bench.box_workload(0, scale=0.2)
+    p = bench.solver_params()
+    a, b = _pair(m, p)
+    if arm == "warm":
+        from phybs_gb300.warmstart import DEFAULT_MODEL, WarmStartModel
+        model = WarmStartModel.load(DEFAULT_MODEL)
+        a.set_warm_start(model)
+        b.set_warm_start(model)
+    diag = bbox_diag(m.rest)
+    errs, iters = [], []
+    for f in range(8):
+        xb = bench.bottom_positions(m, bottom, length, f)
+        a.set_node_positions(bottom, xb)
+        b.set_node_positions(bottom, xb)
+        ia, ib = a.step(), b.step()
+        sb = b.stats()
+        assert sb["status"] == 0 and sb["converged"] == 1 and sb["residual_ratio"] <= 1e-4, (f, sb)
+        iters.append((ia, ib))
+        errs.append(float(np.abs(a.positions() - b.positions()).max() / diag))
+    print(f"{arm}: iterations (graph, frame) = {iters}; max |x_graph - x_frame| / diag = "
+          f"{[f'{e:.1e}' for e in errs]}")
+    ta, tb = sum(i for i, _ in iters), sum(i for _, i in iters)
+    assert abs(ta - tb) <= 0.01 * ta + 4, iters
+    assert max(errs) < 1e-4, errs
+    a.close()
+    b.close()
+
+
+def test_frame_engine_applies_to_one_unstaged_instance():
+    packed = M.batch_of_boxes(4, seed=3, nxy=(4, 6), nz=(6, 10))
+    s = DescentSolver(packed, params=make_params("cpu_reference", h=1 / 30, max_iters=16))
+    with pytest.raises(L.PhybsError) as e:
+        s.set_pass_engine("frame")
+    assert e.value.code == L.PBS_E_INVALID_ARG
+    assert s.pass_engine() == "graph"
+    s.close()
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    s = DescentSolver(m, params=make_params("cpu_reference", h=1 / 30, max_iters=16))
+    s.set_chunk_shape(128, 128, 96, 1, 1)  # staged rows: not the frame kernel's
+    with pytest.raises(L.PhybsError):
+        s.set_pass_engine("frame")
+    s.set_chunk_shape(*SHAPE)
+    s.set_pass_engine("frame")
+    s.step()
+    # a later staged shape leaves the handle outside the frame engine's set
+    s.set_chunk_shape(128, 128, 96, 1, 1)
+    with pytest.raises(L.PhybsError) as e:
+        s.step()
+    assert e.value.code == L.PBS_E_INVALID_ARG
+    s.set_pass_engine("graph")
+    s.step()
+    s.close()
+
+
+def test_profile_frame_runs_the_passes():
+    m = M.bar_mesh(16, 6, 6, edge=0.025, young=5e4, poisson=0.4)
+    s = DescentSolver(m, params=make_params("cpu_reference", h=1 / 30, max_iters=96))
+    s.set_chunk_shape(*SHAPE)
+    s.step()
+    x = s.positions()
+    ms = s.profile_frame(40)
+    assert 0.0 < ms < 5.0
+    tet, node = s.profile_kernels(40)
+    print(f"frame engine {ms * 1e3:.1f} us a pass; graph engine kernels {tet * 1e3:.1f} + {node * 1e3:.1f} us")
+    assert np.array_equal(s.positions(), x)  # the state is left as it was
+    s.close()
