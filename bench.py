@@ -163,11 +163,19 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
+def ncu_traffic(tune, stress):
+    """DRAM bytes of one plain pass (k_tchunk + k_node) that ncu measured on
+    this workload with the same chunk shape and stress mode; None when no
+    capture of that shape is committed (the tuned shape varies run to run)."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
+    if not os.path.exists(p) or tune is None:
+        return None
+    with open(p) as f:
+        entries = json.load(f).get("entries", [])
+    shape = [tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"], tune["node_npt"]]
+    for e in entries:
+        if e.get("shape") == shape and e.get("stress") == stress:
+            return e
     return None
 
 
@@ -323,7 +331,7 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
         s.set_node_positions(bottom, pin_xyz[f])
         s.step(raise_on_error=False)
 
-    res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0, "rejections": []}
+    res = {"iters": [], "passes": 0, "launches": 0, "status": [], "ws_used": 0, "rejections": [], "converged": []}
     # the state the first timed frame starts from (the CPU baseline's start)
     res["state"] = (s.positions(), *s.velocities())
     sync_ranks(world)
@@ -343,6 +351,8 @@ def run_arm(args, m, bottom, length, model, world, e2e: bool, tune=None):
             res["status"].append(st["status"])
             res["ws_used"] += st["warm_start_used"]
             res["rejections"].append(st["rejections"])
+            # 0: the frame stopped at the iteration limit short of the residual bar
+            res["converged"].append(st["converged"])
         e1.record(stream)
         sync_ranks(world)
         t_host = time.perf_counter() - t0
@@ -419,10 +429,12 @@ def run_ours(args, rank, world):
         tet_ms, node_ms = prof
         pass_ms = tet_ms + node_ms
         achieved = alg_bytes / (pass_ms * 1e-3) / 1e9
-        traffic = ncu_traffic()
+        traffic = ncu_traffic(tune, "incremental" if INCREMENTAL_STRESS else "full")
         roof = {"bound": "hbm", "kernel": "descent pass = k_tchunk + k_node", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                "traffic": (traffic or {}).get("bytes_per_pass"), "algorithmic_bytes_per_pass": alg_bytes,
+                "traffic": (traffic or {}).get("bytes_per_pass"),
+                "traffic_source": (traffic or {}).get("source", "no ncu capture of this chunk shape committed"),
+                "algorithmic_bytes_per_pass": alg_bytes,
                 "tet_ms": tet_ms, "node_ms": node_ms}
     else:
         roof = {"error": prof_err}
@@ -431,7 +443,8 @@ def run_ours(args, rank, world):
         return {"frames_per_s": r["frames_per_s"], "ms_per_frame": r["seconds"] / args.steps * 1e3,
                 "iterations_per_frame": float(np.mean(r["iters"])), "iterations": r["iters"],
                 "iterations_per_s": r["passes"] / r["seconds"], "status": r["status"],
-                "line_search_rejections": r["rejections"]}
+                "line_search_rejections": r["rejections"], "converged": r["converged"],
+                "unconverged_frames": int(len(r["converged"]) - sum(r["converged"]))}
 
     mode = "warm-started (learned per-node MLP, plain descent as fallback and judge)" if warm else \
         "plain descent (no trained warm-start model present)"

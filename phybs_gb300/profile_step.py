@@ -41,6 +41,7 @@ def main():
     ap.add_argument("--engine", choices=["graph", "frame"], default="graph")
     ap.add_argument("--warm", action="store_true")
     ap.add_argument("--train-steps", type=int, default=0)
+    ap.add_argument("--stress", choices=["incremental", "full"], default="incremental")
     args = ap.parse_args()
 
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -49,10 +50,10 @@ def main():
     from .solver import DescentSolver
 
     m, bottom, length, young = bench.box_workload(args.seed, args.scale)
-    s = DescentSolver(m, params=bench.solver_params())
+    s = DescentSolver(m, params=bench.solver_params(incremental=1 if args.stress == "incremental" else 0))
     s.set_chunk_shape(*[int(x) for x in args.shape.split(",")])
     s.set_node_positions(bottom, bench.bottom_positions(m, bottom, length, args.frame))
-    out = {"tets": m.n_tets, "nodes": m.n_nodes, "shape": args.shape}
+    out = {"tets": m.n_tets, "nodes": m.n_nodes, "shape": args.shape, "stress": args.stress}
     tet, node = s.profile_kernels(args.passes)
     out["tet_us"], out["node_us"] = tet * 1e3, node * 1e3
     if args.engine == "frame":
