@@ -166,15 +166,17 @@ def measured_peak():
 def ncu_traffic(tune, stress):
     """DRAM bytes of one plain pass (k_tchunk + k_node) that ncu measured on
     this workload with the same chunk shape and stress mode; None when no
-    capture of that shape is committed (the tuned shape varies run to run)."""
+    capture of that shape is committed (the tuned shape varies run to run).
+    The node kernel reads and writes the same words with one or two nodes a
+    thread, so the chunk shape (threads, tets, nodes, staging) decides."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p) or tune is None:
         return None
     with open(p) as f:
         entries = json.load(f).get("entries", [])
-    shape = [tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"], tune["node_npt"]]
+    shape = [tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"]]
     for e in entries:
-        if e.get("shape") == shape and e.get("stress") == stress:
+        if e.get("shape", [])[:4] == shape and e.get("stress") == stress:
             return e
     return None
 

@@ -221,6 +221,17 @@ int pbs_eval_tets(pbs_handle *h, const float *positions, float *corner_forces, f
  * value is below 0.3: the FP64 SVD of the near-inverted tets the reference's
  * modified SVD, IsotropicMaterial.cpp:16-60, resolves). */
 int pbs_eval_fp64_svd_count(pbs_handle *h, int *count);
+/* Parity probe of the incremental stress's per-step base force: the elastic
+ * node forces (3*N doubles, free nodes; pinned nodes get 0) at `positions`,
+ * from the kernels pbs_step runs once a step at its initial guess (each tet's
+ * neo-Hookean stress in double-float arithmetic, corner forces summed per
+ * node in FP64 in incidence order), on the displacements' FP32 hi words as
+ * the step's base uses them.  The per-node elastic force of
+ * IsotropicNeohookeanMaterial::computeInnerForceFromPos
+ * (IsotropicNeohookeanMaterial.cpp:93-114) without its gravity, external and
+ * pin-spring terms, to about 1e-12 relative.  Neo-Hookean handles only
+ * (PBS_E_INVALID_ARG otherwise). */
+int pbs_eval_base_force(pbs_handle *h, const float *positions, double *forces);
 /* Elastic forces (3*N) and Hessian diagonal (3*N) assembled by the
  * deterministic gather at the given positions (NULL = current). */
 int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag);

@@ -44,7 +44,7 @@ EXPORTS = (
     "pbs_set_surface", "pbs_get_face_ring", "pbs_pick_face", "pbs_drag_face_ring", "pbs_backward_euler_step",
     "pbs_set_guess", "pbs_autotune", "pbs_get_instance_stats", "pbs_set_chunk_shape",
     "pbs_pbd_step", "pbs_pd_step", "pbs_eval_fp64_svd_count",
-    "pbs_set_pass_engine", "pbs_get_pass_engine", "pbs_profile_frame",
+    "pbs_set_pass_engine", "pbs_get_pass_engine", "pbs_profile_frame", "pbs_eval_base_force",
 )
 
 PBS_EVAL_STATIC_MAX_TETS = 524288

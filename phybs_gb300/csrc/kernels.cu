@@ -320,51 +320,56 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     if (ci.done) atomicSub(st.active, 1);
 }
 
-// Per-step node constant b = f_el(u_base) (incremental mode, FP64) +
-// body_force_scale (external + gravity), split into FP32 (hi, lo).
+// Per-step node constant b = f_el(u_base) (incremental mode, double-float /
+// FP64) + body_force_scale (external + gravity), split into FP32 (hi, lo).
 // k_ref_tet evaluates each tet's full neo-Hookean stress at the base (the
-// step's initial guess, whose increments the passes evaluate) in FP64 once and
-// writes its 4 corner forces into FP64 gather slots; k_ref_gather sums each
-// node's slots in the canonical (tet, corner) order.
+// step's initial guess, whose increments the passes evaluate) once, in the
+// double-float type DD (about 2^-44 relative per operation; FP64 only for
+// 1 / J and log1p(d)), and writes its 4 corner forces into FP64 gather slots;
+// k_ref_gather sums each node's slots in FP64 in the canonical (tet, corner)
+// order.
 __global__ void k_ref_tet(DevMesh m, DevParams p, DevState st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.Tp) return;
     const int4 q = m.tets[t];
     if (q.x < 0) return;
     const int id[4] = {q.x, q.y, q.z, q.w};
-    double u[4][3];
+    // the base displacements are FP32 words: their differences are exact in
+    // the double-float type
+    DD u[4][3];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const float4 hh = st.ub[id[a]];
-        u[a][0] = hh.x;
-        u[a][1] = hh.y;
-        u[a][2] = hh.z;
+        u[a][0] = DD(hh.x);
+        u[a][1] = DD(hh.y);
+        u[a][2] = DD(hh.z);
     }
     const float4 r0 = m.row0[t], r1 = m.row1[t], r2 = m.row2[t];
-    const double dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-    Kin<double> k;
+    const float dinv[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
+    Kin<DD> k;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int cc = 0; cc < 3; ++cc)
-            k.G[3 * r + cc] = (u[1][r] - u[0][r]) * dinv[cc] + (u[2][r] - u[0][r]) * dinv[3 + cc] +
-                              (u[3][r] - u[0][r]) * dinv[6 + cc];
+            k.G[3 * r + cc] = (u[1][r] - u[0][r]) * DD(dinv[cc]) + (u[2][r] - u[0][r]) * DD(dinv[3 + cc]) +
+                              (u[3][r] - u[0][r]) * DD(dinv[6 + cc]);
     kinematics(k);
-    double P[9];
-    pk1_neohookean<double>(k, (double)r1.w, (double)r2.w, P);
-    const double sv = (double)r0.w;
+    DD P[9];
+    pk1_neohookean<DD>(k, DD(r1.w), DD(r2.w), P);
+    const DD sv(r0.w);
     const int4 sl = m.tslot[t];
     const int slot[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         // corner c: -svol P w_c (w_c = row c-1 of Dm^-1, w_0 = -sum of rows)
-        double w[3];
+        DD w[3];
 #pragma unroll
         for (int qq = 0; qq < 3; ++qq)
-            w[qq] = c == 0 ? -(dinv[qq] + dinv[3 + qq] + dinv[6 + qq]) : dinv[3 * (c - 1) + qq];
+            w[qq] = c == 0 ? -(DD(dinv[qq]) + DD(dinv[3 + qq]) + DD(dinv[6 + qq])) : DD(dinv[3 * (c - 1) + qq]);
         double *o = st.rslot + 3 * (size_t)slot[c];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) o[d] = -sv * (P[3 * d] * w[0] + P[3 * d + 1] * w[1] + P[3 * d + 2] * w[2]);
+        for (int d = 0; d < 3; ++d)
+            o[d] = (-sv * (P[3 * d] * w[0] + P[3 * d + 1] * w[1] + P[3 * d + 2] * w[2])).value();
     }
 }
 

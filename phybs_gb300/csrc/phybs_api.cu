@@ -1620,6 +1620,42 @@ int pbs_eval_fp64_svd_count(pbs_handle *h, int *count) {
     return PBS_OK;
 }
 
+int pbs_eval_base_force(pbs_handle *h, const float *positions, double *forces) {
+    if (!h || !positions || !forces) return PBS_E_INVALID_ARG;
+    if (h->material != PBS_MATERIAL_NEOHOOKEAN) return PBS_E_INVALID_ARG;
+    PBS_DEVICE_SCOPE(h->device);
+    const float4 *x;
+    int rc = eval_common(h, positions, &x);
+    if (rc != PBS_OK) return rc;
+    struct Scratch {  // freed on every return path
+        DevBuf<float4> b;
+        ~Scratch() { b.release(); }
+    } sb;
+    CK(sb.b.alloc(2 * (size_t)h->Np));
+    // the step's base-force kernels on the displacement's hi words, with the
+    // body forces off and the sums landing in the scratch pair
+    DevParams p = h->dparams;
+    p.incremental = 1;
+    p.body_scale = 0.f;
+    DevState st = h->state();
+    st.ub = const_cast<float4 *>(x);
+    st.bh = sb.b.p;
+    st.bl = sb.b.p + h->Np;
+    CK(launch_ref_force(h->stream, h->mesh(), p, st));
+    std::vector<float4> b(2 * (size_t)h->Np);
+    CK(cudaMemcpyAsync(b.data(), sb.b.p, sizeof(float4) * b.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < h->Np; ++i) {
+        const int u = h->h_pad2user[i];
+        if (u < 0) continue;
+        const float4 hi = b[i], lo = b[h->Np + i];
+        forces[3 * (size_t)u] = (double)hi.x + (double)lo.x;
+        forces[3 * (size_t)u + 1] = (double)hi.y + (double)lo.y;
+        forces[3 * (size_t)u + 2] = (double)hi.z + (double)lo.z;
+    }
+    return PBS_OK;
+}
+
 int pbs_eval_nodes(pbs_handle *h, const float *positions, float *forces, float *hess_diag) {
     if (!h) return PBS_E_INVALID_ARG;
     PBS_DEVICE_SCOPE(h->device);

@@ -555,4 +555,35 @@ __device__ __forceinline__ DFloat df_mul(DFloat a, DFloat b) {
 }
 __device__ __forceinline__ double df_double(DFloat a) { return (double)a.hi + (double)a.lo; }
 
+// The same double-float arithmetic as a number type, so that the templated
+// tet math above (disp-gradient, kinematics, stress) runs in it unchanged:
+// about 2^-44 relative per operation on the FP32 pipes, against GB300's
+// double-precision pipe, which ran the per-step base force at 0.5 ms on the
+// 1M-tet box.  The two scalar functions of a tet, 1 / J and log1p(d), are
+// taken in FP64 from the pair's value (one of each per tet).
+struct DD {
+    float hi, lo;
+    DD() = default;
+    __device__ __forceinline__ DD(float h) : hi(h), lo(0.f) {}
+    __device__ __forceinline__ DD(int v) : hi((float)v), lo(0.f) {}
+    __device__ __forceinline__ DD(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit DD(double v) {
+        hi = __double2float_rn(v);
+        lo = __double2float_rn(v - (double)hi);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ DD operator+(DD a, DD b) {
+    const DFloat r = df_add(DFloat{a.hi, a.lo}, DFloat{b.hi, b.lo});
+    return DD(r.hi, r.lo);
+}
+__device__ __forceinline__ DD operator-(DD a) { return DD(-a.hi, -a.lo); }
+__device__ __forceinline__ DD operator-(DD a, DD b) { return a + (-b); }
+__device__ __forceinline__ DD operator*(DD a, DD b) {
+    const DFloat r = df_mul(DFloat{a.hi, a.lo}, DFloat{b.hi, b.lo});
+    return DD(r.hi, r.lo);
+}
+__device__ __forceinline__ DD operator/(DD a, DD b) { return DD(a.value() / b.value()); }
+template <> __device__ __forceinline__ DD log1p_t<DD>(DD x) { return DD(log1p(x.value())); }
+
 }  // namespace pbs

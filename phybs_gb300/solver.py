@@ -315,6 +315,14 @@ class DescentSolver:
         L.check(L.lib().pbs_eval_nodes(self._h, _ptr(xx), _ptr(f), _ptr(hd)), "pbs_eval_nodes")
         return f, hd
 
+    def eval_base_force(self, x) -> np.ndarray:
+        """Elastic node forces (FP64 values, pins 0) at x from the incremental
+        stress's per-step base-force kernels (double-float, neo-Hookean)."""
+        f = np.empty((self.n, 3), np.float64)
+        xx = _f32(x, (-1, 3))
+        L.check(L.lib().pbs_eval_base_force(self._h, _ptr(xx), _ptr(f)), "pbs_eval_base_force")
+        return f
+
     def incidence(self):
         row = np.empty(self.n + 1, np.int32)
         ent = np.empty(4 * self.t, np.int32)

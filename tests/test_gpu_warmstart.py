@@ -164,6 +164,9 @@ def test_trained_network_gains_over_plain():
         ib.append(b.step())
         assert a.stats()["converged"] == 1 and b.stats()["converged"] == 1
         used += b.stats()["warm_start_used"]
+    gain = sum(ia[2:]) / sum(ib[2:])
+    print(f"held-out pull: iterations plain {ia}, warm-started {ib}; gain {gain:.3f}x on frames 2-11, "
+          f"learned guess kept on {used} of 12")
     assert sum(ib[2:]) < sum(ia[2:]), (ia, ib)
     assert used >= 6
     assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-3
