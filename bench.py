@@ -267,8 +267,8 @@ def run_reference(args):
 
 def launches_per_frame(graph_launches: int, warm: bool) -> int:
     """Kernels of one frame: the boundary scatter; init_ctl, prologue, the
-    base force (per-tet FP64 + gather with incremental stress, the gather
-    alone otherwise), epilogue; with the warm start the plain guess's corner
+    base force (per-tet double-float + gather with incremental stress, the
+    gather alone otherwise), epilogue; with the warm start the plain guess's corner
     forces (full stress only), reference gradient, tet F, inference, judge,
     select and the base force again; 2 x 16 per graph launch."""
     ref = 2 if INCREMENTAL_STRESS else 1

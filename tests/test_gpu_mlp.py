@@ -55,13 +55,16 @@ def test_gradient_matches_oracle(n):
     lref, gref = OM.loss_and_grad(theta, X, Y, round_bf16=True)
     assert abs(loss - lref) / lref < 1e-2
     off = 0
+    errs = []
     for o, i in OM.SIZES:
         for sz in (o * i, o):
             a, b = g[off:off + sz].astype(np.float64), gref[off:off + sz]
             off += sz
             nb = np.linalg.norm(b)
+            errs.append(np.linalg.norm(a - b) / nb)
             assert np.linalg.norm(a - b) / nb < 3e-2, (off, np.linalg.norm(a - b) / nb)
             assert a @ b / (np.linalg.norm(a) * nb) > 0.999
+    print(f"n={n}: per-block gradient error {[f'{e:.1e}' for e in errs]}")
     t.close()
 
 

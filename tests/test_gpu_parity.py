@@ -85,12 +85,24 @@ def test_per_tet_corner_forces(g, material):
 
 
 def test_node_forces_vs_reference(g):
+    """Assembled node forces: within 1e-5 of the all-FP64 restatement (on the
+    reference's rest data), and within 2e-5 of the reference's own FP32
+    forces, which carry FP32 rounding of their own (their distance from FP64
+    is printed beside the GPU's)."""
     for material, key in ((L.PBS_MATERIAL_NEOHOOKEAN, "probe_force_nh"), (L.PBS_MATERIAL_STRETCH, "probe_force_stretch")):
         s = solver_of(g, material=material)
         f, _ = s.eval_nodes(g["probe_x"])
         f = f.astype(np.float64)
         f[g["pins"]] = 0.0
-        assert rel_max(f, elastic_from_ref(g, key)) < 2e-5
+        f64, _ = O.node_eval(g["probe_x"], g["tets"], g["dminv"], g["an"], g["vol"], g["mu"], g["lam"],
+                             material=material, prec=64)
+        f64[g["pins"]] = 0.0
+        ref = elastic_from_ref(g, key)
+        e_gpu, e_ref, e_gr = rel_max(f, f64), rel_max(ref, f64), rel_max(f, ref)
+        print(f"material {material}: node forces vs FP64 {e_gpu:.2e} (reference vs FP64 {e_ref:.2e}); "
+              f"vs reference {e_gr:.2e}")
+        assert e_gpu < 1e-5
+        assert e_gr < 2e-5
         s.close()
 
 
