@@ -267,13 +267,15 @@ def run_reference(args):
 
 def launches_per_frame(graph_launches: int, warm: bool) -> int:
     """Kernels of one frame: the boundary scatter; init_ctl, prologue, the
-    base force (per-tet double-float + gather with incremental stress, the
-    gather alone otherwise), epilogue; with the warm start the plain guess's corner
+    RESTART control's guess check and fallback, the base force (per-tet
+    double-float + gather with incremental stress, the gather alone
+    otherwise), epilogue; with the warm start the plain guess's corner
     forces (full stress only), reference gradient, tet F, inference, judge,
-    select and the base force again; 2 x 16 per graph launch."""
+    select and the base force again; 2 x 16 per graph launch (the counts of a
+    launch list of one plain and one warm-started frame)."""
     ref = 2 if INCREMENTAL_STRESS else 1
     warm_extra = (0 if INCREMENTAL_STRESS else 1) + 5 + ref if warm else 0
-    return 1 + 3 + ref + warm_extra + 2 * 16 * graph_launches
+    return 1 + 3 + 2 + ref + warm_extra + 2 * 16 * graph_launches
 
 
 def tune_shape(args, m):

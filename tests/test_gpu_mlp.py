@@ -46,8 +46,8 @@ def test_forward_matches_oracle():
 @pytest.mark.parametrize("n", [37, 300, 4096])
 def test_gradient_matches_oracle(n):
     """Every parameter block's gradient against the FP64 backward with the
-    kernels' BF16 operand rounding: relative error of the block norm < 3e-2,
-    cosine > 0.999."""
+    kernels' BF16 operand rounding: relative error of the block norm < 5e-3
+    (measured 2.2e-3 at most, on the 37-sample batch), cosine > 0.999."""
     theta = OM.init_params(5).astype(np.float32)
     t = MLPTrainer(theta)
     X, Y = _data(n, 2)
@@ -62,7 +62,7 @@ def test_gradient_matches_oracle(n):
             off += sz
             nb = np.linalg.norm(b)
             errs.append(np.linalg.norm(a - b) / nb)
-            assert np.linalg.norm(a - b) / nb < 3e-2, (off, np.linalg.norm(a - b) / nb)
+            assert np.linalg.norm(a - b) / nb < 5e-3, (off, np.linalg.norm(a - b) / nb)
             assert a @ b / (np.linalg.norm(a) * nb) > 0.999
     print(f"n={n}: per-block gradient error {[f'{e:.1e}' for e in errs]}")
     t.close()

@@ -86,9 +86,10 @@ def test_per_tet_corner_forces(g, material):
 
 def test_node_forces_vs_reference(g):
     """Assembled node forces: within 1e-5 of the all-FP64 restatement (on the
-    reference's rest data), and within 2e-5 of the reference's own FP32
-    forces, which carry FP32 rounding of their own (their distance from FP64
-    is printed beside the GPU's)."""
+    reference's rest data) and within 1e-5 of the reference's own FP32 forces,
+    which carry FP32 rounding of their own (their distance from FP64 is
+    printed beside the GPU's: up to 5e-6 for the stretch material's FP32 SVD
+    route, against 2e-6 for the device)."""
     for material, key in ((L.PBS_MATERIAL_NEOHOOKEAN, "probe_force_nh"), (L.PBS_MATERIAL_STRETCH, "probe_force_stretch")):
         s = solver_of(g, material=material)
         f, _ = s.eval_nodes(g["probe_x"])
@@ -102,7 +103,7 @@ def test_node_forces_vs_reference(g):
         print(f"material {material}: node forces vs FP64 {e_gpu:.2e} (reference vs FP64 {e_ref:.2e}); "
               f"vs reference {e_gr:.2e}")
         assert e_gpu < 1e-5
-        assert e_gr < 2e-5
+        assert e_gr < 1e-5
         s.close()
 
 

@@ -148,9 +148,12 @@ def test_bad_prediction_falls_back():
 
 @pytest.mark.skipif(not os.path.exists(DEFAULT_MODEL), reason="no trained model committed")
 def test_trained_network_gains_over_plain():
-    """On a held-out pull scenario (seed not used in training) the trained
-    network cuts the iterations to the same residual bar, is used on most
-    frames, and both runs end within 1e-3 of the bbox diagonal of each other."""
+    """On a held-out pull scenario (a mesh seed not used in training; 51,200
+    tets) the trained network cuts the iterations to the same residual bar by
+    at least 8% over frames 2-11 (measured 1.125x: 4,571 against 5,143), is
+    kept on at least half the frames, and both runs end within 1e-3 of the
+    bbox diagonal of each other.  The step is bit-reproducible, so the gain
+    is a fixed number for the committed model."""
     model = WarmStartModel.load(DEFAULT_MODEL)
     m, x0, boundary = _pull_case(seed=987654, n=(20, 20, 32))
     a = DescentSolver(m, positions=x0, params=residual_params())
@@ -167,7 +170,7 @@ def test_trained_network_gains_over_plain():
     gain = sum(ia[2:]) / sum(ib[2:])
     print(f"held-out pull: iterations plain {ia}, warm-started {ib}; gain {gain:.3f}x on frames 2-11, "
           f"learned guess kept on {used} of 12")
-    assert sum(ib[2:]) < sum(ia[2:]), (ia, ib)
+    assert gain >= 1.08, (ia, ib)
     assert used >= 6
     assert np.abs(a.positions() - b.positions()).max() / m.bbox_diagonal() < 1e-3
     a.close()
