@@ -1063,11 +1063,8 @@ __global__ void __launch_bounds__(THREADS,
         float r2 = 0.f;
         for (int i = b * THREADS + threadIdx.x; i < m.Np; i += (int)G * THREADS) {
             NodeConst nc;
-            nc.info = m.info[i];
-            nc.th = st.th[i];
-            nc.tl = st.tl[i];
-            nc.bh = st.bh[i];
-            nc.bl = st.bl[i];
+            nc.ch = st.ch[i];
+            nc.cl = st.cl[i];
             NodeIn nn;
             nn.pa = m.pptr[i];
             nn.pe = m.pptr[i + 1];

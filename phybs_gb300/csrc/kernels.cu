@@ -216,18 +216,15 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     __shared__ float sh[TH / 32];
     __shared__ float2 shf[TH / 32];
     __shared__ int is_last;
-    __shared__ __align__(16) float4 s_c[5][BLOCK];  // info, th, tl, bh, bl of the block's nodes
+    __shared__ __align__(16) float4 s_c[2][BLOCK];  // c hi (.w = M/h^2), c lo (.w = state) of the block's nodes
     const int b = blockIdx.x;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     NodeIn in[NPT];
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
         const int l = threadIdx.x + j * TH, i = b * BLOCK + l;  // < Np: the grid covers the padded nodes exactly
-        cp_async16(&s_c[0][l], m.info + i);
-        cp_async16(&s_c[1][l], st.th + i);
-        cp_async16(&s_c[2][l], st.tl + i);
-        cp_async16(&s_c[3][l], st.bh + i);
-        cp_async16(&s_c[4][l], st.bl + i);
+        cp_async16(&s_c[0][l], st.ch + i);
+        cp_async16(&s_c[1][l], st.cl + i);
         in[j].pa = m.pptr[i];
         in[j].pe = m.pptr[i + 1];
     }
@@ -277,11 +274,8 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     for (int j = 0; j < NPT; ++j) {
         const int l = threadIdx.x + j * TH;
         NodeConst nc;
-        nc.info = s_c[0][l];
-        nc.th = s_c[1][l];
-        nc.tl = s_c[2][l];
-        nc.bh = s_c[3][l];
-        nc.bl = s_c[4][l];
+        nc.ch = s_c[0][l];
+        nc.cl = s_c[1][l];
         r2 += node_update<NPRE>(m, p, st, b * BLOCK + l, nc, in[j], fp[j], ctx);
     }
     const float sr = block_sum_f(r2, sh);
@@ -377,7 +371,11 @@ __global__ void k_ref_gather(DevMesh m, DevParams p, DevState st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.Np) return;
     const float4 info = m.info[i];
-    if (info.z == 2.f) return;
+    if (info.z == 2.f) {  // padding: only the node update's state word
+        st.ch[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        st.cl[i] = make_float4(0.f, 0.f, 0.f, 2.f);
+        return;
+    }
     const float4 ex = st.ext[i];
     double b[3] = {(double)p.body_scale * ex.x, (double)p.body_scale * ((double)ex.y + info.y),
                    (double)p.body_scale * ex.z};
@@ -396,6 +394,20 @@ __global__ void k_ref_gather(DevMesh m, DevParams p, DevState st) {
     }
     st.bh[i] = make_float4(hi[0], hi[1], hi[2], 0.f);
     st.bl[i] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    // c = (M / h^2) x~ + b with the node update's FP32 M / h^2, in FP64,
+    // split into (hi, lo); .w carries M / h^2 and the node's state, so that
+    // the node update reads these two words and no other per-step constant
+    const float mh = info.x * p.h2inv;
+    const float4 th = st.th[i], tl = st.tl[i];
+    const double t[3] = {(double)th.x + (double)tl.x, (double)th.y + (double)tl.y, (double)th.z + (double)tl.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double c = (double)mh * t[d] + b[d];
+        hi[d] = (float)c;
+        lo[d] = (float)(c - (double)hi[d]);
+    }
+    st.ch[i] = make_float4(hi[0], hi[1], hi[2], mh);
+    st.cl[i] = make_float4(lo[0], lo[1], lo[2], info.z);
 }
 
 // ------------------------------------------------------------ helpers

@@ -10,6 +10,13 @@
 
 namespace pbs {
 
+// One component of g = M/h^2 (u_hi + u_lo) - (c_hi + c_lo) - f.
+__device__ __forceinline__ float node_gradient(float uh, float ul, float mh, float ch, float cl, float f) {
+    const float ph = __fmul_rn(uh, mh);
+    const float pl = __fmaf_rn(uh, mh, -ph);  // ph + pl = uh * mh exactly
+    return __fsub_rn(__fadd_rn(__fsub_rn(ph, ch), __fsub_rn(__fmaf_rn(ul, mh, pl), cl)), f);
+}
+
 // The inputs of one node: the state-independent ones loaded before the
 // grid-dependency wait, the state words right after it.
 struct NodeIn {
@@ -18,9 +25,10 @@ struct NodeIn {
 };
 
 // Per-step node constants staged in shared memory before the grid-dependency
-// wait: mass / gravity / state, x~ (hi, lo), b (hi, lo).
+// wait: c = (M / h^2) x~ + b as (hi, lo), with M / h^2 in ch.w and the node's
+// state (0 free, 1 pinned, 2 padding) in cl.w.
 struct NodeConst {
-    float4 info, th, tl, bh, bl;
+    float4 ch, cl;
 };
 
 // The instance's pass state as the node update needs it.
@@ -41,7 +49,8 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
                                              const NodeConst &in, const NodeIn &nn, const float4 (&f)[NPRE],
                                              const PassCtx &c) {
     float r2 = 0.f;
-    if (in.info.z == 2.f) return r2;
+    const float state = in.cl.w;
+    if (state == 2.f) return r2;
     const size_t nxt = c.nxt;
     const float4 uh = nn.uh, ul = nn.ul, dd = nn.dd;
     float4 nh = uh, nl = ul, nd = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -51,7 +60,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
         // restarts it under PBS_CONTROL_RESTART
         nh = st.oh[i];
         nl = st.ol[i];
-        if (in.info.z == 0.f && p.control == PBS_CONTROL_REFERENCE)
+        if (state == 0.f && p.control == PBS_CONTROL_REFERENCE)
             nd = make_float4(((nh.x - uh.x) + (nl.x - ul.x)) + dd.x, ((nh.y - uh.y) + (nl.y - ul.y)) + dd.y,
                              ((nh.z - uh.z) + (nl.z - ul.z)) + dd.z, 0.f);
     } else {
@@ -59,7 +68,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
             st.oh[i] = uh;
             st.ol[i] = ul;
         }
-        if (in.info.z == 0.f) {
+        if (state == 0.f) {
             float fx = 0.f, fy = 0.f, fz = 0.f, hx = 0.f, hy = 0.f, hz = 0.f;
             // this node's per-chunk partial sums, in chunk order (the first
             // NPRE loaded with the state words, the rest here)
@@ -83,7 +92,7 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
                     hz += q.z;
                 }
             }
-            const float mh = in.info.x * p.h2inv;
+            const float mh = in.ch.w;  // M / h^2
             float4 D;
             if (c.do_h) {
                 D = make_float4(hx + mh, hy + mh, hz + mh, 0.f);
@@ -92,11 +101,14 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
                 D = nn.diag;
             }
             // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
-            // force (incremental mode) + body_force_scale (external + gravity)
-            const float4 th = in.th, tl = in.tl, bh = in.bh, bl = in.bl;
-            const float gx = ((((uh.x - th.x) + (ul.x - tl.x)) * mh - bh.x) - bl.x) - fx;
-            const float gy = ((((uh.y - th.y) + (ul.y - tl.y)) * mh - bh.y) - bl.y) - fy;
-            const float gz = ((((uh.z - th.z) + (ul.z - tl.z)) * mh - bh.z) - bl.z) - fz;
+            // force (incremental mode) + body_force_scale (external + gravity),
+            // formed as M/h^2 u - c - f with the per-step c = M/h^2 u~ + b: the
+            // product M/h^2 u_hi exactly (fma), its large part cancelled
+            // against c hi, the small terms added after
+            const float4 ch = in.ch, cl = in.cl;
+            const float gx = node_gradient(uh.x, ul.x, mh, ch.x, cl.x, fx);
+            const float gy = node_gradient(uh.y, ul.y, mh, ch.y, cl.y, fy);
+            const float gz = node_gradient(uh.z, ul.z, mh, ch.z, cl.z, fz);
             r2 = fmaf(gx, gx, fmaf(gy, gy, gz * gz));
             // Jacobi step delta = alpha * (g / -H) (DescentOptimize.cpp:142-150), then the
             // Chebyshev extrapolation x' = omega (x + delta - x_last) + x_last written as

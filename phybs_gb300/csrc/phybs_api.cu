@@ -65,7 +65,7 @@ struct pbs_handle {
     DevBuf<double2> cpart;
     DevBuf<double> rslot;
     // device state
-    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl, ub;
+    DevBuf<float4> uh, ul, dd, oh, ol, u0h, u0l, th, tl, v, vold, ext, diag, hist1, hist2, bh, bl, ub, ch, cl;
     // learned warm start
     DevBuf<float> ws_theta, ws_stats;  // NPARAM; feat mean 24, feat std 24, out std 3
     bool ws_enabled = false;
@@ -152,7 +152,7 @@ struct pbs_handle {
         DevState s;
         s.uh = uh.p; s.ul = ul.p; s.dd = dd.p; s.oh = oh.p; s.ol = ol.p; s.u0h = u0h.p; s.u0l = u0l.p;
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
-        s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p;
+        s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p; s.ch = ch.p; s.cl = cl.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.npartf = npartf.p; s.ctl = ctl.p; s.active = active.p;
         s.cpart = cpart.p; s.part = part.p; s.parth = parth.p; s.rslot = rslot.p;
         return s;
@@ -163,7 +163,7 @@ struct pbs_handle {
         DevBuf<int4> *i4[] = {&tets, &tslot};
         for (auto b : i4) b->release();
         DevBuf<float4> *f4[] = {&row0, &row1, &row2, &info, &rest4, &uh, &ul, &dd, &oh, &ol, &u0h, &u0l, &th, &tl,
-                                &v, &vold, &ext, &diag, &hist1, &hist2, &bh, &bl, &ub};
+                                &v, &vold, &ext, &diag, &hist1, &hist2, &bh, &bl, &ub, &ch, &cl};
         for (auto b : f4) b->release();
         DevBuf<int> *ii[] = {&inc_ptr, &inc, &tblk_inst, &nblk_inst, &pad2user, &tet_user, &node_state, &bad, &active,
                              &staging_ids};
@@ -484,6 +484,7 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->th.alloc(Np)); CKC(h->tl.alloc(Np)); CKC(h->v.alloc(Np)); CKC(h->vold.alloc(Np));
     CKC(h->ext.alloc(Np)); CKC(h->diag.alloc(Np)); CKC(h->rest4.alloc(Np));
     CKC(h->hist1.alloc(Np)); CKC(h->hist2.alloc(Np)); CKC(h->bh.alloc(Np)); CKC(h->bl.alloc(Np));
+    CKC(h->ch.alloc(Np)); CKC(h->cl.alloc(Np));
     CKC(h->ub.alloc(Np));
     // slot-ordered hot-loop buffers (3 * 4T) also serve the per-tet probes (12 * Tp)
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
@@ -1631,7 +1632,7 @@ int pbs_eval_base_force(pbs_handle *h, const float *positions, double *forces) {
         DevBuf<float4> b;
         ~Scratch() { b.release(); }
     } sb;
-    CK(sb.b.alloc(2 * (size_t)h->Np));
+    CK(sb.b.alloc(4 * (size_t)h->Np));
     // the step's base-force kernels on the displacement's hi words, with the
     // body forces off and the sums landing in the scratch pair
     DevParams p = h->dparams;
@@ -1641,6 +1642,8 @@ int pbs_eval_base_force(pbs_handle *h, const float *positions, double *forces) {
     st.ub = const_cast<float4 *>(x);
     st.bh = sb.b.p;
     st.bl = sb.b.p + h->Np;
+    st.ch = sb.b.p + 2 * (size_t)h->Np;  // the gather's gradient constant: scratch too
+    st.cl = sb.b.p + 3 * (size_t)h->Np;
     CK(launch_ref_force(h->stream, h->mesh(), p, st));
     std::vector<float4> b(2 * (size_t)h->Np);
     CK(cudaMemcpyAsync(b.data(), sb.b.p, sizeof(float4) * b.size(), cudaMemcpyDeviceToHost, h->stream));

@@ -11,6 +11,8 @@
 //                                  line-search check (the reference's x_old)
 //   u0h, u0l    float4[Np]         displacement at the start of the step
 //   th, tl      float4[Np]         inertial target x~ - X (hi, lo)
+//   bh, bl      float4[Np]         per-step force constant b (hi, lo)
+//   ch, cl      float4[Np]         per-step gradient constant c = (M / h^2) x~ + b (hi, lo)
 //   v, vold     float4[Np]         velocities of this and the previous step
 //   ext, diag   float4[Np]         external force; Jacobi diagonal + M/h^2
 //   info        float4[Np]         {effective mass (pins 1e8), gravity_y,
@@ -156,6 +158,9 @@ struct DevState {
     float4 *ub;             // base displacement of the increments: the step's initial guess (hi word)
     float4 *bh, *bl;        // per node (hi, lo): elastic force at the base (incremental mode)
                             // plus body_force_scale * (external + gravity)
+    float4 *ch, *cl;        // per node (hi, lo): c = (M / h^2) x~ + b, the step-constant part of
+                            // the gradient g = (M / h^2) u - c - f (the node update reads these
+                            // two words instead of x~ and b)
     float *tf, *hd;
     double2 *tpart, *cpart;
     double *npart;
