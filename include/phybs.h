@@ -328,6 +328,17 @@ int pbs_set_chunk_shape(pbs_handle *h, int threads, int chunk_tets, int chunk_no
  * pbs_stats.graph_launches is 0 for a frame-engine step.  No counterpart in
  * the reference, which launches each kernel from the host. */
 int pbs_set_pass_engine(pbs_handle *h, int engine);
+/* L2 residency of the per-tet pass data (the tets' Dm^-1 rows and corner
+ * records, 64 B a tet, read by every pass).  pbs_create takes the persisting-L2
+ * set-aside of the calling process's CUDA context (at most that data's size,
+ * at most what the device allows) and the per-tet kernels then launch with an
+ * L2 access-policy window over that data (persisting hits, streaming misses);
+ * pbs_destroy resets the persisting lines and sets the set-aside back to 0,
+ * for the whole context.  enable = 0 launches without the window (for a
+ * caller that shares L2 with other work, or to compare), 1 with it (the
+ * default); PBS_E_INVALID_ARG when the device has no persisting L2.  Results
+ * do not depend on it.  No counterpart in the reference. */
+int pbs_set_l2_residency(pbs_handle *h, int enable);
 int pbs_get_pass_engine(pbs_handle *h, int *engine);
 /* pbs_profile_kernels for the frame engine: one frame launch of `passes`
  * passes from the current state (left as it was), timed with CUDA events;

@@ -45,6 +45,7 @@ EXPORTS = (
     "pbs_set_guess", "pbs_autotune", "pbs_get_instance_stats", "pbs_set_chunk_shape",
     "pbs_pbd_step", "pbs_pd_step", "pbs_eval_fp64_svd_count",
     "pbs_set_pass_engine", "pbs_get_pass_engine", "pbs_profile_frame", "pbs_eval_base_force",
+    "pbs_set_l2_residency",
 )
 
 PBS_EVAL_STATIC_MAX_TETS = 524288

@@ -776,26 +776,42 @@ cudaError_t launch_pass_rows(cudaStream_t s, int T, const int *qperm, const floa
     return cudaGetLastError();
 }
 
+// Launch of a per-tet pass kernel: programmatic dependent launch (pdl), and
+// the mesh's L2 access-policy window over the pass rows when it has one.  at:
+// room for two attributes.
 static cudaLaunchConfig_t chunk_config(cudaStream_t s, int grid, int threads, size_t smem, bool pdl,
-                                       cudaLaunchAttribute *at) {
+                                       cudaLaunchAttribute *at, const DevMesh &m) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
+    int n = 0;
+    if (pdl) {
+        at[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[n].val.programmaticStreamSerializationAllowed = 1;
+        ++n;
+    }
+    if (m.l2_base) {
+        at[n].id = cudaLaunchAttributeAccessPolicyWindow;
+        at[n].val.accessPolicyWindow.base_ptr = const_cast<void *>(m.l2_base);
+        at[n].val.accessPolicyWindow.num_bytes = m.l2_bytes;
+        at[n].val.accessPolicyWindow.hitRatio = m.l2_hit;
+        at[n].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        at[n].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        ++n;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = pdl ? 1 : 0;
+    cfg.numAttrs = n;
     return cfg;
 }
 
 template <int MATERIAL, int THREADS, bool INC, bool STAGE>
 static cudaError_t launch_tchunk_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, int par,
                                    bool pdl) {
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     cudaLaunchConfig_t cfg = chunk_config(s, m.n_chunks, THREADS,
-                                          chunk_smem(m.chunk_tets, m.chunk_nodes, INC, STAGE ? 1 : 0), pdl, at);
+                                          chunk_smem(m.chunk_tets, m.chunk_nodes, INC, STAGE ? 1 : 0), pdl, at, m);
     return cudaLaunchKernelEx(&cfg, k_tchunk<MATERIAL, THREADS, INC, STAGE>, m, p, st, par);
 }
 
@@ -803,9 +819,9 @@ template <int MATERIAL, int THREADS, bool INC>
 static cudaError_t launch_tstream_t(cudaStream_t s, const DevMesh &m, const DevParams &p, const DevState &st, int par,
                                     bool pdl) {
     if (m.stream_grid <= 0) return cudaErrorInvalidConfiguration;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     cudaLaunchConfig_t cfg =
-        chunk_config(s, m.stream_grid, THREADS, chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 2), pdl, at);
+        chunk_config(s, m.stream_grid, THREADS, chunk_smem(m.chunk_tets, m.chunk_nodes, INC, 2), pdl, at, m);
     return cudaLaunchKernelEx(&cfg, k_tstream<MATERIAL, THREADS, INC>, m, p, st, par);
 }
 

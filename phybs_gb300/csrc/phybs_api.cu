@@ -59,9 +59,17 @@ struct pbs_handle {
     std::vector<double> h_rest_pad;
     DevBuf<int4> chunk;
     DevBuf<int> chunk_inst, qperm, pptr;
-    DevBuf<uint4> qcor;
+    uint4 *qcor = nullptr;  // in qrows, after the three row arrays
     DevBuf<int4> lmeta;
-    DevBuf<float4> qrow0, qrow1, qrow2, part, parth;
+    // the pass tets' rows and corner records, one allocation (4 x 16 B a tet):
+    // the L2 access-policy window of the per-tet kernel covers it
+    DevBuf<float4> qrows, part, parth;
+    float4 *qrow0 = nullptr, *qrow1 = nullptr, *qrow2 = nullptr;
+    // L2 residency of the pass rows: persisting set-aside taken, window bytes,
+    // hit ratio, and whether the launches use it (pbs_set_l2_residency)
+    bool l2_setaside = false, l2_use = true;
+    size_t l2_window = 0;
+    float l2_hit = 0.f;
     DevBuf<double2> cpart;
     DevBuf<double> rslot;
     // device state
@@ -143,7 +151,10 @@ struct pbs_handle {
         m.chunk_tets = chunk_tets; m.chunk_nodes = chunk_nodes; m.chunk_threads = chunk_threads;
         m.chunk_stage = chunk_stage;
         m.node_npt = node_npt;
-        m.qrow0 = qrow0.p; m.qrow1 = qrow1.p; m.qrow2 = qrow2.p; m.qcor = qcor.p; m.lmeta = lmeta.p;
+        m.qrow0 = qrow0; m.qrow1 = qrow1; m.qrow2 = qrow2; m.qcor = qcor; m.lmeta = lmeta.p;
+        m.l2_base = l2_use && l2_window ? (const void *)qrows.p : nullptr;
+        m.l2_bytes = l2_window;
+        m.l2_hit = l2_hit;
         m.pptr = pptr.p;
         m.stream_grid = stream_grid(m, material, dparams.incremental != 0, sms);
         return m;
@@ -169,10 +180,10 @@ struct pbs_handle {
                              &staging_ids};
         for (auto b : ii) b->release();
         ws_theta.release(); ws_stats.release();
-        chunk.release(); qcor.release(); lmeta.release(); cpart.release(); rslot.release();
+        chunk.release(); lmeta.release(); cpart.release(); rslot.release();
         DevBuf<int> *ci[] = {&chunk_inst, &qperm, &pptr};
         for (auto b : ci) b->release();
-        DevBuf<float4> *cf[] = {&qrow0, &qrow1, &qrow2, &part, &parth};
+        DevBuf<float4> *cf[] = {&qrows, &part, &parth};
         for (auto b : cf) b->release();
         tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release();
         fsync.release(); fce.release(); fcr.release();
@@ -223,18 +234,18 @@ static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, int stage
     build_chunks(h->Np, h->h_tets_pad, h->h_rest_pad, ctl, ct, cn, cl);
     const int nc = (int)cl.chunk.size();
     const size_t L = cl.lmeta.size(), T = (size_t)h->T;
-    h->chunk.release(); h->chunk_inst.release(); h->cpart.release(); h->qperm.release(); h->qcor.release();
+    h->chunk.release(); h->chunk_inst.release(); h->cpart.release(); h->qperm.release();
     h->lmeta.release(); h->pptr.release();
     h->part.release(); h->parth.release();
     CK(h->chunk.alloc(nc)); CK(h->chunk_inst.alloc(nc)); CK(h->cpart.alloc(nc));
-    CK(h->qperm.alloc(T)); CK(h->qcor.alloc(T));
+    CK(h->qperm.alloc(T));
     CK(h->lmeta.alloc(L)); CK(h->pptr.alloc(h->Np + 1));
     CK(h->part.alloc(L)); CK(h->parth.alloc(L));
     cudaStream_t s = h->stream;
     CK(cudaMemcpyAsync(h->chunk.p, cl.chunk.data(), sizeof(int4) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->chunk_inst.p, cl.chunk_inst.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->qperm.p, cl.qperm.data(), sizeof(int) * T, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->qcor.p, cl.qcor.data(), sizeof(uint4) * T, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->qcor, cl.qcor.data(), sizeof(uint4) * T, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->lmeta.p, cl.lmeta.data(), sizeof(int4) * L, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->pptr.p, cl.pptr.data(), sizeof(int) * (h->Np + 1), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(h->part.p, 0, sizeof(float4) * std::max<size_t>(L, 1), s));
@@ -248,8 +259,8 @@ static int set_pass_layout(pbs_handle *h, int threads, int ct, int cn, int stage
         *host_ctl = ctl;
     } else {
         CK(cudaMemcpyAsync(h->ctl.p, ctl.data(), sizeof(InstCtl) * h->B, cudaMemcpyHostToDevice, s));
-        CK(launch_pass_rows(s, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0.p, h->qrow1.p,
-                            h->qrow2.p));
+        CK(launch_pass_rows(s, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0, h->qrow1,
+                            h->qrow2));
     }
     CK(cudaStreamSynchronize(s));
     h->graph_valid = false;
@@ -333,6 +344,26 @@ static int validate_params(const pbs_step_params *p) {
         !std::isfinite(p->alpha_grow))
         return PBS_E_INVALID_ARG;
     return PBS_OK;
+}
+
+// L2 residency of the pass rows (the per-tet kernels' 64 B a tet, read every
+// pass): without it they stream from HBM on every pass although the step's
+// working set is near L2's size.  Takes the persisting-L2 set-aside of this
+// process's context (at most the rows' size, at most what the device allows)
+// and sizes the window and its hit ratio to it; the limit belongs to the
+// context, and pbs_destroy gives it back.  Devices without persisting L2 run
+// without a window.
+static void setup_l2_residency(pbs_handle *h, const cudaDeviceProp &prop) {
+    const size_t bytes = h->qrows.n * sizeof(float4);
+    if (prop.persistingL2CacheMaxSize <= 0 || prop.accessPolicyMaxWindowSize <= 0 || bytes == 0) return;
+    const size_t aside = std::min<size_t>((size_t)prop.persistingL2CacheMaxSize, bytes);
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, aside) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    h->l2_setaside = true;
+    h->l2_window = std::min<size_t>(bytes, (size_t)prop.accessPolicyMaxWindowSize);
+    h->l2_hit = (float)std::min(1.0, (double)aside / (double)h->l2_window);
 }
 
 int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
@@ -491,7 +522,12 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk)); CKC(h->npartf.alloc(h->n_nblk));
     CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
-    CKC(h->qrow0.alloc(T)); CKC(h->qrow1.alloc(T)); CKC(h->qrow2.alloc(T)); CKC(h->rslot.alloc(12 * (size_t)T));
+    CKC(h->qrows.alloc(4 * (size_t)T)); CKC(h->rslot.alloc(12 * (size_t)T));
+    h->qrow0 = h->qrows.p;
+    h->qrow1 = h->qrows.p + (size_t)T;
+    h->qrow2 = h->qrows.p + 2 * (size_t)T;
+    h->qcor = reinterpret_cast<uint4 *>(h->qrows.p + 3 * (size_t)T);
+    setup_l2_residency(h, prop);
     CKC(prepare_chunk_kernels());
     cudaStream_t s = h->stream;
     {
@@ -560,8 +596,24 @@ void pbs_destroy(pbs_handle *h) {
     if (!h) return;
     DeviceScope scope(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->l2_setaside) {  // the persisting lines back to normal, the set-aside returned
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
     h->release();
     delete h;
+}
+
+int pbs_set_l2_residency(pbs_handle *h, int enable) {
+    if (!h || (enable != 0 && enable != 1)) return PBS_E_INVALID_ARG;
+    PBS_DEVICE_SCOPE(h->device);
+    if (enable && !h->l2_setaside) return PBS_E_INVALID_ARG;  // the device offers no persisting L2
+    if ((enable != 0) != h->l2_use) {
+        h->l2_use = enable != 0;
+        h->graph_valid = false;  // the captured launches carry the window
+        if (!enable) cudaCtxResetPersistingL2Cache();
+    }
+    return PBS_OK;
 }
 
 int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lambda, int count) {
@@ -577,8 +629,8 @@ int pbs_set_material(pbs_handle *h, int model, const float *mu, const float *lam
     if (e == cudaSuccess) e = cudaMemcpyAsync(buf.p + count, lambda, sizeof(float) * count, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = launch_set_lame(h->stream, h->Tp, h->tets.p, buf.p, buf.p + count, count, h->row1.p, h->row2.p, h->tet_user.p);
     if (e == cudaSuccess)  // the pass kernel's copy of the rows, in chunk order
-        e = launch_pass_rows(h->stream, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0.p, h->qrow1.p,
-                             h->qrow2.p);
+        e = launch_pass_rows(h->stream, h->T, h->qperm.p, h->row0.p, h->row1.p, h->row2.p, h->qrow0, h->qrow1,
+                             h->qrow2);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     buf.release();
     CK(e);

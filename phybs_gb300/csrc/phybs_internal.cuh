@@ -148,6 +148,11 @@ struct DevMesh {
     const int4 *lmeta;
     const int *pptr;
     int stream_grid;  // CTAs of the persistent chunk kernel (chunk_stage 2)
+    // L2 access-policy window of the per-tet kernels' launches (host side):
+    // the pass rows and records persist in L2 at hit ratio l2_hit; null = off
+    const void *l2_base;
+    size_t l2_bytes;
+    float l2_hit;
 };
 
 struct DevState {

@@ -42,6 +42,7 @@ def main():
     ap.add_argument("--warm", action="store_true")
     ap.add_argument("--train-steps", type=int, default=0)
     ap.add_argument("--stress", choices=["incremental", "full"], default="incremental")
+    ap.add_argument("--l2", choices=["on", "off"], default="on", help="L2 residency window of the pass rows")
     args = ap.parse_args()
 
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -52,8 +53,10 @@ def main():
     m, bottom, length, young = bench.box_workload(args.seed, args.scale)
     s = DescentSolver(m, params=bench.solver_params(incremental=1 if args.stress == "incremental" else 0))
     s.set_chunk_shape(*[int(x) for x in args.shape.split(",")])
+    if args.l2 == "off":
+        s.set_l2_residency(False)
     s.set_node_positions(bottom, bench.bottom_positions(m, bottom, length, args.frame))
-    out = {"tets": m.n_tets, "nodes": m.n_nodes, "shape": args.shape, "stress": args.stress}
+    out = {"tets": m.n_tets, "nodes": m.n_nodes, "shape": args.shape, "stress": args.stress, "l2": args.l2}
     tet, node = s.profile_kernels(args.passes)
     out["tet_us"], out["node_us"] = tet * 1e3, node * 1e3
     if args.engine == "frame":

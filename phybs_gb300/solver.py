@@ -161,6 +161,11 @@ class DescentSolver:
         code = {"graph": L.PBS_ENGINE_GRAPH, "frame": L.PBS_ENGINE_FRAME}[engine]
         L.check(L.lib().pbs_set_pass_engine(self._h, C.c_int(code)), "pbs_set_pass_engine")
 
+    def set_l2_residency(self, enable: bool):
+        """Launch the per-tet kernels with (True, the default) or without an L2
+        access-policy window that keeps the pass rows resident."""
+        L.check(L.lib().pbs_set_l2_residency(self._h, C.c_int(1 if enable else 0)), "pbs_set_l2_residency")
+
     def pass_engine(self) -> str:
         e = C.c_int()
         L.check(L.lib().pbs_get_pass_engine(self._h, C.byref(e)), "pbs_get_pass_engine")
