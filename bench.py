@@ -23,9 +23,12 @@ headline arm through the same calls plus each frame's read-back of all
 positions to pinned host memory (pbs_read_positions), on the host clock.
 
 ``--impl reference`` times the CPU restatement of the reference's descent
-step (serial, like DescentOptimize) on the same workload: each step is a
-bounded sample of 32 iterations of a frame, converted to frames/s with the
-iterations a frame of the plain descent takes.
+step (DescentOptimize with the benchmark's control, FP64, its per-tet loops
+on all host threads) on the same workload: frames 0 .. W-1 untimed, frames
+W .. W+K-1 timed whole on the host clock, every frame iterated to the same
+residual bar.  The GPU arm's ``cpu_baseline`` times frames W .. W+2 the same
+way from the plain GPU arm's state, and ``cpu_force_eval`` the port of the
+reference's OpenMP force path (computeInnerForcesfromFhats2).
 """
 from __future__ import annotations
 
@@ -88,8 +91,8 @@ RHO = 0.9999
 ALPHA_GROW = 1.2
 
 
-# Stress evaluation of the passes: incremental (P(F) - P(F0) against an FP64
-# force at the step's initial guess).  The full FP32 stress is ~13% faster per
+# Stress evaluation of the passes: incremental (P(F) - P(F0) against a
+# double-float force at the step's initial guess).  The full FP32 stress is ~13% faster per
 # pass, but with alpha_grow its residual floor stalls the last, most stretched
 # frames of this pull just above 1e-4 |g0| (frame 29 ran into the iteration
 # cap in both arms); the incremental form has no floor there.
@@ -270,11 +273,11 @@ def launches_per_frame(graph_launches: int, warm: bool) -> int:
     RESTART control's guess check and fallback, the base force (per-tet
     double-float + gather with incremental stress, the gather alone
     otherwise), epilogue; with the warm start the plain guess's corner
-    forces (full stress only), reference gradient, tet F, inference, judge,
-    select and the base force again; 2 x 16 per graph launch (the counts of a
-    launch list of one plain and one warm-started frame)."""
+    forces (full stress only), reference gradient, tet F, inference, judge and
+    select; 2 x 16 per graph launch (the counts of a launch list of one plain
+    and one warm-started frame)."""
     ref = 2 if INCREMENTAL_STRESS else 1
-    warm_extra = (0 if INCREMENTAL_STRESS else 1) + 5 + ref if warm else 0
+    warm_extra = (0 if INCREMENTAL_STRESS else 1) + 5 if warm else 0
     return 1 + 3 + 2 + ref + warm_extra + 2 * 16 * graph_launches
 
 

@@ -13,7 +13,11 @@
 //   k_ws_judge     energies of both guesses (tets + node terms, FP64 sums);
 //                  the instance keeps the candidate only if its energy is not
 //                  higher (the plain descent is the fallback and the judge)
-//   k_ws_select    copies the chosen guess into the pass state
+//   k_ws_select    copies the chosen guess into the pass state.  The base of
+//                  the incremental stress stays at the plain guess, whose
+//                  elastic force the step already formed: the increments are
+//                  exact from any base, so a kept guess needs no second base
+//                  force
 #include <algorithm>
 
 #include "../../include/phybs.h"
@@ -373,7 +377,6 @@ __global__ void k_ws_select(DevMesh m, DevState st) {
     if (!node_ctl_ws(m, st, i)) return;
     st.uh[i] = st.uh[m.Np + i];
     st.ul[i] = st.ul[m.Np + i];
-    st.ub[i] = st.uh[m.Np + i];
 }
 
 // A caller-supplied candidate (parity 1) keeps the prescribed positions of
@@ -392,9 +395,7 @@ cudaError_t launch_ws_choose(cudaStream_t s, const DevMesh &m, const DevParams &
     k_ws_guess_pins<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
     k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, 0);
     k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    return launch_ref_force(s, m, p, st);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material) {
@@ -426,9 +427,7 @@ cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams 
     }
     k_ws_judge<<<m.n_tblk, BLOCK, 0, s>>>(m, p, st, base == 1);
     k_ws_select<<<nblk(m.Np, 256), 256, 0, s>>>(m, st);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    return launch_ref_force(s, m, p, st);  // the base moved where the learned guess was kept
+    return cudaGetLastError();
 }
 
 cudaError_t launch_ws_features(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, float *tetF,
