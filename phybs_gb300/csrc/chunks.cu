@@ -24,6 +24,12 @@
 // share of the instance's node energy terms (FP64, fixed order); the
 // instance's last chunk to finish decides accept / reject
 // (DescentOptimize.cpp:107-128) before any node moves.
+//
+// The pass decision of the previous node update (residual test, Chebyshev
+// state, caps) is taken by the instance's first chunk CTA (settle_pass) from
+// one control-block copy into the other, while every CTA runs on its
+// foreseen outcome (pass_view): the next k, or work that goes unused when the
+// instance stopped.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -330,21 +336,27 @@ __device__ __forceinline__ void chunk_partials(const int4 *meta, int nl, const f
 // Line-search pass: adds the chunk's share of the instance's node energy terms
 // to the thread's tet energies e, stores the chunk's {sum e, sum e^2}, and in
 // the instance's last chunk to finish sums the chunks in order and decides
-// accept / reject (DescentOptimize.cpp:107-128).  The sums run in
-// double-float (e) and FP32 (e^2, a noise scale), the chunk totals and their
-// sum in FP64.  Called by every thread of the CTA; *is_last is a shared word.
+// accept / reject (DescentOptimize.cpp:107-128) on dst, the control-block copy
+// the pass's node kernel reads (its first chunk settled the last pass into
+// it before counting itself in).  The sums run in double-float (e) and FP32
+// (e^2, a noise scale), the chunk totals and their sum in FP64.  Called by
+// every thread of the CTA; *is_last is a shared word.
 template <int THREADS>
 __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevParams &p, const DevState &st, int c,
-                                                  InstCtl *cp, int k, size_t cur, DFloat e, double *sh,
+                                                  int inst, int par, int k, size_t cur, DFloat e, double *sh,
                                                   int *is_last) {
     __shared__ float2 shf[THREADS / 32];
+    // (formed here, not carried through the tet loop: registers are short)
+    const InstCtl *src = ctl_buf(st, par) + inst;
+    InstCtl *dst = ctl_buf(st, par ^ 1) + inst;
+    unsigned int *cnt = st.tcount + inst;
     __shared__ float shs[THREADS / 32];
     float e2 = e.hi * e.hi;
+    const int cb = src->cblk_begin, ce = src->cblk_end;
     {
-        const int nb = cp->cblk_end - cp->cblk_begin;
+        const int nb = ce - cb;
         const float4 *U = st.uh + cur;
-        for (int i = cp->node_begin + (c - cp->cblk_begin) * THREADS + threadIdx.x; i < cp->node_end;
-             i += nb * THREADS) {
+        for (int i = src->node_begin + (c - cb) * THREADS + threadIdx.x; i < src->node_end; i += nb * THREADS) {
             const float4 info = m.info[i];
             if (info.z != 0.f) continue;
             const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv);
@@ -357,8 +369,8 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     if (threadIdx.x == 0) {
         st.cpart[c] = make_double2(df_double(se), (double)se2);
         __threadfence();
-        const unsigned int prev = atomicAdd(&cp->counter_t, 1u);
-        *is_last = (prev == (unsigned int)(cp->cblk_end - cp->cblk_begin - 1));
+        const unsigned int prev = atomicAdd(cnt, 1u);
+        *is_last = (prev == (unsigned int)(ce - cb - 1));
     }
     __syncthreads();
     if (!*is_last) return;
@@ -370,7 +382,6 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     // per partial made it several microseconds
     constexpr int U = 8;
     double ea = 0.0, eb = 0.0;
-    const int cb = cp->cblk_begin, ce = cp->cblk_end;
     for (int j0 = cb + threadIdx.x; j0 < ce; j0 += U * THREADS) {
         double2 v[U];
 #pragma unroll
@@ -387,10 +398,13 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
     const double E = block_sum(ea, sh);
     const double E2 = block_sum(eb, sh);
     if (threadIdx.x != 0) return;
-    InstCtl ci = *cp;  // one load, updates in registers, one store (as in the node kernel)
-    ci.counter_t = 0;
+    *cnt = 0;
+    // one load, updates in registers, one store; an instance the settled
+    // decision stopped keeps its control block (this pass ran on speculation)
+    InstCtl ci = load_ctl_cg(dst);
+    if (ci.done) return;
     decide_line_search(ci, p, k, E, E2);
-    *cp = ci;
+    *dst = ci;
     if (ci.done) atomicSub(st.active, 1);
 }
 
@@ -399,17 +413,23 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
 // hd_every passes, and the line-search tail.
 template <int MATERIAL, int THREADS, bool INC>
 __device__ __forceinline__ void chunk_body(const DevMesh &m, const DevParams &p, const DevState &st, int c,
-                                           InstCtl *cp, int k, bool check, bool do_h, size_t cur, const ChunkView &v,
-                                           const int4 *meta, int nt, int nl, float4 *sf, double *sh, int *is_last) {
-    const DFloat e = chunk_forces_all<MATERIAL, THREADS, INC>(p, v, nt, check, sf);
+                                           int inst, int par, const PassView &pv, size_t cur, const ChunkView &v,
+                                           const int4 *meta, int nt, int nl, float4 *sf, double *sh,
+                                           int *is_last) {
+    const DFloat e = chunk_forces_all<MATERIAL, THREADS, INC>(p, v, nt, pv.check, sf);
     chunk_partials<THREADS>(meta, nl, sf, st.part);
-    if (do_h) {
+    if (pv.do_h) {
         __syncthreads();
         chunk_hdiag<MATERIAL, THREADS, INC>(v, nt, sf);
         __syncthreads();
         chunk_partials<THREADS>(meta, nl, sf, st.parth);
     }
-    if (check) chunk_line_search<THREADS>(m, p, st, c, cp, k, cur, e, sh, is_last);
+    // the instance's first chunk takes the last pass's pending decision after
+    // its own tets (the other chunks run on its foreseen outcome without
+    // waiting), and before it counts itself into a line search
+    const InstCtl *src = ctl_buf(st, par) + inst;
+    if (c == src->cblk_begin) settle_pass<THREADS>(p, st, src, ctl_buf(st, par ^ 1) + inst, true);
+    if (pv.check) chunk_line_search<THREADS>(m, p, st, c, inst, par, pv.k, cur, e, sh, is_last);
 }
 
 // One CTA per chunk.  STAGE: every thread first issues asynchronous copies of
@@ -461,7 +481,8 @@ __global__ void __launch_bounds__(THREADS,
     const size_t cur = (size_t)par * m.Np;
     pdl_launch_dependents();
     pdl_wait();
-    InstCtl *cp = st.ctl + inst;
+    const InstCtl *src = ctl_buf(st, par) + inst;
+    InstCtl *dst = ctl_buf(st, par ^ 1) + inst;
     const int4 *meta = STAGE ? s_meta : m.lmeta + l0;
     if (STAGE) {
         // each thread stages the node words of the records it copied itself;
@@ -476,13 +497,14 @@ __global__ void __launch_bounds__(THREADS,
         }
         cp_async_commit();
     }
-    if (cp->done) {
+    const PassView pv = pass_view(src, p);
+    if (pv.skip) {
+        // an instance that stopped: its first chunk carries the control block
+        // over to the copy the node kernel reads
+        if (c == src->cblk_begin) settle_pass<THREADS>(p, st, src, dst, true);
         if (STAGE) cp_async_wait_all();
         return;
     }
-    const int k = cp->k;
-    const bool check = (k % p.ls_every) == 0 || cp->force_check;
-    const bool do_h = (k % p.hd_every) == 0;
     if (STAGE) {
         cp_async_wait_all();
         if (INC)  // the increments of the nodes this thread staged
@@ -512,8 +534,7 @@ __global__ void __launch_bounds__(THREADS,
     v.cor = STAGE ? s_cor : m.qcor + tq0;
     v.meta = meta;
     v.rest = m.rest;
-    chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cp, k, check, do_h, cur, v, meta, nt, nl, s_f, sh,
-                                       &is_last);
+    chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, inst, par, pv, cur, v, meta, nt, nl, s_f, sh, &is_last);
 }
 
 // ------------------------------------------------------------ persistent, TMA-fed variant
@@ -611,25 +632,28 @@ __device__ __forceinline__ void stage_chunk_bulk(const DevMesh &m, int c, const 
     if (nl) bulk_g2s(b.meta, m.lmeta + cd.z, 16u * nl, bar);
 }
 
-// What a chunk's pass needs from its instance's control block.
+// What a chunk's pass needs from its instance's control blocks.
 struct StreamCtx {
-    InstCtl *cp;
-    int k, nt, nl;
-    bool skip, check, do_h;
+    const InstCtl *src;
+    InstCtl *dst;
+    int inst, nt, nl;
+    bool first, skip;
+    PassView pv;
     size_t cur;
 };
 
 __device__ __forceinline__ StreamCtx stream_ctx(const DevMesh &m, const DevParams &p, const DevState &st, int c,
-                                                size_t cur) {
+                                                int par, size_t cur) {
     StreamCtx x;
     const int4 cd = m.chunk[c];
     x.nt = cd.y;
     x.nl = cd.w;
-    x.cp = st.ctl + m.chunk_inst[c];
-    x.skip = x.cp->done != 0;
-    x.k = x.cp->k;
-    x.check = (x.k % p.ls_every) == 0 || x.cp->force_check;
-    x.do_h = (x.k % p.hd_every) == 0;
+    x.inst = m.chunk_inst[c];
+    x.src = ctl_buf(st, par) + x.inst;
+    x.dst = ctl_buf(st, par ^ 1) + x.inst;
+    x.first = c == x.src->cblk_begin;
+    x.pv = pass_view(x.src, p);
+    x.skip = x.pv.skip;
     x.cur = cur;
     return x;
 }
@@ -683,12 +707,12 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
     // chunk 0: its records, then its node words
     bool ok = mbar_wait_bounded(&bar[0], 0u, STREAM_WAIT_NS);
     if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicExch(&st.ctl[m.chunk_inst[c0]].status, PBS_E_DEVICE_TIMEOUT);
+        if (threadIdx.x == 0) atomicExch(st.active + 1, 1);  // the instances stop with PBS_E_DEVICE_TIMEOUT
         if (nj > 1) mbar_wait_bounded(&bar[1], 0u, STREAM_WAIT_NS);
         return;
     }
     const size_t pcur = (size_t)par * m.Np;
-    cur = stream_ctx(m, p, st, c0, pcur);
+    cur = stream_ctx(m, p, st, c0, par, pcur);
     if (!cur.skip) stage_nodes<THREADS, INC>(st, stage_buf(smem4, 0, CT, CN, stride), cur.nl, cur.cur);
     cp_async_commit();
     for (int j = 0; j < nj; ++j) {
@@ -697,12 +721,12 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             // chunk j+1: wait for its records, start its node words
             ok = mbar_wait_bounded(&bar[b ^ 1], (unsigned)((j + 1) >> 1) & 1u, STREAM_WAIT_NS);
             if (__syncthreads_or(!ok)) {
-                if (threadIdx.x == 0) atomicExch(&st.ctl[m.chunk_inst[c + G]].status, PBS_E_DEVICE_TIMEOUT);
+                if (threadIdx.x == 0) atomicExch(st.active + 1, 1);
                 cp_async_wait_all();
                 mbar_wait_bounded(&bar[b ^ 1], (unsigned)((j + 1) >> 1) & 1u, STREAM_WAIT_NS);
                 return;
             }
-            nxt = stream_ctx(m, p, st, c + G, pcur);
+            nxt = stream_ctx(m, p, st, c + G, par, pcur);
             if (!nxt.skip) stage_nodes<THREADS, INC>(st, stage_buf(smem4, b ^ 1, CT, CN, stride), nxt.nl, nxt.cur);
             cp_async_commit();
             asm volatile("cp.async.wait_group 1;" ::: "memory");  // chunk j's node words (this thread's)
@@ -713,6 +737,7 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
         if (INC && !cur.skip)  // the increments of the nodes this thread staged
             for (int i = threadIdx.x; i < cur.nl; i += THREADS) sb.ul[i] = node_increment(sb.uh[i], sb.ul[i], sb.ub[i]);
         __syncthreads();
+        if (cur.first && cur.skip) settle_pass<THREADS>(p, st, cur.src, cur.dst, true);
         if (!cur.skip) {
             ChunkView v;
             v.uh = sb.uh;
@@ -724,8 +749,8 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             v.cor = sb.cor;
             v.meta = sb.meta;
             v.rest = m.rest;
-            chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cur.cp, cur.k, cur.check, cur.do_h, cur.cur, v, sb.meta,
-                                               cur.nt, cur.nl, s_f, sh, &is_last);
+            chunk_body<MATERIAL, THREADS, INC>(m, p, st, c, cur.inst, par, cur.pv, cur.cur, v, sb.meta, cur.nt,
+                                               cur.nl, s_f, sh, &is_last);
         }
         __syncthreads();  // buffer b and the slots are free again
         if (threadIdx.x == 0 && j + 2 < nj) stage_chunk_bulk(m, c + 2 * G, sb, &bar[b]);

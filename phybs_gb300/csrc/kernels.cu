@@ -16,10 +16,13 @@
 //           Chebyshev extrapolation (updateNodesNextIter + updateChebyshev,
 //           CUDAInterface.cu:572-623) in step form, d' = (omega-1) d +
 //           omega alpha delta, u' = u + d' in compensated FP32, or restores the
-//           saved state after a rejection.  |g|^2 is reduced in FP64; the last
-//           block runs the stopping / Chebyshev / iteration-count logic, so a
-//           step needs no host round trip (the reference syncs every 8
-//           iterations, CUDAInterface.cu:886-890).
+//           saved state after a rejection.  |g|^2 is summed per block; the
+//           stopping / Chebyshev / iteration-count logic on the FP64 total
+//           runs in the next pass's first chunk CTA while the other chunks
+//           already evaluate their tets (or in k_settle after a run of
+//           passes), so a step needs no host round trip (the reference syncs
+//           every 8 iterations, CUDAInterface.cu:886-890) and no pass waits
+//           on a one-CTA tail.
 #include "../../include/phybs.h"
 #include "node_update.cuh"
 #include "pass_ctl.cuh"
@@ -88,10 +91,11 @@ __global__ void k_set_lame(int Tp, const float *mu, const float *lambda, int cou
 }
 
 // ------------------------------------------------------------ step control
-__global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
+__global__ void k_init_ctl(int n_inst, DevParams p, DevState st) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_inst) return;
-    InstCtl c = ctl[b];
+    st.tcount[b] = 0;
+    InstCtl c = st.ctl[b];
     c.k = 0;
     c.iters = p.max_iters;
     c.done = (c.tet_end == c.tet_begin || p.max_iters <= 0) ? 1 : 0;
@@ -108,13 +112,16 @@ __global__ void k_init_ctl(int n_inst, DevParams p, InstCtl *ctl, int *active) {
     c.guess_bad = 0;
     c.counter_t = 0;
     c.counter_n = 0;
+    c.pending = 0;
+    c.void_pass = 0;
     c.alpha = p.alpha0;
     c.energy = 0.0;
     c.energy_old = 0.0;
     c.g0 = -1.0;
     c.r2 = -1.0;
-    ctl[b] = c;
-    if (!c.done) atomicAdd(active, 1);
+    st.ctl[b] = c;
+    st.ctl2[b] = c;  // an instance without chunks is never settled into it
+    if (!c.done) atomicAdd(st.active, 1);
 }
 
 __device__ __forceinline__ const InstCtl &node_ctl(const DevMesh &m, const DevState &st, int i) {
@@ -208,14 +215,14 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
 // grid-dependency wait, so no registers hold them across it.  With two nodes
 // a thread the kernel is held to 85 registers: six 128-thread CTAs fit an SM,
 // and the 1M-tet box's 823 node blocks run as one wave.  |g|^2 is summed in
-// FP32 within the block (256 positive terms: relative error < 1e-6) and in
-// FP64 over the blocks.
+// FP32 within the block (256 positive terms: relative error < 1e-6); the
+// pass decision on the block sums (FP64 over the blocks) is taken by the
+// next pass's tet kernel or by k_settle, so the kernel ends with its blocks
+// and no CTA waits for the instance's last one.
 template <int NPT>
 __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh m, DevParams p, DevState st, int par) {
     constexpr int TH = BLOCK / NPT;
     __shared__ float sh[TH / 32];
-    __shared__ float2 shf[TH / 32];
-    __shared__ int is_last;
     __shared__ __align__(16) float4 s_c[2][BLOCK];  // c hi (.w = M/h^2), c lo (.w = state) of the block's nodes
     const int b = blockIdx.x;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -247,20 +254,29 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
         in[j].dd = st.dd[cur + i];
         in[j].diag = st.diag[i];
     }
-    InstCtl *cp = st.ctl + inst;
-    // the control block the instance's last block decides on, fetched now with
-    // the state words instead of after the block reduction (no other block
-    // writes it during this kernel but for counter_n, which the decision resets)
-    __shared__ InstCtl s_ci;
-    if (threadIdx.x == 0) s_ci = *cp;
+    // the copy of the control block this pass's tet kernel settled
+    const InstCtl *cp = ctl_buf(st, par ^ 1) + inst;
     cp_async_wait_all();  // this thread's own constants
     if (cp->done) return;
+    const size_t nxt = (size_t)(1 - par) * m.Np;
+    if (cp->void_pass) {
+        // a forced energy check this pass did not make: the state goes on
+        // unchanged to the next pass, which makes it
+#pragma unroll
+        for (int j = 0; j < NPT; ++j) {
+            const int l = threadIdx.x + j * TH, i = b * BLOCK + l;
+            if (s_c[1][l].w == 2.f) continue;
+            st.uh[nxt + i] = in[j].uh;
+            st.ul[nxt + i] = in[j].ul;
+            st.dd[nxt + i] = in[j].dd;
+        }
+        return;
+    }
     const int k = cp->k;
     const bool check = (k % p.ls_every) == 0 || cp->force_check;
     const int action = check ? cp->action : ACT_STEP;
     const bool do_h = (k % p.hd_every) == 0;
-    const float rho_in = cp->rho, omega_in = cp->omega;
-    float rho = rho_in, omega = omega_in;
+    float rho = cp->rho, omega = cp->omega;
     chebyshev_schedule(p, k - cp->k_restart, rho, omega);
     PassCtx ctx;
     ctx.action = action;
@@ -268,7 +284,7 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
     ctx.alpha = cp->alpha;
     ctx.omega = omega;
     ctx.cur = cur;
-    ctx.nxt = (size_t)(1 - par) * m.Np;
+    ctx.nxt = nxt;
     float r2 = 0.f;
 #pragma unroll
     for (int j = 0; j < NPT; ++j) {
@@ -279,39 +295,15 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
         r2 += node_update<NPRE>(m, p, st, b * BLOCK + l, nc, in[j], fp[j], ctx);
     }
     const float sr = block_sum_f(r2, sh);
-    if (threadIdx.x == 0) {
-        st.npartf[b] = sr;
-        __threadfence();
-        const unsigned int prev = atomicAdd(&cp->counter_n, 1u);
-        is_last = (prev == (unsigned int)(cp->nblk_end - cp->nblk_begin - 1));
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    // the instance's last block: double-float sum of the block partials in a
-    // fixed order (FP32 pipe; GB300's FP64 pipe made this tail several us)
-    const int nb0 = cp->nblk_begin, nb1 = cp->nblk_end;
-    DFloat acc{0.f, 0.f};
-    // eight partials in flight a thread ahead of their additions (ascending
-    // order per thread, as one at a time would add them)
-    constexpr int U = 8;
-    for (int j0 = nb0 + threadIdx.x; j0 < nb1; j0 += U * TH) {
-        float v[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) v[u] = j0 + u * TH < nb1 ? __ldcg(st.npartf + j0 + u * TH) : 0.f;
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (j0 + u * TH < nb1) acc = df_add(acc, v[u]);
-    }
-    const double R2 = df_double(block_sum_df(acc, shf));
-    if (threadIdx.x != 0) return;
-    // the decision on the prefetched copy, stored back whole: every other block
-    // has read the control block, and the next kernel reads it only after its
-    // grid-dependency wait
-    InstCtl ci = s_ci;
-    decide_pass(ci, p, k, action, rho, omega, R2);
-    *cp = ci;
-    if (ci.done) atomicSub(st.active, 1);
+    if (threadIdx.x == 0) st.npartf[b] = sr;
+}
+
+// The pending pass decisions after the last pass of a run, one CTA an
+// instance; par: the parity the next pass would have (the copy they are in).
+// The result goes to st.ctl.
+__global__ void __launch_bounds__(BLOCK) k_settle(DevParams p, DevState st, int par) {
+    pdl_wait();
+    settle_pass<BLOCK>(p, st, ctl_buf(st, par) + blockIdx.x, st.ctl + blockIdx.x, false);
 }
 
 // Per-step node constant b = f_el(u_base) (incremental mode, double-float /
@@ -557,8 +549,8 @@ cudaError_t launch_set_lame(cudaStream_t s, int Tp, const int4 *, const float *m
     k_set_lame<<<nblk(Tp, 256), 256, 0, s>>>(Tp, mu, lambda, count, row1, row2, tet_user);
     return cudaGetLastError();
 }
-cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, InstCtl *ctl, int *active) {
-    k_init_ctl<<<nblk(n_inst, 128), 128, 0, s>>>(n_inst, p, ctl, active);
+cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, const DevState &st) {
+    k_init_ctl<<<nblk(n_inst, 128), 128, 0, s>>>(n_inst, p, st);
     return cudaGetLastError();
 }
 cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
@@ -581,6 +573,18 @@ static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevPara
 }
 cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
     return m.node_npt == 2 ? launch_node_t<2>(s, m, p, st, par, pdl) : launch_node_t<1>(s, m, p, st, par, pdl);
+}
+cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(m.n_inst);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_settle, p, st, par);
 }
 // One pass of the step graph: both kernels with programmatic dependent launch.
 cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par) {

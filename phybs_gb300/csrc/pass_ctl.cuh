@@ -1,13 +1,16 @@
 // The per-instance decisions of a descent pass, on a copy of the instance's
 // control block: the line-search accept / reject of a check pass and the
 // residual test, Chebyshev state, parity and caps after the node update.  The
-// graph path takes them in the last CTA of a pass kernel (chunks.cu,
-// kernels.cu); the persistent frame kernel (chunks.cu) takes them in every CTA
-// from the same sums, so every CTA's copy stays the same.
+// graph path takes the line search in the last CTA of the pass's tet kernel
+// and the pass decision in the first chunk CTA of the next pass's tet kernel
+// (settle_pass, chunks.cu) or in k_settle after the last pass of a run
+// (kernels.cu); the persistent frame kernel (chunks.cu) takes them in every
+// CTA from the same sums, so every CTA's copy stays the same.
 #pragma once
 #include <math.h>
 
 #include "../../include/phybs.h"
+#include "pass_math.cuh"
 #include "phybs_internal.cuh"
 
 namespace pbs {
@@ -98,6 +101,108 @@ __device__ __forceinline__ void decide_pass(InstCtl &ci, const DevParams &p, int
     ci.converged = converged;
     ci.status = status;
     ci.done = done;
+}
+
+// What a pass's tet kernel works from: the control block of its instance as
+// the last pass left it, whose pass decision may still be pending.  That
+// decision moves k on by one unless the last node update restored the saved
+// iterate (k is then redone) or the instance stops (this pass's work is then
+// unused: nothing reads it).  The one outcome the tet CTAs cannot foresee, a
+// residual that turned non-finite and forces an energy check at a k without
+// one, makes the pass void (settle_pass).
+struct PassView {
+    int k;
+    bool skip, check, do_h;
+};
+
+__device__ __forceinline__ PassView pass_view(const InstCtl *c, const DevParams &p) {
+    PassView v;
+    const int k = c->k, fc = c->force_check;
+    v.skip = c->done != 0;
+    if (c->pending) {
+        const int act = ((k % p.ls_every) == 0 || fc) ? c->action : ACT_STEP;
+        v.k = act == ACT_RESTORE ? k : k + 1;
+        v.check = (v.k % p.ls_every) == 0;
+    } else {
+        v.k = k;
+        v.check = (k % p.ls_every) == 0 || fc;
+    }
+    v.do_h = (v.k % p.hd_every) == 0;
+    return v;
+}
+
+// A control block read around L1: written by another CTA of the running
+// kernel.
+__device__ __forceinline__ InstCtl load_ctl_cg(const InstCtl *p) {
+    static_assert(sizeof(InstCtl) % 16 == 0, "InstCtl is read as 16-byte words");
+    InstCtl c;
+    const int4 *s = reinterpret_cast<const int4 *>(p);
+    int4 *d = reinterpret_cast<int4 *>(&c);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(InstCtl) / 16); ++i) d[i] = __ldcg(s + i);
+    return c;
+}
+
+// The pass decision of the instance's last node update, taken by one CTA from
+// the control block src into dst: |g|^2 summed in double-float from the node
+// blocks' partials (each thread its blocks in ascending order, then the block
+// tree), then decide_pass with the action, rho and omega that update used.
+// in_pass: the first chunk CTA of a pass that already runs on the outcome
+// (pass_view); dst is then the copy this pass's line search and node kernel
+// read, its decision pending again, and a forced energy check at a k without
+// one makes this pass void.  Otherwise (k_settle, after the last pass of a
+// run) the decision is left settled.  A device wait that gave up (active[1])
+// stops the instance with PBS_E_DEVICE_TIMEOUT.  Called by every thread.
+template <int THREADS>
+__device__ __forceinline__ void settle_pass(const DevParams &p, const DevState &st, const InstCtl *src,
+                                            InstCtl *dst, bool in_pass) {
+    __shared__ float2 shf[THREADS / 32];
+    const bool pend = src->pending && !src->done;
+    const int nb0 = src->nblk_begin, nb1 = src->nblk_end;
+    DFloat acc{0.f, 0.f};
+    if (pend) {
+        // eight partials in flight a thread ahead of their additions
+        constexpr int U = 8;
+        for (int j0 = nb0 + (int)threadIdx.x; j0 < nb1; j0 += U * THREADS) {
+            float v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = j0 + u * THREADS < nb1 ? __ldcg(st.npartf + j0 + u * THREADS) : 0.f;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (j0 + u * THREADS < nb1) acc = df_add(acc, v[u]);
+        }
+    }
+    // (its barriers also order every thread's reads of src before the store)
+    const DFloat R = block_sum_df(acc, shf);
+    if (threadIdx.x != 0) return;
+    InstCtl ci = *src;
+    const bool was_done = ci.done != 0;
+    if (!ci.done) {
+        if (ci.void_pass) {
+            // the void pass copied the state to the other parity
+            ci.void_pass = 0;
+            ci.par = 1 - ci.par;
+            ci.passes += 1;
+            if (ci.passes >= p.pass_cap) {
+                ci.done = 1;
+                ci.status = PBS_E_ITER_CAP;
+            }
+        } else if (ci.pending) {
+            const int k = ci.k;
+            const int action = ((k % p.ls_every) == 0 || ci.force_check) ? ci.action : ACT_STEP;
+            float rho = ci.rho, omega = ci.omega;
+            chebyshev_schedule(p, k - ci.k_restart, rho, omega);
+            decide_pass(ci, p, k, action, rho, omega, df_double(R));
+            if (in_pass && !ci.done && ci.force_check && (ci.k % p.ls_every) != 0) ci.void_pass = 1;
+        }
+        if (!ci.done && __ldcg(st.active + 1) != 0) {
+            ci.status = PBS_E_DEVICE_TIMEOUT;
+            ci.done = 1;
+        }
+    }
+    ci.pending = in_pass && !ci.done && !ci.void_pass;
+    *dst = ci;
+    if (ci.done && !was_done) atomicSub(st.active, 1);
 }
 
 }  // namespace pbs

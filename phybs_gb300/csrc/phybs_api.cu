@@ -108,8 +108,9 @@ struct pbs_handle {
     DevBuf<double2> tpart;
     DevBuf<double> npart;
     DevBuf<float> npartf;
-    DevBuf<InstCtl> ctl;
-    DevBuf<int> active;
+    DevBuf<InstCtl> ctl, ctl2;  // ctl2: the pass graph's second control-block copy
+    DevBuf<unsigned int> tcount;
+    DevBuf<int> active;  // [0] instances running, [1] a device wait gave up
     // strain-based PBD (levels built on first use) and projective dynamics
     // (its matrix built per (dt_matrix, stiffness)); dyn_* are their per-step
     // positions, start positions and right-hand-side base
@@ -165,6 +166,7 @@ struct pbs_handle {
         s.th = th.p; s.tl = tl.p; s.v = v.p; s.vold = vold.p; s.ext = ext.p; s.diag = diag.p;
         s.hist1 = hist1.p; s.hist2 = hist2.p; s.bh = bh.p; s.bl = bl.p; s.ub = ub.p; s.ch = ch.p; s.cl = cl.p;
         s.tf = tf.p; s.hd = hd.p; s.tpart = tpart.p; s.npart = npart.p; s.npartf = npartf.p; s.ctl = ctl.p; s.active = active.p;
+        s.ctl2 = ctl2.p; s.tcount = tcount.p;
         s.cpart = cpart.p; s.part = part.p; s.parth = parth.p; s.rslot = rslot.p;
         return s;
     }
@@ -185,7 +187,7 @@ struct pbs_handle {
         for (auto b : ci) b->release();
         DevBuf<float4> *cf[] = {&qrows, &part, &parth};
         for (auto b : cf) b->release();
-        tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release();
+        tf.release(); hd.release(); staging.release(); staging2.release(); tpart.release(); npart.release(); npartf.release(); ctl.release(); ctl2.release(); tcount.release();
         fsync.release(); fce.release(); fcr.release();
         faces_pad.release(); ring_pad.release(); pick_id.release(); pick_d2.release(); drag_ext.release();
         bsr_ptr.release(); bsr_col.release(); bsr_val.release(); cg_dinv.release(); cg_part.release(); cg_state.release();
@@ -521,7 +523,10 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk)); CKC(h->npartf.alloc(h->n_nblk));
-    CKC(h->ctl.alloc(B)); CKC(h->active.alloc(1));
+    CKC(h->ctl.alloc(B)); CKC(h->ctl2.alloc(B)); CKC(h->tcount.alloc(B)); CKC(h->active.alloc(2));
+    CKC(cudaMemsetAsync(h->ctl2.p, 0, sizeof(InstCtl) * B, h->stream));
+    CKC(cudaMemsetAsync(h->tcount.p, 0, sizeof(unsigned int) * B, h->stream));
+    CKC(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), h->stream));
     CKC(h->qrows.alloc(4 * (size_t)T)); CKC(h->rslot.alloc(12 * (size_t)T));
     h->qrow0 = h->qrows.p;
     h->qrow1 = h->qrows.p + (size_t)T;
@@ -667,6 +672,9 @@ static int ensure_graph(pbs_handle *h) {
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < CHUNK_PASSES && e == cudaSuccess; ++i)
         e = launch_pass(h->stream, m, h->dparams, st, h->material, i & 1);
+    // the last pass's decision, so that the host's poll and the next launch
+    // see settled control blocks
+    if (e == cudaSuccess) e = launch_settle(h->stream, m, h->dparams, st, CHUNK_PASSES & 1, true);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return PBS_E_CUDA; }
     e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -719,8 +727,8 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     DevState st = h->state();
     CK(cudaEventRecord(h->ev_start, s));
     if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
-    CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
+    CK(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s));
+    CK(launch_init_ctl(s, h->B, h->dparams, st));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     CK(launch_guess_check(s, m, h->dparams, st));
     CK(launch_ref_force(s, m, h->dparams, st));
@@ -881,8 +889,8 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
     DevMesh m = h->mesh();
     DevState st = h->state();
     if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(h->active.p, 0, sizeof(int), s));
-    CK(launch_init_ctl(s, h->B, h->dparams, h->ctl.p, h->active.p));
+    CK(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s));
+    CK(launch_init_ctl(s, h->B, h->dparams, st));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     DevBuf<float> out;
     CK(out.alloc(25 * (size_t)h->N));
@@ -933,8 +941,8 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     DevState st = h->state();
     std::vector<cudaEvent_t> ev(2 * passes + 1, nullptr);
     for (auto &e : ev) CK(cudaEventCreate(&e));
-    cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s);
+    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, st);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
@@ -945,6 +953,7 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
         if (e == cudaSuccess) e = launch_node_only(s, m, p, st, i & 1);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 2], s);
     }
+    if (e == cudaSuccess) e = launch_settle(s, m, p, st, passes & 1);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     double tt = 0.0, tn = 0.0;
     for (int i = 0; i < passes && e == cudaSuccess; ++i) {
@@ -988,8 +997,8 @@ static int time_frame(pbs_handle *h, int passes, double *pass_ms) {
     DevState st = h->state();
     cudaEvent_t ev[2] = {nullptr, nullptr};
     for (auto &e : ev) CK(cudaEventCreate(&e));
-    cudaError_t e = cudaMemsetAsync(h->active.p, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, h->ctl.p, h->active.p);
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s);
+    if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, st);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);

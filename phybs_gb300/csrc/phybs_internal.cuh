@@ -118,7 +118,12 @@ struct __align__(16) InstCtl {
     // static ranges (padded indices)
     int node_begin, node_end, tet_begin, tet_end;
     int tblk_begin, tblk_end, nblk_begin, nblk_end;
-    int cblk_begin, cblk_end, pad4, pad5;  // the instance's chunks
+    int cblk_begin, cblk_end;  // the instance's chunks
+    // graph path: the pass decision of the last node update is not taken yet
+    // (the next pass's first chunk or k_settle takes it); void_pass: this
+    // pass's node update copies the state unchanged (a residual that turned
+    // non-finite forces an energy check the pass's tet kernel did not make)
+    int pending, void_pass;
     double g1;                             // |g| at the learned candidate (extrapolation base)
     double pad6;
 };
@@ -172,9 +177,15 @@ struct DevState {
     float *npartf;
     float4 *part, *parth;
     double *rslot;  // 3 * 4T: FP64 corner forces at the base, by gather slot
-    InstCtl *ctl;
-    int *active;  // instances not yet done
+    InstCtl *ctl;   // the control blocks between passes (and between steps)
+    InstCtl *ctl2;  // the graph path's second copy: a pass reads one and writes the other
+    unsigned int *tcount;  // per instance: the chunks of a line-search pass that finished
+    int *active;  // [0] instances not yet done, [1] a device wait gave up (sticky for the step)
 };
+
+// The control-block copy a pass with parity q reads (its tet kernel) or, with
+// q ^ 1, the one its decisions go to and its node kernel reads.
+__device__ __forceinline__ InstCtl *ctl_buf(const DevState &st, int q) { return q ? st.ctl2 : st.ctl; }
 
 // Chebyshev omega for iteration k from the persistent (rho, omega), as
 // DescentOptimize.cpp:156-175 / CUDAInterface.cu:967-986 compute it in FP32.
@@ -266,7 +277,9 @@ cudaError_t launch_mass(cudaStream_t s, const DevMesh &m, const double *tmass, c
                         float4 *info);
 cudaError_t launch_set_lame(cudaStream_t s, int Tp, const int4 *tets, const float *mu, const float *lambda, int count,
                             float4 *row1, float4 *row2, const int *tet_user);
-cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, InstCtl *ctl, int *active);
+// Resets the control blocks (both copies), the running count and the
+// line-search counters for a step.
+cudaError_t launch_init_ctl(cudaStream_t s, int n_inst, const DevParams &p, const DevState &st);
 cudaError_t launch_prologue(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *ext_user,
                             const int *pad2user);
 // par: the pass's parity, the state buffer (0 or 1) it reads.  A step starts
@@ -278,6 +291,11 @@ cudaError_t launch_tet_only(cudaStream_t s, const DevMesh &m, const DevParams &p
                             bool pdl = false);
 cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par,
                              bool pdl = false);
+// Takes the pending pass decisions after a run of passes whose next parity is
+// par (the copy they are in), leaving them in st.ctl.  A run of passes must
+// end with it before anything else reads the control blocks.
+cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par,
+                          bool pdl = false);
 // RESTART control: replaces an instance's inertial guess by the step's start
 // positions when the guess inverts a tet (kernels.cu)
 cudaError_t launch_guess_check(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);

@@ -122,6 +122,32 @@ def test_frame_engine_line_search_rejections():
     b.close()
 
 
+def test_frame_engine_nonfinite_recovery():
+    """alpha0 = 3 inverts tets within a few passes: the residual turns
+    non-finite before a scheduled energy check and RESTART control forces one.
+    The graph path learns of it only in the next pass's tet kernel, which
+    already runs on the foreseen iteration: that pass is void (the state is
+    carried over) and the check follows; the frame kernel checks at once.
+    Both take the same rejections and iterations and land on the same
+    positions; the graph path spends one pass more a forced check."""
+    m = M.bar_mesh(8, 4, 4, edge=0.025, young=5e4, poisson=0.4)
+    p = make_params("gpu_reference", h=1 / 30, max_iters=20000, tol=1e-4, control=L.PBS_CONTROL_RESTART,
+                    alpha0=3.0, energy_slack=16.0, profile=((10, 0.995),))
+    a, b = _pair(m, p, shape=(128, 64, 64, 0, 1))
+    diag = bbox_diag(m.rest)
+    a.step()
+    b.step()
+    sa, sb = a.stats(), b.stats()
+    assert sa["status"] == sb["status"] == 0 and sa["converged"] == sb["converged"] == 1, (sa, sb)
+    assert sa["rejections"] == sb["rejections"] >= 1, (sa["rejections"], sb["rejections"])
+    assert abs(sa["iterations"] - sb["iterations"]) <= 2, (sa["iterations"], sb["iterations"])
+    assert sb["passes"] <= sa["passes"] <= sb["passes"] + sa["rejections"] + 2, (sa["passes"], sb["passes"])
+    assert np.abs(a.positions() - b.positions()).max() < 1e-4 * diag
+    print(f"passes graph {sa['passes']} frame {sb['passes']}, rejections {sa['rejections']}")
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("arm", ["plain", "warm"])
 def test_frame_engine_benchmark_settings(arm):
     """The benchmark's solver settings on its box at 1/5 resolution (8,000
