@@ -227,9 +227,11 @@ __device__ __forceinline__ void corner_words(const ChunkView &v, const int lc[4]
 
 // A near-inverted tet (full stress) gets its FP32 forces here and a mark in
 // its corner-0 slot's .w; *any_exact tells whether the thread marked one.
-template <int MATERIAL, int THREADS, bool INC>
-__device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, bool check,
-                                               float4 *sf, bool *any_exact) {
+// CHECK: a line-search pass (the tet energies too); the loop is compiled once
+// with and once without them.
+template <int MATERIAL, int THREADS, bool INC, bool CHECK>
+__device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkView &v, int nt, float4 *sf,
+                                               bool *any_exact) {
     DFloat e{0.f, 0.f};
     bool any = false;
     for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
@@ -241,14 +243,14 @@ __device__ __forceinline__ DFloat chunk_forces(const DevParams &p, const ChunkVi
         float f[12];
         float4 x[4], l[4], a[4];
         corner_words<INC>(v, lc, x, l, a);
-        const bool ex = pass_forces_c<MATERIAL, INC, true>(x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0],
-                                                           a[1], a[2], a[3], dinv, r0.w, r1.w, r2.w, kin, f,
-                                                           CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
+        const bool ex = pass_forces_c<MATERIAL, INC, true, CHECK>(
+            x[0], x[1], x[2], x[3], l[0], l[1], l[2], l[3], a[0], a[1], a[2], a[3], dinv, r0.w, r1.w, r2.w, kin, f,
+            CornerRest{v.rest, v.meta, {lc[0], lc[1], lc[2], lc[3]}});
         any |= ex;
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc)
             sts128(sf + sl[cc], f[3 * cc], f[3 * cc + 1], f[3 * cc + 2], cc == 0 && ex ? 1.f : 0.f);
-        if (check)
+        if (CHECK)
             e = df_add(e, search_energy(energy_density<float>(kin, r1.w, r2.w) * fabsf(r0.w), p.clamp_cpu,
                                         p.control == PBS_CONTROL_RESTART));
     }
@@ -284,7 +286,8 @@ template <int MATERIAL, int THREADS, bool INC>
 __device__ __forceinline__ DFloat chunk_forces_all(const DevParams &p, const ChunkView &v, int nt, bool check,
                                                    float4 *sf) {
     bool ex;
-    const DFloat e = chunk_forces<MATERIAL, THREADS, INC>(p, v, nt, check, sf, &ex);
+    const DFloat e = check ? chunk_forces<MATERIAL, THREADS, INC, true>(p, v, nt, sf, &ex)
+                           : chunk_forces<MATERIAL, THREADS, INC, false>(p, v, nt, sf, &ex);
     if (INC) {
         __syncthreads();
     } else if (__syncthreads_or(ex)) {

@@ -171,8 +171,10 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 // unused; without INC, a is unused.  cr locates the corners' rest positions
 // for the FP64 stress of a near-inverted tet (full stress only).  DEFER:
 // leave that stress out (f is then not the tet's) and return whether the tet
-// needs it, for a caller that forms it after its loop.
-template <int MATERIAL, bool INC, bool DEFER = false>
+// needs it, for a caller that forms it after its loop.  KIN = false: with
+// INC, kin holds only d and lnJ (a pass that needs neither the energy nor the
+// Jacobi diagonal; a loop without them also needs fewer registers).
+template <int MATERIAL, bool INC, bool DEFER = false, bool KIN = true>
 __device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1, const float4 &x2, const float4 &x3,
                                               const float4 &l0, const float4 &l1, const float4 &l2, const float4 &l3,
                                               const float4 &a0, const float4 &a1, const float4 &a2, const float4 &a3,
@@ -186,7 +188,7 @@ __device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1
         kinematics(k0);
         float dG[9];
         disp_gradient<float>(l0, l1, l2, l3, dinv, dG);
-        pk1_neohookean_inc(k0, dG, mu, lambda, kin, P);
+        pk1_neohookean_inc<KIN>(k0, dG, mu, lambda, kin, P);
     } else {
         // Du = (u_j,hi - u_0,hi) + (u_j,lo - u_0,lo)
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);

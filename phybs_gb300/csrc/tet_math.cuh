@@ -130,61 +130,88 @@ template <typename T> __device__ __forceinline__ void pk1_neohookean(const Kin<T
         }
 }
 
+// log1p(x) of a volume increment.  For |x| < 1/32 its Taylor series
+// x - x^2/2 + x^3/3 - ... to the x^6 term by Horner's rule (the first term
+// left out is below 2^-26 |x| there: a few FP32 ulp in all); otherwise log1pf.
+// The increments of a descent pass against its step's base are almost always
+// in the series' range.
+__device__ __forceinline__ float log1p_increment(float x) {
+    if (fabsf(x) < 0.03125f) {
+        float s = -1.0f / 6.0f;
+        s = fmaf(x, s, 0.2f);
+        s = fmaf(x, s, -0.25f);
+        s = fmaf(x, s, 1.0f / 3.0f);
+        s = fmaf(x, s, -0.5f);
+        s = fmaf(x, s, 1.0f);
+        return x * s;
+    }
+    return log1pf(x);
+}
+
 // dP = P(F0 + dG) - P(F0) of the neo-Hookean stress, from the base kinematics
-// k0 (the step's start, with ln J0) and the increment dG.  With P = mu F +
-// (lambda ln J - mu) F^-T:
-//   dP = mu dG - (lambda ln J - mu) F0^-T dG^T F^-T + lambda (ln J - ln J0) F0^-T
-// (F^-T - F0^-T = -F0^-T dF^T F^-T), ln J - ln J0 = log1p(dJ / J0) and
-//   dJ = cof(F0) : dG + F0 : cof(dG) + det dG
-// -- no term subtracts the two states' O(1) quantities, so dP is accurate to
-// FP32 relative to itself rather than to P.  The scale factors 1/J0 and 1/J
-// multiply only O(|dG|) terms and use the fast reciprocal (a few ulp).
-// Also returns the current kinematics k: G = G0 + dG, det F - 1 = d0 + dJ and
-// ln J = ln J0 + log1p(dJ / J0).
+// k0 (the step's start, with ln J0) and the increment dG.  With
+// P = mu F + (lambda ln J - mu) F^-T:
+//   dP = mu dG + (lambda ln J - mu) (F^-T - F0^-T) + lambda (ln J - ln J0) F0^-T
+// where, with cof(F) = cof(F0) + L(F0, dG) + cof(dG) (L: the part of the
+// cofactor bilinear in F0 and dG) and dJ = cof(F0) : dG + F0 : cof(dG) +
+// det dG,
+//   F^-T - F0^-T = (L(F0, dG) + cof(dG) - F0^-T dJ) / J
+// and ln J - ln J0 = log1p(dJ / J0) -- no term subtracts the two states'
+// O(1) quantities, so dP is accurate to FP32 relative to itself rather than
+// to P.  The scale factors 1/J0 and 1/J multiply only O(|dG|) terms and use
+// the fast reciprocal (a few ulp).  Returns in k the current det F - 1 =
+// d0 + dJ and ln J = ln J0 + log1p(dJ / J0), and with FULL_KIN the rest of
+// the current kinematics (G = G0 + dG, its cofactor and invariants: the
+// energy and the Jacobi diagonal need them, the forces do not).
+template <bool FULL_KIN>
 __device__ __forceinline__ void pk1_neohookean_inc(const Kin<float> &k0, const float dG[9], float mu, float lambda,
                                                    Kin<float> &k, float dP[9]) {
-    float F0iT[9], FiT[9], cofdG[9];
+    float F0iT[9];
     const float rJ0 = __fdividef(1.0f, 1.0f + k0.d);
-    cofactor3<float>(dG, cofdG);
-    float dJ = dG[0] * cofdG[0] + dG[1] * cofdG[1] + dG[2] * cofdG[2];  // det dG
+    // F0 = I + G0 and cof(F0) = (1 + tr G0) I - G0^T + cof(G0), entry by entry
+    auto F0 = [&](int r, int c) { return ((r == c) ? 1.0f : 0.0f) + k0.G[3 * r + c]; };
+    float dJ = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
+            const int c = (j + 1) % 3, d = (j + 2) % 3;
+            const float cofdG = dG[3 * a + c] * dG[3 * b + d] - dG[3 * a + d] * dG[3 * b + c];
             const float cof0 = ((i == j) ? 1.0f + k0.tr : 0.0f) - k0.G[3 * j + i] + k0.cofG[3 * i + j];
-            const float F0 = ((i == j) ? 1.0f : 0.0f) + k0.G[3 * i + j];
-            dJ += cof0 * dG[3 * i + j] + F0 * cofdG[3 * i + j];
+            // dJ = cof(F0) : dG + F0 : cof(dG) + det dG (det dG = dG row 0 . cof(dG) row 0)
+            dJ += cof0 * dG[3 * i + j] + (F0(i, j) + ((i == 0) ? dG[j] : 0.0f)) * cofdG;
             F0iT[3 * i + j] = cof0 * rJ0;
         }
-    const float dl = log1pf(dJ * rJ0);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
-    cofactor3<float>(k.G, k.cofG);
-    k.tr = k.G[0] + k.G[4] + k.G[8];
-    k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
-    k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+    }
+    const float dl = log1p_increment(dJ * rJ0);
     k.d = k0.d + dJ;
     k.lnJ = k0.lnJ + dl;
     const float rJ = __fdividef(1.0f, 1.0f + k.d);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            FiT[3 * i + j] = ((i == j ? 1.0f + k.tr : 0.0f) - k.G[3 * j + i] + k.cofG[3 * i + j]) * rJ;
-    // M = F0^-T dG^T F^-T
-    float A[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) A[3 * i + j] = F0iT[3 * i] * dG[3 * j] + F0iT[3 * i + 1] * dG[3 * j + 1] + F0iT[3 * i + 2] * dG[3 * j + 2];
     const float c1 = lambda * k.lnJ - mu, c2 = lambda * dl;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+        const int a = (i + 1) % 3, b = (i + 2) % 3;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float M = A[3 * i] * FiT[j] + A[3 * i + 1] * FiT[3 + j] + A[3 * i + 2] * FiT[6 + j];
-            dP[3 * i + j] = mu * dG[3 * i + j] - c1 * M + c2 * F0iT[3 * i + j];
+            const int c = (j + 1) % 3, d = (j + 2) % 3;
+            // cof(F)_ij - cof(F0)_ij = L(F0, dG)_ij + cof(dG)_ij
+            //   = F_ac dG_bd + dG_ac F0_bd - F_ad dG_bc - dG_ad F0_bc  (F = F0 + dG)
+            const float Fac = F0(a, c) + dG[3 * a + c], Fad = F0(a, d) + dG[3 * a + d];
+            const float dcof = Fac * dG[3 * b + d] + dG[3 * a + c] * F0(b, d) - Fad * dG[3 * b + c] -
+                               dG[3 * a + d] * F0(b, c);
+            const float t = (dcof - F0iT[3 * i + j] * dJ) * rJ;  // F^-T - F0^-T
+            dP[3 * i + j] = mu * dG[3 * i + j] + c1 * t + c2 * F0iT[3 * i + j];
         }
+    }
+    if (FULL_KIN) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) k.G[i] = k0.G[i] + dG[i];
+        cofactor3<float>(k.G, k.cofG);
+        k.tr = k.G[0] + k.G[4] + k.G[8];
+        k.c2 = k.cofG[0] + k.cofG[4] + k.cofG[8];
+        k.c3 = k.G[0] * k.cofG[0] + k.G[1] * k.cofG[1] + k.G[2] * k.cofG[2];
+    }
 }
 
 // phi(d) = d - log1p(d) >= 0, by its Taylor series where that is exact to FP32.
