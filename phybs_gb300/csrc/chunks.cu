@@ -212,7 +212,8 @@ struct ChunkView {
 // returns the thread's sum of clamped tet energies.
 // The node words of a tet's four corners from the chunk's shared-memory
 // staging (one 128-bit access each): x = u hi (full stress) or nothing (the
-// incremental form), l = u lo or the increment, a = the base (incremental).
+// incremental form), l = u lo or the increment relative to the chunk's
+// reference node, a = the base (incremental).
 template <bool INC>
 __device__ __forceinline__ void corner_words(const ChunkView &v, const int lc[4], float4 x[4], float4 l[4],
                                              float4 a[4]) {
@@ -470,6 +471,8 @@ __global__ void __launch_bounds__(THREADS,
     const int4 cd = m.chunk[c];
     const int inst = m.chunk_inst[c];
     const int tq0 = cd.x, nt = cd.y, l0 = cd.z, nl = cd.w;
+    // the chunk's reference node for the increments (incremental form)
+    const int g_ref = INC && !STAGE ? m.lmeta[l0].x : 0;
     if (STAGE) {
         for (int lt = threadIdx.x; lt < nt; lt += THREADS) {
             const int q = tq0 + lt;
@@ -510,15 +513,26 @@ __global__ void __launch_bounds__(THREADS,
     }
     if (STAGE) {
         cp_async_wait_all();
-        if (INC)  // the increments of the nodes this thread staged
-            for (int j = threadIdx.x; j < nl; j += THREADS) s_ul[j] = node_increment(s_uh[j], s_ul[j], s_ub[j]);
+        if (INC) {
+            // the increments of the nodes this thread staged, relative to the
+            // chunk's local node 0 (staged by thread 0)
+            __syncthreads();
+            float4 rh, rl;
+            node_increment(s_uh[0], s_ul[0], s_ub[0], rh, rl);
+            __syncthreads();
+            for (int j = threadIdx.x; j < nl; j += THREADS)
+                s_ul[j] = node_increment_rel(s_uh[j], s_ul[j], s_ub[j], rh, rl);
+        }
     } else {
+        // (the increments relative to the chunk's local node 0)
+        float4 rh, rl;
+        if (INC) node_increment(st.uh[cur + g_ref], st.ul[cur + g_ref], st.ub[g_ref], rh, rl);
         for (int j = threadIdx.x; j < nl; j += THREADS) {
             const int g = meta[j].x;
             const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
             if (INC) {
                 const float4 ub = st.ub[g];
-                s_ul[j] = node_increment(uh, ul, ub);
+                s_ul[j] = node_increment_rel(uh, ul, ub, rh, rl);
                 s_ub[j] = ub;
             } else {
                 s_uh[j] = uh;
@@ -737,8 +751,16 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             cp_async_wait_all();
         }
         const StageBuf sb = stage_buf(smem4, b, CT, CN, stride);
-        if (INC && !cur.skip)  // the increments of the nodes this thread staged
-            for (int i = threadIdx.x; i < cur.nl; i += THREADS) sb.ul[i] = node_increment(sb.uh[i], sb.ul[i], sb.ub[i]);
+        if (INC && !cur.skip) {
+            // the increments of the nodes this thread staged, relative to the
+            // chunk's local node 0 (staged by thread 0)
+            __syncthreads();
+            float4 rh, rl;
+            node_increment(sb.uh[0], sb.ul[0], sb.ub[0], rh, rl);
+            __syncthreads();
+            for (int i = threadIdx.x; i < cur.nl; i += THREADS)
+                sb.ul[i] = node_increment_rel(sb.uh[i], sb.ul[i], sb.ub[i], rh, rl);
+        }
         __syncthreads();
         if (cur.first && cur.skip) settle_pass<THREADS>(p, st, cur.src, cur.dst, true);
         if (!cur.skip) {
@@ -1033,12 +1055,18 @@ __global__ void __launch_bounds__(THREADS,
             const int4 cd = m.chunk[c];
             const int nt = cd.y, nl = cd.w;
             const int4 *meta = m.lmeta + cd.z;
+            // (the increments relative to the chunk's local node 0)
+            float4 rh, rl;
+            if (INC) {
+                const int g0 = meta[0].x;
+                node_increment(st.uh[cur + g0], st.ul[cur + g0], st.ub[g0], rh, rl);
+            }
             for (int j = threadIdx.x; j < nl; j += THREADS) {
                 const int g = meta[j].x;
                 const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
                 if (INC) {
                     const float4 ub = st.ub[g];
-                    s_ul[j] = node_increment(uh, ul, ub);
+                    s_ul[j] = node_increment_rel(uh, ul, ub, rh, rl);
                     s_ub[j] = ub;
                 } else {
                     s_uh[j] = uh;

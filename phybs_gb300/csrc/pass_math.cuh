@@ -167,8 +167,9 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 
 // Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
 // INC (compile time): the incremental neo-Hookean form, where l carries the
-// corner's increment w = (u hi - base) + u lo (formed once per node) and x is
-// unused; without INC, a is unused.  cr locates the corners' rest positions
+// corner's increment u - base less a reference increment common to the tet
+// (node_increment_rel, formed once per node) and x is unused; without INC, a
+// is unused.  cr locates the corners' rest positions
 // for the FP64 stress of a near-inverted tet (full stress only).  DEFER:
 // leave that stress out (f is then not the tet's) and return whether the tet
 // needs it, for a caller that forms it after its loop.  KIN = false: with
@@ -211,9 +212,37 @@ __device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1
     return exact;
 }
 
-// The increment of a node for the incremental form: (u hi - base) + u lo.
-__device__ __forceinline__ float4 node_increment(const float4 &uh, const float4 &ul, const float4 &ub) {
-    return f4add(f4sub(uh, ub), ul);
+// The increment u - base of a node for the incremental form, as a pair: hi =
+// fl(u hi - base), lo = that subtraction's rounding error (TwoSum) + u lo.
+__device__ __forceinline__ void node_increment(const float4 &uh, const float4 &ul, const float4 &ub, float4 &wh,
+                                               float4 &wl) {
+    float e;
+    two_sum(uh.x, -ub.x, wh.x, e);
+    wl.x = __fadd_rn(e, ul.x);
+    two_sum(uh.y, -ub.y, wh.y, e);
+    wl.y = __fadd_rn(e, ul.y);
+    two_sum(uh.z, -ub.z, wh.z, e);
+    wl.z = __fadd_rn(e, ul.z);
+    wh.w = 0.f;
+    wl.w = 0.f;
+}
+
+// The increment of a node less a reference increment (rh, rl) (a node of
+// the same chunk, or the tet's corner 0), rounded once: the tets evaluate
+// only differences of increments, which the common part leaves unchanged.
+// An increment that is large and nearly the same across a chunk (a soft
+// body that moves far in one frame) then no longer rounds away the small
+// differences dG is made of; one rounded FP32 increment a node lost them,
+// and the residual of such frames stalled near 1.5e-4 of its initial value.
+// hi - rh is exact wherever the two are within a factor 2 of each other,
+// which is where the cancellation was.
+__device__ __forceinline__ float4 node_increment_rel(const float4 &uh, const float4 &ul, const float4 &ub,
+                                                     const float4 &rh, const float4 &rl) {
+    float4 wh, wl;
+    node_increment(uh, ul, ub, wh, wl);
+    return make_float4(__fadd_rn(__fsub_rn(wh.x, rh.x), __fsub_rn(wl.x, rl.x)),
+                       __fadd_rn(__fsub_rn(wh.y, rh.y), __fsub_rn(wl.y, rl.y)),
+                       __fadd_rn(__fsub_rn(wh.z, rh.z), __fsub_rn(wl.z, rl.z)), 0.f);
 }
 
 template <int MATERIAL>
@@ -241,10 +270,15 @@ __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U,
     const float4 x0 = U[q.x], x1 = U[q.y], x2 = U[q.z], x3 = U[q.w];
     const float4 l0 = UL[q.x], l1 = UL[q.y], l2 = UL[q.z], l3 = UL[q.w];
     const float4 a0 = inc ? U0[q.x] : z, a1 = inc ? U0[q.y] : z, a2 = inc ? U0[q.z] : z, a3 = inc ? U0[q.w] : z;
-    if (inc)
-        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment(x0, l0, a0), node_increment(x1, l1, a1),
-                                node_increment(x2, l2, a2), node_increment(x3, l3, a3), a0, a1, a2, a3, dinv, svol,
-                                mu, lambda, kin, f, cr);
+    if (inc) {
+        // increments relative to corner 0's
+        float4 rh, rl;
+        node_increment(x0, l0, a0, rh, rl);
+        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment_rel(x0, l0, a0, rh, rl),
+                                node_increment_rel(x1, l1, a1, rh, rl), node_increment_rel(x2, l2, a2, rh, rl),
+                                node_increment_rel(x3, l3, a3, rh, rl), a0, a1, a2, a3, dinv, svol, mu, lambda, kin,
+                                f, cr);
+    }
     else
         pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f,
                                 cr);
