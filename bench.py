@@ -182,10 +182,12 @@ def ncu_traffic(tune, stress):
     with open(p) as f:
         entries = json.load(f).get("entries", [])
     shape = [tune["chunk_threads"], tune["chunk_tets"], tune["chunk_nodes"], tune["chunk_staged"]]
-    for e in entries:
-        if e.get("shape", [])[:4] == shape and e.get("stress") == stress:
+    full = shape + [tune.get("node_npt")]
+    same = [e for e in entries if e.get("shape", [])[:4] == shape and e.get("stress") == stress]
+    for e in same:  # the capture of this very shape first, then one of the same chunk shape
+        if e.get("shape") == full:
             return e
-    return None
+    return same[0] if same else None
 
 
 class CpuFrames:
