@@ -517,22 +517,20 @@ __global__ void __launch_bounds__(THREADS,
             // the increments of the nodes this thread staged, relative to the
             // chunk's local node 0 (staged by thread 0)
             __syncthreads();
-            float4 rh, rl;
-            node_increment(s_uh[0], s_ul[0], s_ub[0], rh, rl);
+            const float4 r = increment_ref(s_uh[0], s_ub[0]);
             __syncthreads();
-            for (int j = threadIdx.x; j < nl; j += THREADS)
-                s_ul[j] = node_increment_rel(s_uh[j], s_ul[j], s_ub[j], rh, rl);
+            for (int j = threadIdx.x; j < nl; j += THREADS) s_ul[j] = node_increment_rel(s_uh[j], s_ul[j], s_ub[j], r);
         }
     } else {
         // (the increments relative to the chunk's local node 0)
-        float4 rh, rl;
-        if (INC) node_increment(st.uh[cur + g_ref], st.ul[cur + g_ref], st.ub[g_ref], rh, rl);
+        float4 r;
+        if (INC) r = increment_ref(st.uh[cur + g_ref], st.ub[g_ref]);
         for (int j = threadIdx.x; j < nl; j += THREADS) {
             const int g = meta[j].x;
             const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
             if (INC) {
                 const float4 ub = st.ub[g];
-                s_ul[j] = node_increment_rel(uh, ul, ub, rh, rl);
+                s_ul[j] = node_increment_rel(uh, ul, ub, r);
                 s_ub[j] = ub;
             } else {
                 s_uh[j] = uh;
@@ -755,11 +753,10 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             // the increments of the nodes this thread staged, relative to the
             // chunk's local node 0 (staged by thread 0)
             __syncthreads();
-            float4 rh, rl;
-            node_increment(sb.uh[0], sb.ul[0], sb.ub[0], rh, rl);
+            const float4 r = increment_ref(sb.uh[0], sb.ub[0]);
             __syncthreads();
             for (int i = threadIdx.x; i < cur.nl; i += THREADS)
-                sb.ul[i] = node_increment_rel(sb.uh[i], sb.ul[i], sb.ub[i], rh, rl);
+                sb.ul[i] = node_increment_rel(sb.uh[i], sb.ul[i], sb.ub[i], r);
         }
         __syncthreads();
         if (cur.first && cur.skip) settle_pass<THREADS>(p, st, cur.src, cur.dst, true);
@@ -1056,17 +1053,17 @@ __global__ void __launch_bounds__(THREADS,
             const int nt = cd.y, nl = cd.w;
             const int4 *meta = m.lmeta + cd.z;
             // (the increments relative to the chunk's local node 0)
-            float4 rh, rl;
+            float4 r;
             if (INC) {
                 const int g0 = meta[0].x;
-                node_increment(st.uh[cur + g0], st.ul[cur + g0], st.ub[g0], rh, rl);
+                r = increment_ref(st.uh[cur + g0], st.ub[g0]);
             }
             for (int j = threadIdx.x; j < nl; j += THREADS) {
                 const int g = meta[j].x;
                 const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
                 if (INC) {
                     const float4 ub = st.ub[g];
-                    s_ul[j] = node_increment_rel(uh, ul, ub, rh, rl);
+                    s_ul[j] = node_increment_rel(uh, ul, ub, r);
                     s_ub[j] = ub;
                 } else {
                     s_uh[j] = uh;

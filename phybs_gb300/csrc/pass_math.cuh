@@ -212,37 +212,33 @@ __device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1
     return exact;
 }
 
-// The increment u - base of a node for the incremental form, as a pair: hi =
-// fl(u hi - base), lo = that subtraction's rounding error (TwoSum) + u lo.
-__device__ __forceinline__ void node_increment(const float4 &uh, const float4 &ul, const float4 &ub, float4 &wh,
-                                               float4 &wl) {
-    float e;
-    two_sum(uh.x, -ub.x, wh.x, e);
-    wl.x = __fadd_rn(e, ul.x);
-    two_sum(uh.y, -ub.y, wh.y, e);
-    wl.y = __fadd_rn(e, ul.y);
-    two_sum(uh.z, -ub.z, wh.z, e);
-    wl.z = __fadd_rn(e, ul.z);
-    wh.w = 0.f;
-    wl.w = 0.f;
+// A reference for node_increment_rel: fl(u hi - base) of one node (a chunk's
+// local node 0, or a tet's corner 0).  Its rounding does not matter: any
+// constant common to the nodes would do.
+__device__ __forceinline__ float4 increment_ref(const float4 &uh, const float4 &ub) {
+    return make_float4(__fsub_rn(uh.x, ub.x), __fsub_rn(uh.y, ub.y), __fsub_rn(uh.z, ub.z), 0.f);
 }
 
-// The increment of a node less a reference increment (rh, rl) (a node of
-// the same chunk, or the tet's corner 0), rounded once: the tets evaluate
-// only differences of increments, which the common part leaves unchanged.
-// An increment that is large and nearly the same across a chunk (a soft
-// body that moves far in one frame) then no longer rounds away the small
-// differences dG is made of; one rounded FP32 increment a node lost them,
-// and the residual of such frames stalled near 1.5e-4 of its initial value.
-// hi - rh is exact wherever the two are within a factor 2 of each other,
-// which is where the cancellation was.
+// One component: (s - r) + (e + lo), s + e = hi - base exactly (TwoSum).
+__device__ __forceinline__ float increment_rel1(float hi, float lo, float base, float r) {
+    float s, e;
+    two_sum(hi, -base, s, e);
+    return __fadd_rn(__fsub_rn(s, r), __fadd_rn(e, lo));
+}
+
+// The increment u - base = (u hi - base) + u lo of a node, less a reference
+// r common to the nodes that are differenced together (increment_ref), and
+// rounded once.  The tets evaluate only differences of increments, which r
+// leaves unchanged.  An increment that is large and nearly the same across a
+// chunk (a soft body that moves far in one frame) then keeps the small
+// differences dG is made of: u hi - base is split exactly into s + e, and
+// s - r is exact wherever the two are within a factor 2 of each other, which
+// is where the cancellation is.  With one rounded FP32 increment a node the
+// residual of such frames stalled near 1.5e-4 of its initial value.
 __device__ __forceinline__ float4 node_increment_rel(const float4 &uh, const float4 &ul, const float4 &ub,
-                                                     const float4 &rh, const float4 &rl) {
-    float4 wh, wl;
-    node_increment(uh, ul, ub, wh, wl);
-    return make_float4(__fadd_rn(__fsub_rn(wh.x, rh.x), __fsub_rn(wl.x, rl.x)),
-                       __fadd_rn(__fsub_rn(wh.y, rh.y), __fsub_rn(wl.y, rl.y)),
-                       __fadd_rn(__fsub_rn(wh.z, rh.z), __fsub_rn(wl.z, rl.z)), 0.f);
+                                                     const float4 &r) {
+    return make_float4(increment_rel1(uh.x, ul.x, ub.x, r.x), increment_rel1(uh.y, ul.y, ub.y, r.y),
+                       increment_rel1(uh.z, ul.z, ub.z, r.z), 0.f);
 }
 
 template <int MATERIAL>
@@ -272,12 +268,10 @@ __device__ __forceinline__ void pass_forces(const DevParams &p, const float4 *U,
     const float4 a0 = inc ? U0[q.x] : z, a1 = inc ? U0[q.y] : z, a2 = inc ? U0[q.z] : z, a3 = inc ? U0[q.w] : z;
     if (inc) {
         // increments relative to corner 0's
-        float4 rh, rl;
-        node_increment(x0, l0, a0, rh, rl);
-        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment_rel(x0, l0, a0, rh, rl),
-                                node_increment_rel(x1, l1, a1, rh, rl), node_increment_rel(x2, l2, a2, rh, rl),
-                                node_increment_rel(x3, l3, a3, rh, rl), a0, a1, a2, a3, dinv, svol, mu, lambda, kin,
-                                f, cr);
+        const float4 r = increment_ref(x0, a0);
+        pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, node_increment_rel(x0, l0, a0, r),
+                                node_increment_rel(x1, l1, a1, r), node_increment_rel(x2, l2, a2, r),
+                                node_increment_rel(x3, l3, a3, r), a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f, cr);
     }
     else
         pass_forces_v<MATERIAL>(p, x0, x1, x2, x3, l0, l1, l2, l3, a0, a1, a2, a3, dinv, svol, mu, lambda, kin, f,
