@@ -363,7 +363,7 @@ __device__ __forceinline__ void chunk_line_search(const DevMesh &m, const DevPar
         for (int i = src->node_begin + (c - cb) * THREADS + threadIdx.x; i < src->node_end; i += nb * THREADS) {
             const float4 info = m.info[i];
             if (info.z != 0.f) continue;
-            const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+            const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv, p.incremental ? st.ub : nullptr);
             e = df_add(e, en);
             e2 = fmaf(en.hi, en.hi, e2);
         }
@@ -517,20 +517,20 @@ __global__ void __launch_bounds__(THREADS,
             // the increments of the nodes this thread staged, relative to the
             // chunk's local node 0 (staged by thread 0)
             __syncthreads();
-            const float4 r = increment_ref(s_uh[0], s_ub[0]);
+            const float4 r = s_uh[0];
             __syncthreads();
-            for (int j = threadIdx.x; j < nl; j += THREADS) s_ul[j] = node_increment_rel(s_uh[j], s_ul[j], s_ub[j], r);
+            for (int j = threadIdx.x; j < nl; j += THREADS) s_ul[j] = increment_rel(s_uh[j], s_ul[j], r);
         }
     } else {
         // (the increments relative to the chunk's local node 0)
         float4 r;
-        if (INC) r = increment_ref(st.uh[cur + g_ref], st.ub[g_ref]);
+        if (INC) r = st.uh[cur + g_ref];
         for (int j = threadIdx.x; j < nl; j += THREADS) {
             const int g = meta[j].x;
             const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
             if (INC) {
                 const float4 ub = st.ub[g];
-                s_ul[j] = node_increment_rel(uh, ul, ub, r);
+                s_ul[j] = increment_rel(uh, ul, r);
                 s_ub[j] = ub;
             } else {
                 s_uh[j] = uh;
@@ -753,10 +753,9 @@ __global__ void __launch_bounds__(THREADS, 768 / THREADS) k_tstream(DevMesh m, D
             // the increments of the nodes this thread staged, relative to the
             // chunk's local node 0 (staged by thread 0)
             __syncthreads();
-            const float4 r = increment_ref(sb.uh[0], sb.ub[0]);
+            const float4 r = sb.uh[0];
             __syncthreads();
-            for (int i = threadIdx.x; i < cur.nl; i += THREADS)
-                sb.ul[i] = node_increment_rel(sb.uh[i], sb.ul[i], sb.ub[i], r);
+            for (int i = threadIdx.x; i < cur.nl; i += THREADS) sb.ul[i] = increment_rel(sb.uh[i], sb.ul[i], r);
         }
         __syncthreads();
         if (cur.first && cur.skip) settle_pass<THREADS>(p, st, cur.src, cur.dst, true);
@@ -1056,14 +1055,14 @@ __global__ void __launch_bounds__(THREADS,
             float4 r;
             if (INC) {
                 const int g0 = meta[0].x;
-                r = increment_ref(st.uh[cur + g0], st.ub[g0]);
+                r = st.uh[cur + g0];
             }
             for (int j = threadIdx.x; j < nl; j += THREADS) {
                 const int g = meta[j].x;
                 const float4 uh = st.uh[cur + g], ul = st.ul[cur + g];
                 if (INC) {
                     const float4 ub = st.ub[g];
-                    s_ul[j] = node_increment_rel(uh, ul, ub, r);
+                    s_ul[j] = increment_rel(uh, ul, r);
                     s_ub[j] = ub;
                 } else {
                     s_uh[j] = uh;
@@ -1101,7 +1100,8 @@ __global__ void __launch_bounds__(THREADS,
             for (int i = b * THREADS + threadIdx.x; i < m.Np; i += (int)G * THREADS) {
                 const float4 info = m.info[i];
                 if (info.z != 0.f) continue;
-                const DFloat en = node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv);
+                const DFloat en =
+                    node_energy_df(st, info, U[i], st.ul[cur + i], i, p.h2inv, INC ? st.ub : nullptr);
                 e = df_add(e, en);
                 e2 = fmaf(en.hi, en.hi, e2);
             }

@@ -206,6 +206,50 @@ __global__ void k_epilogue(DevMesh m, DevParams p, DevState st, const int *pad2u
     st.u0l[i] = lo;
 }
 
+// Incremental stress: the passes hold the state as its increment over the
+// step's base, w = u - base as a pair (hi, lo), so that a tet's increments
+// need no exact subtraction each pass (pass_math.cuh, increment_rel).  Before
+// the first pass the parity-0 state u = (hi, lo) becomes (s, e + lo) with
+// s + e = hi - base exactly (TwoSum); a node whose hi word is its base (a
+// pinned node, or any node of the plain guess) gets (0, lo) exactly.  After
+// the last pass each node's final state goes back to u = base + w, hi =
+// fl(base + w hi), lo = that rounding error + w lo: bit for bit the state of
+// a node that did not move.
+__global__ void k_to_increment(DevMesh m, DevState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np || m.info[i].z == 2.f) return;
+    const float4 uh = st.uh[i], ul = st.ul[i], ub = st.ub[i];
+    float4 wh, wl;
+    float e;
+    two_sum(uh.x, -ub.x, wh.x, e);
+    wl.x = __fadd_rn(e, ul.x);
+    two_sum(uh.y, -ub.y, wh.y, e);
+    wl.y = __fadd_rn(e, ul.y);
+    two_sum(uh.z, -ub.z, wh.z, e);
+    wl.z = __fadd_rn(e, ul.z);
+    wh.w = wl.w = 0.f;
+    st.uh[i] = wh;
+    st.ul[i] = wl;
+}
+
+__global__ void k_from_increment(DevMesh m, DevState st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.Np || m.info[i].z == 2.f) return;
+    const size_t off = (size_t)node_ctl(m, st, i).par * m.Np + i;
+    const float4 wh = st.uh[off], wl = st.ul[off], ub = st.ub[i];
+    float4 uh, ul;
+    float e;
+    two_sum(ub.x, wh.x, uh.x, e);
+    ul.x = __fadd_rn(e, wl.x);
+    two_sum(ub.y, wh.y, uh.y, e);
+    ul.y = __fadd_rn(e, wl.y);
+    two_sum(ub.z, wh.z, uh.z, e);
+    ul.z = __fadd_rn(e, wl.z);
+    uh.w = ul.w = 0.f;
+    st.uh[off] = uh;
+    st.ul[off] = ul;
+}
+
 // ------------------------------------------------------------ one pass
 // (the per-node update itself is node_update.cuh's, shared with the frame
 // kernel)
@@ -388,10 +432,18 @@ __global__ void k_ref_gather(DevMesh m, DevParams p, DevState st) {
     st.bl[i] = make_float4(lo[0], lo[1], lo[2], 0.f);
     // c = (M / h^2) x~ + b with the node update's FP32 M / h^2, in FP64,
     // split into (hi, lo); .w carries M / h^2 and the node's state, so that
-    // the node update reads these two words and no other per-step constant
+    // the node update reads these two words and no other per-step constant.
+    // Incremental stress: the passes hold u - base (k_to_increment), so
+    // c = (M / h^2) (x~ - base) + b
     const float mh = info.x * p.h2inv;
     const float4 th = st.th[i], tl = st.tl[i];
-    const double t[3] = {(double)th.x + (double)tl.x, (double)th.y + (double)tl.y, (double)th.z + (double)tl.z};
+    double t[3] = {(double)th.x + (double)tl.x, (double)th.y + (double)tl.y, (double)th.z + (double)tl.z};
+    if (p.incremental) {
+        const float4 ub = st.ub[i];
+        t[0] -= (double)ub.x;
+        t[1] -= (double)ub.y;
+        t[2] -= (double)ub.z;
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double c = (double)mh * t[d] + b[d];
@@ -591,6 +643,16 @@ cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, De
     cudaError_t e = launch_tet_only(s, m, p, st, material, par, true);
     if (e != cudaSuccess) return e;
     return launch_node_only(s, m, p, st, par, true);
+}
+cudaError_t launch_to_increment(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    if (!p.incremental) return cudaSuccess;
+    k_to_increment<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, st);
+    return cudaGetLastError();
+}
+cudaError_t launch_from_increment(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
+    if (!p.incremental) return cudaSuccess;
+    k_from_increment<<<nblk(m.Np, BLOCK), BLOCK, 0, s>>>(m, st);
+    return cudaGetLastError();
 }
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st) {
     if (p.incremental) k_ref_tet<<<nblk(m.Tp, 128), 128, 0, s>>>(m, p, st);

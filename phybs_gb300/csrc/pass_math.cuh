@@ -126,22 +126,37 @@ __device__ __forceinline__ DFloat block_sum_df(DFloat v, float2 *sh) {
     return r;
 }
 
-// node_energy in double-float: the same terms, FP32 operations only.
+// node_energy in double-float: the same terms, FP32 operations only.  With
+// base (incremental stress) (uh, ul) is the increment w over it: u = base +
+// w, u - u~ = (base - u~hi) + (w hi + (w lo - u~lo)).
 __device__ __forceinline__ DFloat node_energy_df(const DevState &st, const float4 &info, const float4 &uh,
-                                                 const float4 &ul, int i, float h2inv) {
+                                                 const float4 &ul, int i, float h2inv,
+                                                 const float4 *base = nullptr) {
     const float4 th = st.th[i], tl = st.tl[i], ex = st.ext[i];
-    const float dx = (uh.x - th.x) + (ul.x - tl.x);
-    const float dy = (uh.y - th.y) + (ul.y - tl.y);
-    const float dz = (uh.z - th.z) + (ul.z - tl.z);
+    float dx, dy, dz;
+    DFloat ux{uh.x, ul.x}, uy{uh.y, ul.y}, uz{uh.z, ul.z};
+    if (base) {
+        const float4 b = base[i];
+        dx = (b.x - th.x) + (uh.x + (ul.x - tl.x));
+        dy = (b.y - th.y) + (uh.y + (ul.y - tl.y));
+        dz = (b.z - th.z) + (uh.z + (ul.z - tl.z));
+        ux = df_add(DFloat{b.x, 0.f}, ux);
+        uy = df_add(DFloat{b.y, 0.f}, uy);
+        uz = df_add(DFloat{b.z, 0.f}, uz);
+    } else {
+        dx = (uh.x - th.x) + (ul.x - tl.x);
+        dy = (uh.y - th.y) + (ul.y - tl.y);
+        dz = (uh.z - th.z) + (ul.z - tl.z);
+    }
     const DFloat sq = df_add(df_add(df_prod(dx, dx), df_prod(dy, dy)), df_prod(dz, dz));
     DFloat k = df_prod(info.x, h2inv);
     k.hi *= 0.5f;  // exact
     k.lo *= 0.5f;
     DFloat e = df_mul(k, sq);
-    e = df_add(e, df_mul(DFloat{uh.y, ul.y}, -info.y));
-    e = df_add(e, df_mul(DFloat{uh.x, ul.x}, -ex.x));
-    e = df_add(e, df_mul(DFloat{uh.y, ul.y}, -ex.y));
-    e = df_add(e, df_mul(DFloat{uh.z, ul.z}, -ex.z));
+    e = df_add(e, df_mul(uy, -info.y));
+    e = df_add(e, df_mul(ux, -ex.x));
+    e = df_add(e, df_mul(uy, -ex.y));
+    e = df_add(e, df_mul(uz, -ex.z));
     return e;
 }
 
@@ -212,9 +227,23 @@ __device__ __forceinline__ bool pass_forces_c(const float4 &x0, const float4 &x1
     return exact;
 }
 
-// A reference for node_increment_rel: fl(u hi - base) of one node (a chunk's
-// local node 0, or a tet's corner 0).  Its rounding does not matter: any
-// constant common to the nodes would do.
+// The staged increment of a node in a pass: the state holds w = u - base as
+// (w hi, w lo) (k_to_increment), and a chunk stages (w hi - r) + w lo with r
+// the w hi of its local node 0.  The tets use only differences of
+// increments, which r leaves unchanged; w hi - r is exact wherever the two
+// are within a factor 2 of each other, so an increment that is large and
+// nearly the same across a chunk (a soft body that moves far in one frame)
+// keeps the small differences dG is made of.  (One rounded FP32 increment
+// (u hi - base) + u lo a node lost them there, and the residual of such
+// frames stalled near 1.5e-4 of its initial value.)
+__device__ __forceinline__ float4 increment_rel(const float4 &wh, const float4 &wl, const float4 &r) {
+    return make_float4(__fadd_rn(__fsub_rn(wh.x, r.x), wl.x), __fadd_rn(__fsub_rn(wh.y, r.y), wl.y),
+                       __fadd_rn(__fsub_rn(wh.z, r.z), wl.z), 0.f);
+}
+
+// Outside the passes (the state as u = (hi, lo)): a reference for
+// node_increment_rel, fl(u hi - base) of one node (a tet's corner 0).  Its
+// rounding does not matter: any constant common to the nodes would do.
 __device__ __forceinline__ float4 increment_ref(const float4 &uh, const float4 &ub) {
     return make_float4(__fsub_rn(uh.x, ub.x), __fsub_rn(uh.y, ub.y), __fsub_rn(uh.z, ub.z), 0.f);
 }

@@ -741,6 +741,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
                                  h->ws_stats.p + 48, h->hd.p, h->sms, h->ws_base, h->material));
         h->guess_pending = false;
     }
+    CK(launch_to_increment(s, m, h->dparams, st));
     // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
     // of chunk j-1 while chunk j runs, so the device never idles on the poll.
     // The frame engine: one launch runs every pass of the step (its pass cap
@@ -761,6 +762,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
             if (h->h_active[(j - 1) & 1] == 0) break;
         }
     }
+    CK(launch_from_increment(s, m, h->dparams, st));
     CK(launch_epilogue(s, m, h->dparams, st, h->pad2user.p));
     CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(InstCtl) * h->B, cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(h->ev_end, s));
@@ -946,6 +948,7 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
+    if (e == cudaSuccess) e = launch_to_increment(s, m, p, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
     for (int i = 0; i < passes && e == cudaSuccess; ++i) {
         e = launch_tet_only(s, m, p, st, h->material, i & 1);
@@ -1002,6 +1005,7 @@ static int time_frame(pbs_handle *h, int passes, double *pass_ms) {
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
     if (e == cudaSuccess) e = launch_ref_force(s, m, p, st);
+    if (e == cudaSuccess) e = launch_to_increment(s, m, p, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
     int rc = PBS_OK;
     if (e == cudaSuccess) rc = launch_frame_step(h, p, passes);

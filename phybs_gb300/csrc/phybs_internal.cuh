@@ -264,6 +264,11 @@ cudaError_t launch_frame(cudaStream_t s, const DevMesh &m, const DevParams &p, D
 
 // Launchers (kernels.cu, warmstart.cu)
 cudaError_t launch_ref_force(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
+// Incremental stress: the parity-0 state to its increment over the base
+// before the passes, each instance's final state back after them (no-ops
+// without incremental stress; kernels.cu)
+cudaError_t launch_to_increment(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
+cudaError_t launch_from_increment(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
 cudaError_t launch_ws_gref(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material);
 cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, const float *theta,
                               const float *feat_mean, const float *feat_std, const float *out_std, float *tetF,
