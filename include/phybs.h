@@ -122,7 +122,9 @@ typedef struct pbs_step_params {
 } pbs_step_params;
 
 typedef struct pbs_stats {
-    int passes;               /* iterations executed, including redone ones (max over instances) */
+    int passes;               /* iterations executed, including redone ones (max over instances); the
+                                 graph engine also counts a pass that carried the state over
+                                 unchanged because a non-finite residual forced an energy check */
     int iterations;           /* accepted iterations k at exit (max over instances) */
     int rejections;           /* line-search rejections (sum over instances)      */
     int converged;            /* instances that met tol                          */
