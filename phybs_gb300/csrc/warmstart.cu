@@ -146,8 +146,10 @@ __global__ void __launch_bounds__(BLOCK) k_ws_gref(DevMesh m, DevParams p, DevSt
     }
 }
 
-// Per tet at the inertial target: F - I (9 values) and det F - 1, into a
-// [Tp][12] scratch array.
+// Per tet at the inertial target: F - I (9 values) and det F - 1, then the
+// tet's material features log10 E and Poisson's ratio (constant, but formed
+// here once a tet rather than once per incident node), into a [Tp][12]
+// scratch array that the node features read as three 128-bit words.
 __global__ void k_ws_tet_F(DevMesh m, DevState st, float *tetF) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.Tp) return;
@@ -159,9 +161,12 @@ __global__ void k_ws_tet_F(DevMesh m, DevState st, float *tetF) {
     Kin<float> kin;
     disp_gradient<float>(st.th[q.x], st.th[q.y], st.th[q.z], st.th[q.w], dinv, kin.G);
     kinematics(kin);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) o[k] = kin.G[k];
-    o[9] = kin.d;
+    const float mu = r1.w, lam = r2.w;
+    const float nu = 0.5f - mu / lam;  // lambda = 2 mu / (1 - 2 nu)
+    float4 *o4 = reinterpret_cast<float4 *>(o);
+    o4[0] = make_float4(kin.G[0], kin.G[1], kin.G[2], kin.G[3]);
+    o4[1] = make_float4(kin.G[4], kin.G[5], kin.G[6], kin.G[7]);
+    o4[2] = make_float4(kin.G[8], kin.d, log10f(2.0f * mu * (1.0f + nu)), nu);
 }
 
 // The 24 raw features of node i (see phybs_gb300/warmstart.py for the list)
@@ -185,13 +190,13 @@ __device__ __forceinline__ void node_features(const DevMesh &m, const DevState &
     const int a = m.inc_ptr[i], e = m.inc_ptr[i + 1];
     for (int j = a; j < e; ++j) {
         const int t = m.inc[j] >> 2;
-        const float *F = tetF + 12 * (size_t)t;
-#pragma unroll
-        for (int k = 0; k < 10; ++k) acc[k] += F[k];
-        const float mu = m.row1[t].w, lam = m.row2[t].w;
-        const float nu = 0.5f - mu / lam;  // lambda = 2 mu / (1 - 2 nu)
-        acc[10] += log10f(2.0f * mu * (1.0f + nu));
-        acc[11] += nu;
+        const float4 *F = reinterpret_cast<const float4 *>(tetF + 12 * (size_t)t);
+        const float4 f0 = F[0], f1 = F[1], f2 = F[2];
+        acc[0] += f0.x; acc[1] += f0.y; acc[2] += f0.z; acc[3] += f0.w;
+        acc[4] += f1.x; acc[5] += f1.y; acc[6] += f1.z; acc[7] += f1.w;
+        acc[8] += f2.x; acc[9] += f2.y;
+        acc[10] += f2.z;  // log10 E
+        acc[11] += f2.w;  // Poisson's ratio
     }
     const float inv = e > a ? 1.0f / (float)(e - a) : 0.f;
     f[12] = acc[10] * inv;
