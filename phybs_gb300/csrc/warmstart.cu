@@ -4,8 +4,9 @@
 //   k_ws_force     corner forces at the plain guess u_plain (into the gather slots)
 //   k_ws_gref      |g(u_plain)| per instance -> ctl.g0: the residual reference of
 //                  the step, the same with or without the warm start
-//   k_ws_tet_F     per-tet F - I and det F - 1 at the inertial target x~
-//   k_ws_infer     per 16-node tile and warp: node features (velocity history,
+//   k_ws_tet_F     per-tet F - I and det F - 1 at the inertial target x~,
+//                  and the tet's log10 E and Poisson's ratio
+//   k_ws_infer     per 32 nodes and warp: node features (velocity history,
 //                  inertial offset, material, mean incident F and J), the
 //                  standardised 24-vector, the tensor-core MLP, and the
 //                  candidate guess u_plain + s * out_std * output (free nodes;
@@ -227,8 +228,8 @@ struct WsNet {
 // (uh, ul)[parity 1] (free nodes; others copy the plain guess).
 __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevState st, const float *tetF, WsNet net) {
     __shared__ mlp::SmemWeights sw;
-    __shared__ float tile[4][16][25];
-    __shared__ float tscale[4][16];
+    __shared__ float tile[4][32][25];
+    __shared__ float tscale[4][32];
     __shared__ float fm[24], fs[24], os[3];
     mlp::stage_weights(net.theta, sw);
     if (threadIdx.x < 24) {
@@ -239,8 +240,10 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
     const int nwarps = gridDim.x * 4;
-    for (int row0 = (blockIdx.x * 4 + w) * 16; row0 < m.Np; row0 += nwarps * 16) {
-        if (lane < 16) {
+    // 32 nodes a warp and iteration (Np is a multiple of 256): every lane
+    // gathers one node's features, then the MLP runs on two 16-row tiles
+    for (int row0 = (blockIdx.x * 4 + w) * 32; row0 < m.Np; row0 += nwarps * 32) {
+        {
             const int i = row0 + lane;
             float f[24], sc = 0.f;
             const float4 info = m.info[i];
@@ -257,37 +260,41 @@ __global__ void __launch_bounds__(128) k_ws_infer(DevMesh m, DevParams p, DevSta
             tscale[w][lane] = sc;
         }
         __syncwarp();
-        uint32_t x[2][4];
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half) {
+            float(*tl)[25] = tile[w] + 16 * half;
+            uint32_t x[2][4];
 #pragma unroll
-        for (int kb = 0; kb < 2; ++kb) {
-            float v[4][2];
+            for (int kb = 0; kb < 2; ++kb) {
+                float v[4][2];
 #pragma unroll
-            for (int hh = 0; hh < 2; ++hh)
+                for (int hh = 0; hh < 2; ++hh)
 #pragma unroll
-                for (int e2 = 0; e2 < 2; ++e2) {
-                    const int col = 16 * kb + 8 * hh + 2 * t + e2;
-                    v[2 * hh][e2] = col < 24 ? tile[w][g][col] : 0.f;
-                    v[2 * hh + 1][e2] = col < 24 ? tile[w][g + 8][col] : 0.f;
-                }
-            x[kb][0] = mlp::pack_bf16(v[0][0], v[0][1]);
-            x[kb][1] = mlp::pack_bf16(v[1][0], v[1][1]);
-            x[kb][2] = mlp::pack_bf16(v[2][0], v[2][1]);
-            x[kb][3] = mlp::pack_bf16(v[3][0], v[3][1]);
-        }
-        float out[4];
-        mlp::forward_tile(sw, x, out);
-        __syncwarp();
-        // corrections of rows g and g+8, columns 2t, 2t+1 -> shared tile
-#pragma unroll
-        for (int e2 = 0; e2 < 2; ++e2) {
-            const int col = 2 * t + e2;
-            if (col < 3) {
-                tile[w][g][col] = out[e2];
-                tile[w][g + 8][col] = out[2 + e2];
+                    for (int e2 = 0; e2 < 2; ++e2) {
+                        const int col = 16 * kb + 8 * hh + 2 * t + e2;
+                        v[2 * hh][e2] = col < 24 ? tl[g][col] : 0.f;
+                        v[2 * hh + 1][e2] = col < 24 ? tl[g + 8][col] : 0.f;
+                    }
+                x[kb][0] = mlp::pack_bf16(v[0][0], v[0][1]);
+                x[kb][1] = mlp::pack_bf16(v[1][0], v[1][1]);
+                x[kb][2] = mlp::pack_bf16(v[2][0], v[2][1]);
+                x[kb][3] = mlp::pack_bf16(v[3][0], v[3][1]);
             }
+            float out[4];
+            mlp::forward_tile(sw, x, out);
+            __syncwarp();
+            // corrections of rows g and g+8, columns 2t, 2t+1 -> shared tile
+#pragma unroll
+            for (int e2 = 0; e2 < 2; ++e2) {
+                const int col = 2 * t + e2;
+                if (col < 3) {
+                    tl[g][col] = out[e2];
+                    tl[g + 8][col] = out[2 + e2];
+                }
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        if (lane < 16) {
+        {
             const int i = row0 + lane;
             const float4 info = m.info[i];
             if (info.z != 2.f) {
@@ -418,8 +425,8 @@ cudaError_t launch_ws_predict(cudaStream_t s, const DevMesh &m, const DevParams 
                               int sms, int base, int material) {
     k_ws_tet_F<<<nblk(m.Tp, 256), 256, 0, s>>>(m, st, tetF);
     WsNet net{theta, feat_mean, feat_std, out_std, base};
-    const int tiles = nblk(m.Np, 16);
-    const int blocks = std::min(nblk(tiles, 4), 8 * sms);
+    const int rows32 = nblk(m.Np, 32);  // 32 nodes a warp and iteration
+    const int blocks = std::min(nblk(rows32, 4), 8 * sms);
     k_ws_infer<<<blocks, 128, 0, s>>>(m, p, st, tetF, net);
     if (base == 1) {  // the candidate's gradient for the residual test
         DevState s1 = st;
