@@ -4,7 +4,7 @@ benchmark's mesh.
 bench.py times the 1M-tet box pull (50 x 50 x 80 cubes, 5-tet split, nodes
 jittered by 0.1 cell, top face pinned, bottom face pulled to 1.5x its length
 over 30 frames, h = 1/30) with RESTART control, alpha0 0.4, alpha growth 1.2,
-a single Chebyshev stage rho = 0.9999, incremental stress, the GPU energy
+the three-stage Chebyshev schedule bench.PROFILE, incremental stress, the GPU energy
 clamp and every frame iterated to |g| <= 1e-4 |g_0|.  This test runs the same
 settings (bench.solver_params, bench.box_workload, bench.bottom_positions:
 nothing re-typed) on the same box at 1/5 resolution (10 x 10 x 16 cubes,
@@ -47,7 +47,7 @@ def built():
 def _oracle_params():
     """bench.solver_params() as the restatement takes it."""
     return O.make_params(h=1 / 30, max_iters=20000, tol=1e-4, control=1, alpha0=bench.ALPHA0,
-                         profile=((10, bench.RHO),), body_force_scale=1.0, energy_clamp=1, hessian_closed=1,
+                         profile=bench.PROFILE, body_force_scale=1.0, energy_clamp=1, hessian_closed=1,
                          alpha_grow=bench.ALPHA_GROW)
 
 
