@@ -89,11 +89,12 @@ ALPHA0 = 0.4
 # recurrence, in the reference's multi-stage form (DescentOptimize.cpp:
 # 156-175).  The frame's fast modes go first with a small rho, the slowest
 # ones last with rho = 0.9999; against one stage of 0.9999 from iteration 10
-# it is faster in both arms on four of the five mesh seeds and in total (the
-# plain arm's five-seed time 4.80 -> 4.44 s; seed 0 plain +16%, warm-started
-# +30%), with no line-search rejection in the plain arm.
+# it is faster in total over the five mesh seeds (the plain arm's time over
+# frames 3..29, 4.80 -> 4.41 s; seed 0 plain +20%, warm-started +38%), with no
+# line-search rejection in the plain arm; of the schedules tried, the least
+# plain time in total.
 RHO = 0.9999
-PROFILE = ((5, 0.99), (20, 0.999), (80, RHO))
+PROFILE = ((5, 0.99), (25, 0.999), (100, RHO))
 # The step size recovers by 1.2x per accepted energy check (up to alpha0):
 # with the reference's shrink-only rule one early rejection slows a whole
 # frame, most of all from a good (learned) start, whose Chebyshev ramp raises
