@@ -76,15 +76,14 @@ def bottom_positions(m, bottom, length, frame):
 
 
 # Residual-target solver settings for the box workload.  The reference's
-# alpha0 = 0.1 needs ~15,000 iterations per frame at 1M tets.  Over the five
-# mesh seeds (E from 15 kPa to 770 kPa) and a body at the range's softest
-# 10 kPa, alpha0 = 0.4 is faster than 0.3 in both arms on every one (seed 0
-# plain 26.4 -> 32.4 frames/s), 0.45 a little faster still but closer to the
-# step at which the softest seed's line search starts rejecting in a cascade
-# (640 rejections at 0.5), so the benchmark keeps the margin.  The GPU
-# energy clamp max(e, 0) is used: the CPU reference's e > 1e-6 J clamp zeroes
-# the energy of these small tets.
-ALPHA0 = 0.4
+# alpha0 = 0.1 needs ~15,000 iterations per frame at 1M tets.  With the
+# Chebyshev stages below, alpha0 = 0.45 is 5-21% faster than 0.4 in both arms
+# on each of the five mesh seeds (E from 15 kPa to 770 kPa) and converges
+# every frame of a body at the range's softest 10 kPa (15 line-search
+# rejections over 27 frames); at 0.5 the softest seed's line search rejects in
+# a cascade (1,740 rejections).  The GPU energy clamp max(e, 0) is used: the
+# CPU reference's e > 1e-6 J clamp zeroes the energy of these small tets.
+ALPHA0 = 0.45
 # Chebyshev schedule: (first iteration, rho) stages, each restarting the
 # recurrence, in the reference's multi-stage form (DescentOptimize.cpp:
 # 156-175).  The frame's fast modes go first with a small rho, the slowest

@@ -3,7 +3,7 @@ benchmark's mesh.
 
 bench.py times the 1M-tet box pull (50 x 50 x 80 cubes, 5-tet split, nodes
 jittered by 0.1 cell, top face pinned, bottom face pulled to 1.5x its length
-over 30 frames, h = 1/30) with RESTART control, alpha0 0.4, alpha growth 1.2,
+over 30 frames, h = 1/30) with RESTART control, alpha0 0.45, alpha growth 1.2,
 the three-stage Chebyshev schedule bench.PROFILE, incremental stress, the GPU energy
 clamp and every frame iterated to |g| <= 1e-4 |g_0|.  This test runs the same
 settings (bench.solver_params, bench.box_workload, bench.bottom_positions:
