@@ -25,8 +25,10 @@ struct NodeIn {
 };
 
 // Per-step node constants staged in shared memory before the grid-dependency
-// wait: c = (M / h^2) x~ + b as (hi, lo), with M / h^2 in ch.w and the node's
-// state (0 free, 1 pinned, 2 padding) in cl.w.
+// wait: c = (M / h^2) x~ + b as (hi, lo) -- with incremental stress, where the
+// state u is the increment over the step's base, c = (M / h^2)(x~ - base) + b
+// -- with M / h^2 in ch.w and the node's state (0 free, 1 pinned, 2 padding)
+// in cl.w.
 struct NodeConst {
     float4 ch, cl;
 };
@@ -102,7 +104,8 @@ __device__ __forceinline__ float node_update(const DevMesh &m, const DevParams &
             }
             // g = M/h^2 (u - u~) - (b + sum of corner forces), b = step-start elastic
             // force (incremental mode) + body_force_scale (external + gravity),
-            // formed as M/h^2 u - c - f with the per-step c = M/h^2 u~ + b: the
+            // formed as M/h^2 u - c - f with the per-step c = M/h^2 u~ + b (u
+            // and c relative to the base with incremental stress): the
             // product M/h^2 u_hi exactly (fma), its large part cancelled
             // against c hi, the small terms added after
             const float4 ch = in.ch, cl = in.cl;

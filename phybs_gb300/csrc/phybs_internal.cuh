@@ -12,7 +12,8 @@
 //   u0h, u0l    float4[Np]         displacement at the start of the step
 //   th, tl      float4[Np]         inertial target x~ - X (hi, lo)
 //   bh, bl      float4[Np]         per-step force constant b (hi, lo)
-//   ch, cl      float4[Np]         per-step gradient constant c = (M / h^2) x~ + b (hi, lo)
+//   ch, cl      float4[Np]         per-step gradient constant c = (M / h^2) x~ + b (hi, lo);
+//                                  incremental stress: (M / h^2)(x~ - base) + b
 //   v, vold     float4[Np]         velocities of this and the previous step
 //   ext, diag   float4[Np]         external force; Jacobi diagonal + M/h^2
 //   info        float4[Np]         {effective mass (pins 1e8), gravity_y,
@@ -161,7 +162,8 @@ struct DevMesh {
 };
 
 struct DevState {
-    float4 *uh, *ul, *dd;  // [2][Np] each
+    float4 *uh, *ul, *dd;  // [2][Np] each; with incremental stress, during the passes (uh, ul) is
+                           // the increment over ub (k_to_increment / k_from_increment)
     float4 *oh, *ol, *u0h, *u0l, *th, *tl;
     float4 *v, *vold, *ext, *diag;
     float4 *hist1, *hist2;  // displacement of the last step and of the one before
@@ -170,7 +172,8 @@ struct DevState {
                             // plus body_force_scale * (external + gravity)
     float4 *ch, *cl;        // per node (hi, lo): c = (M / h^2) x~ + b, the step-constant part of
                             // the gradient g = (M / h^2) u - c - f (the node update reads these
-                            // two words instead of x~ and b)
+                            // two words instead of x~ and b); with incremental stress the passes'
+                            // u is the increment over the base and c = (M / h^2)(x~ - base) + b
     float *tf, *hd;
     double2 *tpart, *cpart;
     double *npart;
