@@ -5,7 +5,9 @@
 //   tets        int4[Tp]           padded node ids of the 4 corners
 //   row0..2     float4[Tp] each    rows of Dm^-1; .w = {det Dm/6, mu, lambda}
 //   uh, ul      float4[2][Np]      displacement u = x - X as an FP32 (hi, lo)
-//                                  pair, ping-ponged between passes
+//                                  pair, ping-ponged between passes (with
+//                                  incremental stress, during the passes: the
+//                                  increment u - ub as such a pair)
 //   dd          float4[2][Np]      last step d = u_k - u_{k-1} (Chebyshev history)
 //   oh, ol      float4[Np]         displacement saved at the last accepted
 //                                  line-search check (the reference's x_old)
