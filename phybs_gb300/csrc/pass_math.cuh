@@ -182,9 +182,10 @@ __device__ __forceinline__ float4 f4add(const float4 &a, const float4 &b) {
 
 // Corner values: x = u hi word, l = u lo word, a = base (hi) of the 4 corners.
 // INC (compile time): the incremental neo-Hookean form, where l carries the
-// corner's increment u - base less a reference increment common to the tet
-// (node_increment_rel, formed once per node) and x is unused; without INC, a
-// is unused.  cr locates the corners' rest positions
+// corner's increment u - base less a reference common to the tet, formed once
+// per node (increment_rel from the passes' increment state in the chunk
+// kernels, node_increment_rel from a (hi, lo) state elsewhere), and x is
+// unused; without INC, a is unused.  cr locates the corners' rest positions
 // for the FP64 stress of a near-inverted tet (full stress only).  DEFER:
 // leave that stress out (f is then not the tet's) and return whether the tet
 // needs it, for a caller that forms it after its loop.  KIN = false: with
