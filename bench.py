@@ -287,9 +287,9 @@ def launches_per_frame(graph_launches: int, warm: bool) -> int:
     double-float + gather with incremental stress, the gather alone
     otherwise), epilogue; with the warm start the plain guess's corner
     forces (full stress only), reference gradient, tet F, inference, judge and
-    select; 2 x 16 passes plus the closing decision (k_settle) per graph
-    launch (the counts of a launch list of one plain and one warm-started
-    frame)."""
+    select; 2 x 16 passes plus the closing decision (k_settle) per body of
+    the step graph's loop (the counts of a launch list of one plain and one
+    warm-started frame)."""
     ref = 2 if INCREMENTAL_STRESS else 1
     warm_extra = (0 if INCREMENTAL_STRESS else 1) + 5 if warm else 0
     return 1 + 3 + 2 + ref + warm_extra + (2 * 16 + 1) * graph_launches

@@ -134,7 +134,7 @@ typedef struct pbs_stats {
     double energy;            /* instance 0 energy at its last check             */
     double residual_ratio;    /* instance 0 |g_k| / |g_0|                         */
     double device_ms;         /* device time of the last pbs_step (CUDA events)   */
-    int graph_launches;       /* captured 16-pass graphs launched by the last step */
+    int graph_launches;       /* 16-pass bodies the last step's graph ran */
     int warm_start_used;      /* instances whose step started from the learned guess */
     int guess_fallbacks;      /* RESTART control: instances whose inertial guess inverted a
                                  tet, started from the step's start positions instead */

@@ -345,9 +345,21 @@ __global__ void __launch_bounds__(BLOCK / NPT, NPT == 2 ? 6 : 0) k_node(DevMesh 
 // The pending pass decisions after the last pass of a run, one CTA an
 // instance; par: the parity the next pass would have (the copy they are in).
 // The result goes to st.ctl.
-__global__ void __launch_bounds__(BLOCK) k_settle(DevParams p, DevState st, int par) {
+template <bool LOOP>
+__global__ void __launch_bounds__(BLOCK) k_settle(DevParams p, DevState st, int par, LoopCtl lc) {
     pdl_wait();
     settle_pass<BLOCK>(p, st, ctl_buf(st, par) + blockIdx.x, st.ctl + blockIdx.x, false);
+    if (!LOOP || threadIdx.x != 0) return;
+    // each CTA's atomicSub of active[0] comes before its ticket, so the last
+    // ticket sees every instance's outcome of this run
+    __threadfence();
+    if (atomicAdd(st.active + 3, 1) != (int)gridDim.x - 1) return;
+    __threadfence();
+    st.active[3] = 0;
+    const int runs = __ldcg(st.active + 2) + 1;
+    st.active[2] = runs;
+    const int live = atomicAdd(st.active, 0);
+    cudaGraphSetConditional(lc.cond, (live > 0 && runs < lc.max_runs) ? 1u : 0u);
 }
 
 // Per-step node constant b = f_el(u_base) (incremental mode, double-float /
@@ -626,7 +638,8 @@ static cudaError_t launch_node_t(cudaStream_t s, const DevMesh &m, const DevPara
 cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
     return m.node_npt == 2 ? launch_node_t<2>(s, m, p, st, par, pdl) : launch_node_t<1>(s, m, p, st, par, pdl);
 }
-cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl) {
+cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par, bool pdl,
+                          const LoopCtl *loop) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m.n_inst);
     cfg.blockDim = dim3(BLOCK);
@@ -636,7 +649,8 @@ cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, 
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_settle, p, st, par);
+    if (loop) return cudaLaunchKernelEx(&cfg, k_settle<true>, p, st, par, *loop);
+    return cudaLaunchKernelEx(&cfg, k_settle<false>, p, st, par, LoopCtl{});
 }
 // One pass of the step graph: both kernels with programmatic dependent launch.
 cudaError_t launch_pass(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int material, int par) {

@@ -17,7 +17,7 @@ using namespace pbs;
 
 namespace {
 
-constexpr int CHUNK_PASSES = 16;  // passes per captured graph launch
+constexpr int CHUNK_PASSES = 16;  // passes per body of the step graph
 
 template <typename T> struct DevBuf {
     T *p = nullptr;
@@ -130,11 +130,12 @@ struct pbs_handle {
     DevBuf<float> pd_val, pd_dinv;
     DevBuf<float4> dyn_px, dyn_x0, dyn_s;
     // host pinned
-    int *h_active = nullptr;   // 2 slots
+    int *h_active = nullptr;   // 2 slots: running counts of the host loop, or the bodies the loop ran
     InstCtl *h_ctl = nullptr;
     cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_chunk[2] = {nullptr, nullptr};
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    bool graph_loop = false;  // graph is the WHILE node over the pass body (else the body alone)
     // persistent frame kernel: its barrier words and per-CTA sums
     int engine = PBS_ENGINE_GRAPH;
     DevBuf<FrameSync> fsync;
@@ -523,10 +524,10 @@ int pbs_create(const pbs_mesh_desc *d, pbs_handle **out) {
     CKC(h->tf.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T))); CKC(h->hd.alloc(std::max(12 * (size_t)Tp, 16 * (size_t)T)));
     CKC(h->staging.alloc(3 * (size_t)N)); CKC(h->staging2.alloc(12 * (size_t)Tp)); CKC(h->staging_ids.alloc(N));
     CKC(h->tpart.alloc(h->n_tblk)); CKC(h->npart.alloc(h->n_nblk)); CKC(h->npartf.alloc(h->n_nblk));
-    CKC(h->ctl.alloc(B)); CKC(h->ctl2.alloc(B)); CKC(h->tcount.alloc(B)); CKC(h->active.alloc(2));
+    CKC(h->ctl.alloc(B)); CKC(h->ctl2.alloc(B)); CKC(h->tcount.alloc(B)); CKC(h->active.alloc(4));
     CKC(cudaMemsetAsync(h->ctl2.p, 0, sizeof(InstCtl) * B, h->stream));
     CKC(cudaMemsetAsync(h->tcount.p, 0, sizeof(unsigned int) * B, h->stream));
-    CKC(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), h->stream));
+    CKC(cudaMemsetAsync(h->active.p, 0, 4 * sizeof(int), h->stream));
     CKC(h->qrows.alloc(4 * (size_t)T)); CKC(h->rslot.alloc(12 * (size_t)T));
     h->qrow0 = h->qrows.p;
     h->qrow1 = h->qrows.p + (size_t)T;
@@ -662,24 +663,72 @@ int pbs_get_params(pbs_handle *h, pbs_step_params *p) {
     return PBS_OK;
 }
 
-static int ensure_graph(pbs_handle *h) {
-    if (h->graph_valid) return PBS_OK;
-    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
-    cudaGraph_t g = nullptr;
+// CHUNK_PASSES passes and the closing settle, captured from h->stream.
+static cudaError_t capture_body(pbs_handle *h, const LoopCtl *loop) {
     DevMesh m = h->mesh();
     DevState st = h->state();
-    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < CHUNK_PASSES && e == cudaSuccess; ++i)
         e = launch_pass(h->stream, m, h->dparams, st, h->material, i & 1);
-    // the last pass's decision, so that the host's poll and the next launch
-    // see settled control blocks
-    if (e == cudaSuccess) e = launch_settle(h->stream, m, h->dparams, st, CHUNK_PASSES & 1, true);
-    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
-    if (e != cudaSuccess || e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return PBS_E_CUDA; }
-    e = cudaGraphInstantiate(&h->graph, g, 0);
+    // the last pass's decision, so that the next run, the host and the
+    // epilogue see settled control blocks
+    if (e == cudaSuccess) e = launch_settle(h->stream, m, h->dparams, st, CHUNK_PASSES & 1, true, loop);
+    return e;
+}
+
+// Bodies of CHUNK_PASSES passes a step needs at most (its pass cap).
+static int max_runs(const pbs_handle *h) { return (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES; }
+
+// The step graph as a WHILE node over the body: k_settle's last CTA ends the
+// loop when no instance runs or max_runs bodies ran, so a step is one graph
+// launch and neither the host nor an extra body waits on the outcome.
+static cudaError_t build_loop_graph(pbs_handle *h, cudaGraphExec_t *out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    LoopCtl lc{};
+    lc.max_runs = max_runs(h);
+    e = cudaGraphConditionalHandleCreate(&lc.cond, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {};
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = lc.cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(h->stream, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t ec = capture_body(h, &lc);
+        cudaGraph_t body = nullptr;
+        e = cudaStreamEndCapture(h->stream, &body);
+        if (ec != cudaSuccess) e = ec;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
-    CK(e);
+    return e;
+}
+
+static int ensure_graph(pbs_handle *h) {
+    if (h->graph_valid) return PBS_OK;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    h->graph_loop = build_loop_graph(h, &h->graph) == cudaSuccess;
+    if (!h->graph_loop) {
+        // without conditional nodes: the body alone, launched by the host
+        (void)cudaGetLastError();
+        h->graph = nullptr;
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t e = capture_body(h, nullptr);
+        const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) { if (g) cudaGraphDestroy(g); return PBS_E_CUDA; }
+        const cudaError_t e3 = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(e3);
+    }
     h->graph_valid = true;
     return PBS_OK;
 }
@@ -727,7 +776,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     DevState st = h->state();
     CK(cudaEventRecord(h->ev_start, s));
     if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s));
+    CK(cudaMemsetAsync(h->active.p, 0, 4 * sizeof(int), s));
     CK(launch_init_ctl(s, h->B, h->dparams, st));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     CK(launch_guess_check(s, m, h->dparams, st));
@@ -742,15 +791,20 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
         h->guess_pending = false;
     }
     CK(launch_to_increment(s, m, h->dparams, st));
-    // Chunks of CHUNK_PASSES passes; the host reads the active-instance count
-    // of chunk j-1 while chunk j runs, so the device never idles on the poll.
-    // The frame engine: one launch runs every pass of the step (its pass cap
-    // ends it at the latest).
-    const int max_chunks = frame ? 0 : (h->dparams.pass_cap + CHUNK_PASSES - 1) / CHUNK_PASSES;
+    // The graph's WHILE node runs bodies of CHUNK_PASSES passes until no
+    // instance runs; without it the host launches the body and reads the
+    // active-instance count of body j-1 while body j runs, so the device never
+    // idles on the poll (body j may then find every instance done).  The frame
+    // engine: one launch runs every pass of the step (its pass cap ends it at
+    // the latest).
+    const int max_chunks = frame || h->graph_loop ? 0 : max_runs(h);
     int launched = 0;
     if (frame) {
         rc = launch_frame_step(h, h->dparams, h->dparams.pass_cap);
         if (rc != PBS_OK) return rc;
+    } else if (h->graph_loop) {
+        CK(cudaGraphLaunch(h->graph, s));
+        CK(cudaMemcpyAsync(h->h_active, h->active.p + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     }
     for (int j = 0; j < max_chunks; ++j) {
         ++launched;
@@ -771,6 +825,7 @@ int pbs_step(pbs_handle *h, const float *ext, int *iters_out) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, h->ev_start, h->ev_end);
     h->last_ms = ms;
+    if (!frame && h->graph_loop) launched = h->h_active[0];
     pbs_stats S{};
     S.status = PBS_OK;
     for (int b = 0; b < h->B; ++b) {
@@ -891,7 +946,7 @@ int pbs_warm_start_features(pbs_handle *h, const float *ext, float *features, fl
     DevMesh m = h->mesh();
     DevState st = h->state();
     if (ext) CK(cudaMemcpyAsync(h->staging.p, ext, sizeof(float) * 3 * (size_t)h->N, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s));
+    CK(cudaMemsetAsync(h->active.p, 0, 4 * sizeof(int), s));
     CK(launch_init_ctl(s, h->B, h->dparams, st));
     CK(launch_prologue(s, m, h->dparams, st, ext ? h->staging.p : nullptr, h->pad2user.p));
     DevBuf<float> out;
@@ -943,7 +998,7 @@ static int time_passes(pbs_handle *h, int passes, double *tet_ms, double *node_m
     DevState st = h->state();
     std::vector<cudaEvent_t> ev(2 * passes + 1, nullptr);
     for (auto &e : ev) CK(cudaEventCreate(&e));
-    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 4 * sizeof(int), s);
     if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, st);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);
@@ -1000,7 +1055,7 @@ static int time_frame(pbs_handle *h, int passes, double *pass_ms) {
     DevState st = h->state();
     cudaEvent_t ev[2] = {nullptr, nullptr};
     for (auto &e : ev) CK(cudaEventCreate(&e));
-    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 2 * sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(h->active.p, 0, 4 * sizeof(int), s);
     if (e == cudaSuccess) e = launch_init_ctl(s, h->B, p, st);
     if (e == cudaSuccess) e = launch_prologue(s, m, p, st, nullptr, h->pad2user.p);
     if (e == cudaSuccess) e = launch_guess_check(s, m, p, st);

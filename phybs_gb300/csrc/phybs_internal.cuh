@@ -185,7 +185,8 @@ struct DevState {
     InstCtl *ctl;   // the control blocks between passes (and between steps)
     InstCtl *ctl2;  // the graph path's second copy: a pass reads one and writes the other
     unsigned int *tcount;  // per instance: the chunks of a line-search pass that finished
-    int *active;  // [0] instances not yet done, [1] a device wait gave up (sticky for the step)
+    int *active;  // [0] instances not yet done, [1] a device wait gave up (sticky for the step),
+                  // [2] bodies of the step graph's loop run so far, [3] k_settle's ticket
 };
 
 // The control-block copy a pass with parity q reads (its tet kernel) or, with
@@ -304,8 +305,15 @@ cudaError_t launch_node_only(cudaStream_t s, const DevMesh &m, const DevParams &
 // Takes the pending pass decisions after a run of passes whose next parity is
 // par (the copy they are in), leaving them in st.ctl.  A run of passes must
 // end with it before anything else reads the control blocks.
+// With loop (the body of the step graph's WHILE node): the last CTA to settle
+// counts the body run in active[2] and sets the node's condition, so the
+// loop goes on while an instance runs and fewer than max_runs bodies ran.
+struct LoopCtl {
+    cudaGraphConditionalHandle cond;
+    int max_runs;
+};
 cudaError_t launch_settle(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st, int par,
-                          bool pdl = false);
+                          bool pdl = false, const LoopCtl *loop = nullptr);
 // RESTART control: replaces an instance's inertial guess by the step's start
 // positions when the guess inverts a tet (kernels.cu)
 cudaError_t launch_guess_check(cudaStream_t s, const DevMesh &m, const DevParams &p, DevState st);
